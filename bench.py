@@ -1,0 +1,346 @@
+"""Benchmark: PMC samples/s of one full iteration on the mixture microbench.
+
+Workload (per GPU): D=32, K=64 Student-t (nu=3) proposal with condition-1e6
+covariances, target a different normalised 16-component Gaussian mixture,
+N = 2^20 samples; one step = draw -> log q -> log posterior -> weights /
+evidence / perplexity -> Rao-Blackwellised EM update (+ Cholesky, burial).
+Synthetic, seeded data of the named shapes.
+
+`value`  : mixed-precision engine, device-resident run, samples/s over all ranks.
+`e2e`    : same metric through the pmclib-named drop-in C ABI with host
+           (pinned) buffers, host<->device copies inside the timed region.
+fp64     : the plain FP64 path on the same workload (the drop-in baseline).
+--impl reference : the CPU restatement (oracle) on all host cores, on a bounded
+           sample of the same workload.
+Multi-GPU: replicas only (independent runs, one per rank, no collective on the
+data path); `value` = total samples / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PMC samples/s (one full iteration: draw, log q, log posterior, weights+evidence, RB-EM update)"
+UNIT = "samples/s"
+WORKLOAD = "mixture microbench: D=32, K=64 Student-t nu=3 (cond 1e6), 16-comp Gaussian-mixture target, N=2^20"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nsamples", type=int, default=1 << 20)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- workload
+def build_workload(P, W, N, seed_offset=0):
+    wl = W.mixture_workload(D=32, K=64, Kt=16, nu=3, seed=64)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+    post = P.Posterior(32).add_mix(target)
+    return prop, target, post
+
+
+def flush_l2(buf):
+    """Write a buffer larger than L2 (the engine's own arrays are larger too)."""
+    if buf is not None:
+        buf.add_(1.0)
+
+
+def time_run(P, run, steps, warmup, l2buf, sync, prop):
+    """Every step is one full iteration from the same starting proposal (reset
+    outside the timed events), so each step does identical work."""
+    for _ in range(warmup):
+        run.set_proposal(prop)
+        run.iterate(1.0)
+    run.set_timing(True)
+    launches = 0
+    stats = None
+    sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        run.set_proposal(prop)
+        flush_l2(l2buf)
+        sync()
+        stats = run.iterate(1.0)
+        launches += run.last_launches()
+    sync()
+    wall = time.perf_counter() - t0
+    ms, n = run.stage_ms()
+    run.set_timing(False)
+    return stats, ms, n, launches, wall
+
+
+def cpu_baseline(O, W, nsample, seed=5):
+    wl = W.mixture_workload(D=32, K=64, Kt=16, nu=3, seed=64)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = O.Mix(w, mu, cov, df=df)
+    target = O.Mix(wt, mut, covt, df=-1)
+    O.iterate_mix(prop.copy(), target, 0.0, 1024, seed, 0)  # warm the pages
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.iterate_mix(prop.copy(), target, 0.0, nsample, seed, reps)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > 8.0 or reps >= 4:
+            break
+    return nsample * reps / el, O.num_threads(), reps
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from cosmopmc_gb300 import workloads as W
+    O.build()
+    wl = W.mixture_workload(D=32, K=64, Kt=16, nu=3, seed=64)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = O.Mix(w, mu, cov, df=df)
+    target = O.Mix(wt, mut, covt, df=-1)
+    n = args.cpu_sample
+    for i in range(args.warmup):
+        O.iterate_mix(prop.copy(), target, 0.0, n, 5, i)
+    times = []
+    for i in range(args.steps):
+        p = prop.copy()  # same starting proposal every step, as in the GPU arm
+        t0 = time.perf_counter()
+        O.iterate_mix(p, target, 0.0, n, 5, args.warmup + i)
+        times.append(time.perf_counter() - t0)
+    ms = 1000.0 * sum(times) / len(times)
+    v = n / (ms / 1000.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded, shapes of the mixture microbench)",
+        "config": {"workload": WORKLOAD, "global_batch": n, "sample_per_step": n, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                         "sample": f"{n} samples of the N=2^20 workload per step (oracle/pmc_oracle.c, OpenMP)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cosmopmc_gb300 import pmcg as P
+    from cosmopmc_gb300 import workloads as W
+
+    P.load()
+    N = args.nsamples
+    prop, target, post = build_workload(P, W, N)
+    l2buf = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    sync = torch.cuda.synchronize
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        sync()
+
+    # ---------------- mixed-precision engine (the headline)
+    run = P.Run(prop, post, N, precision=P.MIXED, seed=1000 + rank)
+    barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    stats, stage_ms, nt, launches, wall = time_run(P, run, args.steps, args.warmup, l2buf, sync, prop)
+    clocks = clk.stop()
+    barrier()
+    step_ms = sum(stage_ms) / nt
+    t_local = torch.tensor([step_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    step_ms_max = float(t_local.item())
+    value = N * world / (step_ms_max / 1000.0)
+
+    # ---------------- plain FP64 path on the same workload
+    run64 = P.Run(prop, post, N, precision=P.FP64, seed=1000 + rank)
+    s64, ms64, n64, _, _ = time_run(P, run64, args.fp64_steps, 1, l2buf, sync, prop)
+    fp64_ms = sum(ms64) / n64
+    fp64_value = N * world / (fp64_ms / 1000.0)
+    run64.free()
+
+    # ---------------- e2e: drop-in C ABI with host buffers (mixed precision)
+    P.set_dropin_precision(P.MIXED)
+    ps = P.PmcSimu(N, 32)
+    rng = P.Rng(7 + rank)
+    w0, mu0, L0 = prop.arrays()
+    m = P.MixMvdens.from_arrays(w0, mu0, L=L0, df=prop.df)
+
+    def dropin_step():
+        P.simulate_mix_mvdens(ps, m, rng, None)
+        P.importance_weights(ps, m, post, 1.0)
+        P.normalize_importance_weight(ps)
+        P.update_prop_rb(m, ps)
+        P.perplexity_and_ess(ps)
+        return P.evidence(ps)
+
+    for _ in range(args.warmup):
+        m.set(w0, mu0, L=L0, df=prop.df)
+        dropin_step()
+    barrier()
+    e2e_tot = 0.0
+    for _ in range(args.steps):
+        m.set(w0, mu0, L=L0, df=prop.df)   # same starting proposal every step (host side, untimed)
+        flush_l2(l2buf)
+        sync()
+        t0 = time.perf_counter()
+        dropin_step()
+        e2e_tot += time.perf_counter() - t0
+    e2e_ms = 1000.0 * e2e_tot / args.steps
+    e2e_t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = N * world / (float(e2e_t.item()) / 1000.0)
+    K, D = 64, 32
+    h2d = K * (1 + D + D * D) * 8 + 2 * K * (1 + D + D * D) * 8   # proposal uploads (draw + update)
+    d2h = N * D * 8 + N * 4 + N * 2 + N * 8 + N * 2 + N * 8 + K * (1 + D + D * D) * 8
+
+    # ---------------- roofline of the dominant kernel (FP32 CUDA-core contraction)
+    stage_names = ["draw", "logq", "logpost", "weights", "em"]
+    per_stage = {nm: v / nt for nm, v in zip(stage_names, stage_ms)}
+    top = max(per_stage, key=per_stage.get)
+    tri = D * (D + 1) // 2
+    flops = {"logq": N * K * (2 * tri + 2 * D), "logpost": N * 16 * (2 * tri + 2 * D),
+             "em": N * K * (D * D + 3 * D)}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * (sm_mhz * 1e6) / 1e12
+    if top in flops:
+        achieved = flops[top] / (per_stage[top] / 1000.0) / 1e12
+        roof = {"bound": "fp32", "kernel": {"logq": "mixlogpdf_f32_kernel", "logpost": "mixlogpdf_f32_kernel",
+                                           "em": "em_stats_f32_kernel"}[top],
+                "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                "traffic": None, "stage_ms": per_stage,
+                "peak_note": "FP32 CUDA-core peak derived from 152 SMs x 128 lanes x 2 x median SM clock under load"}
+    else:
+        roof = {"bound": "hbm", "stage_ms": per_stage}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "global_batch": N * world, "nsamples_per_gpu": N, "D": 32, "K": 64,
+                   "nu": 3, "target_components": 16, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between steps (256 MB write); per-iteration arrays also exceed L2"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
+                 "speedup_mixed_vs_fp64": value / fp64_value},
+        "iteration_stats": {k: stats[k] for k in ("ln_evidence", "perplexity", "ess", "enc")},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "simulate_mix_mvdens + generic_get_importance_weight + normalize + update_prop_rb + "
+                        "perplexity_and_ess + evidence, pinned pmc_simu host arrays"},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        v, cores, reps = cpu_baseline(O, W, args.cpu_sample)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{reps} x {args.cpu_sample} samples of this workload "
+                                          f"(oracle/pmc_oracle.c, OpenMP)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,888 @@
+// pmcg_engine.cu — the PMC iteration engine behind the C ABI:
+//  * device-resident runs (pmcg_run_*), one stream each;
+//  * device posterior plugins (Gaussian mixture, SN Ia, dense template);
+//  * the pmclib-named drop-in entry points, which keep a device mirror of
+//    each pmc_simu they see (exec/cosmo_pmc.c:293-402 is the caller).
+// Every per-sample computation runs in the CUDA kernels of k_*.cu; the host
+// code here only moves data, sequences launches and reports errors.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/pmcg.h"
+#include "pmcg_internal.h"
+#include "pmcg_kernels.h"
+
+using pmcg::set_error;
+
+namespace pmcg {
+
+static bool ck(cudaError_t e, error **err, int line, const char *what) {
+  if (e == cudaSuccess) return true;
+  set_error(err, PMCG_ECUDA, line, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+#define CK(expr, what) ck((expr), err, __LINE__, (what))
+
+// Carves one device allocation into 256-byte aligned arrays. First pass
+// (base == nullptr) only measures.
+struct Carver {
+  char *base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  T *take(size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+enum PluginType { kPluginMix = 1, kPluginSn = 2, kPluginTpl = 3 };
+struct Plugin {
+  int type = 0;
+  DevMix mix;
+  SnDev sn;
+  TplDev tpl;
+};
+
+}  // namespace pmcg
+
+struct pmcg_posterior {
+  int npar = 0;
+  double logpr = 0.0;
+  std::vector<double> min, max;
+  std::vector<pmcg::Plugin> plugins;
+};
+
+namespace pmcg {
+
+// Buffers and scratch for one sample of N points (one run or one drop-in mirror).
+struct Work {
+  int K = 0, D = 0, df = -1, prec = 0, ldx = 0, S = 0;
+  size_t N = 0;
+  cudaStream_t s = nullptr;
+  DevMix prop;
+  double *bmin = nullptr, *bmax = nullptr;
+  double *X64 = nullptr;
+  float *X32 = nullptr;
+  int *idx = nullptr, *counts = nullptr;
+  short *flg = nullptr;
+  double *logq = nullptr, *logpost = nullptr, *logw = nullptr, *wbar = nullptr;
+  double *lt64 = nullptr, *Q64 = nullptr;
+  float *lt32 = nullptr, *Q32 = nullptr;
+  WRed *wpart = nullptr;
+  double *empart = nullptr;
+  DevStats *dstats = nullptr, *hstats = nullptr;
+  void *arena = nullptr;
+  int launches = 0;
+};
+
+static void work_free(Work &w) {
+  devmix_free(w.prop);
+  if (w.arena) cudaFree(w.arena);
+  if (w.hstats) cudaFreeHost(w.hstats);
+  if (w.s) cudaStreamDestroy(w.s);
+  w = Work();
+}
+
+static bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) {
+  if (D < 1 || D > kMaxD || K < 1 || K > kMaxK) {
+    set_error(err, PMCG_EDIM, __LINE__, "unsupported shape K=%d D=%d (K<=%d, D<=%d)", K, D, kMaxK, kMaxD);
+    return false;
+  }
+  w.K = K; w.D = D; w.df = df; w.prec = prec; w.N = N; w.ldx = round4(D);
+  size_t empart_bytes = em_partials_size(prec, K, D, &w.S, N);
+  const bool t = df > 0;
+  Carver c;
+  for (int pass = 0; pass < 2; pass++) {
+    c.off = 0;
+    w.bmin = c.take<double>(D);
+    w.bmax = c.take<double>(D);
+    w.X64 = c.take<double>(N * D);
+    w.X32 = prec ? c.take<float>(N * w.ldx) : nullptr;
+    w.idx = c.take<int>(N);
+    w.counts = c.take<int>(K);
+    w.flg = c.take<short>(N);
+    w.logq = c.take<double>(N);
+    w.logpost = c.take<double>(N);
+    w.logw = c.take<double>(N);
+    w.wbar = c.take<double>(N);
+    w.lt64 = prec ? nullptr : c.take<double>(N * K);
+    w.Q64 = (!prec && t) ? c.take<double>(N * K) : nullptr;
+    w.lt32 = prec ? c.take<float>(N * K) : nullptr;
+    w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
+    w.wpart = c.take<WRed>(kWeightBlocks);
+    w.empart = c.take<double>(empart_bytes / sizeof(double));
+    w.dstats = c.take<DevStats>(1);
+    if (pass == 0) {
+      if (!CK(cudaMalloc(&w.arena, c.off + 256), "device buffers")) return false;
+      c.base = (char *)w.arena;
+    }
+  }
+  if (!CK(cudaMallocHost(&w.hstats, sizeof(DevStats)), "pinned stats")) return false;
+  if (!CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking), "stream")) return false;
+  if (!CK(devmix_alloc(w.prop, K, D, df), "proposal buffers")) return false;
+  return true;
+}
+
+static bool upload_box(Work &w, const double *bmin, const double *bmax, error **err) {
+  if (!bmin) return true;
+  return CK(cudaMemcpyAsync(w.bmin, bmin, sizeof(double) * w.D, cudaMemcpyHostToDevice, w.s), "box") &&
+         CK(cudaMemcpyAsync(w.bmax, bmax, sizeof(double) * w.D, cudaMemcpyHostToDevice, w.s), "box");
+}
+
+static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **err) {
+  if (!CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts")) return false;
+  w.launches += 1;
+  return CK(launch_draw(w.prec, w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
+                        nullptr, nullptr, nullptr, w.X64, w.X32, w.idx, w.flg, w.counts, w.s),
+            "draw kernel");
+}
+
+static bool stage_logq(Work &w, error **err) {
+  w.launches += 1;
+  return CK(launch_mixlogpdf(w.prec, w.prop.view(), w.N, w.X64, w.X32, w.logq, 0, 0.0, w.lt64, w.Q64, w.lt32,
+                             w.Q32, w.s),
+            "mixture log-pdf kernel");
+}
+
+static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
+  if (p->npar != w.D) {
+    set_error(err, PMCG_EDIM, __LINE__, "posterior has %d parameters, sample %d", p->npar, w.D);
+    return false;
+  }
+  w.launches += 1;
+  if (!CK(launch_fill_f64(w.logpost, w.N, p->logpr, w.s), "fill")) return false;
+  for (const Plugin &pl : p->plugins) {
+    w.launches += 1;
+    if (pl.type == kPluginMix) {
+      if (!CK(launch_mixlogpdf(w.prec, pl.mix.view(), w.N, w.X64, w.X32, w.logpost, 1, 0.0, nullptr, nullptr,
+                               nullptr, nullptr, w.s),
+              "target mixture kernel"))
+        return false;
+    } else if (pl.type == kPluginSn) {
+      if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "SN kernel"))
+        return false;
+    } else if (pl.type == kPluginTpl) {
+      if (!CK(launch_tpl(w.prec, pl.tpl, w.N, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "template kernel"))
+        return false;
+    }
+  }
+  return true;
+}
+
+static bool stage_weights(Work &w, double beta, bool with_logq, error **err) {
+  w.launches += 2;
+  return CK(launch_weights(w.N, beta, w.logpost, with_logq ? w.logq : nullptr, w.flg, w.logw, w.wpart, w.dstats,
+                           w.s),
+            "weight kernels");
+}
+
+static bool stage_em(Work &w, error **err) {
+  w.launches += 5;
+  return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
+                      w.empart, w.S, w.dstats, w.D, w.s),
+            "EM kernels");
+}
+
+static bool fetch_stats(Work &w, error **err) {
+  if (!CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "stats") ||
+      !CK(cudaStreamSynchronize(w.s), "iteration"))
+    return false;
+  if (w.hstats->status != 0) {
+    set_error(err, w.hstats->status, __LINE__,
+              w.hstats->status == PMCG_ENOWEIGHT ? "every sample has zero weight" : "all component weights are zero");
+    return false;
+  }
+  return true;
+}
+
+static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error **err) {
+  std::vector<double> w, mu, L;
+  if (!flatten_mix(mix, w, mu, L, err)) return false;
+  return CK(devmix_upload(m, w.data(), mu.data(), L.data(), s), "mixture upload") &&
+         CK(cudaStreamSynchronize(s), "mixture upload");
+}
+
+}  // namespace pmcg
+
+using namespace pmcg;
+
+// ===================================================================== posterior
+extern "C" pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, const double *max, error **err) {
+  if (npar < 1 || npar > kMaxD) {
+    set_error(err, PMCG_EDIM, __LINE__, "npar %d", npar);
+    return nullptr;
+  }
+  pmcg_posterior *p = new pmcg_posterior();
+  p->npar = npar;
+  p->logpr = 0.0;
+  if (min && max) {
+    p->min.assign(min, min + npar);
+    p->max.assign(max, max + npar);
+    for (int j = 0; j < npar; j++) {
+      if (!(max[j] > min[j])) {
+        set_error(err, PMCG_EARG, __LINE__, "The minimum #%d (%g) is not smaller than the maximum (%g)", j, min[j],
+                  max[j]);
+        delete p;
+        return nullptr;
+      }
+      p->logpr -= std::log(max[j] - min[j]);
+    }
+  }
+  return p;
+}
+
+extern "C" void pmcg_posterior_free(pmcg_posterior **p) {
+  if (!p || !*p) return;
+  for (Plugin &pl : (*p)->plugins) {
+    devmix_free(pl.mix);
+    if (pl.sn.arena) cudaFree(pl.sn.arena);
+    if (pl.tpl.arena) cudaFree(pl.tpl.arena);
+  }
+  delete *p;
+  *p = nullptr;
+}
+
+extern "C" void pmcg_posterior_add_mixmvdens(pmcg_posterior *p, const mix_mvdens *target, error **err) {
+  if (!p || !target || target->ndim != p->npar) {
+    set_error(err, PMCG_EDIM, __LINE__, "target dimension does not match the posterior");
+    return;
+  }
+  Plugin pl;
+  pl.type = kPluginMix;
+  int df = target->comp[0]->df;
+  if (!CK(devmix_alloc(pl.mix, target->ncomp, target->ndim, df), "target buffers")) return;
+  if (!upload_mix(pl.mix, target, 0, err)) { devmix_free(pl.mix); return; }
+  p->plugins.push_back(pl);
+}
+
+extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *sd, error **err) {
+  if (!p || !sd || sd->nsn < 1 || sd->quad_nodes < 1 || sd->quad_nodes > 16 || !(sd->h > 0.0)) {
+    set_error(err, PMCG_EARG, __LINE__, "invalid SN data");
+    return;
+  }
+  const int n = sd->nsn, G = sd->quad_nodes;
+  std::vector<int> ix(n);
+  for (int i = 0; i < n; i++) ix[i] = i;
+  std::stable_sort(ix.begin(), ix.end(), [&](int a, int b) { return sd->z[a] < sd->z[b]; });
+  if (!(sd->z[ix[0]] > 0.0)) {
+    set_error(err, PMCG_EARG, __LINE__, "SN redshifts must be positive");
+    return;
+  }
+  // Gauss-Legendre nodes by Newton iteration on P_G.
+  std::vector<double> xg(G), wg(G);
+  for (int i = 0; i < G; i++) {
+    double t = std::cos(M_PI * (i + 0.75) / (G + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = t;
+      for (int k = 2; k <= G; k++) { double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k; p0 = p1; p1 = p2; }
+      if (G == 1) { p1 = t; p0 = 1.0; }
+      dp = G * (t * p1 - p0) / (t * t - 1.0);
+      double dt = p1 / dp;
+      t -= dt;
+      if (std::fabs(dt) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = t;
+    for (int k = 2; k <= G; k++) { double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k; p0 = p1; p1 = p2; }
+    if (G == 1) { p1 = t; p0 = 1.0; }
+    dp = G * (t * p1 - p0) / (t * t - 1.0);
+    xg[i] = t;
+    wg[i] = 2.0 / ((1.0 - t * t) * dp * dp);
+  }
+  const double ckms = 299792.458;
+  std::vector<double> z(n), spv2(n), mB(n), x1(n), c(n), cov6(6 * (size_t)n), za2(n), za3(n), zla(n);
+  std::vector<double> na2((size_t)n * G), na3((size_t)n * G), nla((size_t)n * G), nw((size_t)n * G);
+  double zprev = 0.0;
+  for (int t = 0; t < n; t++) {
+    int i = ix[t];
+    z[t] = sd->z[i]; mB[t] = sd->mB[i]; x1[t] = sd->x1[i]; c[t] = sd->c[i];
+    for (int q = 0; q < 6; q++) cov6[6 * (size_t)t + q] = sd->cov6[6 * (size_t)i + q];
+    double spv = (5.0 / std::log(10.0)) * sd->v_pec / (ckms * z[t]);
+    spv2[t] = spv * spv;
+    double a = 1.0 + z[t];
+    za2[t] = a * a; za3[t] = a * a * a; zla[t] = std::log(a);
+    double hw = 0.5 * (z[t] - zprev), cc = 0.5 * (z[t] + zprev);
+    for (int g = 0; g < G; g++) {
+      double ag = 1.0 + cc + hw * xg[g];
+      size_t q = (size_t)t * G + g;
+      na2[q] = ag * ag; na3[q] = ag * ag * ag; nla[q] = std::log(ag); nw[q] = hw * wg[g];
+    }
+    zprev = z[t];
+  }
+  Plugin pl;
+  pl.type = kPluginSn;
+  SnDev &s = pl.sn;
+  s.nsn = n; s.G = G; s.chi2mode = sd->chi2mode; s.add_logdet = sd->add_logdet;
+  s.ip_om = sd->ip_Omegam; s.ip_ode = sd->ip_Omegade; s.ip_w0 = sd->ip_w0; s.ip_M = sd->ip_M;
+  s.ip_alpha = sd->ip_alpha; s.ip_beta = sd->ip_beta;
+  s.def_om = sd->def_Omegam; s.def_w0 = sd->def_w0; s.def_M = sd->def_M; s.def_alpha = sd->def_alpha;
+  s.def_beta = sd->def_beta;
+  s.dh = ckms / (100.0 * sd->h);
+  s.sig_int2 = sd->sig_int * sd->sig_int;
+  Carver cv;
+  for (int pass = 0; pass < 2; pass++) {
+    cv.off = 0;
+    s.z = cv.take<double>(n); s.spv2 = cv.take<double>(n); s.mB = cv.take<double>(n); s.x1 = cv.take<double>(n);
+    s.c = cv.take<double>(n); s.cov6 = cv.take<double>(6 * (size_t)n);
+    s.za2 = cv.take<double>(n); s.za3 = cv.take<double>(n); s.zla = cv.take<double>(n);
+    s.na2 = cv.take<double>((size_t)n * G); s.na3 = cv.take<double>((size_t)n * G);
+    s.nla = cv.take<double>((size_t)n * G); s.nw = cv.take<double>((size_t)n * G);
+    s.fna2 = cv.take<float>((size_t)n * G); s.fna3 = cv.take<float>((size_t)n * G);
+    s.fnla = cv.take<float>((size_t)n * G); s.fnw = cv.take<float>((size_t)n * G);
+    if (pass == 0) {
+      if (!CK(cudaMalloc(&s.arena, cv.off + 256), "SN buffers")) return;
+      cv.base = (char *)s.arena;
+    }
+  }
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    return CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "SN upload");
+  };
+  auto tof = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+  std::vector<float> f2 = tof(na2), f3 = tof(na3), fl = tof(nla), fw = tof(nw);
+  bool ok = up(s.z, z.data(), 8 * n) && up(s.spv2, spv2.data(), 8 * n) && up(s.mB, mB.data(), 8 * n) &&
+            up(s.x1, x1.data(), 8 * n) && up(s.c, c.data(), 8 * n) && up(s.cov6, cov6.data(), 48 * (size_t)n) &&
+            up(s.za2, za2.data(), 8 * n) && up(s.za3, za3.data(), 8 * n) && up(s.zla, zla.data(), 8 * n) &&
+            up(s.na2, na2.data(), 8 * na2.size()) && up(s.na3, na3.data(), 8 * na3.size()) &&
+            up(s.nla, nla.data(), 8 * nla.size()) && up(s.nw, nw.data(), 8 * nw.size()) &&
+            up(s.fna2, f2.data(), 4 * f2.size()) && up(s.fna3, f3.data(), 4 * f3.size()) &&
+            up(s.fnla, fl.data(), 4 * fl.size()) && up(s.fnw, fw.data(), 4 * fw.size());
+  if (!ok) { cudaFree(s.arena); return; }
+  p->plugins.push_back(pl);
+}
+
+extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const double *A, const double *C,
+                                            const double *dobs, error **err) {
+  if (!p || ndata < 1 || !A || !C || !dobs) {
+    set_error(err, PMCG_EARG, __LINE__, "invalid template data");
+    return;
+  }
+  const int M = ndata, D = p->npar, P = 1 + D + D * (D + 1) / 2;
+  // C = L L^T (FP64), At = L^-1 A, dt = L^-1 dobs: set-up, once per posterior.
+  std::vector<double> L((size_t)M * M), At((size_t)M * P), dt(M);
+  if (host_cholesky(M, C, L.data(), nullptr) != 0) {
+    set_error(err, PMCG_ECHOL, __LINE__, "template data covariance is not positive definite");
+    return;
+  }
+  for (int i = 0; i < M; i++) {
+    const double *Li = &L[(size_t)i * M];
+    for (int q = 0; q < P; q++) {
+      double t = A[(size_t)i * P + q];
+      for (int j = 0; j < i; j++) t -= Li[j] * At[(size_t)j * P + q];
+      At[(size_t)i * P + q] = t / Li[i];
+    }
+    double t = dobs[i];
+    for (int j = 0; j < i; j++) t -= Li[j] * dt[j];
+    dt[i] = t / Li[i];
+  }
+  Plugin pl;
+  pl.type = kPluginTpl;
+  TplDev &t = pl.tpl;
+  t.M = M; t.P = P; t.Dpar = D;
+  Carver cv;
+  for (int pass = 0; pass < 2; pass++) {
+    cv.off = 0;
+    t.At = cv.take<double>((size_t)M * P); t.dt = cv.take<double>(M);
+    t.At32 = cv.take<float>((size_t)M * P); t.dt32 = cv.take<float>(M);
+    if (pass == 0) {
+      if (!CK(cudaMalloc(&t.arena, cv.off + 256), "template buffers")) return;
+      cv.base = (char *)t.arena;
+    }
+  }
+  std::vector<float> At32(At.begin(), At.end()), dt32(dt.begin(), dt.end());
+  bool ok = CK(cudaMemcpy(t.At, At.data(), 8 * At.size(), cudaMemcpyHostToDevice), "template upload") &&
+            CK(cudaMemcpy(t.dt, dt.data(), 8 * dt.size(), cudaMemcpyHostToDevice), "template upload") &&
+            CK(cudaMemcpy(t.At32, At32.data(), 4 * At32.size(), cudaMemcpyHostToDevice), "template upload") &&
+            CK(cudaMemcpy(t.dt32, dt32.data(), 4 * dt32.size(), cudaMemcpyHostToDevice), "template upload");
+  if (!ok) { cudaFree(t.arena); return; }
+  p->plugins.push_back(pl);
+}
+
+// Batched log-posterior over N points (one Work scratch per call).
+extern "C" void pmcg_posterior_log_pdf_batch(const pmcg_posterior *p, size_t N, const double *X, double *logpost,
+                                             short *flg, int on_device, int precision, void *stream, error **err) {
+  (void)stream;
+  if (!p || N == 0) return;
+  Work w;
+  if (!work_alloc(w, 1, p->npar, -1, precision ? 1 : 0, N, err)) { work_free(w); return; }
+  const int D = p->npar;
+  const cudaMemcpyKind in = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  bool ok = CK(cudaMemcpyAsync(w.X64, X, sizeof(double) * N * D, in, w.s), "X upload");
+  if (ok && precision) ok = CK(launch_x64_to_x32(N, D, w.ldx, w.X64, w.X32, w.s), "convert");
+  std::vector<short> ones(N, 1);
+  ok = ok && CK(cudaMemcpyAsync(w.flg, ones.data(), sizeof(short) * N, cudaMemcpyHostToDevice, w.s), "flg");
+  ok = ok && stage_logpost(w, p, err);
+  ok = ok && CK(cudaMemcpyAsync(logpost, w.logpost, sizeof(double) * N, out, w.s), "logpost");
+  if (ok && flg) ok = CK(cudaMemcpyAsync(flg, w.flg, sizeof(short) * N, out, w.s), "flg");
+  ok = ok && CK(cudaStreamSynchronize(w.s), "posterior");
+  work_free(w);
+}
+
+extern "C" double pmcg_posterior_log_pdf_void(void *post, const double *x, error **err) {
+  double lp = 0.0;
+  short f = 1;
+  pmcg_posterior_log_pdf_batch((const pmcg_posterior *)post, 1, x, &lp, &f, 0, PMCG_FP64, nullptr, err);
+  if (!f) set_error(err, PMCG_EARG, __LINE__, "likelihood error at this point");
+  return lp;
+}
+
+extern "C" void pmcg_mix_log_pdf_batch(const mix_mvdens *m, size_t N, const double *X, double *logq, double *lt,
+                                       int precision, error **err) {
+  if (!m || N == 0) return;
+  Work w;
+  if (!work_alloc(w, m->ncomp, m->ndim, m->comp[0]->df, precision ? 1 : 0, N, err)) { work_free(w); return; }
+  const int D = m->ndim;
+  bool ok = upload_mix(w.prop, m, w.s, err);
+  ok = ok && CK(cudaMemcpyAsync(w.X64, X, sizeof(double) * N * D, cudaMemcpyHostToDevice, w.s), "X upload");
+  if (ok && precision) ok = CK(launch_x64_to_x32(N, D, w.ldx, w.X64, w.X32, w.s), "convert");
+  ok = ok && stage_logq(w, err);
+  ok = ok && CK(cudaMemcpyAsync(logq, w.logq, sizeof(double) * N, cudaMemcpyDeviceToHost, w.s), "logq");
+  if (ok && lt) {
+    if (precision) {
+      std::vector<float> t((size_t)m->ncomp * N);
+      ok = CK(cudaMemcpyAsync(t.data(), w.lt32, 4 * t.size(), cudaMemcpyDeviceToHost, w.s), "lt") &&
+           CK(cudaStreamSynchronize(w.s), "lt");
+      for (size_t i = 0; ok && i < t.size(); i++) lt[i] = t[i];
+    } else {
+      ok = CK(cudaMemcpyAsync(lt, w.lt64, 8 * (size_t)m->ncomp * N, cudaMemcpyDeviceToHost, w.s), "lt");
+    }
+  }
+  ok = ok && CK(cudaStreamSynchronize(w.s), "mixture log-pdf");
+  work_free(w);
+}
+
+extern "C" double mix_mvdens_log_pdf(mix_mvdens *m, const double *x, error **err) {
+  double r = 0.0;
+  pmcg_mix_log_pdf_batch(m, 1, x, &r, nullptr, PMCG_FP64, err);
+  return r;
+}
+extern "C" double mix_mvdens_log_pdf_void(void *m, const double *x, error **err) {
+  return mix_mvdens_log_pdf((mix_mvdens *)m, x, err);
+}
+extern "C" double mvdens_log_pdf(mvdens *g, const double *x, error **err) {
+  mix_mvdens mm;
+  double one = 1.0;
+  mvdens *cp[1] = {g};
+  mm.ncomp = 1; mm.ndim = g->ndim; mm.wght = &one; mm.comp = cp;
+  return mix_mvdens_log_pdf(&mm, x, err);
+}
+extern "C" double mvdens_log_pdf_void(void *g, const double *x, error **err) {
+  return mvdens_log_pdf((mvdens *)g, x, err);
+}
+
+// ===================================================================== runs
+struct pmcg_run {
+  Work w;
+  const pmcg_posterior *post = nullptr;
+  bool box = false;
+  uint64_t seed = 0;
+  uint32_t calls = 0;
+  bool timing = false;
+  cudaEvent_t ev[PMCG_NSTAGE + 1] = {};
+  double stage_ms[PMCG_NSTAGE] = {};
+  int timed = 0;
+  int last_launches = 0;
+};
+
+extern "C" pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_posterior *post, const parabox *pb,
+                                     size_t nsamples, int precision, uint64_t seed, error **err) {
+  if (!proposal || !post || nsamples == 0) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_create: null argument or zero samples");
+    return nullptr;
+  }
+  if (post->npar != proposal->ndim || (pb && pb->ndim != proposal->ndim)) {
+    set_error(err, PMCG_EDIM, __LINE__, "dimensions of proposal/posterior/box differ");
+    return nullptr;
+  }
+  pmcg_run *r = new pmcg_run();
+  if (!work_alloc(r->w, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, precision ? 1 : 0, nsamples,
+                  err) ||
+      !upload_mix(r->w.prop, proposal, r->w.s, err)) {
+    work_free(r->w);
+    delete r;
+    return nullptr;
+  }
+  r->post = post;
+  r->seed = seed;
+  if (pb) {
+    r->box = true;
+    if (!upload_box(r->w, pb->min, pb->max, err)) { work_free(r->w); delete r; return nullptr; }
+  }
+  for (int i = 0; i <= PMCG_NSTAGE; i++) cudaEventCreate(&r->ev[i]);
+  return r;
+}
+
+extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err) {
+  Work &w = r->w;
+  w.launches = 0;
+  auto mark = [&](int i) { if (r->timing) cudaEventRecord(r->ev[i], w.s); };
+  mark(0);
+  bool ok = stage_draw(w, r->box, r->seed, r->calls, err);
+  mark(1);
+  ok = ok && stage_logq(w, err);
+  mark(2);
+  ok = ok && stage_logpost(w, r->post, err);
+  mark(3);
+  ok = ok && stage_weights(w, beta, true, err);
+  mark(4);
+  ok = ok && stage_em(w, err);
+  mark(5);
+  r->calls++;
+  r->last_launches = w.launches;
+  if (!ok) return;
+  if (!fetch_stats(w, err)) return;
+  if (r->timing) {
+    for (int i = 0; i < PMCG_NSTAGE; i++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r->ev[i], r->ev[i + 1]);
+      r->stage_ms[i] += ms;
+    }
+    r->timed++;
+  }
+  if (stats) {
+    const DevStats &h = *w.hstats;
+    stats->ln_evidence = h.ln_evidence;
+    stats->perplexity = h.perplexity;
+    stats->ess = h.ess;
+    stats->enc = h.enc;
+    stats->logSum = h.logSum;
+    stats->maxW = h.maxW;
+    stats->nok = (size_t)h.nok;
+    stats->ndead = h.ndead;
+  }
+}
+
+extern "C" void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err) {
+  Work &w = r->w;
+  if (out->ncomp != w.K || out->ndim != w.D) {
+    set_error(err, PMCG_EDIM, __LINE__, "output proposal shape differs");
+    return;
+  }
+  const int K = w.K, D = w.D;
+  std::vector<double> wt(K), mu((size_t)K * D), L((size_t)K * D * D);
+  bool ok = CK(cudaMemcpyAsync(wt.data(), w.prop.w, 8 * K, cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(mu.data(), w.prop.mu, 8 * mu.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(L.data(), w.prop.L, 8 * L.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaStreamSynchronize(w.s), "proposal");
+  if (!ok) return;
+  for (int k = 0; k < K; k++) {
+    out->wght[k] = wt[k];
+    mvdens *c = out->comp[k];
+    c->df = w.df;
+    memcpy(c->mean, &mu[(size_t)k * D], 8 * D);
+    memcpy(c->std, &L[(size_t)k * D * D], 8 * (size_t)D * D);
+    c->chol = 1;
+    double ld = 0.0;
+    for (int i = 0; i < D; i++) ld += std::log(c->std[i * D + i]);
+    c->det = 2.0 * ld;
+  }
+}
+
+extern "C" void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, error **err) {
+  Work &w = r->w;
+  if (!proposal || proposal->ncomp != w.K || proposal->ndim != w.D || proposal->comp[0]->df != w.df) {
+    set_error(err, PMCG_EDIM, __LINE__, "proposal shape differs from the run's");
+    return;
+  }
+  upload_mix(w.prop, proposal, w.s, err);
+}
+
+extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {
+  Work &w = r->w;
+  if (psim->ndim != w.D) { set_error(err, PMCG_EDIM, __LINE__, "sample dimension differs"); return; }
+  pmc_simu_realloc(psim, w.N, err);
+  if (isError(err ? *err : nullptr)) return;
+  bool ok = true;
+  if (w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
+  ok = ok && CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, w.s), "X") &&
+       CK(cudaMemcpyAsync(psim->weights, w.logw, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
+       CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
+       CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, w.s), "indices") &&
+       CK(cudaStreamSynchronize(w.s), "sample");
+  if (!ok) return;
+  psim->isLog = 1;
+  psim->logSum = w.hstats->logSum;
+  psim->maxW = w.hstats->maxW;
+  psim->nok = (size_t)w.hstats->nok;
+}
+
+extern "C" void pmcg_run_free(pmcg_run **r) {
+  if (!r || !*r) return;
+  for (int i = 0; i <= PMCG_NSTAGE; i++)
+    if ((*r)->ev[i]) cudaEventDestroy((*r)->ev[i]);
+  work_free((*r)->w);
+  delete *r;
+  *r = nullptr;
+}
+
+extern "C" void pmcg_run_set_timing(pmcg_run *r, int on) {
+  r->timing = on != 0;
+  for (int i = 0; i < PMCG_NSTAGE; i++) r->stage_ms[i] = 0.0;
+  r->timed = 0;
+}
+
+extern "C" int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage) {
+  for (int i = 0; i < nstage && i < PMCG_NSTAGE; i++) ms[i] = r->stage_ms[i];
+  return r->timed;
+}
+
+extern "C" int pmcg_run_last_launches(const pmcg_run *r) { return r->last_launches; }
+
+extern "C" int pmcg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+extern "C" void pmcg_device_synchronize(error **err) { CK(cudaDeviceSynchronize(), "device synchronize"); }
+
+// ===================================================================== drop-in
+namespace pmcg {
+
+static int g_dropin_precision = PMCG_FP64;
+
+struct SimMirror {
+  Work w;
+  bool x_valid = false;    // device X/flg/indices/counts match the host sample
+  bool lt_valid = false;   // logq/lt/Q valid for (X, snapshot proposal)
+  bool w_valid = false;    // logw and the device statistics valid
+  std::vector<double> snap_w, snap_mu, snap_L;
+};
+
+static std::mutex g_mu;
+static std::unordered_map<const pmc_simu *, SimMirror *> g_sims;
+
+static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error **err) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  SimMirror *&m = g_sims[psim];
+  const int prec = g_dropin_precision;
+  if (m && (m->w.K != K || m->w.D != D || m->w.df != df || m->w.N != psim->nsamples || m->w.prec != prec)) {
+    work_free(m->w);
+    delete m;
+    m = nullptr;
+  }
+  if (!m) {
+    m = new SimMirror();
+    if (!work_alloc(m->w, K, D, df, prec, psim->nsamples, err)) {
+      work_free(m->w);
+      delete m;
+      m = nullptr;
+      g_sims.erase(psim);
+      return nullptr;
+    }
+  }
+  return m;
+}
+
+static SimMirror *find_mirror(const pmc_simu *psim) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_sims.find(psim);
+  return it == g_sims.end() ? nullptr : it->second;
+}
+
+// Mirror for the weight-only entry points: any existing mirror of this
+// sample size is reused; otherwise a one-component mirror is made.
+static SimMirror *mirror_any(const pmc_simu *psim, error **err) {
+  SimMirror *m = find_mirror(psim);
+  if (m && m->w.N == psim->nsamples) return m;
+  return mirror_for(psim, 1, psim->ndim, -1, err);
+}
+
+void forget_simu(const pmc_simu *p) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_sims.find(p);
+  if (it == g_sims.end()) return;
+  work_free(it->second->w);
+  delete it->second;
+  g_sims.erase(it);
+}
+
+void forget_mix(const mix_mvdens *) {}
+
+// Upload the proposal when it differs from the mirror's snapshot.
+static bool sync_proposal(SimMirror *m, const mix_mvdens *prop, error **err) {
+  std::vector<double> w, mu, L;
+  if (!flatten_mix(prop, w, mu, L, err)) return false;
+  if (w == m->snap_w && mu == m->snap_mu && L == m->snap_L) return true;
+  if (!CK(devmix_upload(m->w.prop, w.data(), mu.data(), L.data(), m->w.s), "proposal upload")) return false;
+  m->snap_w.swap(w);
+  m->snap_mu.swap(mu);
+  m->snap_L.swap(L);
+  m->lt_valid = false;
+  return true;
+}
+
+// Make the device sample match the host one (after a host-side rewrite).
+static bool sync_sample(SimMirror *m, const pmc_simu *psim, error **err) {
+  if (m->x_valid) return true;
+  Work &w = m->w;
+  bool ok = CK(cudaMemcpyAsync(w.X64, psim->X, 8 * w.N * w.D, cudaMemcpyHostToDevice, w.s), "X upload") &&
+            CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload") &&
+            CK(cudaMemcpyAsync(w.idx, psim->indices, 4 * w.N, cudaMemcpyHostToDevice, w.s), "indices upload") &&
+            CK(launch_counts(w.N, w.K, w.idx, w.counts, w.s), "counts");
+  if (ok && w.prec) ok = CK(launch_x64_to_x32(w.N, w.D, w.ldx, w.X64, w.X32, w.s), "convert");
+  if (!ok) return false;
+  m->x_valid = true;
+  m->lt_valid = false;
+  m->w_valid = false;
+  return true;
+}
+
+// Make the device log-weights and statistics match the host weights.
+static bool sync_weights(SimMirror *m, const pmc_simu *psim, error **err) {
+  if (m->w_valid) return true;
+  Work &w = m->w;
+  bool ok = CK(cudaMemcpyAsync(w.logpost, psim->weights, 8 * w.N, cudaMemcpyHostToDevice, w.s), "weights upload");
+  if (ok && !psim->isLog) ok = CK(launch_log_weights(w.N, w.logpost, w.flg, w.s), "log weights");
+  ok = ok && stage_weights(w, 1.0, false, err) && fetch_stats(w, err);
+  if (ok) m->w_valid = true;
+  return ok;
+}
+
+}  // namespace pmcg
+
+extern "C" void pmcg_set_dropin_precision(int precision) { g_dropin_precision = precision ? PMCG_MIXED : PMCG_FP64; }
+
+extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {
+  SimMirror *m = find_mirror(psim);
+  if (m) m->x_valid = m->lt_valid = m->w_valid = false;
+}
+
+extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg_rng *rng, parabox *pb,
+                                      error **err) {
+  if (!psim || !proposal || !rng || proposal->ndim != psim->ndim || (pb && pb->ndim != psim->ndim)) {
+    set_error(err, PMCG_EARG, __LINE__, "simulate_mix_mvdens: invalid arguments");
+    return 0;
+  }
+  SimMirror *m = mirror_for(psim, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, err);
+  if (!m) return 0;
+  Work &w = m->w;
+  if (!sync_proposal(m, proposal, err)) return 0;
+  if (pb && !upload_box(w, pb->min, pb->max, err)) return 0;
+  bool ok = stage_draw(w, pb != nullptr, rng->seed, rng->calls, err);
+  if (ok && w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
+  ok = ok && CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, w.s), "X") &&
+       CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, w.s), "indices") &&
+       CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
+       CK(cudaStreamSynchronize(w.s), "draw");
+  rng->calls++;
+  if (!ok) return 0;
+  m->x_valid = true;
+  m->lt_valid = false;
+  m->w_valid = false;
+  size_t nok = 0;
+  for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
+  psim->isLog = 1;
+  return nok;
+}
+
+extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim, mix_mvdens *proposal,
+                                                                 logpdf_fn *q, logpdf_fn *post,
+                                                                 retrieve_ded_fn *ded, void *extra, double beta,
+                                                                 int quiet, error **err) {
+  (void)ded;
+  (void)quiet;
+  if (q != mix_mvdens_log_pdf_void || post != pmcg_posterior_log_pdf_void || !extra) {
+    set_error(err, PMCG_EUNSUPPORTED, __LINE__,
+              "the device weight step needs q = mix_mvdens_log_pdf_void and post = pmcg_posterior_log_pdf_void "
+              "with extra = pmcg_posterior*");
+    return 0;
+  }
+  const pmcg_posterior *p = (const pmcg_posterior *)extra;
+  SimMirror *m = mirror_for(psim, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, err);
+  if (!m) return 0;
+  Work &w = m->w;
+  if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err)) return 0;
+  bool ok = stage_logq(w, err) && stage_logpost(w, p, err) && stage_weights(w, beta, true, err);
+  ok = ok && CK(cudaMemcpyAsync(psim->weights, w.logw, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
+       CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg");
+  if (!ok) return 0;
+  if (!fetch_stats(w, err)) return 0;
+  m->lt_valid = true;
+  m->w_valid = true;
+  psim->isLog = 1;
+  psim->logSum = w.hstats->logSum;
+  psim->maxW = w.hstats->maxW;
+  psim->nok = (size_t)w.hstats->nok;
+  return psim->nok;
+}
+
+extern "C" double normalize_importance_weight(pmc_simu *psim, error **err) {
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return 0.0;
+  Work &w = m->w;
+  if (!m->x_valid) {
+    if (!CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload")) return 0.0;
+  }
+  if (!sync_weights(m, psim, err)) return 0.0;
+  bool ok = CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise") &&
+            CK(cudaMemcpyAsync(psim->weights, w.wbar, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
+            CK(cudaStreamSynchronize(w.s), "normalise");
+  if (!ok) return 0.0;
+  psim->isLog = 0;
+  psim->logSum = w.hstats->logSum;
+  psim->maxW = w.hstats->maxW;
+  return psim->logSum;
+}
+
+extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err) {
+  SimMirror *m = mirror_for(psim, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, err);
+  if (!m) return;
+  Work &w = m->w;
+  if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err) || !sync_weights(m, psim, err)) return;
+  if (!m->lt_valid && !stage_logq(w, err)) return;
+  m->lt_valid = true;
+  if (!stage_em(w, err) || !fetch_stats(w, err)) return;
+  const int K = w.K, D = w.D;
+  std::vector<double> wt(K), mu((size_t)K * D), L((size_t)K * D * D);
+  bool ok = CK(cudaMemcpyAsync(wt.data(), w.prop.w, 8 * K, cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(mu.data(), w.prop.mu, 8 * mu.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(L.data(), w.prop.L, 8 * L.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaStreamSynchronize(w.s), "update");
+  if (!ok) return;
+  for (int k = 0; k < K; k++) {
+    proposal->wght[k] = wt[k];
+    mvdens *c = proposal->comp[k];
+    if (wt[k] > 0.0) {
+      memcpy(c->mean, &mu[(size_t)k * D], 8 * D);
+      memcpy(c->std, &L[(size_t)k * D * D], 8 * (size_t)D * D);
+      c->chol = 1;
+      double ld = 0.0;
+      for (int i = 0; i < D; i++) ld += std::log(c->std[i * D + i]);
+      c->det = 2.0 * ld;
+    }
+  }
+  // The device proposal now equals the host one.
+  flatten_mix(proposal, m->snap_w, m->snap_mu, m->snap_L, err);
+  m->lt_valid = false;
+}
+
+extern "C" double perplexity_and_ess(pmc_simu *psim, int mode, double *ess, error **err) {
+  (void)mode;
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return 0.0;
+  if (!m->x_valid &&
+      !CK(cudaMemcpyAsync(m->w.flg, psim->flg, 2 * m->w.N, cudaMemcpyHostToDevice, m->w.s), "flg upload"))
+    return 0.0;
+  if (!sync_weights(m, psim, err)) return 0.0;
+  if (ess) *ess = m->w.hstats->ess;
+  return m->w.hstats->perplexity;
+}
+
+extern "C" double evidence(pmc_simu *psim, double *ln_evi, error **err) {
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return 0.0;
+  if (!m->x_valid &&
+      !CK(cudaMemcpyAsync(m->w.flg, psim->flg, 2 * m->w.N, cudaMemcpyHostToDevice, m->w.s), "flg upload"))
+    return 0.0;
+  if (!sync_weights(m, psim, err)) return 0.0;
+  if (ln_evi) *ln_evi = m->w.hstats->ln_evidence;
+  return std::exp(m->w.hstats->ln_evidence);
+}

@@ -1,0 +1,426 @@
+// pmcg_host.cpp — host-side part of the pmclib-compatible C ABI: the error
+// chain, density/sample containers, the prior box, the random stream handle,
+// the tempering schedule and the mix_mvdens text format. None of these
+// touches a per-sample computation; the hot path is in pmcg_engine.cu.
+#include "../../include/pmcg.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pmcg_internal.h"
+
+// ------------------------------------------------------------------ errors
+extern "C" error *addError(int code, const char *text, error *next, int line) {
+  error *e = (error *)calloc(1, sizeof(error));
+  if (!e) return next;
+  e->errValue = code;
+  e->line = line;
+  snprintf(e->errText, sizeof(e->errText), "%s", text ? text : "");
+  snprintf(e->errWhere, sizeof(e->errWhere), "libpmcg");
+  e->next = next;
+  return e;
+}
+
+extern "C" int isError(const error *err) { return err != nullptr && err->errValue != 0; }
+extern "C" int getErrorValue(const error *err) { return err ? err->errValue : 0; }
+
+extern "C" void purgeError(error **err) {
+  if (!err) return;
+  error *e = *err;
+  while (e) {
+    error *n = e->next;
+    free(e);
+    e = n;
+  }
+  *err = nullptr;
+}
+
+extern "C" void printError(FILE *f, const error *err) {
+  for (const error *e = err; e; e = e->next)
+    fprintf(f, "Error %d (%s:%d): %s\n", e->errValue, e->errWhere, e->line, e->errText);
+}
+
+namespace pmcg {
+void set_error(error **err, int code, int line, const char *fmt, ...) {
+  if (!err) return;
+  char buf[384];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  *err = addError(code, buf, *err, line);
+}
+
+int host_cholesky(int D, const double *C, double *L, double *logdetL) {
+  double ld = 0.0;
+  for (int i = 0; i < D * D; i++) L[i] = 0.0;
+  for (int j = 0; j < D; j++) {
+    double s = C[j * D + j];
+    for (int k = 0; k < j; k++) s -= L[j * D + k] * L[j * D + k];
+    if (!(s > 0.0) || !std::isfinite(s)) return -1;
+    double d = std::sqrt(s);
+    L[j * D + j] = d;
+    ld += std::log(d);
+    for (int i = j + 1; i < D; i++) {
+      double t = C[i * D + j];
+      for (int k = 0; k < j; k++) t -= L[i * D + k] * L[j * D + k];
+      L[i * D + j] = t / d;
+    }
+  }
+  if (logdetL) *logdetL = ld;
+  return 0;
+}
+
+// Flatten a host mixture into (w, mu, L) with Cholesky factors.
+bool flatten_mix(const mix_mvdens *m, std::vector<double> &w, std::vector<double> &mu, std::vector<double> &L,
+                 error **err) {
+  const int K = m->ncomp, D = m->ndim;
+  w.assign(m->wght, m->wght + K);
+  mu.resize((size_t)K * D);
+  L.resize((size_t)K * D * D);
+  for (int k = 0; k < K; k++) {
+    const mvdens *c = m->comp[k];
+    if (c->ndim != D) {
+      set_error(err, PMCG_EDIM, __LINE__, "component %d has dimension %d, mixture %d", k, c->ndim, D);
+      return false;
+    }
+    memcpy(&mu[(size_t)k * D], c->mean, sizeof(double) * D);
+    if (c->chol) {
+      for (int i = 0; i < D; i++)
+        for (int j = 0; j < D; j++) L[(size_t)k * D * D + i * D + j] = (j <= i) ? c->std[i * D + j] : 0.0;
+    } else if (host_cholesky(D, c->std, &L[(size_t)k * D * D], nullptr) != 0) {
+      set_error(err, PMCG_ECHOL, __LINE__, "covariance of component %d is not positive definite", k);
+      return false;
+    }
+  }
+  return true;
+}
+}  // namespace pmcg
+
+using pmcg::set_error;
+
+// ------------------------------------------------------------------ densities
+extern "C" mvdens *mvdens_alloc(int ndim, error **err) {
+  if (ndim < 1) { set_error(err, PMCG_EARG, __LINE__, "ndim %d", ndim); return nullptr; }
+  mvdens *m = (mvdens *)calloc(1, sizeof(mvdens));
+  if (!m) { set_error(err, PMCG_EALLOC, __LINE__, "mvdens"); return nullptr; }
+  m->ndim = ndim;
+  m->df = -1;
+  m->band_limit = ndim;
+  m->mean = (double *)calloc((size_t)ndim, sizeof(double));
+  m->std = (double *)calloc((size_t)ndim * ndim, sizeof(double));
+  if (!m->mean || !m->std) {
+    free(m->mean); free(m->std); free(m);
+    set_error(err, PMCG_EALLOC, __LINE__, "mvdens arrays");
+    return nullptr;
+  }
+  for (int i = 0; i < ndim; i++) m->std[i * ndim + i] = 1.0;
+  return m;
+}
+
+extern "C" void mvdens_free(mvdens **m) {
+  if (!m || !*m) return;
+  free((*m)->mean);
+  free((*m)->std);
+  free(*m);
+  *m = nullptr;
+}
+
+extern "C" mix_mvdens *mix_mvdens_alloc(int ncomp, int ndim, error **err) {
+  if (ncomp < 1) { set_error(err, PMCG_EARG, __LINE__, "ncomp %d", ncomp); return nullptr; }
+  mix_mvdens *m = (mix_mvdens *)calloc(1, sizeof(mix_mvdens));
+  if (!m) { set_error(err, PMCG_EALLOC, __LINE__, "mix_mvdens"); return nullptr; }
+  m->ncomp = ncomp;
+  m->ndim = ndim;
+  m->wght = (double *)calloc((size_t)ncomp, sizeof(double));
+  m->comp = (mvdens **)calloc((size_t)ncomp, sizeof(mvdens *));
+  if (!m->wght || !m->comp) {
+    free(m->wght); free(m->comp); free(m);
+    set_error(err, PMCG_EALLOC, __LINE__, "mix_mvdens arrays");
+    return nullptr;
+  }
+  for (int k = 0; k < ncomp; k++) {
+    m->wght[k] = 1.0 / ncomp;
+    m->comp[k] = mvdens_alloc(ndim, err);
+    if (!m->comp[k]) { mix_mvdens_free(&m); return nullptr; }
+  }
+  return m;
+}
+
+extern "C" void mix_mvdens_free(mix_mvdens **m) {
+  if (!m || !*m) return;
+  pmcg::forget_mix(*m);
+  if ((*m)->comp)
+    for (int k = 0; k < (*m)->ncomp; k++) mvdens_free(&(*m)->comp[k]);
+  free((*m)->comp);
+  free((*m)->wght);
+  free(*m);
+  *m = nullptr;
+}
+
+extern "C" void mix_mvdens_copy(mix_mvdens *dst, const mix_mvdens *src, error **err) {
+  if (!dst || !src || dst->ncomp != src->ncomp || dst->ndim != src->ndim) {
+    set_error(err, PMCG_EDIM, __LINE__, "mix_mvdens_copy: shape mismatch");
+    return;
+  }
+  const int D = src->ndim;
+  memcpy(dst->wght, src->wght, sizeof(double) * src->ncomp);
+  for (int k = 0; k < src->ncomp; k++) {
+    mvdens *a = dst->comp[k];
+    const mvdens *b = src->comp[k];
+    a->df = b->df; a->band_limit = b->band_limit; a->chol = b->chol; a->det = b->det;
+    memcpy(a->mean, b->mean, sizeof(double) * D);
+    memcpy(a->std, b->std, sizeof(double) * D * D);
+  }
+}
+
+extern "C" void mvdens_cholesky_decomp(mvdens *m, error **err) {
+  if (!m || m->chol) return;
+  const int D = m->ndim;
+  std::vector<double> L((size_t)D * D);
+  double ld;
+  if (pmcg::host_cholesky(D, m->std, L.data(), &ld) != 0) {
+    set_error(err, PMCG_ECHOL, __LINE__, "covariance is not positive definite");
+    return;
+  }
+  memcpy(m->std, L.data(), sizeof(double) * D * D);
+  m->chol = 1;
+  m->det = 2.0 * ld;
+}
+
+extern "C" void mix_mvdens_cholesky_decomp(mix_mvdens *m, error **err) {
+  for (int k = 0; k < m->ncomp; k++) {
+    mvdens_cholesky_decomp(m->comp[k], err);
+    if (isError(err ? *err : nullptr)) return;
+  }
+}
+
+extern "C" void mvdens_from_meanvar(mvdens *m, const double *mean, const double *cov, double correct) {
+  const int D = m->ndim;
+  if (mean) memcpy(m->mean, mean, sizeof(double) * D);
+  if (cov) {
+    for (int i = 0; i < D * D; i++) m->std[i] = cov[i] * correct;
+    m->chol = 0;
+  }
+}
+
+extern "C" double effective_number_of_components(const mix_mvdens *m, error **err) {
+  double s = 0.0;
+  for (int k = 0; k < m->ncomp; k++) s += m->wght[k] * m->wght[k];
+  if (!(s > 0.0)) {
+    set_error(err, PMCG_ENEGWEIGHT, __LINE__, "all component weights are zero");
+    return 0.0;
+  }
+  return 1.0 / s;
+}
+
+// Text format of Manual/manual.tex:3199-3260 (covariance written, chol flag 0).
+static void dump_mvdens(FILE *f, const mvdens *c) {
+  const int D = c->ndim;
+  fprintf(f, "%d %d %d %d\n", D, c->df, c->band_limit, 0);
+  for (int i = 0; i < D; i++) fprintf(f, "%.17g ", c->mean[i]);
+  fprintf(f, "\n");
+  for (int i = 0; i < D; i++) {
+    for (int j = 0; j < D; j++) {
+      double v;
+      if (c->chol) {
+        v = 0.0;
+        for (int q = 0; q <= (i < j ? i : j); q++) v += c->std[i * D + q] * c->std[j * D + q];
+      } else {
+        v = c->std[i * D + j];
+      }
+      fprintf(f, "%.17g ", v);
+    }
+    fprintf(f, "\n");
+  }
+}
+
+extern "C" void mix_mvdens_dump(FILE *f, const mix_mvdens *m) {
+  fprintf(f, "%d %d\n", m->ncomp, m->ndim);
+  for (int k = 0; k < m->ncomp; k++) {
+    fprintf(f, "%.17g\n", m->wght[k]);
+    dump_mvdens(f, m->comp[k]);
+  }
+}
+
+extern "C" void mix_mvdens_print(FILE *f, const mix_mvdens *m) { mix_mvdens_dump(f, m); }
+
+extern "C" mix_mvdens *mix_mvdens_dwnp(FILE *f, error **err) {
+  int K, D;
+  if (fscanf(f, "%d %d", &K, &D) != 2 || K < 1 || D < 1) {
+    set_error(err, PMCG_EIO, __LINE__, "mix_mvdens header");
+    return nullptr;
+  }
+  mix_mvdens *m = mix_mvdens_alloc(K, D, err);
+  if (!m) return nullptr;
+  for (int k = 0; k < K; k++) {
+    mvdens *c = m->comp[k];
+    int d, df, bl, ch;
+    if (fscanf(f, "%lf", &m->wght[k]) != 1 || fscanf(f, "%d %d %d %d", &d, &df, &bl, &ch) != 4 || d != D) {
+      set_error(err, PMCG_EIO, __LINE__, "component %d header", k);
+      mix_mvdens_free(&m);
+      return nullptr;
+    }
+    c->df = df; c->band_limit = bl; c->chol = ch;
+    for (int i = 0; i < D; i++)
+      if (fscanf(f, "%lf", &c->mean[i]) != 1) { set_error(err, PMCG_EIO, __LINE__, "mean"); mix_mvdens_free(&m); return nullptr; }
+    for (int i = 0; i < D * D; i++)
+      if (fscanf(f, "%lf", &c->std[i]) != 1) { set_error(err, PMCG_EIO, __LINE__, "matrix"); mix_mvdens_free(&m); return nullptr; }
+    if (ch) {
+      double ld = 0.0;
+      for (int i = 0; i < D; i++) ld += std::log(c->std[i * D + i]);
+      c->det = 2.0 * ld;
+    }
+  }
+  return m;
+}
+
+// ------------------------------------------------------------------ prior box
+extern "C" parabox *init_parabox(int ndim, error **err) {
+  parabox *pb = (parabox *)calloc(1, sizeof(parabox));
+  if (!pb) { set_error(err, PMCG_EALLOC, __LINE__, "parabox"); return nullptr; }
+  pb->ndim = ndim;
+  pb->min = (double *)malloc(sizeof(double) * ndim);
+  pb->max = (double *)malloc(sizeof(double) * ndim);
+  for (int i = 0; i < ndim; i++) { pb->min[i] = -INFINITY; pb->max[i] = INFINITY; }
+  return pb;
+}
+
+extern "C" void add_slab(parabox *pb, int dim, double min, double max, error **err) {
+  if (!pb || dim < 0 || dim >= pb->ndim || !(max > min)) {
+    set_error(err, PMCG_EARG, __LINE__, "add_slab(%d, %g, %g)", dim, min, max);
+    return;
+  }
+  pb->min[dim] = min;
+  pb->max[dim] = max;
+}
+
+extern "C" void free_parabox(parabox **pb) {
+  if (!pb || !*pb) return;
+  free((*pb)->min);
+  free((*pb)->max);
+  free(*pb);
+  *pb = nullptr;
+}
+
+extern "C" int isinBox(const parabox *pb, const double *x) {
+  for (int i = 0; i < pb->ndim; i++)
+    if (x[i] < pb->min[i] || x[i] > pb->max[i]) return 0;
+  return 1;
+}
+
+// ------------------------------------------------------------------ samples
+extern "C" pmc_simu *pmc_simu_init_plus_ded(size_t nsamples, int ndim, int n_ded, error **err) {
+  pmc_simu *p = (pmc_simu *)calloc(1, sizeof(pmc_simu));
+  if (!p) { set_error(err, PMCG_EALLOC, __LINE__, "pmc_simu"); return nullptr; }
+  p->ndim = ndim;
+  p->n_ded = n_ded;
+  pmc_simu_realloc(p, nsamples, err);
+  if (isError(err ? *err : nullptr)) { pmc_simu_free(&p); return nullptr; }
+  return p;
+}
+
+extern "C" pmc_simu *pmc_simu_init_mpi(size_t nsamples, int ndim, int n_ded, error **err) {
+  return pmc_simu_init_plus_ded(nsamples, ndim, n_ded, err);
+}
+
+// Sample arrays are page-locked when a CUDA device is present, so the
+// drop-in entry points copy them at full host-link bandwidth; without a
+// device they are ordinary heap memory (the device entry points then fail).
+static void *host_alloc(size_t bytes, int pinned) {
+  void *p = nullptr;
+  if (pinned) return cudaMallocHost(&p, bytes) == cudaSuccess ? p : nullptr;
+  return malloc(bytes);
+}
+static void host_free(void *p, int pinned) {
+  if (!p) return;
+  if (pinned) cudaFreeHost(p);
+  else free(p);
+}
+
+extern "C" void pmc_simu_realloc(pmc_simu *p, size_t nsamples, error **err) {
+  if (nsamples > p->maxsamples) {
+    if (p->maxsamples == 0) {
+      int n = 0;
+      p->pinned = (cudaGetDeviceCount(&n) == cudaSuccess && n > 0) ? 1 : 0;
+    }
+    const int pin = p->pinned;
+    size_t D = (size_t)p->ndim, Dd = (size_t)(p->n_ded > 0 ? p->n_ded : 0), old = p->nsamples;
+    double *X = (double *)host_alloc(sizeof(double) * nsamples * D, pin);
+    double *Xd = Dd ? (double *)host_alloc(sizeof(double) * nsamples * Dd, pin) : nullptr;
+    double *w = (double *)host_alloc(sizeof(double) * nsamples, pin);
+    short *f = (short *)host_alloc(sizeof(short) * nsamples, pin);
+    int *ix = (int *)host_alloc(sizeof(int) * nsamples, pin);
+    if (!X || (Dd && !Xd) || !w || !f || !ix) {
+      host_free(X, pin); host_free(Xd, pin); host_free(w, pin); host_free(f, pin); host_free(ix, pin);
+      set_error(err, PMCG_EALLOC, __LINE__, "pmc_simu_realloc(%zu)", nsamples);
+      return;
+    }
+    if (p->X) {
+      memcpy(X, p->X, sizeof(double) * old * D);
+      if (Dd && p->X_ded) memcpy(Xd, p->X_ded, sizeof(double) * old * Dd);
+      memcpy(w, p->weights, sizeof(double) * old);
+      memcpy(f, p->flg, sizeof(short) * old);
+      memcpy(ix, p->indices, sizeof(int) * old);
+    }
+    host_free(p->X, pin); host_free(p->X_ded, pin); host_free(p->weights, pin);
+    host_free(p->flg, pin); host_free(p->indices, pin);
+    p->X = X; p->X_ded = Xd; p->weights = w; p->flg = f; p->indices = ix;
+    p->maxsamples = nsamples;
+  }
+  p->nsamples = nsamples;
+  pmcg_simu_host_modified(p);
+}
+
+extern "C" void pmc_simu_free(pmc_simu **p) {
+  if (!p || !*p) return;
+  pmcg::forget_simu(*p);
+  const int pin = (*p)->pinned;
+  host_free((*p)->X, pin);
+  host_free((*p)->X_ded, pin);
+  host_free((*p)->weights, pin);
+  host_free((*p)->flg, pin);
+  host_free((*p)->indices, pin);
+  free(*p);
+  *p = nullptr;
+}
+
+extern "C" pmcg_rng *pmcg_rng_alloc(uint64_t seed) {
+  pmcg_rng *r = (pmcg_rng *)calloc(1, sizeof(pmcg_rng));
+  if (r) r->seed = seed;
+  return r;
+}
+
+extern "C" void pmcg_rng_free(pmcg_rng **r) {
+  if (!r) return;
+  free(*r);
+  *r = nullptr;
+}
+
+// get_tempering_beta, exec/cosmo_pmc.c:464-495.
+extern "C" double get_tempering_beta(int tempering, int iter, double t_min, int nmax, error **err) {
+  switch (tempering) {
+    case PMCG_TEMPERING_NONE:
+      return 1.0;
+    case PMCG_TEMPERING_LINEAR:
+      if (iter == nmax - 1) return 1.0;
+      return (double)iter / (nmax - 2.0) * (1.0 - t_min) + t_min;
+    case PMCG_TEMPERING_LOG:
+      if (iter == nmax - 1) return 1.0;
+      if (t_min <= 0) {
+        set_error(err, PMCG_EARG, __LINE__, "Minimal temperature needs to be positive, found %g", t_min);
+        return 0.0;
+      }
+      return std::exp((double)iter / (nmax - 2.0) * (-std::log(t_min)) + std::log(t_min));
+    default:
+      set_error(err, PMCG_EARG, __LINE__, "Unknown tempering type %d", tempering);
+      return 0.0;
+  }
+}
+
+extern "C" const char *pmcg_version(void) { return "pmcg 0.1 (sm_103a)"; }

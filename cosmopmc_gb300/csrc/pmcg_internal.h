@@ -1,0 +1,16 @@
+// pmcg_internal.h — host-side helpers shared by pmcg_host.cpp and
+// pmcg_engine.cu (internal; not part of the C ABI).
+#pragma once
+#include <vector>
+
+#include "../../include/pmcg.h"
+
+namespace pmcg {
+void set_error(error **err, int code, int line, const char *fmt, ...);
+int host_cholesky(int D, const double *C, double *L, double *logdetL);
+bool flatten_mix(const mix_mvdens *m, std::vector<double> &w, std::vector<double> &mu, std::vector<double> &L,
+                 error **err);
+// Drop the device mirrors the library keeps for a host object.
+void forget_mix(const mix_mvdens *m);
+void forget_simu(const pmc_simu *p);
+}  // namespace pmcg

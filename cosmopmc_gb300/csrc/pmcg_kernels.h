@@ -1,0 +1,110 @@
+// pmcg_kernels.h — host-side launchers of the libpmcg CUDA kernels (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "pmcg_common.cuh"
+
+namespace pmcg {
+
+constexpr int kMaxD = 64;    // largest parameter dimension
+constexpr int kMaxK = 256;   // largest component count
+constexpr int kWeightBlocks = 608;  // fixed grid of the weight reduction (4 x 152 SMs)
+
+// Per-iteration scalars computed on the device (one small D2H per iteration).
+struct DevStats {
+  double logSum, maxW, H, sumw2, nok;
+  double ln_evidence, perplexity, ess, enc;
+  double wsum;      // sum of updated weights before renormalisation
+  int ndead;        // components with weight 0 after the update
+  int status;       // 0 ok, else a PMCG_E* code
+};
+
+// Device-resident mixture; one allocation, carved into the arrays below.
+struct DevMix {
+  int K = 0, D = 0, df = -1, ldx = 0;
+  double *w = nullptr, *cw = nullptr, *mu = nullptr, *L = nullptr, *Wt = nullptr, *b = nullptr;
+  double *logdetL = nullptr, *lconst = nullptr;
+  float *W32 = nullptr, *b32 = nullptr, *lconst32 = nullptr;
+  void *arena = nullptr;
+  DevMixView view() const {
+    DevMixView v;
+    v.K = K; v.D = D; v.df = df; v.ldx = ldx;
+    v.w = w; v.cw = cw; v.mu = mu; v.L = L; v.Wt = Wt; v.b = b; v.lconst = lconst;
+    v.W32 = W32; v.b32 = b32; v.lconst32 = lconst32;
+    return v;
+  }
+};
+
+cudaError_t devmix_alloc(DevMix &m, int K, int D, int df);
+void devmix_free(DevMix &m);
+// Upload w, mu, L (host, FP64) and derive L^-1, L^-1 mu, constants, cumulative weights.
+cudaError_t devmix_upload(DevMix &m, const double *w, const double *mu, const double *L, cudaStream_t s);
+// Recompute the derived arrays from w, mu, L already on the device.
+cudaError_t devmix_prepare(DevMix &m, cudaStream_t s);
+
+inline int round4(int d) { return (d + 3) & ~3; }
+
+// (a) draw. X64 [N x D] (FP64 path) or X32 [N x ldx] (mixed path). pre_* optional.
+cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t seed, uint32_t call,
+                        const double *bmin, const double *bmax, const double *pre_u, const double *pre_z,
+                        const double *pre_chi2, double *X64, float *X32, int *idx, short *flg, int *counts,
+                        cudaStream_t s);
+
+// (b) mixture log-pdf of N points. out[n] = LSE (accumulate=0) or out[n] += LSE + add (accumulate=1).
+// lt/Q optional, [K x N].
+cudaError_t launch_mixlogpdf(int precision, const DevMixView &m, size_t N, const double *X64, const float *X32,
+                             double *out, int accumulate, double add, double *lt64, double *Q64, float *lt32,
+                             float *Q32, cudaStream_t s);
+
+// (d) weights + reduction; writes logw and the scalars of DevStats.
+cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
+                           double *logw, WRed *partials, DevStats *st, cudaStream_t s);
+
+// (e) EM statistics, finalisation (Cholesky on the device) and renormalisation.
+size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);
+cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, const float *X32,
+                      const double *logw, const double *logq, const double *lt64, const double *Q64,
+                      const float *lt32, const float *Q32, const int *counts, double *partials, int S,
+                      DevStats *st, int band_limit, cudaStream_t s);
+
+// Convert the mixed-precision sample to FP64 row-major.
+cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
+// Normalised weights wbar = exp(logw - logSum) (0 where flg == 0).
+cudaError_t launch_normalise(size_t N, const double *logw, const short *flg, const DevStats *st, double *wbar,
+                             cudaStream_t s);
+
+// (c) SN Ia likelihood. Constant data lives in SnDev.
+struct SnDev {
+  int nsn = 0, G = 0, chi2mode = 0, add_logdet = 0;
+  int ip_om = -1, ip_ode = -1, ip_w0 = -1, ip_M = -1, ip_alpha = -1, ip_beta = -1;
+  double def_om = 0.3, def_w0 = -1.0, def_M = -19.3, def_alpha = 0.0, def_beta = 0.0;
+  double dh = 0.0, sig_int2 = 0.0;
+  // sorted by redshift: z, 1/z-dependent peculiar-velocity variance, m_B, x1, c, cov6;
+  // per node (nsn*G): a^2, a^3, ln a, weight * half-interval
+  double *z = nullptr, *spv2 = nullptr, *mB = nullptr, *x1 = nullptr, *c = nullptr, *cov6 = nullptr;
+  double *na2 = nullptr, *na3 = nullptr, *nla = nullptr, *nw = nullptr;
+  double *za2 = nullptr, *za3 = nullptr, *zla = nullptr;  // at the SN redshifts
+  float *fna2 = nullptr, *fna3 = nullptr, *fnla = nullptr, *fnw = nullptr;
+  void *arena = nullptr;
+};
+cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
+                      int ldx, double *logpost, short *flg, cudaStream_t s);
+
+// (c) dense template likelihood (whitened): logpost += -1/2 |dt - At phi(x)|^2.
+struct TplDev {
+  int M = 0, P = 0, Dpar = 0;
+  double *At = nullptr, *dt = nullptr;   // [M x P], [M]
+  float *At32 = nullptr, *dt32 = nullptr;
+  void *arena = nullptr;
+};
+cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X64, const float *X32, int ldx,
+                       double *logpost, const short *flg, cudaStream_t s);
+
+// Helpers.
+cudaError_t launch_fill_f64(double *p, size_t n, double v, cudaStream_t s);
+cudaError_t launch_x64_to_x32(size_t N, int D, int ldx, const double *X64, float *X32, cudaStream_t s);
+cudaError_t launch_counts(size_t N, int K, const int *idx, int *counts, cudaStream_t s);
+cudaError_t launch_log_weights(size_t N, double *w, const short *flg, cudaStream_t s);
+
+}  // namespace pmcg

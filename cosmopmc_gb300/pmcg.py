@@ -1,0 +1,524 @@
+"""ctypes mirror of the libpmcg C ABI (include/pmcg.h).
+
+The library is the product: every per-sample computation runs in its CUDA
+kernels. This module only declares the structs and signatures, converts
+numpy arrays, and turns the error chain into `PmcgError`. It raises when the
+shared library is missing; there is no Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpmcg.so")
+
+FP64 = 0
+MIXED = 1
+TEMPERING_NONE, TEMPERING_LINEAR, TEMPERING_LOG = 0, 1, 2
+SN_CHI2_FULL, SN_CHI2_MARG = 0, 1
+
+ERRORS = {
+    -9001: "PMCG_ECUDA", -9002: "PMCG_EDIM", -9003: "PMCG_ECHOL", -9004: "PMCG_ENOSAMPLE",
+    -9005: "PMCG_ENEGWEIGHT", -9006: "PMCG_EUNSUPPORTED", -9007: "PMCG_EALLOC", -9008: "PMCG_EARG",
+    -9009: "PMCG_ETIMEOUT", -9010: "PMCG_EIO", -9011: "PMCG_ENOWEIGHT",
+}
+
+
+class PmcgError(RuntimeError):
+    def __init__(self, code, text):
+        super().__init__(f"{ERRORS.get(code, code)}: {text}")
+        self.code = code
+
+
+class Error(C.Structure):
+    pass
+
+
+Error._fields_ = [("errWhere", C.c_char * 128), ("errText", C.c_char * 384), ("errValue", C.c_int),
+                  ("line", C.c_int), ("next", C.POINTER(Error))]
+
+
+class Mvdens(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("df", C.c_int), ("mean", C.POINTER(C.c_double)),
+                ("std", C.POINTER(C.c_double)), ("band_limit", C.c_int), ("chol", C.c_int), ("det", C.c_double)]
+
+
+class MixMvdensS(C.Structure):
+    _fields_ = [("ncomp", C.c_int), ("ndim", C.c_int), ("wght", C.POINTER(C.c_double)),
+                ("comp", C.POINTER(C.POINTER(Mvdens)))]
+
+
+class ParaboxS(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("min", C.POINTER(C.c_double)), ("max", C.POINTER(C.c_double))]
+
+
+class PmcSimuS(C.Structure):
+    _fields_ = [("nsamples", C.c_size_t), ("maxsamples", C.c_size_t), ("ndim", C.c_int), ("n_ded", C.c_int),
+                ("X", C.POINTER(C.c_double)), ("X_ded", C.POINTER(C.c_double)),
+                ("weights", C.POINTER(C.c_double)), ("flg", C.POINTER(C.c_short)),
+                ("indices", C.POINTER(C.c_int)), ("isLog", C.c_int), ("logSum", C.c_double),
+                ("maxW", C.c_double), ("nok", C.c_size_t), ("pinned", C.c_int)]
+
+
+class RngS(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("calls", C.c_uint32)]
+
+
+class SnData(C.Structure):
+    _fields_ = [("nsn", C.c_int), ("z", C.c_void_p), ("mB", C.c_void_p), ("x1", C.c_void_p), ("c", C.c_void_p),
+                ("cov6", C.c_void_p), ("sig_int", C.c_double), ("v_pec", C.c_double), ("h", C.c_double),
+                ("chi2mode", C.c_int), ("add_logdet", C.c_int), ("quad_nodes", C.c_int),
+                ("ip_Omegam", C.c_int), ("ip_Omegade", C.c_int), ("ip_w0", C.c_int), ("ip_M", C.c_int),
+                ("ip_alpha", C.c_int), ("ip_beta", C.c_int),
+                ("def_Omegam", C.c_double), ("def_w0", C.c_double), ("def_M", C.c_double),
+                ("def_alpha", C.c_double), ("def_beta", C.c_double)]
+
+
+class IterStats(C.Structure):
+    _fields_ = [("ln_evidence", C.c_double), ("perplexity", C.c_double), ("ess", C.c_double), ("enc", C.c_double),
+                ("logSum", C.c_double), ("maxW", C.c_double), ("nok", C.c_size_t), ("ndead", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+PErr = C.POINTER(C.POINTER(Error))
+_dp = C.POINTER(C.c_double)
+LOGPDF_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, _dp, PErr)
+
+# (name, restype, argtypes) of every exported function
+SIGNATURES = [
+    ("addError", C.POINTER(Error), [C.c_int, C.c_char_p, C.POINTER(Error), C.c_int]),
+    ("isError", C.c_int, [C.POINTER(Error)]),
+    ("getErrorValue", C.c_int, [C.POINTER(Error)]),
+    ("purgeError", None, [PErr]),
+    ("printError", None, [C.c_void_p, C.POINTER(Error)]),
+    ("mvdens_alloc", C.POINTER(Mvdens), [C.c_int, PErr]),
+    ("mvdens_free", None, [C.POINTER(C.POINTER(Mvdens))]),
+    ("mix_mvdens_alloc", C.POINTER(MixMvdensS), [C.c_int, C.c_int, PErr]),
+    ("mix_mvdens_free", None, [C.POINTER(C.POINTER(MixMvdensS))]),
+    ("mix_mvdens_copy", None, [C.POINTER(MixMvdensS), C.POINTER(MixMvdensS), PErr]),
+    ("mvdens_cholesky_decomp", None, [C.POINTER(Mvdens), PErr]),
+    ("mix_mvdens_cholesky_decomp", None, [C.POINTER(MixMvdensS), PErr]),
+    ("mvdens_from_meanvar", None, [C.POINTER(Mvdens), _dp, _dp, C.c_double]),
+    ("mvdens_log_pdf", C.c_double, [C.POINTER(Mvdens), _dp, PErr]),
+    ("mvdens_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
+    ("mix_mvdens_log_pdf", C.c_double, [C.POINTER(MixMvdensS), _dp, PErr]),
+    ("mix_mvdens_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
+    ("mix_mvdens_dump", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
+    ("mix_mvdens_dwnp", C.POINTER(MixMvdensS), [C.c_void_p, PErr]),
+    ("mix_mvdens_print", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
+    ("effective_number_of_components", C.c_double, [C.POINTER(MixMvdensS), PErr]),
+    ("init_parabox", C.POINTER(ParaboxS), [C.c_int, PErr]),
+    ("add_slab", None, [C.POINTER(ParaboxS), C.c_int, C.c_double, C.c_double, PErr]),
+    ("free_parabox", None, [C.POINTER(C.POINTER(ParaboxS))]),
+    ("isinBox", C.c_int, [C.POINTER(ParaboxS), _dp]),
+    ("pmc_simu_init_mpi", C.POINTER(PmcSimuS), [C.c_size_t, C.c_int, C.c_int, PErr]),
+    ("pmc_simu_init_plus_ded", C.POINTER(PmcSimuS), [C.c_size_t, C.c_int, C.c_int, PErr]),
+    ("pmc_simu_realloc", None, [C.POINTER(PmcSimuS), C.c_size_t, PErr]),
+    ("pmc_simu_free", None, [C.POINTER(C.POINTER(PmcSimuS))]),
+    ("pmcg_rng_alloc", C.POINTER(RngS), [C.c_uint64]),
+    ("pmcg_rng_free", None, [C.POINTER(C.POINTER(RngS))]),
+    ("simulate_mix_mvdens", C.c_size_t, [C.POINTER(PmcSimuS), C.POINTER(MixMvdensS), C.POINTER(RngS),
+                                         C.POINTER(ParaboxS), PErr]),
+    ("generic_get_importance_weight_and_deduced_verb", C.c_size_t,
+     [C.POINTER(PmcSimuS), C.POINTER(MixMvdensS), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+      C.c_int, PErr]),
+    ("normalize_importance_weight", C.c_double, [C.POINTER(PmcSimuS), PErr]),
+    ("update_prop_rb", None, [C.POINTER(MixMvdensS), C.POINTER(PmcSimuS), PErr]),
+    ("perplexity_and_ess", C.c_double, [C.POINTER(PmcSimuS), C.c_int, _dp, PErr]),
+    ("evidence", C.c_double, [C.POINTER(PmcSimuS), _dp, PErr]),
+    ("get_tempering_beta", C.c_double, [C.c_int, C.c_int, C.c_double, C.c_int, PErr]),
+    ("pmcg_simu_host_modified", None, [C.POINTER(PmcSimuS)]),
+    ("pmcg_set_dropin_precision", None, [C.c_int]),
+    ("pmcg_posterior_alloc", C.c_void_p, [C.c_int, _dp, _dp, PErr]),
+    ("pmcg_posterior_free", None, [C.POINTER(C.c_void_p)]),
+    ("pmcg_posterior_add_mixmvdens", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
+    ("pmcg_posterior_add_snia", None, [C.c_void_p, C.POINTER(SnData), PErr]),
+    ("pmcg_posterior_add_template", None, [C.c_void_p, C.c_int, _dp, _dp, _dp, PErr]),
+    ("pmcg_posterior_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
+    ("pmcg_posterior_log_pdf_batch", None, [C.c_void_p, C.c_size_t, _dp, _dp, C.POINTER(C.c_short), C.c_int,
+                                            C.c_int, C.c_void_p, PErr]),
+    ("pmcg_mix_log_pdf_batch", None, [C.POINTER(MixMvdensS), C.c_size_t, _dp, _dp, _dp, C.c_int, PErr]),
+    ("pmcg_run_create", C.c_void_p, [C.POINTER(MixMvdensS), C.c_void_p, C.POINTER(ParaboxS), C.c_size_t, C.c_int,
+                                     C.c_uint64, PErr]),
+    ("pmcg_run_iterate", None, [C.c_void_p, C.c_double, C.POINTER(IterStats), PErr]),
+    ("pmcg_run_get_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
+    ("pmcg_run_get_sample", None, [C.c_void_p, C.POINTER(PmcSimuS), PErr]),
+    ("pmcg_run_set_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
+    ("pmcg_run_free", None, [C.POINTER(C.c_void_p)]),
+    ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
+    ("pmcg_run_stage_ms", C.c_int, [C.c_void_p, _dp, C.c_int]),
+    ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
+    ("pmcg_version", C.c_char_p, []),
+    ("pmcg_device_count", C.c_int, []),
+    ("pmcg_device_synchronize", None, [PErr]),
+]
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libpmcg.so (built in-tree); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"libpmcg.so not built at {p}: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(p)
+    for name, res, args in SIGNATURES:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+class _Err:
+    """Holds an `error*` for one call and raises on a non-empty chain."""
+
+    def __init__(self):
+        self.p = C.POINTER(Error)()
+
+    @property
+    def ref(self):
+        return C.byref(self.p)
+
+    def check(self):
+        if self.p:
+            code, text = self.p.contents.errValue, self.p.contents.errText.decode(errors="replace")
+            load().purgeError(C.byref(self.p))
+            raise PmcgError(code, text)
+
+
+def call(name, *args):
+    e = _Err()
+    r = getattr(load(), name)(*args, e.ref)
+    e.check()
+    return r
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ----------------------------------------------------------------- mixtures
+class MixMvdens:
+    """Owning wrapper of a `mix_mvdens*` (covariances or Cholesky factors)."""
+
+    def __init__(self, ncomp, ndim):
+        self.p = call("mix_mvdens_alloc", ncomp, ndim)
+        self.K, self.D = ncomp, ndim
+
+    @classmethod
+    def from_arrays(cls, w, mu, cov=None, df=-1, L=None):
+        mu = _f64(mu)
+        K, D = mu.shape
+        m = cls(K, D)
+        m.set(w, mu, cov=cov, df=df, L=L)
+        return m
+
+    def set(self, w, mu, cov=None, df=-1, L=None):
+        s = self.p.contents
+        w = _f64(w)
+        for k in range(self.K):
+            s.wght[k] = float(w[k])
+            c = s.comp[k].contents
+            c.df = int(df)
+            c.band_limit = self.D
+            for i in range(self.D):
+                c.mean[i] = float(mu[k, i])
+            M = _f64(L[k] if L is not None else cov[k]).ravel()
+            C.memmove(c.std, M.ctypes.data, 8 * self.D * self.D)
+            c.chol = 1 if L is not None else 0
+            if L is not None:
+                c.det = 2.0 * float(np.sum(np.log(np.diag(L[k]))))
+        return self
+
+    def cholesky(self):
+        call("mix_mvdens_cholesky_decomp", self.p)
+        return self
+
+    def arrays(self):
+        """(w[K], mu[K,D], L[K,D,D] lower Cholesky) as numpy copies."""
+        s = self.p.contents
+        K, D = self.K, self.D
+        w = np.array([s.wght[k] for k in range(K)])
+        mu = np.empty((K, D))
+        L = np.empty((K, D, D))
+        for k in range(K):
+            c = s.comp[k].contents
+            mu[k] = np.ctypeslib.as_array(c.mean, shape=(D,))
+            A = np.ctypeslib.as_array(c.std, shape=(D, D)).copy()
+            L[k] = np.tril(A) if c.chol else np.linalg.cholesky(A)
+        return w, mu, L
+
+    @property
+    def df(self):
+        return self.p.contents.comp[0].contents.df
+
+    def free(self):
+        if self.p:
+            load().mix_mvdens_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Parabox:
+    def __init__(self, bmin, bmax):
+        bmin, bmax = _f64(bmin), _f64(bmax)
+        self.p = call("init_parabox", len(bmin))
+        for i in range(len(bmin)):
+            call("add_slab", self.p, i, float(bmin[i]), float(bmax[i]))
+        self.min, self.max = bmin, bmax
+
+    def free(self):
+        if self.p:
+            load().free_parabox(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PmcSimu:
+    """Owning wrapper of a `pmc_simu*` with numpy views of its arrays."""
+
+    def __init__(self, nsamples, ndim, n_ded=0):
+        self.p = call("pmc_simu_init_mpi", nsamples, ndim, n_ded)
+
+    @property
+    def s(self):
+        return self.p.contents
+
+    @property
+    def N(self):
+        return self.s.nsamples
+
+    @property
+    def X(self):
+        return np.ctypeslib.as_array(self.s.X, shape=(self.N, self.s.ndim))
+
+    @property
+    def weights(self):
+        return np.ctypeslib.as_array(self.s.weights, shape=(self.N,))
+
+    @property
+    def flg(self):
+        return np.ctypeslib.as_array(self.s.flg, shape=(self.N,))
+
+    @property
+    def indices(self):
+        return np.ctypeslib.as_array(self.s.indices, shape=(self.N,))
+
+    def host_modified(self):
+        load().pmcg_simu_host_modified(self.p)
+
+    def free(self):
+        if self.p:
+            load().pmc_simu_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Rng:
+    def __init__(self, seed):
+        self.p = load().pmcg_rng_alloc(seed)
+
+    @property
+    def calls(self):
+        return self.p.contents.calls
+
+    def __del__(self):
+        try:
+            load().pmcg_rng_free(C.byref(self.p))
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------- posterior
+class Posterior:
+    def __init__(self, npar, bmin=None, bmax=None):
+        self._keep = []
+        if bmin is not None:
+            bmin, bmax = _f64(bmin), _f64(bmax)
+            self.p = C.c_void_p(call("pmcg_posterior_alloc", npar, _dptr(bmin), _dptr(bmax)))
+        else:
+            self.p = C.c_void_p(call("pmcg_posterior_alloc", npar, None, None))
+        self.npar = npar
+
+    def add_mix(self, target: MixMvdens):
+        call("pmcg_posterior_add_mixmvdens", self.p, target.p)
+        return self
+
+    def add_snia(self, sn: dict):
+        s = SnData()
+        arrs = {k: _f64(sn[k]) for k in ("z", "mB", "x1", "c", "cov6")}
+        self._keep.append(arrs)
+        s.nsn = len(arrs["z"])
+        for k, a in arrs.items():
+            setattr(s, k, a.ctypes.data)
+        for k in ("sig_int", "v_pec", "h"):
+            setattr(s, k, float(sn[k]))
+        s.chi2mode, s.add_logdet, s.quad_nodes = int(sn["chi2mode"]), int(sn["add_logdet"]), int(sn["quad_nodes"])
+        s.ip_Omegam, s.ip_Omegade, s.ip_w0 = int(sn["ip_om"]), int(sn["ip_ode"]), int(sn["ip_w0"])
+        s.ip_M, s.ip_alpha, s.ip_beta = int(sn["ip_M"]), int(sn["ip_alpha"]), int(sn["ip_beta"])
+        s.def_Omegam, s.def_w0, s.def_M = float(sn["def_om"]), float(sn["def_w0"]), float(sn["def_M"])
+        s.def_alpha, s.def_beta = float(sn["def_alpha"]), float(sn["def_beta"])
+        call("pmcg_posterior_add_snia", self.p, C.byref(s))
+        return self
+
+    def add_template(self, A, Cm, dobs):
+        A, Cm, dobs = _f64(A), _f64(Cm), _f64(dobs)
+        call("pmcg_posterior_add_template", self.p, A.shape[0], _dptr(A), _dptr(Cm), _dptr(dobs))
+        return self
+
+    def log_pdf_batch(self, X, precision=FP64):
+        X = _f64(X)
+        N = X.shape[0]
+        out = np.empty(N)
+        flg = np.empty(N, dtype=np.int16)
+        call("pmcg_posterior_log_pdf_batch", self.p, N, _dptr(X), _dptr(out),
+             flg.ctypes.data_as(C.POINTER(C.c_short)), 0, precision, None)
+        return out, flg
+
+    def free(self):
+        if self.p:
+            load().pmcg_posterior_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def mix_log_pdf_batch(mix: MixMvdens, X, precision=FP64, want_terms=False):
+    X = _f64(X)
+    N = X.shape[0]
+    logq = np.empty(N)
+    lt = np.empty((mix.K, N)) if want_terms else None
+    call("pmcg_mix_log_pdf_batch", mix.p, N, _dptr(X), _dptr(logq), None if lt is None else _dptr(lt), precision)
+    return (logq, lt) if want_terms else logq
+
+
+# ----------------------------------------------------------------- runs
+class Run:
+    """Device-resident PMC run (pmcg_run_*)."""
+
+    def __init__(self, proposal: MixMvdens, posterior: Posterior, nsamples, precision=FP64, seed=1, box=None):
+        self.p = C.c_void_p(call("pmcg_run_create", proposal.p, posterior.p, box.p if box is not None else None,
+                                 nsamples, precision, seed))
+        self.K, self.D, self.N = proposal.K, proposal.D, nsamples
+        self.df = proposal.df
+        self._post = posterior
+
+    def iterate(self, beta=1.0):
+        st = IterStats()
+        call("pmcg_run_iterate", self.p, beta, C.byref(st))
+        return st.as_dict()
+
+    def proposal(self) -> MixMvdens:
+        m = MixMvdens(self.K, self.D)
+        call("pmcg_run_get_proposal", self.p, m.p)
+        return m
+
+    def set_proposal(self, m: MixMvdens):
+        call("pmcg_run_set_proposal", self.p, m.p)
+
+    def sample(self) -> PmcSimu:
+        ps = PmcSimu(self.N, self.D)
+        call("pmcg_run_get_sample", self.p, ps.p)
+        return ps
+
+    def set_timing(self, on=True):
+        load().pmcg_run_set_timing(self.p, 1 if on else 0)
+
+    def stage_ms(self):
+        ms = (C.c_double * 5)()
+        n = load().pmcg_run_stage_ms(self.p, ms, 5)
+        return list(ms), n
+
+    def last_launches(self):
+        return load().pmcg_run_last_launches(self.p)
+
+    def free(self):
+        if self.p:
+            load().pmcg_run_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------- drop-in calls
+def simulate_mix_mvdens(psim: PmcSimu, prop: MixMvdens, rng: Rng, pb: Parabox | None = None):
+    return call("simulate_mix_mvdens", psim.p, prop.p, rng.p, pb.p if pb is not None else None)
+
+
+def importance_weights(psim: PmcSimu, prop: MixMvdens, post: Posterior, beta=1.0):
+    L = load()
+    q = C.cast(L.mix_mvdens_log_pdf_void, C.c_void_p)
+    f = C.cast(L.pmcg_posterior_log_pdf_void, C.c_void_p)
+    return call("generic_get_importance_weight_and_deduced_verb", psim.p, prop.p, q, f, None, post.p, beta, 1)
+
+
+def normalize_importance_weight(psim: PmcSimu):
+    return call("normalize_importance_weight", psim.p)
+
+
+def update_prop_rb(prop: MixMvdens, psim: PmcSimu):
+    call("update_prop_rb", prop.p, psim.p)
+
+
+def perplexity_and_ess(psim: PmcSimu):
+    ess = C.c_double()
+    p = call("perplexity_and_ess", psim.p, 1, C.byref(ess))
+    return p, ess.value
+
+
+def evidence(psim: PmcSimu):
+    ln = C.c_double()
+    e = call("evidence", psim.p, C.byref(ln))
+    return e, ln.value
+
+
+def effective_number_of_components(prop: MixMvdens):
+    return call("effective_number_of_components", prop.p)
+
+
+def get_tempering_beta(kind, it, tmin, nmax):
+    return call("get_tempering_beta", kind, it, tmin, nmax)
+
+
+def set_dropin_precision(prec):
+    load().pmcg_set_dropin_precision(prec)
+
+
+def device_count():
+    return load().pmcg_device_count()

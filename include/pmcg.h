@@ -1,0 +1,321 @@
+/*
+ * pmcg.h — C ABI of libpmcg, a GB300 (sm_103a) Population Monte Carlo
+ * iteration engine that stands in for pmclib underneath CosmoPMC.
+ *
+ * Part 1 re-declares the pmclib types and entry points that the CosmoPMC
+ * driver binds (exec/cosmo_pmc.c); their names, argument meaning and
+ * error behaviour follow the reference call sites cited beside each one.
+ * pmclib itself is an external library that the reference only includes
+ * (exec/cosmo_pmc.h:26-31), so the struct layouts below are this
+ * library's own, carrying exactly the fields the reference reads.
+ *
+ * Part 2 is the GB300-native surface the reference has no counterpart for:
+ * device-resident runs, batched likelihood evaluation, and the batch/serve
+ * engines.
+ *
+ * No symbol here takes or returns a CUDA or torch type; streams are passed
+ * as `void*` (a cudaStream_t, NULL = the library's own stream).
+ */
+#ifndef PMCG_H
+#define PMCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ------------------------------------------------------------------ *
+ * Error chain (pmctools errorlist semantics: negative codes, newest   *
+ * first; exec/cosmo_pmc.c uses forwardError/quitOnError on it).       *
+ * ------------------------------------------------------------------ */
+typedef struct _err {
+  char errWhere[128];
+  char errText[384];
+  int errValue;
+  int line;
+  struct _err *next;
+} error;
+
+#define PMCG_OK              0
+#define pmcg_base        -9000
+#define PMCG_ECUDA        (-1 + pmcg_base)  /* CUDA runtime error (text holds cudaGetErrorString) */
+#define PMCG_EDIM         (-2 + pmcg_base)  /* dimension mismatch / unsupported size            */
+#define PMCG_ECHOL        (-3 + pmcg_base)  /* covariance not positive definite (pmclib mv_cholesky) */
+#define PMCG_ENOSAMPLE    (-4 + pmcg_base)  /* no point inside the prior box (pmc_nosamplep)      */
+#define PMCG_ENEGWEIGHT   (-5 + pmcg_base)  /* all component weights zero (pmc_negWeight)        */
+#define PMCG_EUNSUPPORTED (-6 + pmcg_base)  /* callback/feature not supported on the device path  */
+#define PMCG_EALLOC       (-7 + pmcg_base)  /* host or device allocation failed                   */
+#define PMCG_EARG         (-8 + pmcg_base)  /* invalid argument                                   */
+#define PMCG_ETIMEOUT     (-9 + pmcg_base)  /* bounded wait ran out (serving loop)                */
+#define PMCG_EIO          (-10 + pmcg_base) /* file read/write error                              */
+#define PMCG_ENOWEIGHT    (-11 + pmcg_base) /* every sample has zero weight                       */
+
+error *addError(int code, const char *text, error *next, int line);
+int isError(const error *err);
+int getErrorValue(const error *err);
+void purgeError(error **err);
+void printError(FILE *f, const error *err);
+
+/* ------------------------------------------------------------------ *
+ * Densities: mvdens / mix_mvdens (Manual/manual.tex:3199-3260;       *
+ * fields read at wrappers/src/param.c:543-549,1506-1528 and          *
+ * exec/cosmo_pmc.c:211-234).                                          *
+ * ------------------------------------------------------------------ */
+typedef struct {
+  int ndim;
+  int df;          /* <= 0: Gaussian (pmclib writes -1); > 0: Student-t degrees of freedom */
+  double *mean;    /* [ndim] */
+  double *std;     /* [ndim*ndim] row-major covariance, or its lower Cholesky factor when chol==1 */
+  int band_limit;  /* covariance entries with |i-j| >= band_limit are zero after an update */
+  int chol;        /* 1 if std holds the Cholesky factor */
+  double det;      /* log det of the covariance (valid when chol==1) */
+} mvdens;
+
+typedef struct {
+  int ncomp;
+  int ndim;
+  double *wght;    /* [ncomp], sum 1; a buried component has weight 0 */
+  mvdens **comp;   /* [ncomp] */
+} mix_mvdens;
+
+mvdens *mvdens_alloc(int ndim, error **err);
+void mvdens_free(mvdens **m);
+mix_mvdens *mix_mvdens_alloc(int ncomp, int ndim, error **err);
+void mix_mvdens_free(mix_mvdens **m);
+void mix_mvdens_copy(mix_mvdens *dst, const mix_mvdens *src, error **err);          /* cosmo_pmc.c:366 */
+void mvdens_cholesky_decomp(mvdens *m, error **err);                                /* param.c:56,1476 */
+void mix_mvdens_cholesky_decomp(mix_mvdens *m, error **err);                        /* param.c:700,1526 */
+void mvdens_from_meanvar(mvdens *m, const double *mean, const double *cov, double correct); /* cosmo_pmc.c:230 */
+double mvdens_log_pdf(mvdens *m, const double *x, error **err);                     /* param.c:1023 */
+double mvdens_log_pdf_void(void *m, const double *x, error **err);                  /* param.c:1489 */
+double mix_mvdens_log_pdf(mix_mvdens *m, const double *x, error **err);
+double mix_mvdens_log_pdf_void(void *m, const double *x, error **err);              /* cosmo_pmc.c:343, param.c:1534 */
+void mix_mvdens_dump(FILE *f, const mix_mvdens *m);                                 /* cosmo_pmc.c:37 */
+mix_mvdens *mix_mvdens_dwnp(FILE *f, error **err);                                  /* cosmo_pmc.c:415 */
+void mix_mvdens_print(FILE *f, const mix_mvdens *m);                                /* cosmo_pmc.c:29 */
+double effective_number_of_components(const mix_mvdens *m, error **err);            /* cosmo_pmc.c:84 */
+
+/* ------------------------------------------------------------------ *
+ * Prior box (parabox; built at wrappers/src/param.c:915-926, passed  *
+ * to the draw at exec/cosmo_pmc.c:320). Axis-aligned slabs.          *
+ * ------------------------------------------------------------------ */
+typedef struct {
+  int ndim;
+  double *min;     /* [ndim], -inf when the coordinate has no slab */
+  double *max;     /* [ndim], +inf when the coordinate has no slab */
+} parabox;
+
+parabox *init_parabox(int ndim, error **err);
+void add_slab(parabox *pb, int dim, double min, double max, error **err);
+void free_parabox(parabox **pb);
+int isinBox(const parabox *pb, const double *x);
+
+/* ------------------------------------------------------------------ *
+ * PMC sample (pmc_simu; fields used at exec/exec_helper.c:72-110,    *
+ * 408-423 and exec/importance_sample.c:34-41,265-284).               *
+ * ------------------------------------------------------------------ */
+typedef struct {
+  size_t nsamples;   /* samples drawn this iteration */
+  size_t maxsamples; /* capacity */
+  int ndim;
+  int n_ded;
+  double *X;         /* [nsamples*ndim] row-major */
+  double *X_ded;     /* [nsamples*n_ded] (deduced parameters; not filled by the device path) */
+  double *weights;   /* log-weights when isLog==1, normalised weights when isLog==0 */
+  short *flg;        /* 1 = sample counts; 0 = outside the prior box or likelihood error */
+  int *indices;      /* component each sample was drawn from */
+  int isLog;
+  double logSum;     /* log sum_{flg} exp(log-weight) */
+  double maxW;       /* max log-weight over flg==1 */
+  size_t nok;        /* samples with flg==1 after the weight step */
+  int pinned;        /* 1 when the arrays are page-locked (set by the allocator) */
+} pmc_simu;
+
+pmc_simu *pmc_simu_init_mpi(size_t nsamples, int ndim, int n_ded, error **err);     /* cosmo_pmc.c:633 */
+pmc_simu *pmc_simu_init_plus_ded(size_t nsamples, int ndim, int n_ded, error **err);/* cosmo_pmc.c:429 */
+void pmc_simu_realloc(pmc_simu *psim, size_t nsamples, error **err);                /* cosmo_pmc.c:313 */
+void pmc_simu_free(pmc_simu **psim);                                                /* cosmo_pmc.c:738 */
+
+/* Random stream replacing the gsl_rng the driver passes to the draw.
+ * Philox4x32-10 (Salmon et al. 2011), keyed by a 64-bit seed; each draw
+ * call consumes one counter block per sample and advances `calls`. */
+typedef struct {
+  uint64_t seed;
+  uint32_t calls;
+} pmcg_rng;
+
+pmcg_rng *pmcg_rng_alloc(uint64_t seed);
+void pmcg_rng_free(pmcg_rng **r);
+
+/* Draw psim->nsamples points from the proposal into psim->X/indices/flg.
+ * Points outside `pb` get flg=0 (weight 0, no redraw). Returns the number
+ * inside the box. Replaces pmclib simulate_mix_mvdens (exec/cosmo_pmc.c:320). */
+size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg_rng *rng, parabox *pb, error **err);
+
+/* Log-density callback type (wrappers/src/param.c:948). */
+typedef double logpdf_fn(void *extra, const double *x, error **err);
+typedef void retrieve_ded_fn(const void *extra, double *x_ded);
+
+/* Importance log-weights: logw = beta*logpost(x) - log q(x); errors give
+ * flg=0. q must be mix_mvdens_log_pdf_void and post must be
+ * pmcg_posterior_log_pdf_void (extra = pmcg_posterior*): both are
+ * evaluated on the GPU for the whole sample. Other host callbacks are
+ * rejected with PMCG_EUNSUPPORTED (there is no CPU evaluation path).
+ * Returns the number of samples with flg==1.
+ * Replaces pmclib (exec/cosmo_pmc.c:343-345). */
+size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim, mix_mvdens *proposal,
+    logpdf_fn *q, logpdf_fn *post, retrieve_ded_fn *ded, void *extra, double beta, int quiet, error **err);
+
+/* logSum = log sum exp(logw) over flg==1; weights become normalised
+ * (isLog=0). Returns logSum (exec/cosmo_pmc.c:378). */
+double normalize_importance_weight(pmc_simu *psim, error **err);
+
+/* Rao-Blackwellised EM update of the proposal from the last weighted
+ * sample; dead components (fewer than 20 draws or weight < 1/N, or a
+ * non-positive-definite update) are buried (weight 0) and the weights
+ * renormalised (exec/cosmo_pmc.c:247; Manual/manual.tex:479-500). */
+void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err);
+
+#define MC_UNORM 1
+/* perplexity = exp(-sum wbar ln wbar)/N, *ess = 1/sum wbar^2
+ * (exec/cosmo_pmc.c:46; Manual/manual.tex:556-575). */
+double perplexity_and_ess(pmc_simu *psim, int mode, double *ess, error **err);
+/* ln E = logSum - ln N; returns E (exec/cosmo_pmc.c:62). */
+double evidence(pmc_simu *psim, double *ln_evi, error **err);
+
+/* Tempering schedule (exec/cosmo_pmc.c:464-495). */
+#define PMCG_TEMPERING_NONE   0
+#define PMCG_TEMPERING_LINEAR 1
+#define PMCG_TEMPERING_LOG    2
+double get_tempering_beta(int tempering, int iter, double t_min, int nmax, error **err);
+
+/* Tell the library that the caller rewrote psim->X on the host (the
+ * device copy is re-uploaded before the next weight step). */
+void pmcg_simu_host_modified(pmc_simu *psim);
+
+/* Precision of the drop-in entry points above: PMCG_FP64 (default, the
+ * plain FP64 path) or PMCG_MIXED. */
+void pmcg_set_dropin_precision(int precision);
+
+/* ------------------------------------------------------------------ *
+ * Part 2 — device posterior plugins (the batched counterpart of the  *
+ * per-point func_likeli_t of wrappers/include/init_wrappers.h:15-42). *
+ * ------------------------------------------------------------------ */
+typedef struct pmcg_posterior pmcg_posterior;
+
+/* Flat box prior: logpr_default = -sum log(max-min) added once per point
+ * (wrappers/src/param.c:124-129, 988-1003). */
+pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, const double *max, error **err);
+void pmcg_posterior_free(pmcg_posterior **p);
+
+/* Gaussian(-mixture) target likelihood (likeli_MixMvdens / likeli_Mvdens,
+ * wrappers/src/param.c:1485-1537). The mixture is copied and
+ * Cholesky-decomposed if needed. */
+void pmcg_posterior_add_mixmvdens(pmcg_posterior *p, const mix_mvdens *target, error **err);
+
+/* SN Ia likelihood (likeli_SNIa, wrappers/src/sn.c:138-281).
+ * Per supernova: z, m_B, x1 (stretch), colour c and the 3x3 covariance of
+ * (m_B, x1, c) as 6 numbers (mm, xx, cc, mx, mc, xc).
+ * mu_obs = m_B - M + alpha*x1 - beta*c; D_L from a Gauss-Legendre quadrature
+ * of 1/E(z) between consecutive sorted redshifts. */
+#define PMCG_SN_CHI2_FULL 0   /* M is a sampled parameter */
+#define PMCG_SN_CHI2_MARG 1   /* M analytically marginalised */
+typedef struct {
+  int nsn;
+  const double *z, *mB, *x1, *c;
+  const double *cov6;        /* [nsn*6] */
+  double sig_int;            /* intrinsic dispersion (mag) */
+  double v_pec;              /* peculiar velocity (km/s) */
+  double h;                  /* Hubble parameter inside D_L (absorbed in M) */
+  int chi2mode;              /* PMCG_SN_CHI2_FULL / _MARG */
+  int add_logdet;            /* add -1/2 sum ln sigma_i^2 */
+  int quad_nodes;            /* Gauss-Legendre nodes per redshift interval (1..16) */
+  /* parameter indices in the sample vector, -1 when absent */
+  int ip_Omegam, ip_Omegade, ip_w0, ip_M, ip_alpha, ip_beta;
+  /* defaults for absent parameters */
+  double def_Omegam, def_w0, def_M, def_alpha, def_beta;
+} pmcg_sn_data;
+void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *sn, error **err);
+
+/* Dense template likelihood: d(theta) = A phi(theta), phi = the monomials of
+ * degree <= 2 in the npar parameters (1, theta_i, theta_i theta_j for i<=j);
+ * logL = -1/2 (d_obs - d)^T C^-1 (d_obs - d). A is [ndata x nphi] row-major,
+ * C [ndata x ndata]. C is Cholesky-factored in FP64 at set-up. */
+void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const double *A, const double *C,
+                                 const double *dobs, error **err);
+
+/* Single-point log-posterior (the per-point callback shape); evaluates one
+ * point on the GPU. Passing this function to the weight step selects the
+ * batched device evaluation. */
+double pmcg_posterior_log_pdf_void(void *post, const double *x, error **err);
+
+/* Batched log-posterior of N points. X and logpost/flg are host pointers
+ * when on_device==0, device pointers otherwise. flg[n] is 0 on a
+ * likelihood error. Precision: PMCG_FP64 or PMCG_MIXED. */
+#define PMCG_FP64  0
+#define PMCG_MIXED 1
+void pmcg_posterior_log_pdf_batch(const pmcg_posterior *p, size_t N, const double *X, double *logpost,
+                                  short *flg, int on_device, int precision, void *stream, error **err);
+
+/* Batched mixture log-density of N points (host pointers); lt (optional,
+ * [ncomp x N]) receives log(alpha_k) + log f_k(x_n). */
+void pmcg_mix_log_pdf_batch(const mix_mvdens *m, size_t N, const double *X, double *logq, double *lt,
+                            int precision, error **err);
+
+/* ------------------------------------------------------------------ *
+ * Part 2 — device-resident PMC runs                                   *
+ * ------------------------------------------------------------------ */
+typedef struct pmcg_run pmcg_run;
+
+typedef struct {
+  double ln_evidence;  /* logSum - ln N */
+  double perplexity;
+  double ess;
+  double enc;          /* of the updated proposal */
+  double logSum;
+  double maxW;
+  size_t nok;          /* samples with flg==1 */
+  int ndead;           /* components buried by this update */
+} pmcg_iter_stats;
+
+/* A run keeps its proposal, sample and scratch on the GPU. nsamples is
+ * fixed at creation. pb may be NULL (no box). */
+pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_posterior *post, const parabox *pb,
+                          size_t nsamples, int precision, uint64_t seed, error **err);
+/* One PMC iteration (draw, log q, log posterior, weights, evidence,
+ * perplexity, EM update, dead-component burial). stats may be NULL. */
+void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err);
+void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err);
+/* Replace the run's proposal (same ncomp/ndim/df), e.g. to restart or to
+ * apply a host-side revive step between iterations. */
+void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, error **err);
+/* Copy the last sample (X, log-weights, flg, indices) into psim. */
+void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err);
+void pmcg_run_free(pmcg_run **r);
+/* Stage timing with CUDA events on the run's stream: enable, then read
+ * the summed milliseconds per stage (draw, logq, logpost, weights, em)
+ * and the number of iterations they cover; reset clears the sums. */
+#define PMCG_NSTAGE 5
+void pmcg_run_set_timing(pmcg_run *r, int on);
+int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage);
+/* Number of kernel launches issued by the last pmcg_run_iterate call. */
+int pmcg_run_last_launches(const pmcg_run *r);
+
+/* Library / device information. */
+const char *pmcg_version(void);
+int pmcg_device_count(void);
+void pmcg_device_synchronize(error **err);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMCG_H */

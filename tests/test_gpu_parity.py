@@ -1,0 +1,388 @@
+"""CUDA path vs the FP64 oracle and the golden fixtures, through the C ABI.
+
+Tolerances: the FP64 path must agree with the oracle to rounding (stated per
+test, 1e-9..1e-12). The mixed path (FP32 quadratic forms / likelihoods with
+FP64 reductions) must give |d log Z| <= 1e-3 and posterior means/covariances
+within 0.05 sigma; per-sample log-densities are checked at the stated looser
+absolute tolerances.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from cosmopmc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+G = np.load(os.path.join(GOLD, "golden.npz"))
+META = json.load(open(os.path.join(GOLD, "golden.json")))
+
+PRECS = [0, 1]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu(pmcg):
+    assert pmcg.device_count() > 0, "no CUDA device visible"
+
+
+def make_mix(pmcg, w, mu, cov, df):
+    return pmcg.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+
+
+def oracle_mix(oracle, m):
+    w, mu, L = m.arrays()
+    return oracle.Mix(w, mu, df=m.df, L=L)
+
+
+def small_mixture(K=7, D=5, df=-1, seed=3):
+    rng = np.random.default_rng(seed)
+    mu = rng.normal(0, 2, (K, D))
+    A = rng.normal(0, 1, (K, D, D))
+    cov = np.einsum("kij,klj->kil", A, A) + np.eye(D)[None]
+    w = rng.dirichlet(np.ones(K) * 3)
+    return w, mu, cov, df
+
+
+# ----------------------------------------------------------------- (a) draws
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("shape", [(7, 5, -1), (7, 5, 3), (64, 32, 3), (1, 1, -1), (3, 7, 5)])
+def test_draw_indices_bit_exact(pmcg, oracle, prec, shape):
+    K, D, df = shape
+    w, mu, cov, _ = small_mixture(K, D, df)
+    m = make_mix(pmcg, w, mu, cov, df)
+    N = 5003
+    pmcg.set_dropin_precision(prec)
+    ps = pmcg.PmcSimu(N, D)
+    rng = pmcg.Rng(1234)
+    bmin, bmax = mu.min(0) - 1.0, mu.max(0) + 1.0
+    pb = pmcg.Parabox(bmin, bmax)
+    nok = pmcg.simulate_mix_mvdens(ps, m, rng, pb)
+    om = oracle_mix(oracle, m)
+    u, z, chi2 = oracle.randoms(1234, 0, N, D, df)
+    X, idx, flg, nok_o = oracle.draw(om, u, z, chi2, bmin, bmax)
+    np.testing.assert_array_equal(ps.indices, idx)
+    if prec == 0:
+        np.testing.assert_allclose(ps.X, X, rtol=1e-12, atol=1e-12)
+        np.testing.assert_array_equal(ps.flg, flg)
+        assert nok == nok_o
+    else:
+        scale = np.sqrt(np.max(np.diagonal(cov, axis1=1, axis2=2))) + np.abs(mu).max()
+        assert np.max(np.abs(ps.X - X)) < 2e-5 * scale
+        assert np.sum(ps.flg != flg) <= 2
+    assert rng.calls == 1
+
+
+# ----------------------------------------------------------------- (b) mixture log-pdf
+@pytest.mark.parametrize("tag", ["gauss", "t"])
+def test_mix_logpdf_golden(pmcg, tag):
+    m = make_mix(pmcg, G[f"mix_{tag}_w"], G[f"mix_{tag}_mu"], G[f"mix_{tag}_cov"], META[f"mix_{tag}_df"])
+    lq = pmcg.mix_log_pdf_batch(m, G[f"mix_{tag}_X"], precision=0)
+    np.testing.assert_allclose(lq, G[f"mix_{tag}_logq"], rtol=0, atol=1e-10)
+    lq32 = pmcg.mix_log_pdf_batch(m, G[f"mix_{tag}_X"], precision=1)
+    np.testing.assert_allclose(lq32, G[f"mix_{tag}_logq"], rtol=0, atol=2e-4)
+
+
+def test_mix_logpdf_condition_1e6(pmcg, oracle):
+    """D=32, K=64 Student-t nu=3 with covariance condition 1e6, points drawn from it."""
+    wl = W.mixture_workload(D=32, K=64, seed=5)
+    w, mu, cov, df = wl["prop"]
+    m = make_mix(pmcg, w, mu, cov, df)
+    om = oracle_mix(oracle, m)
+    u, z, chi2 = oracle.randoms(9, 0, 3000, 32, df)
+    X, idx, flg, _ = oracle.draw(om, u, z, chi2)
+    ref, lt_ref, _ = oracle.mix_logpdf(om, X, want_terms=True)
+    lq, lt = pmcg.mix_log_pdf_batch(m, X, precision=0, want_terms=True)
+    np.testing.assert_allclose(lq, ref, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(lt, lt_ref, rtol=1e-12, atol=1e-8)
+    lq32 = pmcg.mix_log_pdf_batch(m, X, precision=1)
+    err = np.abs(lq32 - ref)
+    assert np.max(err) < 5e-3 and np.mean(err) < 5e-4, (np.max(err), np.mean(err))
+
+
+# ----------------------------------------------------------------- (c) likelihoods
+@pytest.mark.parametrize("tag", ["full", "marg", "logdet"])
+def test_sn_loglike_golden(pmcg, tag):
+    sn = dict(META[f"sn_{tag}"])
+    for k in ("z", "mB", "x1", "c", "cov6"):
+        sn[k] = G[f"sn_{tag}_{k}"]
+    post = pmcg.Posterior(6).add_snia(sn)
+    ll, flg = post.log_pdf_batch(G[f"sn_{tag}_P"], precision=0)
+    assert flg.all()
+    np.testing.assert_allclose(ll, G[f"sn_{tag}_ll"], rtol=1e-11, atol=1e-8)
+    ll32, flg32 = post.log_pdf_batch(G[f"sn_{tag}_P"], precision=1)
+    assert flg32.all()
+    np.testing.assert_allclose(ll32, G[f"sn_{tag}_ll"], rtol=0, atol=2e-3)
+
+
+def test_sn_740_vs_oracle_and_loitering(pmcg, oracle):
+    wl = W.sn_workload()
+    sn = wl["sn"]
+    post = pmcg.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(sn)
+    rng = np.random.default_rng(4)
+    P = rng.uniform(wl["bmin"], wl["bmax"], (701, 6))
+    P[0] = [0.0, 1.5, -3.0, -19.1, 0.1, 3.0]   # loitering: E^2 < 0
+    ref, ok = oracle.sn_loglike(sn, P)
+    ll, flg = post.log_pdf_batch(P, precision=0)
+    np.testing.assert_array_equal(flg, ok)
+    logpr = -np.sum(np.log(wl["bmax"] - wl["bmin"]))
+    good = ok == 1
+    assert flg[0] == 0
+    np.testing.assert_allclose(ll[good], ref[good] + logpr, rtol=1e-11, atol=1e-8)
+    ll32, flg32 = post.log_pdf_batch(P, precision=1)
+    both = good & (flg32 == 1)
+    assert np.sum(flg32 != ok) <= 2
+    assert np.max(np.abs(ll32[both] - ll[both]) / np.maximum(1.0, np.abs(ll[both]))) < 1e-5
+
+
+def test_template_golden_and_c2_shape(pmcg, oracle):
+    post = pmcg.Posterior(3).add_template(G["tpl_A"], G["tpl_C"], G["tpl_dobs"])
+    ll, flg = post.log_pdf_batch(G["tpl_T"], precision=0)
+    np.testing.assert_allclose(ll, G["tpl_ll"], rtol=1e-10)
+    ll32, _ = post.log_pdf_batch(G["tpl_T"], precision=1)
+    np.testing.assert_allclose(ll32, G["tpl_ll"], rtol=0, atol=1e-3)
+    wl = W.template_workload(D=12, M=2048)
+    post2 = pmcg.Posterior(12).add_template(wl["A"], wl["C"], wl["dobs"])
+    At, dt = oracle.tpl_prepare(wl["A"], wl["C"], wl["dobs"])
+    T = np.random.default_rng(1).uniform(-1, 1, (300, 12))
+    T[0] = wl["theta0"]
+    ref = oracle.tpl_loglike(At, dt, T)
+    ll, _ = post2.log_pdf_batch(T, precision=0)
+    np.testing.assert_allclose(ll, ref, rtol=1e-11)
+    ll32, _ = post2.log_pdf_batch(T, precision=1)
+    assert np.max(np.abs(ll32 - ref)) < 1e-2
+    assert np.max(np.abs(ll32[:1] - ref[:1])) < 1e-3  # near the best fit (chi2 ~ 2048)
+
+
+# ----------------------------------------------------------------- (d)+(e) drop-in sequence
+def dropin_iteration(pmcg, m, post, N, seed, beta, box, prec):
+    pmcg.set_dropin_precision(prec)
+    ps = pmcg.PmcSimu(N, m.D)
+    rng = pmcg.Rng(seed)
+    pb = pmcg.Parabox(*box) if box is not None else None
+    pmcg.simulate_mix_mvdens(ps, m, rng, pb)
+    nok = pmcg.importance_weights(ps, m, post, beta)
+    logw = ps.weights.copy()
+    ls = pmcg.normalize_importance_weight(ps)
+    wbar = ps.weights.copy()
+    perp, ess = pmcg.perplexity_and_ess(ps)
+    ev, lnev = pmcg.evidence(ps)
+    X, idx, flg = ps.X.copy(), ps.indices.copy(), ps.flg.copy()
+    pmcg.update_prop_rb(m, ps)
+    return dict(ps=ps, nok=nok, logw=logw, logSum=ls, wbar=wbar, perp=perp, ess=ess, lnev=lnev, X=X, idx=idx,
+                flg=flg)
+
+
+@pytest.mark.parametrize("df", [-1, 4])
+def test_dropin_iteration_fp64_matches_oracle(pmcg, oracle, df):
+    w, mu, cov, _ = small_mixture(K=6, D=4, df=df, seed=8)
+    wt, mut, covt, _ = small_mixture(K=3, D=4, df=-1, seed=9)
+    m = make_mix(pmcg, w, mu, cov, df)
+    om = oracle_mix(oracle, m)
+    target = make_mix(pmcg, wt, mut, covt, -1)
+    ot = oracle_mix(oracle, target)
+    bmin, bmax = np.full(4, -6.0), np.full(4, 6.0)
+    post = pmcg.Posterior(4, bmin, bmax).add_mix(target)
+    N, beta = 20011, 0.8
+    r = dropin_iteration(pmcg, m, post, N, 77, beta, (bmin, bmax), 0)
+    # oracle on the device sample
+    X, flg = r["X"], r["flg"].astype(np.int16)
+    logq, lt, Q = oracle.mix_logpdf(om, X, want_terms=True)
+    lp = oracle.mix_logpdf(ot, X) - np.sum(np.log(bmax - bmin))
+    lw = oracle.logweights(beta, lp, logq, flg)
+    np.testing.assert_allclose(r["logw"][flg == 1], lw[flg == 1], rtol=1e-12, atol=1e-9)
+    assert np.all(np.isneginf(r["logw"][flg == 0]))
+    wbar, ls, mw = oracle.normalize(lw, flg)
+    assert abs(r["logSum"] - ls) < 1e-10
+    np.testing.assert_allclose(r["wbar"], wbar, rtol=1e-9, atol=1e-15)
+    perp, ess = oracle.perplexity(wbar, flg)
+    assert abs(r["perp"] / perp - 1) < 1e-10 and abs(r["ess"] / ess - 1) < 1e-10
+    assert abs(r["lnev"] - (ls - np.log(N))) < 1e-10
+    new, dead = oracle.update_rb(om, X, wbar, flg, lt, logq, Q, r["idx"])
+    w2, mu2, L2 = m.arrays()
+    np.testing.assert_allclose(w2, new.w, rtol=1e-9, atol=1e-14)
+    live = dead == 0
+    np.testing.assert_allclose(mu2[live], new.mu[live], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(L2[live], new.L[live], rtol=1e-8, atol=1e-11)
+
+
+@pytest.mark.parametrize("tag", ["gauss", "t"])
+def test_update_prop_rb_golden(pmcg, tag):
+    """update_prop_rb on a host-built sample (normalised weights) vs the numpy EM."""
+    pmcg.set_dropin_precision(0)
+    df = META[f"em_{tag}_df"]
+    m = make_mix(pmcg, G[f"em_{tag}_w"], G[f"em_{tag}_mu"], G[f"em_{tag}_cov"], df)
+    X = G[f"em_{tag}_X"]
+    N, D = X.shape
+    ps = pmcg.PmcSimu(N, D)
+    ps.X[:] = X
+    ps.flg[:] = G[f"em_{tag}_flg"]
+    ps.indices[:] = G[f"em_{tag}_idx"]
+    ps.weights[:] = G[f"em_{tag}_wbar"]
+    ps.s.isLog = 0
+    ps.host_modified()
+    pmcg.update_prop_rb(m, ps)
+    w, mu, L = m.arrays()
+    dead = G[f"em_{tag}_dead"]
+    np.testing.assert_allclose(w, G[f"em_{tag}_nw"], rtol=1e-10, atol=1e-15)
+    live = dead == 0
+    np.testing.assert_allclose(mu[live], G[f"em_{tag}_nmu"][live], rtol=1e-9, atol=1e-12)
+    cov = np.einsum("kij,klj->kil", L, L)
+    np.testing.assert_allclose(cov[live], G[f"em_{tag}_ncov"][live], rtol=1e-9, atol=1e-12)
+    assert w[dead == 1].sum() == 0.0
+
+
+# ----------------------------------------------------------------- full runs
+def c1_small(pmcg, N, D=32, K=64, Kt=16):
+    wl = W.mixture_workload(D=D, K=K, Kt=Kt, seed=64)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = make_mix(pmcg, w, mu, cov, df)
+    target = make_mix(pmcg, wt, mut, covt, -1)
+    post = pmcg.Posterior(D).add_mix(target)
+    return prop, target, post
+
+
+def test_run_fp64_matches_oracle_three_iterations(pmcg, oracle):
+    prop, target, post = c1_small(pmcg, 0, D=12, K=16, Kt=4)
+    op = oracle_mix(oracle, prop)
+    ot = oracle_mix(oracle, target)
+    N = 30000
+    run = pmcg.Run(prop, post, N, precision=0, seed=42)
+    for it in range(3):
+        st = run.iterate(1.0)
+        so = oracle.iterate_mix(op, ot, 0.0, N, 42, it)
+        for key in ("ln_evidence", "perplexity", "ess", "enc", "logSum", "maxW"):
+            assert abs(st[key] - so[key]) <= 1e-8 * max(1.0, abs(so[key])), (it, key, st[key], so[key])
+        assert st["nok"] == so["nok"] and st["ndead"] == so["ndead"]
+        w, mu, L = run.proposal().arrays()
+        np.testing.assert_allclose(w, op.w, rtol=1e-8, atol=1e-13)
+        np.testing.assert_allclose(mu, op.mu, rtol=1e-8, atol=1e-9)
+        np.testing.assert_allclose(L, op.L, rtol=1e-7, atol=1e-9)
+        # continue both from the device proposal so that rounding cannot accumulate
+        op = oracle.Mix(w, mu, df=op.df, L=L)
+
+
+def weighted_moments(X, wbar):
+    m = wbar @ X
+    d = X - m
+    return m, (wbar[:, None] * d).T @ d
+
+
+def test_run_mixed_meets_precision_targets(pmcg, oracle):
+    """c1 shape (D=32, K=64, nu=3, condition 1e6) at reduced N: |dlogZ| <= 1e-3 and
+    posterior mean/covariance within 0.05 sigma of the FP64 path on the same draws."""
+    prop, target, post = c1_small(pmcg, 0)
+    N = 65536
+    r64 = pmcg.Run(prop, post, N, precision=0, seed=7)
+    r32 = pmcg.Run(prop, post, N, precision=1, seed=7)
+    for it in range(2):
+        s64 = r64.iterate(1.0)
+        s32 = r32.iterate(1.0)
+        assert abs(s64["ln_evidence"] - s32["ln_evidence"]) <= 1e-3, (it, s64, s32)
+        p64, p32 = r64.sample(), r32.sample()
+        np.testing.assert_array_equal(p64.indices, p32.indices)
+        wb64 = np.where(p64.flg == 1, np.exp(p64.weights - s64["logSum"]), 0.0)
+        wb32 = np.where(p32.flg == 1, np.exp(p32.weights - s32["logSum"]), 0.0)
+        m64, c64 = weighted_moments(p64.X, wb64)
+        m32, c32 = weighted_moments(p32.X, wb32)
+        sig = np.sqrt(np.diag(c64))
+        assert np.max(np.abs(m64 - m32) / sig) < 0.05
+        assert np.max(np.abs(c64 - c32) / np.outer(sig, sig)) < 0.05
+        # updated proposals agree too
+        w64, mu64, L64 = r64.proposal().arrays()
+        w32, mu32, L32 = r32.proposal().arrays()
+        live = (w64 > 0) & (w32 > 0)
+        sd = np.sqrt(np.diagonal(np.einsum("kij,klj->kil", L64, L64), axis1=1, axis2=2))
+        assert np.max(np.abs(mu64[live] - mu32[live]) / sd[live]) < 0.05
+        assert np.max(np.abs(w64 - w32)) < 1e-3
+
+
+def test_evidence_known_answer_normalised_target(pmcg):
+    """No prior box, normalised Gaussian-mixture target: log Z = 0."""
+    prop, target, post = c1_small(pmcg, 0, D=6, K=8, Kt=3)
+    run = pmcg.Run(prop, post, 200000, precision=1, seed=3)
+    for it in range(6):
+        st = run.iterate(1.0)
+    assert abs(st["ln_evidence"]) < 0.02, st
+    assert st["perplexity"] > 0.5
+
+
+@pytest.mark.skipif("demo1_mean" not in G.files, reason="reference demo targets not captured")
+@pytest.mark.parametrize("prec", PRECS)
+def test_reference_tempering_demos_unit_evidence(pmcg, prec):
+    """Demo/tempering 1 and 2 (unit box, normalised targets): evidence = 1."""
+    for tag, K in (("demo1", 3), ("demo2", 6)):
+        mean, cov = G[f"{tag}_mean"], G[f"{tag}_cov"]
+        target = make_mix(pmcg, np.full(len(mean), 1.0 / len(mean)), mean, cov, -1)
+        rng = np.random.default_rng(2)
+        prop = make_mix(pmcg, np.full(K, 1.0 / K), rng.uniform(0.2, 0.8, (K, 2)), np.array([np.eye(2) * 0.05] * K),
+                        -1)
+        bmin, bmax = np.zeros(2), np.ones(2)
+        post = pmcg.Posterior(2, bmin, bmax).add_mix(target)
+        run = pmcg.Run(prop, post, 20000, precision=prec, seed=11, box=pmcg.Parabox(bmin, bmax))
+        for it in range(8):
+            st = run.iterate(1.0)
+        assert abs(np.exp(st["ln_evidence"]) - 1.0) < 0.02, (tag, st)
+
+
+# ----------------------------------------------------------------- edge cases
+def test_all_samples_outside_box_raises(pmcg):
+    pmcg.set_dropin_precision(0)
+    m = make_mix(pmcg, [1.0], [[10.0, 10.0]], [np.eye(2) * 0.01], -1)
+    target = make_mix(pmcg, [1.0], [[0.0, 0.0]], [np.eye(2)], -1)
+    post = pmcg.Posterior(2, [-1, -1], [1, 1]).add_mix(target)
+    ps = pmcg.PmcSimu(257, 2)
+    nok = pmcg.simulate_mix_mvdens(ps, m, pmcg.Rng(1), pmcg.Parabox([-1, -1], [1, 1]))
+    assert nok == 0
+    with pytest.raises(pmcg.PmcgError) as e:
+        pmcg.importance_weights(ps, m, post, 1.0)
+    assert e.value.code == -9011
+
+
+def test_dead_component_is_buried(pmcg):
+    w = np.array([0.999, 0.001])
+    m = make_mix(pmcg, w, [[0.0, 0.0], [3.0, 3.0]], [np.eye(2), np.eye(2)], -1)
+    target = make_mix(pmcg, [1.0], [[0.0, 0.0]], [np.eye(2)], -1)
+    post = pmcg.Posterior(2).add_mix(target)
+    for prec in PRECS:
+        run = pmcg.Run(m, post, 5000, precision=prec, seed=5)
+        st = run.iterate(1.0)
+        w2, _, _ = run.proposal().arrays()
+        assert w2[1] == 0.0 and abs(w2[0] - 1.0) < 1e-15 and st["ndead"] == 1
+        assert abs(st["enc"] - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("N", [1, 31, 129, 4097])
+def test_ragged_sample_counts(pmcg, oracle, N):
+    w, mu, cov, _ = small_mixture(K=3, D=3)
+    m = make_mix(pmcg, w, mu, cov, -1)
+    om = oracle_mix(oracle, m)
+    X = np.random.default_rng(N).normal(size=(N, 3))
+    for prec, tol in ((0, 1e-10), (1, 1e-3)):
+        lq = pmcg.mix_log_pdf_batch(m, X, precision=prec)
+        np.testing.assert_allclose(lq, oracle.mix_logpdf(om, X), atol=tol, rtol=0)
+
+
+def test_runs_are_bit_reproducible(pmcg):
+    prop, target, post = c1_small(pmcg, 0, D=8, K=10, Kt=3)
+    out = []
+    for rep in range(2):
+        run = pmcg.Run(prop, post, 50000, precision=1, seed=9)
+        out.append([tuple(sorted(run.iterate(1.0).items())) for _ in range(2)])
+    assert out[0] == out[1]
+
+
+def test_tempered_weights(pmcg, oracle):
+    """beta multiplies the log-posterior only (log w = beta log pi - log q)."""
+    w, mu, cov, _ = small_mixture(K=3, D=2, seed=12)
+    m = make_mix(pmcg, w, mu, cov, -1)
+    target = make_mix(pmcg, [1.0], [[0.0, 0.0]], [np.eye(2)], -1)
+    post = pmcg.Posterior(2, [-10, -10], [10, 10]).add_mix(target)
+    r = dropin_iteration(pmcg, m, post, 4000, 5, 0.25, None, 0)
+    om = oracle_mix(oracle, make_mix(pmcg, w, mu, cov, -1))
+    X = r["X"]
+    lw = 0.25 * (oracle.mix_logpdf(oracle_mix(oracle, target), X) - np.log(400.0)) - oracle.mix_logpdf(om, X)
+    np.testing.assert_allclose(r["logw"], lw, rtol=1e-12, atol=1e-10)
