@@ -268,6 +268,13 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
     set_error(err, PMCG_EARG, __LINE__, "invalid SN data");
     return;
   }
+  const int ips[6] = {sd->ip_Omegam, sd->ip_Omegade, sd->ip_w0, sd->ip_M, sd->ip_alpha, sd->ip_beta};
+  for (int q = 0; q < 6; q++) {
+    if (ips[q] < -1 || ips[q] >= p->npar) {
+      set_error(err, PMCG_EARG, __LINE__, "SN parameter index %d outside [-1, %d)", ips[q], p->npar);
+      return;
+    }
+  }
   const int n = sd->nsn, G = sd->quad_nodes;
   std::vector<int> ix(n);
   for (int i = 0; i < n; i++) ix[i] = i;
