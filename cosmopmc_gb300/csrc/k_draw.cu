@@ -10,7 +10,7 @@ __device__ __forceinline__ void box_muller(double a, double b, Real &g0, Real &g
 
 template <>
 __device__ __forceinline__ void box_muller<double>(double a, double b, double &g0, double &g1) {
-  double r = sqrt(-2.0 * log(1.0 - a));
+  double r = sqrt(-2.0 * log1p(-a));
   double sn, cs;
   sincospi(2.0 * b, &sn, &cs);
   g0 = r * cs;
@@ -18,7 +18,7 @@ __device__ __forceinline__ void box_muller<double>(double a, double b, double &g
 }
 template <>
 __device__ __forceinline__ void box_muller<float>(double a, double b, float &g0, float &g1) {
-  float r = sqrtf(-2.0f * logf((float)(1.0 - a)));
+  float r = sqrtf(-2.0f * log1pf(-(float)a));
   float sn, cs;
   sincospif((float)(2.0 * b), &sn, &cs);
   g0 = r * cs;

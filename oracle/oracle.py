@@ -302,8 +302,9 @@ def update_rb(mix: Mix, X, wbar, flg, lt, logq, Q, idx, band_limit=None):
 
 
 def iterate_mix(prop: Mix, target: Mix, logprior, N, seed, call, beta=1.0, bmin=None, bmax=None,
-                want_sample=False):
-    """One whole FP64 iteration with a Gaussian-mixture target; prop updated in place."""
+                want_sample=False, check=True):
+    """One whole FP64 iteration with a Gaussian-mixture target; prop updated in place.
+    check=False keeps going when the update buries every component (the work is done)."""
     st = Stats()
     X = np.empty((N, prop.D)) if want_sample else None
     logw = np.empty(N) if want_sample else None
@@ -314,7 +315,7 @@ def iterate_mix(prop: Mix, target: Mix, logprior, N, seed, call, beta=1.0, bmin=
                                target.K, target.df, target.w, target.mu, target.L, target.logdetL,
                                float(logprior), _ptr(bmin_a), _ptr(bmax_a), N, seed, call, beta,
                                C.byref(st), _ptr(X), _ptr(logw), _ptr(idx))
-    if rc:
+    if rc and check:
         raise ValueError(f"oracle iteration failed ({rc})")
     stats = {f: getattr(st, f) for f, _ in Stats._fields_}
     return (stats, X, logw, idx) if want_sample else stats

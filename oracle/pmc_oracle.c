@@ -85,7 +85,7 @@ void orc_randoms(uint64_t seed, uint32_t call, size_t n0, size_t N, int D, int n
       ctr[0] = 1u + (uint32_t)m;
       orc_philox(ctr, key, o);
       double a = u53(o[0], o[1]), b = u53(o[2], o[3]);
-      double r = sqrt(-2.0 * log(1.0 - a));
+      double r = sqrt(-2.0 * log1p(-a));
       double t = 2.0 * ORC_PI * b;
       double g[2] = {r * cos(t), r * sin(t)};
       for (int e = 0; e < 2; e++) {

@@ -134,7 +134,13 @@ def test_sn_740_vs_oracle_and_loitering(pmcg, oracle):
     ll32, flg32 = post.log_pdf_batch(P, precision=1)
     both = good & (flg32 == 1)
     assert np.sum(flg32 != ok) <= 2
-    assert np.max(np.abs(ll32[both] - ll[both]) / np.maximum(1.0, np.abs(ll[both]))) < 1e-5
+    # FP32 integrand nodes: the error grows with chi^2 (relative 3e-5 far from the truth) ...
+    assert np.max(np.abs(ll32[both] - ll[both]) / np.maximum(1.0, np.abs(ll[both]))) < 3e-5
+    # ... and stays below 2e-3 absolute near the truth (chi^2 ~ N_SN)
+    truth = np.array([0.3, 0.7, -1.0, -19.1, 0.14, 3.1])[None, :]
+    l64, _ = post.log_pdf_batch(truth, precision=0)
+    l32, _ = post.log_pdf_batch(truth, precision=1)
+    assert abs(l64[0] - l32[0]) < 2e-3
 
 
 def test_template_golden_and_c2_shape(pmcg, oracle):
