@@ -5,11 +5,16 @@
 
 namespace pmcg {
 
+// Box-Muller pair from one Philox block. FP64 path: two 53-bit uniforms (the
+// oracle's mapping). FP32 path: the same 53-bit integers, 1-a and b, rounded
+// once to float (integer conversions, no FP64 arithmetic), so its normals equal
+// the FP64 ones to single precision, tails included.
 template <typename Real>
-__device__ __forceinline__ void box_muller(double a, double b, Real &g0, Real &g1);
+__device__ __forceinline__ void box_muller(P4 o, Real &g0, Real &g1);
 
 template <>
-__device__ __forceinline__ void box_muller<double>(double a, double b, double &g0, double &g1) {
+__device__ __forceinline__ void box_muller<double>(P4 o, double &g0, double &g1) {
+  double a = u53(o.x, o.y), b = u53(o.z, o.w);
   double r = sqrt(-2.0 * log1p(-a));
   double sn, cs;
   sincospi(2.0 * b, &sn, &cs);
@@ -17,10 +22,15 @@ __device__ __forceinline__ void box_muller<double>(double a, double b, double &g
   g1 = r * sn;
 }
 template <>
-__device__ __forceinline__ void box_muller<float>(double a, double b, float &g0, float &g1) {
-  float r = sqrtf(-2.0f * log1pf(-(float)a));
+__device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
+  const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
+  const unsigned long long B = ((unsigned long long)(o.z >> 5) << 26) | (unsigned long long)(o.w >> 6);
+  const float two53inv = 1.1102230246251565e-16f;  // 2^-53
+  const float oma = __ull2float_rn((1ull << 53) - A) * two53inv;  // 1 - a in (0, 1]
+  const float b = __ull2float_rn(B) * two53inv;
+  float r = sqrtf(-2.0f * logf(oma));
   float sn, cs;
-  sincospif((float)(2.0 * b), &sn, &cs);
+  sincospif(2.0f * b, &sn, &cs);
   g0 = r * cs;
   g1 = r * sn;
 }
@@ -79,7 +89,7 @@ __global__ void __launch_bounds__(128) draw_kernel(DevMixView m, size_t N, uint3
           P4 c = {1u + (uint32_t)mm, nlo, nhi, call};
           P4 o = philox4x32_10(c, key0, key1);
           Real g0, g1;
-          box_muller<Real>(u53(o.x, o.y), u53(o.z, o.w), g0, g1);
+          box_muller<Real>(o, g0, g1);
           z[2 * mm] = g0;
           if (2 * mm + 1 < D) {
             z[2 * mm + 1] = g1;
@@ -97,22 +107,24 @@ __global__ void __launch_bounds__(128) draw_kernel(DevMixView m, size_t N, uint3
         P4 c = {1u + (uint32_t)(j / 2), nlo, nhi, call};
         P4 o = philox4x32_10(c, key0, key1);
         Real g0, g1;
-        box_muller<Real>(u53(o.x, o.y), u53(o.z, o.w), g0, g1);
+        box_muller<Real>(o, g0, g1);
         c2 += g0 * g0;
         if (j + 1 < D + nu) c2 += g1 * g1;
       }
     }
     const Real sc = (df > 0) ? (Real)sqrt((double)df / (double)c2) : (Real)1;
-    const double *Lk = m.L + (size_t)k * D * D;
-    const double *mk = m.mu + (size_t)k * D;
+    // Factor and mean in the arithmetic type of the path (no per-element conversions).
+    const Real *Lk = (sizeof(Real) == 8) ? (const Real *)(m.L + (size_t)k * D * D)
+                                         : (const Real *)(m.L32 + (size_t)k * D * D);
+    const Real *mk = (sizeof(Real) == 8) ? (const Real *)(m.mu + (size_t)k * D) : (const Real *)(m.mu32 + (size_t)k * D);
     int in = 1;
 #pragma unroll
     for (int i = 0; i < MAXD; i++) {
       if (i < D) {
         Real acc = (Real)0;
 #pragma unroll
-        for (int j = 0; j <= i; j++) acc += (Real)Lk[i * D + j] * z[j];
-        Real xi = (Real)mk[i] + sc * acc;
+        for (int j = 0; j <= i; j++) acc += __ldg(&Lk[i * D + j]) * z[j];
+        Real xi = __ldg(&mk[i]) + sc * acc;
         s_x[threadIdx.x * ldo + i] = xi;
         if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
       }

@@ -105,35 +105,50 @@ __global__ void __launch_bounds__(256) em_stats_f64_kernel(DevMixView m, size_t 
 }
 
 // ------------------------------------------------------------------ FP32 statistics
-// Augmented rows a = [x-c (padded to Dp), 1, 1/tau, 0, 0] with weight vt: the
-// lower triangle of sum vt a a^T holds S2, S1 (row Dp), St (Dp,Dp) and S0
-// (Dp+1,Dp). Each thread owns one 4x4 block of that triangle for one sample
-// group; products are FP32 and each thread's FP32 sums are flushed into FP64
-// every kFlushTiles tiles.
+// Mixed path: the statistics are accumulated in each component's whitened
+// frame a = L_k^-1 (x - mu_k) (entries O(1)), because a covariance of
+// condition 1e6 cannot even be represented to its small eigenvalues in FP32
+// in the raw frame. The finalise kernel maps them back in FP64:
+// mu' = mu + L d_w, Sigma' = L Sigma_w L^T.
+//
+// Per tile of 64 samples: x rows are staged (row stride ldx+1: conflict-free
+// column reads), then whitened with L^-1 staged transposed (float4 broadcasts,
+// warps paired over i-blocks so every warp does the same number of steps).
+// The augmented rows a = [a (padded to Dp), 1, 1/tau, 0, 0] with weight vt give,
+// in the lower triangle of sum vt a a^T, S2 (whitened), S1 (row Dp), St (Dp,Dp)
+// and S0 (Dp+1,Dp). Each thread owns one 4x4 block for one sample group; FP32
+// sums are flushed into FP64 every kFlushTiles tiles.
 constexpr int kTile32 = 64;
-constexpr int kFlushTiles = 32;
+constexpr int kFlushTiles = 16;
 
 __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t N, int S,
                                                            const float *__restrict__ X,
-                                                           const double *__restrict__ logw,
-                                                           const double *__restrict__ logq,
+                                                           const float *__restrict__ aw,
                                                            const float *__restrict__ lt,
-                                                           const float *__restrict__ Qv, const DevStats *st,
+                                                           const float *__restrict__ Qv,
                                                            double *__restrict__ part) {
-  const int k = blockIdx.y, s = blockIdx.x, D = m.D, E = em_E(D);
+  const int k = blockIdx.x, s = blockIdx.y, D = m.D, E = em_E(D);
   if (m.w[k] <= 0.0) return;
-  const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2;
+  const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, nib = Dp / 4;
+  const int ldt = Dp + 1;  // padded x-tile row stride
   const int G = blockDim.x / NB;
   extern __shared__ float4 smf4[];
-  float *sa = reinterpret_cast<float *>(smf4);  // kTile32 * Da
-  float *svt = sa + kTile32 * Da;               // kTile32
+  float *sWT = reinterpret_cast<float *>(smf4);   // [Dp][Dp]  (L^-1)^T
+  float *sb = sWT + Dp * Dp;                      // [Dp]      L^-1 mu
+  float *sa = sb + Dp;                            // [kTile32][Da] augmented whitened rows
+  float *sx = sa + kTile32 * Da;                  // [kTile32][ldt] raw rows
+  float *svt = sx + kTile32 * ldt;                // [kTile32]
   const size_t chunk = (N + S - 1) / S;
   const size_t n0 = (size_t)s * chunk, n1 = (n0 + chunk < N) ? n0 + chunk : N;
-  const double logSum = st->logSum;
-  const double *ck = m.mu + (size_t)k * D;
   const float nu = (float)m.df, rnd = 1.0f / ((float)m.df + (float)D);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
 
-  const int tid = threadIdx.x;
+  for (int e = tid; e < Dp * Dp; e += blockDim.x) {
+    int i = e / Dp, j = e - i * Dp;  // sWT[j][i] = W[i][j]
+    sWT[j * Dp + i] = (i < D) ? m.W32[(size_t)k * D * Dp + (size_t)i * Dp + j] : 0.f;
+  }
+  for (int i = tid; i < Dp; i += blockDim.x) sb[i] = (i < D) ? m.b32[(size_t)k * D + i] : 0.f;
+
   const int blk = tid % NB, grp = tid / NB;
   const bool active = grp < G;
   int bi = 0;
@@ -151,18 +166,13 @@ __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t 
     if (tid < kTile32) {
       float vt = 0.f, itau = 1.f;
       if (tid < nt) {
-        size_t n = t0 + tid;
-        double lw = logw[n];
-        if (lw > -INFINITY) {
-          float e = (float)(lw - logSum - logq[n]) + lt[(size_t)k * N + n];
-          float v = expf(e);
-          if (m.df > 0) {
-            float q = Qv[(size_t)k * N + n];
-            itau = (nu + q) * rnd;
-            vt = v / itau;
-          } else {
-            vt = v;
-          }
+        const size_t n = t0 + tid;
+        const float v = expf(aw[n] + lt[(size_t)k * N + n]);  // aw = -inf where flg == 0
+        if (m.df > 0) {
+          itau = (nu + Qv[(size_t)k * N + n]) * rnd;
+          vt = v / itau;
+        } else {
+          vt = v;
         }
       }
       svt[tid] = vt;
@@ -173,10 +183,27 @@ __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t 
       row[Dp + 3] = 0.f;
     }
     for (int e = tid; e < kTile32 * Dp; e += blockDim.x) {
-      int r = e / Dp, i = e - r * Dp;
-      float v = 0.f;
-      if (r < nt && i < D) v = X[(t0 + r) * Dp + i] - (float)ck[i];
-      sa[r * Da + i] = v;
+      const int r = e / Dp, i = e - r * Dp;
+      sx[r * ldt + i] = (r < nt) ? X[(t0 + r) * Dp + i] : 0.f;
+    }
+    __syncthreads();
+    // whitening: unit u = (i-block ib, half h of the tile); warp w takes units
+    // (w, 0) and (nib-1-w, 1) so the triangular lengths balance.
+    for (int u = warp; u < 2 * nib; u += nwarp) {
+      const int pair = u % nib, half = u / nib;
+      const int ib = half == 0 ? pair : nib - 1 - pair;
+      const int r = half * 32 + lane;
+      float o0 = -sb[4 * ib], o1 = -sb[4 * ib + 1], o2 = -sb[4 * ib + 2], o3 = -sb[4 * ib + 3];
+      const float *xr = sx + r * ldt;
+      const int jmax = 4 * ib + 4;
+      for (int j = 0; j < jmax; j++) {
+        const float xv = xr[j];
+        const float4 w4 = *reinterpret_cast<const float4 *>(sWT + j * Dp + 4 * ib);
+        o0 = fmaf(w4.x, xv, o0); o1 = fmaf(w4.y, xv, o1); o2 = fmaf(w4.z, xv, o2); o3 = fmaf(w4.w, xv, o3);
+      }
+      float *ar = sa + r * Da + 4 * ib;
+      const bool live = r < nt;
+      ar[0] = live ? o0 : 0.f; ar[1] = live ? o1 : 0.f; ar[2] = live ? o2 : 0.f; ar[3] = live ? o3 : 0.f;
     }
     __syncthreads();
     if (active) {
@@ -225,6 +252,17 @@ __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t 
   }
 }
 
+// Per-sample single-precision weight factor of the mixed EM:
+// aw = log w - logSum - log q (-inf where flg == 0), one FP64 subtraction per sample.
+__global__ void em_weight_factor_kernel(size_t N, const double *__restrict__ logw, const double *__restrict__ logq,
+                                        const DevStats *__restrict__ st, float *__restrict__ aw) {
+  const double ls = st->logSum;
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (size_t)gridDim.x * blockDim.x) {
+    const double l = logw[n];
+    aw[n] = (l > -INFINITY) ? (float)(l - ls - logq[n]) : -INFINITY;
+  }
+}
+
 size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N) {
   int S = (8 * 152 + K - 1) / K;
   size_t maxS = (N + 2047) / 2048;
@@ -238,14 +276,18 @@ size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N) {
 // ------------------------------------------------------------------ finalise
 // One block per component: fixed-order sum of the chunk partials, new mean
 // and covariance, band limit, FP64 Cholesky; the dead rule buries the
-// component (weight 0, parameters kept).
+// component (weight 0, parameters kept). With whitened statistics (mixed
+// path) the moments are mapped back with the old factor: mu' = mu + L d,
+// Sigma' = L Sigma_w L^T, all in FP64.
 __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *L, size_t N, int S,
                                    const double *__restrict__ part, const int *__restrict__ counts,
-                                   int band_limit) {
+                                   int band_limit, int whitened) {
   const int k = blockIdx.x, D = m.D, E = em_E(D);
   extern __shared__ double sh[];
   double *st = sh;             // E
-  double *C = sh + E;          // D*D
+  double *C = st + E;          // D*D
+  double *Lo = C + D * D;      // D*D old factor (whitened only)
+  double *T = Lo + D * D;      // D*D scratch (whitened only)
   __shared__ int s_dead;
   __shared__ double s_piv;
   if (m.w[k] <= 0.0) {
@@ -272,11 +314,43 @@ __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *
     int i = e / D, j = e - i * D;
     int a = i > j ? i : j, b = i > j ? j : i;
     double di = st[2 + i] / St, dj = st[2 + j] / St;
-    double c = (st[2 + D + tri_idx(a, b)] - St * di * dj) / S0;
-    if (band_limit > 0 && (a - b) >= band_limit) c = 0.0;
-    C[e] = c;
+    C[e] = (st[2 + D + tri_idx(a, b)] - St * di * dj) / S0;
+    if (whitened) Lo[e] = (j <= i) ? m.L[(size_t)k * D * D + e] : 0.0;
   }
   __syncthreads();
+  if (whitened) {
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // T = Lo C
+      int i = e / D, j = e - i * D;
+      double t = 0.0;
+      for (int q = 0; q <= i; q++) t += Lo[i * D + q] * C[q * D + j];
+      T[e] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // C = T Lo^T
+      int i = e / D, j = e - i * D;
+      double t = 0.0;
+      for (int q = 0; q <= j; q++) t += T[i * D + q] * Lo[j * D + q];
+      C[e] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // symmetrise exactly
+      int i = e / D, j = e - i * D;
+      if (j < i) { double v = 0.5 * (C[i * D + j] + C[j * D + i]); T[e] = v; }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      int i = e / D, j = e - i * D;
+      if (j < i) { C[i * D + j] = T[e]; C[j * D + i] = T[e]; }
+    }
+    __syncthreads();
+  }
+  if (band_limit > 0 && band_limit < D) {
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      int i = e / D, j = e - i * D;
+      if ((i > j ? i - j : j - i) >= band_limit) C[e] = 0.0;
+    }
+    __syncthreads();
+  }
   // in-place Cholesky, column by column
   for (int j = 0; j < D; j++) {
     if (threadIdx.x == 0) {
@@ -298,11 +372,21 @@ __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *
     if (threadIdx.x == 0) w[k] = 0.0;
     return;
   }
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    double d;
+    if (whitened) {
+      d = 0.0;
+      for (int q = 0; q <= i; q++) d += Lo[i * D + q] * (st[2 + q] / St);
+    } else {
+      d = st[2 + i] / St;
+    }
+    mu[(size_t)k * D + i] = m.mu[(size_t)k * D + i] + d;
+  }
+  __syncthreads();
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
     int i = e / D, j = e - i * D;
     L[(size_t)k * D * D + e] = (j <= i) ? C[e] : 0.0;
   }
-  for (int i = threadIdx.x; i < D; i += blockDim.x) mu[(size_t)k * D + i] = m.mu[(size_t)k * D + i] + st[2 + i] / St;
   if (threadIdx.x == 0) w[k] = S0;
 }
 
@@ -333,35 +417,39 @@ __global__ void em_renorm_kernel(int K, double *w, DevStats *st) {
 cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, const float *X32,
                       const double *logw, const double *logq, const double *lt64, const double *Q64,
                       const float *lt32, const float *Q32, const int *counts, double *partials, int S,
-                      DevStats *st, int band_limit, cudaStream_t s) {
+                      DevStats *st, int band_limit, float *aw32, cudaStream_t s) {
   DevMixView v = m.view();
   const int D = m.D, E = em_E(D);
-  dim3 grid(S, m.K);
   cudaError_t e;
   if (precision == 0) {
     if (E > 10 * 256) return cudaErrorInvalidValue;
     size_t smem = (size_t)(kTile64 * D + 2 * kTile64) * sizeof(double);
-    em_stats_f64_kernel<<<grid, 256, smem, s>>>(v, N, S, X64, logw, logq, lt64, Q64, st, partials);
+    em_stats_f64_kernel<<<dim3(S, m.K), 256, smem, s>>>(v, N, S, X64, logw, logq, lt64, Q64, st, partials);
   } else {
     const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2;
     if (NB > 256) return cudaErrorInvalidValue;
     const int G = 256 / NB;
-    size_t smem_tile = (size_t)(kTile32 * Da + kTile32) * sizeof(float);
+    unsigned fgrid = (unsigned)((N + 255) / 256 < 2048 ? (N + 255) / 256 : 2048);
+    em_weight_factor_kernel<<<fgrid, 256, 0, s>>>(N, logw, logq, st, aw32);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    size_t smem_tile = (size_t)(Dp * Dp + Dp + kTile32 * Da + kTile32 * (Dp + 1) + kTile32) * sizeof(float);
     size_t smem_red = (size_t)G * NB * 16 * sizeof(double);
     size_t smem = smem_tile > smem_red ? smem_tile : smem_red;
     if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(em_stats_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    em_stats_f32_kernel<<<grid, 256, smem, s>>>(v, N, S, X32, logw, logq, lt32, Q32, st, partials);
+    // component-fastest grid: the blocks of one sample chunk run together and share it in L2
+    em_stats_f32_kernel<<<dim3(m.K, S), 256, smem, s>>>(v, N, S, X32, aw32, lt32, Q32, partials);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  size_t fsmem = (size_t)(E + D * D) * sizeof(double);
+  const int whitened = precision != 0;
+  size_t fsmem = (size_t)(E + (whitened ? 3 : 1) * D * D) * sizeof(double);
   if (fsmem > 48 * 1024) {
     e = cudaFuncSetAttribute(em_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
     if (e != cudaSuccess) return e;
   }
-  em_finalize_kernel<<<m.K, 128, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit);
+  em_finalize_kernel<<<m.K, 128, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit, whitened);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   em_renorm_kernel<<<1, 32, 0, s>>>(m.K, m.w, st);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -13,7 +13,7 @@ cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.K = K; m.D = D; m.df = df; m.ldx = round4(D);
   const int T = D * (D + 1) / 2;
   size_t nd = (size_t)K * (1 + 1 + D + D * D + T + D + 1 + 1);
-  size_t nf = (size_t)K * ((size_t)D * m.ldx + D + 1);
+  size_t nf = (size_t)K * ((size_t)D * m.ldx + D + 1 + (size_t)D * D + D + 3);
   size_t bytes = nd * sizeof(double) + nf * sizeof(float) + 256;
   cudaError_t e = cudaMalloc(&m.arena, bytes);
   if (e != cudaSuccess) { m.arena = nullptr; return e; }
@@ -29,7 +29,9 @@ cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   float *f = (float *)p;
   m.W32 = f; f += (size_t)K * D * m.ldx;
   m.b32 = f; f += (size_t)K * D;
-  m.lconst32 = f;
+  m.lconst32 = f; f += K;
+  m.L32 = f; f += (size_t)K * D * D;
+  m.mu32 = f;
   return cudaSuccess;
 }
 
@@ -40,13 +42,18 @@ void devmix_free(DevMix &m) {
 
 // Per component: W = L^-1 by column substitution, b = W mu, log|L|.
 __global__ void mix_prepare_comp_kernel(DevMixView m, double *logdetL, double *Wt, double *b, float *W32,
-                                        float *b32) {
+                                        float *b32, float *L32, float *mu32) {
   const int k = blockIdx.x, D = m.D, T = D * (D + 1) / 2, ldx = m.ldx;
   extern __shared__ double s[];
   double *sL = s;            // D*D
   double *sW = s + D * D;    // D*D
   const double *Lk = m.L + (size_t)k * D * D;
-  for (int e = threadIdx.x; e < D * D; e += blockDim.x) { sL[e] = Lk[e]; sW[e] = 0.0; }
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    sL[e] = Lk[e];
+    sW[e] = 0.0;
+    L32[(size_t)k * D * D + e] = (float)Lk[e];
+  }
+  for (int i = threadIdx.x; i < D; i += blockDim.x) mu32[(size_t)k * D + i] = (float)m.mu[(size_t)k * D + i];
   __syncthreads();
   for (int j = threadIdx.x; j < D; j += blockDim.x) {
     sW[j * D + j] = 1.0 / sL[j * D + j];
@@ -107,7 +114,7 @@ __global__ void mix_prepare_consts_kernel(DevMixView m, const double *logdetL, d
 cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   DevMixView v = m.view();
   size_t smem = 2 * (size_t)m.D * m.D * sizeof(double);
-  mix_prepare_comp_kernel<<<m.K, 64, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32);
+  mix_prepare_comp_kernel<<<m.K, 64, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mix_prepare_consts_kernel<<<1, 256, 0, s>>>(v, m.logdetL, m.cw, m.lconst, m.lconst32);

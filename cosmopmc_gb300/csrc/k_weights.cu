@@ -54,10 +54,20 @@ __global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, con
   }
 }
 
-__global__ void weights_final_kernel(int nb, const WRed *__restrict__ partials, size_t N, DevStats *st) {
+// One block of 256 threads: each thread merges a strided subset of the partials,
+// then a shuffle tree and a sequential pass over the 8 warps (fixed order).
+__global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *__restrict__ partials, size_t N,
+                                                            DevStats *st) {
+  __shared__ WRed s_r[8];
+  WRed a = wred_empty();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge(a, partials[b]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = wred_merge(a, wred_shfl(a, o));
+  if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = a;
+  __syncthreads();
   if (threadIdx.x != 0) return;
-  WRed a = partials[0];
-  for (int b = 1; b < nb; b++) a = wred_merge(a, partials[b]);
+  a = s_r[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge(a, s_r[w]);
   if (a.n == 0.0 || a.m == -INFINITY) {
     st->status = -9011;  // PMCG_ENOWEIGHT
     st->nok = 0.0;
@@ -80,7 +90,7 @@ cudaError_t launch_weights(size_t N, double beta, const double *logpost, const d
   weights_kernel<<<kWeightBlocks, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  weights_final_kernel<<<1, 32, 0, s>>>(kWeightBlocks, partials, N, st);
+  weights_final_kernel<<<1, 256, 0, s>>>(kWeightBlocks, partials, N, st);
   return cudaGetLastError();
 }
 

@@ -75,7 +75,7 @@ struct Work {
   short *flg = nullptr;
   double *logq = nullptr, *logpost = nullptr, *logw = nullptr, *wbar = nullptr;
   double *lt64 = nullptr, *Q64 = nullptr;
-  float *lt32 = nullptr, *Q32 = nullptr;
+  float *lt32 = nullptr, *Q32 = nullptr, *aw32 = nullptr;
   WRed *wpart = nullptr;
   double *empart = nullptr;
   DevStats *dstats = nullptr, *hstats = nullptr;
@@ -117,6 +117,7 @@ static bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error 
     w.Q64 = (!prec && t) ? c.take<double>(N * K) : nullptr;
     w.lt32 = prec ? c.take<float>(N * K) : nullptr;
     w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
+    w.aw32 = prec ? c.take<float>(N) : nullptr;
     w.wpart = c.take<WRed>(kWeightBlocks);
     w.empart = c.take<double>(empart_bytes / sizeof(double));
     w.dstats = c.take<DevStats>(1);
@@ -185,9 +186,9 @@ static bool stage_weights(Work &w, double beta, bool with_logq, error **err) {
 }
 
 static bool stage_em(Work &w, error **err) {
-  w.launches += 5;
+  w.launches += w.prec ? 6 : 5;
   return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
-                      w.empart, w.S, w.dstats, w.D, w.s),
+                      w.empart, w.S, w.dstats, w.D, w.aw32, w.s),
             "EM kernels");
 }
 

@@ -25,13 +25,13 @@ struct DevMix {
   int K = 0, D = 0, df = -1, ldx = 0;
   double *w = nullptr, *cw = nullptr, *mu = nullptr, *L = nullptr, *Wt = nullptr, *b = nullptr;
   double *logdetL = nullptr, *lconst = nullptr;
-  float *W32 = nullptr, *b32 = nullptr, *lconst32 = nullptr;
+  float *W32 = nullptr, *b32 = nullptr, *lconst32 = nullptr, *L32 = nullptr, *mu32 = nullptr;
   void *arena = nullptr;
   DevMixView view() const {
     DevMixView v;
     v.K = K; v.D = D; v.df = df; v.ldx = ldx;
     v.w = w; v.cw = cw; v.mu = mu; v.L = L; v.Wt = Wt; v.b = b; v.lconst = lconst;
-    v.W32 = W32; v.b32 = b32; v.lconst32 = lconst32;
+    v.W32 = W32; v.b32 = b32; v.lconst32 = lconst32; v.L32 = L32; v.mu32 = mu32;
     return v;
   }
 };
@@ -66,7 +66,7 @@ size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);
 cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, const float *X32,
                       const double *logw, const double *logq, const double *lt64, const double *Q64,
                       const float *lt32, const float *Q32, const int *counts, double *partials, int S,
-                      DevStats *st, int band_limit, cudaStream_t s);
+                      DevStats *st, int band_limit, float *aw32, cudaStream_t s);
 
 // Convert the mixed-precision sample to FP64 row-major.
 cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
