@@ -85,6 +85,14 @@ class IterStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class WeightStats(C.Structure):
+    _fields_ = [("logSum", C.c_double), ("maxW", C.c_double), ("ln_evidence", C.c_double),
+                ("perplexity", C.c_double), ("ess", C.c_double), ("nok", C.c_size_t)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 PErr = C.POINTER(C.POINTER(Error))
 _dp = C.POINTER(C.c_double)
 LOGPDF_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, _dp, PErr)
@@ -153,6 +161,8 @@ SIGNATURES = [
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
     ("pmcg_run_stage_ms", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
+    ("pmcg_importance_weights_noalloc", None, [C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.POINTER(WeightStats), C.c_void_p, PErr]),
     ("pmcg_version", C.c_char_p, []),
     ("pmcg_device_count", C.c_int, []),
     ("pmcg_device_synchronize", None, [PErr]),

@@ -307,6 +307,27 @@ int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage);
 /* Number of kernel launches issued by the last pmcg_run_iterate call. */
 int pmcg_run_last_launches(const pmcg_run *r);
 
+/* ------------------------------------------------------------------ *
+ * Part 2 — importance weights without allocation                      *
+ * ------------------------------------------------------------------ */
+/* No counterpart in the reference. For callers that cannot let a library
+ * allocate device memory (code inside another framework's memory pool,
+ * serving loops where an allocation would synchronise the device, runtimes
+ * that forbid driver allocations after start-up): the caller passes device
+ * arrays logpost[N], logq[N], flg[N] (in/out) and logw[N] (out); the
+ * log-weights (beta*logpost - logq, -inf and flg=0 where not finite) are
+ * written on `stream` (NULL = default stream) and the scalars are returned in
+ * *stats (host). The partial sums use a fixed device array inside the library
+ * (one per GPU, held until exit), which limits N to 8,388,608 (larger N:
+ * PMCG_EDIM). The first call on a device looks the array up; make it before
+ * any stream capture. Calls that overlap on the GPU share that array and race. */
+typedef struct {
+  double logSum, maxW, ln_evidence, perplexity, ess;
+  size_t nok;
+} pmcg_weight_stats;
+void pmcg_importance_weights_noalloc(size_t N, double beta, const double *logpost, const double *logq, short *flg,
+                                     double *logw, pmcg_weight_stats *stats, void *stream, error **err);
+
 /* Library / device information. */
 const char *pmcg_version(void);
 int pmcg_device_count(void);
