@@ -1,0 +1,509 @@
+// k_batch.cu — many independent PMC runs, one persistent launch per iteration.
+//
+// A batch holds runs of uneven dimension, component count, sample count and
+// likelihood (mixture, SN Ia or template target), all mixed precision. One
+// iteration of every run is one cooperative kernel: eleven stages (draw, log q,
+// log posterior, weight tiles, weight merge, EM weight factor, EM statistics,
+// EM finalise, renormalise, mixture preparation, constants), separated by grid
+// barriers. In each stage the blocks walk a flat list of work items
+// (per-run tiles, components or runs); a block finds its run by a binary
+// search over the stage's prefix table. The per-item work is the same body the
+// single-run kernels execute, with the same tiling, so each run's results are
+// bit-identical alone and inside any batch.
+//
+// The launch, the upload of the per-iteration parameters (random-stream call,
+// beta) and the download of every run's statistics are captured once in a CUDA
+// graph. The samples per thread of the log-density stages and the resident
+// blocks per SM are picked by an autotuner that times the non-mutating stages
+// (draw, log q, log posterior) and caches the choice per batch shape.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "pmcg_bodies.cuh"
+#include "pmcg_engine.h"
+
+namespace cg = cooperative_groups;
+
+namespace pmcg {
+
+enum BatchStage {
+  kBDraw = 0, kBLogq, kBLogpost, kBWeights, kBWFinal, kBFactor, kBEmStats, kBEmFinal, kBRenorm, kBPrepComp,
+  kBPrepConsts, kBStages
+};
+
+struct BatchDesc {
+  DevMixView prop;
+  int ptype;
+  DevMixView target;
+  SnDev sn;
+  TplDev tpl;
+  double logpr;
+  size_t N;
+  int S, CHp, CHt, maxd;
+  uint32_t key0, key1;
+  const double *bmin, *bmax;
+  float *X32;
+  int *idx, *counts;
+  short *flg;
+  double *logq, *logpost, *logw;
+  float *lt32, *Q32, *aw32;
+  WRed *wpart;
+  double *empart;
+  DevStats *st;
+  double *w, *mu, *L, *Wt, *b, *logdetL, *cw, *lconst;
+  float *W32, *b32, *lconst32, *L32, *mu32;
+};
+
+struct BatchDyn {
+  double beta;
+  uint32_t call;
+  uint32_t pad;
+};
+
+__device__ __forceinline__ int find_run(const uint32_t *__restrict__ pre, int R, uint32_t item) {
+  int lo = 0, hi = R;  // largest lo with pre[lo] <= item
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pre[mid] <= item) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int SPT>
+__device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const BatchDyn &dy, uint32_t li,
+                                           unsigned char *smem, WRed *s_r, int *s_dead, double *s_piv,
+                                           DevStats *stats_out, int r) {
+  const int D = d.prop.D, K = d.prop.K, ldx = d.prop.ldx;
+  switch (stg) {
+    case kBDraw: {
+      const size_t n0 = (size_t)li * blockDim.x;
+      if (d.maxd <= 8)
+        body_draw<8, float>(d.prop, d.N, d.key0, d.key1, dy.call, d.bmin, d.bmax, nullptr, nullptr, nullptr, nullptr,
+                            d.X32, d.idx, d.flg, d.counts, n0, smem);
+      else if (d.maxd <= 16)
+        body_draw<16, float>(d.prop, d.N, d.key0, d.key1, dy.call, d.bmin, d.bmax, nullptr, nullptr, nullptr,
+                             nullptr, d.X32, d.idx, d.flg, d.counts, n0, smem);
+      else
+        body_draw<32, float>(d.prop, d.N, d.key0, d.key1, dy.call, d.bmin, d.bmax, nullptr, nullptr, nullptr,
+                             nullptr, d.X32, d.idx, d.flg, d.counts, n0, smem);
+      break;
+    }
+    case kBLogq: {
+      float *sw = reinterpret_cast<float *>(smem);
+      if (d.maxd <= 8) body_mixlogpdf_f32<8, SPT>(d.prop, d.N, d.X32, d.logq, 0, 0.0, d.lt32, d.Q32, d.CHp, li, sw);
+      else if (d.maxd <= 16)
+        body_mixlogpdf_f32<16, SPT>(d.prop, d.N, d.X32, d.logq, 0, 0.0, d.lt32, d.Q32, d.CHp, li, sw);
+      else body_mixlogpdf_f32<32, SPT>(d.prop, d.N, d.X32, d.logq, 0, 0.0, d.lt32, d.Q32, d.CHp, li, sw);
+      break;
+    }
+    case kBLogpost: {
+      if (d.ptype == kPluginMix) {
+        float *sw = reinterpret_cast<float *>(smem);
+        if (d.maxd <= 8)
+          body_mixlogpdf_f32<8, SPT>(d.target, d.N, d.X32, d.logpost, 0, d.logpr, nullptr, nullptr, d.CHt, li, sw);
+        else if (d.maxd <= 16)
+          body_mixlogpdf_f32<16, SPT>(d.target, d.N, d.X32, d.logpost, 0, d.logpr, nullptr, nullptr, d.CHt, li, sw);
+        else
+          body_mixlogpdf_f32<32, SPT>(d.target, d.N, d.X32, d.logpost, 0, d.logpr, nullptr, nullptr, d.CHt, li, sw);
+      } else if (d.ptype == kPluginSn) {
+        const size_t n = (size_t)li * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        body_sn<true>(d.sn, d.N, D, nullptr, d.X32, ldx, d.logpost, d.flg, n, 1, d.logpr);
+      } else {
+        body_tpl<float>(d.tpl, d.N, nullptr, d.X32, ldx, d.logpost, d.flg, li, reinterpret_cast<float *>(smem), 1,
+                        d.logpr);
+      }
+      break;
+    }
+    case kBWeights:
+      body_weights_tile(d.N, dy.beta, d.logpost, d.logq, d.flg, d.logw, d.wpart, li, s_r);
+      break;
+    case kBWFinal:
+      body_weights_final((int)((d.N + kTileW - 1) / kTileW), d.wpart, d.N, d.st, s_r);
+      break;
+    case kBFactor:
+      body_em_factor(d.N, d.logw, d.logq, d.st, d.aw32, li);
+      break;
+    case kBEmStats:
+      body_em_stats_f32(d.prop, d.N, d.S, d.X32, d.aw32, d.lt32, d.Q32, d.empart, (int)(li % K), (int)(li / K), smem);
+      break;
+    case kBEmFinal:
+      body_em_finalize(d.prop, d.w, d.mu, d.L, d.N, d.S, d.empart, d.counts, D, 1, (int)li, d.st,
+                       reinterpret_cast<double *>(smem), s_dead, s_piv);
+      break;
+    case kBRenorm:
+      body_em_renorm(K, d.w, d.st);
+      break;
+    case kBPrepComp:
+      body_prepare_comp(d.prop, d.logdetL, d.Wt, d.b, d.W32, d.b32, d.L32, d.mu32, (int)li,
+                        reinterpret_cast<double *>(smem));
+      break;
+    case kBPrepConsts:
+      body_prepare_consts(d.prop, d.logdetL, d.cw, d.lconst, d.lconst32);
+      for (int k = threadIdx.x; k < K; k += blockDim.x) d.counts[k] = 0;  // the next draw counts afresh
+      __syncthreads();
+      if (threadIdx.x == 0) stats_out[r] = *d.st;
+      break;
+    default:
+      break;
+  }
+}
+
+template <int SPT>
+__global__ void __launch_bounds__(256, 1) batch_kernel(const BatchDesc *__restrict__ descs,
+                                                       const BatchDyn *__restrict__ dyn, int R,
+                                                       const uint32_t *__restrict__ starts, int first, int last,
+                                                       DevStats *stats_out) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ WRed s_r[8];
+  __shared__ int s_dead;
+  __shared__ double s_piv;
+  for (int stg = first; stg <= last; stg++) {
+    const uint32_t *pre = starts + (size_t)stg * (R + 1);
+    const uint32_t total = pre[R];
+    for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+      const int r = find_run(pre, R, item);
+      batch_item<SPT>(stg, descs[r], dyn[r], item - pre[r], smem, s_r, &s_dead, &s_piv, stats_out, r);
+      __syncthreads();
+    }
+    if (stg < last) grid.sync();
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static size_t items_of(int stg, const BatchDesc &d, int spt, int threads) {
+  const size_t N = d.N;
+  const int K = d.prop.K;
+  switch (stg) {
+    case kBDraw: return (N + threads - 1) / threads;
+    case kBLogq: return (N + (size_t)threads * spt - 1) / ((size_t)threads * spt);
+    case kBLogpost:
+      if (d.ptype == kPluginMix) return (N + (size_t)threads * spt - 1) / ((size_t)threads * spt);
+      if (d.ptype == kPluginSn) return (N + (threads / 32) - 1) / (threads / 32);
+      return (N + threads - 1) / threads;
+    case kBWeights:
+    case kBFactor: return (N + kTileW - 1) / kTileW;
+    case kBEmStats: return (size_t)K * d.S;
+    case kBEmFinal:
+    case kBPrepComp: return (size_t)K;
+    default: return 1;
+  }
+}
+
+static size_t smem_of(const BatchDesc &d, int threads) {
+  const int D = d.prop.D, K = d.prop.K, ldx = d.prop.ldx;
+  size_t s = draw_smem<float>(K, ldx, threads);
+  s = std::max(s, (size_t)d.CHp * mix_cs(D, ldx) * sizeof(float));
+  if (d.ptype == kPluginMix) s = std::max(s, (size_t)d.CHt * mix_cs(D, ldx) * sizeof(float));
+  if (d.ptype == kPluginTpl) s = std::max(s, tpl_smem<float>(d.tpl.P, threads));
+  size_t tb, rb;
+  em32_layout(D, ldx, threads, &tb, &rb);
+  s = std::max(s, std::max(tb, rb));
+  s = std::max(s, finalize_smem(D, 1));
+  s = std::max(s, prepare_smem(D));
+  return align16(s);
+}
+
+struct TuneKey {
+  std::vector<long long> shape;
+  bool operator<(const TuneKey &o) const { return shape < o.shape; }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+}  // namespace pmcg
+
+using namespace pmcg;
+
+struct pmcg_batch {
+  std::vector<pmcg_run *> runs;
+  int R = 0;
+  std::vector<BatchDesc> hdesc;
+  BatchDesc *d_desc = nullptr;
+  BatchDyn *d_dyn = nullptr, *h_dyn = nullptr;
+  uint32_t *d_starts = nullptr;
+  DevStats *d_stats = nullptr, *h_stats = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int spt = 2, bps = 1, grid = 0, sms = 0, threads = 256;
+  size_t smem = 0;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph = false;
+  float last_ms = 0.f;
+};
+
+namespace pmcg {
+
+static bool bck(cudaError_t e, error **err, int line, const char *what) {
+  if (e == cudaSuccess) return true;
+  set_error(err, PMCG_ECUDA, line, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+#define BCK(expr, what) bck((expr), err, __LINE__, (what))
+
+template <int SPT>
+static cudaError_t launch_batch(pmcg_batch *b, int first, int last) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(b->grid);
+  cfg.blockDim = dim3(b->threads);
+  cfg.dynamicSmemBytes = b->smem;
+  cfg.stream = b->s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int R = b->R;
+  return cudaLaunchKernelEx(&cfg, batch_kernel<SPT>, (const BatchDesc *)b->d_desc, (const BatchDyn *)b->d_dyn, R,
+                            (const uint32_t *)b->d_starts, first, last, b->d_stats);
+}
+
+static cudaError_t launch_any(pmcg_batch *b, int first, int last) {
+  return b->spt == 1 ? launch_batch<1>(b, first, last) : launch_batch<2>(b, first, last);
+}
+
+// Prefix tables of all stages for the current samples-per-thread, and the grid.
+static bool batch_configure(pmcg_batch *b, int spt, int bps, error **err) {
+  b->spt = spt;
+  std::vector<uint32_t> st((size_t)kBStages * (b->R + 1));
+  for (int g = 0; g < kBStages; g++) {
+    uint64_t acc = 0;
+    for (int r = 0; r < b->R; r++) {
+      st[(size_t)g * (b->R + 1) + r] = (uint32_t)acc;
+      acc += items_of(g, b->hdesc[r], spt, b->threads);
+    }
+    if (acc > 0xFFFFFFF0ull) {
+      set_error(err, PMCG_EDIM, __LINE__, "batch too large: %llu work items", (unsigned long long)acc);
+      return false;
+    }
+    st[(size_t)g * (b->R + 1) + b->R] = (uint32_t)acc;
+  }
+  if (!BCK(cudaMemcpy(b->d_starts, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "starts"))
+    return false;
+  size_t smem = 0;
+  for (const BatchDesc &d : b->hdesc) smem = std::max(smem, smem_of(d, b->threads));
+  b->smem = smem;
+  const void *fn = spt == 1 ? (const void *)batch_kernel<1> : (const void *)batch_kernel<2>;
+  if (!BCK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute"))
+    return false;
+  int occ = 0;
+  if (!BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, b->threads, smem), "occupancy")) return false;
+  if (occ < 1) {
+    set_error(err, PMCG_EDIM, __LINE__, "batch kernel does not fit on an SM (%zu B shared memory)", smem);
+    return false;
+  }
+  b->bps = std::max(1, std::min(bps, occ));
+  b->grid = b->sms * b->bps;
+  return true;
+}
+
+static void drop_graph(pmcg_batch *b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->graph = false;
+}
+
+// Capture upload + persistent launch + statistics download in one graph.
+static void capture_graph(pmcg_batch *b) {
+  drop_graph(b);
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return; }
+  cudaError_t e1 = cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * b->R, cudaMemcpyHostToDevice, b->s);
+  cudaError_t e2 = launch_any(b, 0, kBStages - 1);
+  cudaError_t e3 = cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(DevStats) * b->R, cudaMemcpyDeviceToHost, b->s);
+  cudaError_t e4 = cudaStreamEndCapture(b->s, &g);
+  if (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && g &&
+      cudaGraphInstantiate(&b->gexec, g, 0) == cudaSuccess) {
+    b->graph = true;
+  } else {
+    b->gexec = nullptr;
+    b->graph = false;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+}
+
+}  // namespace pmcg
+
+extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err) {
+  if (nruns < 1 || !runs) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_batch_create: no runs");
+    return nullptr;
+  }
+  pmcg_batch *b = new pmcg_batch();
+  b->R = nruns;
+  b->runs.assign(runs, runs + nruns);
+  b->hdesc.resize(nruns);
+  for (int r = 0; r < nruns; r++) {
+    pmcg_run *run = runs[r];
+    const Work &w = run->w;
+    if (!run || w.prec != PMCG_MIXED || w.D > 32 || !run->post || run->post->plugins.size() != 1) {
+      set_error(err, PMCG_EUNSUPPORTED, __LINE__,
+                "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood", r);
+      delete b;
+      return nullptr;
+    }
+    const Plugin &pl = run->post->plugins[0];
+    BatchDesc &d = b->hdesc[r];
+    memset(&d, 0, sizeof(d));
+    d.prop = w.prop.view();
+    d.ptype = pl.type;
+    if (pl.type == kPluginMix) d.target = pl.mix.view();
+    if (pl.type == kPluginSn) d.sn = pl.sn;
+    if (pl.type == kPluginTpl) d.tpl = pl.tpl;
+    d.logpr = run->post->logpr;
+    d.N = w.N;
+    d.S = w.S;
+    d.CHp = mix_chunk(w.D, w.ldx, w.K);
+    d.CHt = pl.type == kPluginMix ? mix_chunk(w.D, w.ldx, pl.mix.K) : 1;
+    d.maxd = w.ldx <= 8 ? 8 : (w.ldx <= 16 ? 16 : 32);
+    d.key0 = (uint32_t)run->seed;
+    d.key1 = (uint32_t)(run->seed >> 32);
+    d.bmin = run->box ? w.bmin : nullptr;
+    d.bmax = run->box ? w.bmax : nullptr;
+    d.X32 = w.X32; d.idx = w.idx; d.counts = w.counts; d.flg = w.flg;
+    d.logq = w.logq; d.logpost = w.logpost; d.logw = w.logw;
+    d.lt32 = w.lt32; d.Q32 = w.Q32; d.aw32 = w.aw32;
+    d.wpart = w.wpart; d.empart = w.empart; d.st = w.dstats;
+    d.w = w.prop.w; d.mu = w.prop.mu; d.L = w.prop.L; d.Wt = w.prop.Wt; d.b = w.prop.b;
+    d.logdetL = w.prop.logdetL; d.cw = w.prop.cw; d.lconst = w.prop.lconst;
+    d.W32 = w.prop.W32; d.b32 = w.prop.b32; d.lconst32 = w.prop.lconst32; d.L32 = w.prop.L32; d.mu32 = w.prop.mu32;
+  }
+  int dev = 0;
+  bool ok = BCK(cudaGetDevice(&dev), "device") &&
+            BCK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev), "SM count") &&
+            BCK(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking), "stream") &&
+            BCK(cudaEventCreate(&b->e0), "event") && BCK(cudaEventCreate(&b->e1), "event") &&
+            BCK(cudaMalloc(&b->d_desc, sizeof(BatchDesc) * nruns), "descriptors") &&
+            BCK(cudaMalloc(&b->d_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
+            BCK(cudaMallocHost(&b->h_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
+            BCK(cudaMalloc(&b->d_starts, sizeof(uint32_t) * kBStages * (nruns + 1)), "prefix tables") &&
+            BCK(cudaMalloc(&b->d_stats, sizeof(DevStats) * nruns), "stats") &&
+            BCK(cudaMallocHost(&b->h_stats, sizeof(DevStats) * nruns), "stats") &&
+            BCK(cudaMemcpy(b->d_desc, b->hdesc.data(), sizeof(BatchDesc) * nruns, cudaMemcpyHostToDevice),
+                "descriptors");
+  // the runs' own streams may still have work queued (proposal uploads)
+  for (int r = 0; ok && r < nruns; r++) ok = BCK(cudaStreamSynchronize(runs[r]->w.s), "run stream");
+  // a tuned configuration for this shape, if any
+  int spt = 2, bps = 1;
+  {
+    TuneKey key;
+    for (const BatchDesc &d : b->hdesc) {
+      key.shape.push_back(d.prop.D); key.shape.push_back(d.prop.K);
+      key.shape.push_back((long long)d.N); key.shape.push_back(d.ptype);
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) { spt = it->second.first; bps = it->second.second; }
+  }
+  ok = ok && batch_configure(b, spt, bps, err);
+  if (!ok) {
+    pmcg_batch_free(&b);
+    return nullptr;
+  }
+  capture_graph(b);
+  return b;
+}
+
+extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *stats, error **err) {
+  for (int r = 0; r < b->R; r++) {
+    b->h_dyn[r].beta = betas ? betas[r] : 1.0;
+    b->h_dyn[r].call = b->runs[r]->calls;
+    b->h_dyn[r].pad = 0;
+  }
+  bool ok = BCK(cudaEventRecord(b->e0, b->s), "event");
+  if (ok && b->graph) {
+    ok = BCK(cudaGraphLaunch(b->gexec, b->s), "batch graph");
+  } else if (ok) {
+    ok = BCK(cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * b->R, cudaMemcpyHostToDevice, b->s),
+             "parameters") &&
+         BCK(launch_any(b, 0, kBStages - 1), "batch kernel") &&
+         BCK(cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(DevStats) * b->R, cudaMemcpyDeviceToHost, b->s), "stats");
+  }
+  ok = ok && BCK(cudaEventRecord(b->e1, b->s), "event") && BCK(cudaStreamSynchronize(b->s), "batch iteration");
+  if (!ok) return;
+  cudaEventElapsedTime(&b->last_ms, b->e0, b->e1);
+  for (int r = 0; r < b->R; r++) {
+    pmcg_run *run = b->runs[r];
+    *run->w.hstats = b->h_stats[r];
+    run->calls++;
+    run->last_launches = 1;
+    if (stats) {
+      const DevStats &h = b->h_stats[r];
+      pmcg_iter_stats &o = stats[r];
+      o.ln_evidence = h.ln_evidence; o.perplexity = h.perplexity; o.ess = h.ess; o.enc = h.enc;
+      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead; o.status = h.status;
+    }
+  }
+}
+
+extern "C" void pmcg_batch_autotune(pmcg_batch *b, error **err) {
+  const int spts[2] = {1, 2};
+  const int bpss[3] = {1, 2, 4};
+  float best = 1e30f;
+  int bspt = b->spt, bbps = b->bps;
+  // Time draw..log posterior (they only overwrite the sample buffers, which
+  // the next iteration redraws): twice per candidate, keep the faster.
+  for (int si = 0; si < 2; si++) {
+    for (int bi = 0; bi < 3; bi++) {
+      error *e = nullptr;
+      if (!batch_configure(b, spts[si], bpss[bi], &e)) { purgeError(&e); continue; }
+      if (b->bps != bpss[bi]) continue;  // occupancy clamp: already covered
+      float tmin = 1e30f;
+      for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(b->e0, b->s);
+        cudaError_t ce = launch_any(b, kBDraw, kBLogpost);
+        cudaEventRecord(b->e1, b->s);
+        if (ce != cudaSuccess || cudaStreamSynchronize(b->s) != cudaSuccess) { tmin = 1e30f; cudaGetLastError(); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->e0, b->e1);
+        if (rep > 0) tmin = std::min(tmin, ms);
+      }
+      if (tmin < best) { best = tmin; bspt = spts[si]; bbps = bpss[bi]; }
+    }
+  }
+  if (!batch_configure(b, bspt, bbps, err)) return;
+  {
+    TuneKey key;
+    for (const BatchDesc &d : b->hdesc) {
+      key.shape.push_back(d.prop.D); key.shape.push_back(d.prop.K);
+      key.shape.push_back((long long)d.N); key.shape.push_back(d.ptype);
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {b->spt, b->bps};
+  }
+  capture_graph(b);
+}
+
+extern "C" void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, int *blocks_per_sm, int *grid,
+                                  int *graph) {
+  if (samples_per_thread) *samples_per_thread = b->spt;
+  if (blocks_per_sm) *blocks_per_sm = b->bps;
+  if (grid) *grid = b->grid;
+  if (graph) *graph = b->graph ? 1 : 0;
+}
+
+extern "C" double pmcg_batch_last_ms(const pmcg_batch *b) { return b->last_ms; }
+
+extern "C" void pmcg_batch_free(pmcg_batch **pb) {
+  if (!pb || !*pb) return;
+  pmcg_batch *b = *pb;
+  drop_graph(b);
+  if (b->d_desc) cudaFree(b->d_desc);
+  if (b->d_dyn) cudaFree(b->d_dyn);
+  if (b->h_dyn) cudaFreeHost(b->h_dyn);
+  if (b->d_starts) cudaFree(b->d_starts);
+  if (b->d_stats) cudaFree(b->d_stats);
+  if (b->h_stats) cudaFreeHost(b->h_stats);
+  if (b->e0) cudaEventDestroy(b->e0);
+  if (b->e1) cudaEventDestroy(b->e1);
+  if (b->s) cudaStreamDestroy(b->s);
+  delete b;
+  *pb = nullptr;
+}

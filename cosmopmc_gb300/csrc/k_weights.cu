@@ -4,93 +4,37 @@
 // arithmetic, normalize_importance_weight, evidence and perplexity_and_ess
 // (exec/cosmo_pmc.c:46,62,343-345,378).
 //
-// Reduction record per block: (m, s, t, q, n) with m = max log-weight,
-// s = sum e^{l-m}, t = sum e^{l-m} l, q = sum e^{2(l-m)}, n = count. Then
-// logSum = m + ln s, H = logSum - t/s, sum wbar^2 = q/s^2. A fixed grid and a
-// fixed merge order make the result bit-reproducible.
-#include "pmcg_kernels.h"
+// Reduction record per tile of kTileW samples: (m, s, t, q, n) with m = max
+// log-weight, s = sum e^{l-m}, t = sum e^{l-m} l, q = sum e^{2(l-m)}, n = count.
+// Then logSum = m + ln s, H = logSum - t/s, sum wbar^2 = q/s^2. The tile
+// partition depends only on N and the merge order is fixed, so the result is
+// bit-reproducible and identical inside a batch.
+#include "pmcg_bodies.cuh"
 
 namespace pmcg {
 
-__device__ __forceinline__ void wred_add(WRed &r, double l) {
-  if (l > r.m) {
-    double e = exp(r.m - l);  // r.m == -inf gives 0
-    r.s = r.s * e + 1.0;
-    r.t = r.t * e + l;
-    r.q = r.q * e * e + 1.0;
-    r.m = l;
-  } else {
-    double e = exp(l - r.m);
-    r.s += e;
-    r.t += e * l;
-    r.q += e * e;
-  }
-  r.n += 1.0;
-}
+size_t weight_tiles(size_t N) { return N == 0 ? 1 : (N + kTileW - 1) / kTileW; }
 
 __global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, const double *__restrict__ logpost,
                                                       const double *__restrict__ logq, short *__restrict__ flg,
                                                       double *__restrict__ logw, WRed *__restrict__ partials) {
   __shared__ WRed s_r[8];
-  WRed r = wred_empty();
-  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (size_t)gridDim.x * blockDim.x) {
-    double l = -INFINITY;
-    if (flg[n]) {
-      l = beta * logpost[n] - (logq ? logq[n] : 0.0);
-      if (!isfinite(l)) { l = -INFINITY; flg[n] = 0; }
-    }
-    logw[n] = l;
-    if (l > -INFINITY) wred_add(r, l);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) r = wred_merge(r, wred_shfl(r, o));
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) s_r[wid] = r;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    WRed a = s_r[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge(a, s_r[w]);
-    partials[blockIdx.x] = a;
-  }
+  body_weights_tile(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
 }
 
-// One block of 256 threads: each thread merges a strided subset of the partials,
-// then a shuffle tree and a sequential pass over the 8 warps (fixed order).
 __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *__restrict__ partials, size_t N,
                                                             DevStats *st) {
   __shared__ WRed s_r[8];
-  WRed a = wred_empty();
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge(a, partials[b]);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) a = wred_merge(a, wred_shfl(a, o));
-  if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = a;
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  a = s_r[0];
-  for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge(a, s_r[w]);
-  if (a.n == 0.0 || a.m == -INFINITY) {
-    st->status = -9011;  // PMCG_ENOWEIGHT
-    st->nok = 0.0;
-    return;
-  }
-  st->status = 0;
-  double ls = a.m + log(a.s);
-  st->logSum = ls;
-  st->maxW = a.m;
-  st->H = ls - a.t / a.s;
-  st->sumw2 = a.q / (a.s * a.s);
-  st->nok = a.n;
-  st->ln_evidence = ls - log((double)N);
-  st->perplexity = exp(st->H) / (double)N;
-  st->ess = 1.0 / st->sumw2;
+  body_weights_final(nb, partials, N, st, s_r);
 }
 
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
                            double *logw, WRed *partials, DevStats *st, cudaStream_t s) {
-  weights_kernel<<<kWeightBlocks, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
+  const unsigned nb = (unsigned)weight_tiles(N);
+  weights_kernel<<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  weights_final_kernel<<<1, 256, 0, s>>>(kWeightBlocks, partials, N, st);
+  weights_final_kernel<<<1, 256, 0, s>>>((int)nb, partials, N, st);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,965 @@
+// pmcg_bodies.cuh — the per-work-item bodies of the engine's kernels.
+//
+// Each body processes one work item (a tile of samples, one component, one run)
+// with whatever block size it is launched with. The standalone kernels (one
+// launch per stage and run) and the persistent batch kernel (all stages of all
+// runs in one cooperative launch) call the same bodies, so a run gives
+// bit-identical results alone and inside a batch.
+//
+// Conventions: `smem` is the block's dynamic shared memory; a body that uses
+// __syncthreads() is entered by every thread of the block, and callers that
+// loop over items put a __syncthreads() between items.
+#pragma once
+#include "pmcg_kernels.h"
+
+namespace pmcg {
+
+constexpr int kTileW = 2048;   // samples per weight / weight-factor tile
+constexpr int kTile32 = 64;    // samples per EM staging tile (mixed)
+constexpr int kFlushTiles = 16;
+constexpr int kMinCount = 20;  // MINCOUNT, Manual/manual.tex:483
+
+__host__ __device__ inline int em_E(int D) { return 2 + D + D * (D + 1) / 2; }
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// ================================================================== (a) draw
+// Box-Muller pair from one Philox block. FP64 path: two 53-bit uniforms (the
+// oracle's mapping). FP32 path: the same 53-bit integers, 1-a and b, rounded
+// once to float (integer conversions, no FP64 arithmetic), so its normals equal
+// the FP64 ones to single precision, tails included.
+template <typename Real>
+__device__ __forceinline__ void box_muller(P4 o, Real &g0, Real &g1);
+
+template <>
+__device__ __forceinline__ void box_muller<double>(P4 o, double &g0, double &g1) {
+  double a = u53(o.x, o.y), b = u53(o.z, o.w);
+  double r = sqrt(-2.0 * log1p(-a));
+  double sn, cs;
+  sincospi(2.0 * b, &sn, &cs);
+  g0 = r * cs;
+  g1 = r * sn;
+}
+template <>
+__device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
+  const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
+  const unsigned long long B = ((unsigned long long)(o.z >> 5) << 26) | (unsigned long long)(o.w >> 6);
+  const float two53inv = 1.1102230246251565e-16f;  // 2^-53
+  const float oma = __ull2float_rn((1ull << 53) - A) * two53inv;  // 1 - a in (0, 1]
+  const float b = __ull2float_rn(B) * two53inv;
+  float r = sqrtf(-2.0f * logf(oma));
+  float sn, cs;
+  sincospif(2.0f * b, &sn, &cs);
+  g0 = r * cs;
+  g1 = r * sn;
+}
+
+// Staging rows use stride ldo+1 (odd) so the per-thread row stores do not
+// collide in one bank.
+template <typename Real>
+__host__ __device__ inline size_t draw_smem(int K, int ldo, int threads) {
+  return align16((size_t)K * 8 + (size_t)K * 4) + (size_t)threads * (ldo + 1) * sizeof(Real);
+}
+
+// Samples n0 .. n0+blockDim-1: one thread per sample, rows staged in shared
+// memory and written with coalesced stores. Component k = min{k : u < C_k}.
+template <int MAXD, typename Real>
+__device__ __forceinline__ void body_draw(const DevMixView &m, size_t N, uint32_t key0, uint32_t key1, uint32_t call,
+                                          const double *__restrict__ bmin, const double *__restrict__ bmax,
+                                          const double *__restrict__ pre_u, const double *__restrict__ pre_z,
+                                          const double *__restrict__ pre_chi2, double *__restrict__ X64,
+                                          float *__restrict__ X32, int *__restrict__ idx, short *__restrict__ flg,
+                                          int *__restrict__ counts, size_t n0, unsigned char *smem) {
+  const int K = m.K, D = m.D, df = m.df;
+  const int ldo = (sizeof(Real) == 8) ? D : m.ldx;
+  double *s_cw = reinterpret_cast<double *>(smem);
+  int *s_cnt = reinterpret_cast<int *>(smem + (size_t)K * 8);
+  Real *s_x = reinterpret_cast<Real *>(smem + align16((size_t)K * 8 + (size_t)K * 4));
+  for (int k = threadIdx.x; k < K; k += blockDim.x) { s_cw[k] = m.cw[k]; s_cnt[k] = 0; }
+  __syncthreads();
+  const size_t n = n0 + threadIdx.x;
+  if (n < N) {
+    const uint32_t nlo = (uint32_t)n, nhi = (uint32_t)(n >> 32);
+    double u;
+    if (pre_u) {
+      u = pre_u[n];
+    } else {
+      P4 c = {0u, nlo, nhi, call};
+      P4 o = philox4x32_10(c, key0, key1);
+      u = u53(o.x, o.y);
+    }
+    int k = -1;
+    for (int j = 0; j < K; j++)
+      if (u < s_cw[j]) { k = j; break; }
+    if (k < 0)
+      for (int j = K - 1; j >= 0; j--)
+        if (m.w[j] > 0.0) { k = j; break; }
+    if (k < 0) k = 0;
+    const int nu = df > 0 ? df : 0;
+    Real z[MAXD];
+    Real c2 = (Real)0;
+    if (pre_z) {
+#pragma unroll
+      for (int i = 0; i < MAXD; i++) z[i] = (i < D) ? (Real)pre_z[n * D + i] : (Real)0;
+      c2 = pre_chi2 ? (Real)pre_chi2[n] : (Real)1;
+    } else {
+#pragma unroll
+      for (int mm = 0; mm < MAXD / 2; mm++) {
+        if (2 * mm < D) {
+          P4 c = {1u + (uint32_t)mm, nlo, nhi, call};
+          P4 o = philox4x32_10(c, key0, key1);
+          Real g0, g1;
+          box_muller<Real>(o, g0, g1);
+          z[2 * mm] = g0;
+          if (2 * mm + 1 < D) {
+            z[2 * mm + 1] = g1;
+          } else {
+            z[2 * mm + 1] = (Real)0;
+            if (nu > 0) c2 += g1 * g1;
+          }
+        } else {
+          z[2 * mm] = (Real)0;
+          z[2 * mm + 1] = (Real)0;
+        }
+      }
+      const int jstart = (D % 2 == 0) ? D : D + 1;
+      for (int j = jstart; j < D + nu; j += 2) {
+        P4 c = {1u + (uint32_t)(j / 2), nlo, nhi, call};
+        P4 o = philox4x32_10(c, key0, key1);
+        Real g0, g1;
+        box_muller<Real>(o, g0, g1);
+        c2 += g0 * g0;
+        if (j + 1 < D + nu) c2 += g1 * g1;
+      }
+    }
+    const Real sc = (df > 0) ? (Real)sqrt((double)df / (double)c2) : (Real)1;
+    const int lds = ldo + 1;
+    int in = 1;
+    if (sizeof(Real) == 8) {
+      const double *Lk = m.L + (size_t)k * D * D;
+      const double *mk = m.mu + (size_t)k * D;
+#pragma unroll
+      for (int i = 0; i < MAXD; i++) {
+        if (i < D) {
+          Real acc = (Real)0;
+#pragma unroll
+          for (int j = 0; j <= i; j++) acc += (Real)__ldg(&Lk[i * D + j]) * z[j];
+          Real xi = (Real)__ldg(&mk[i]) + sc * acc;
+          s_x[threadIdx.x * lds + i] = xi;
+          if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
+        }
+      }
+    } else {
+      // L32 rows padded to ldx with zeros above the diagonal: float4 reads.
+      const int ldx = m.ldx;
+      const float *Lk = m.L32 + (size_t)k * D * ldx;
+      const float *mk = m.mu32 + (size_t)k * D;
+#pragma unroll
+      for (int i = 0; i < MAXD; i++) {
+        if (i < D) {
+          float acc = 0.f;
+#pragma unroll
+          for (int j4 = 0; j4 <= i / 4; j4++) {
+            const float4 l4 = __ldg(reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4));
+            acc = fmaf(l4.x, (float)z[4 * j4], acc);
+            acc = fmaf(l4.y, (float)z[4 * j4 + 1], acc);
+            acc = fmaf(l4.z, (float)z[4 * j4 + 2], acc);
+            acc = fmaf(l4.w, (float)z[4 * j4 + 3], acc);
+          }
+          const float xi = __ldg(&mk[i]) + (float)sc * acc;
+          s_x[threadIdx.x * lds + i] = (Real)xi;
+          if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
+        }
+      }
+    }
+    for (int i = D; i < ldo; i++) s_x[threadIdx.x * lds + i] = (Real)0;
+    idx[n] = k;
+    flg[n] = (short)in;
+    atomicAdd(&s_cnt[k], 1);
+  }
+  __syncthreads();
+  // coalesced copy-out: each warp writes whole rows
+  const int rows = (N > n0) ? (int)((N - n0 < (size_t)blockDim.x) ? (N - n0) : (size_t)blockDim.x) : 0;
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int r = threadIdx.x >> 5; r < rows; r += nw) {
+    for (int c = lane; c < ldo; c += 32) {
+      const Real v = s_x[r * (ldo + 1) + c];
+      if (sizeof(Real) == 8) X64[(n0 + r) * ldo + c] = (double)v;
+      else X32[(n0 + r) * ldo + c] = (float)v;
+    }
+  }
+  for (int k = threadIdx.x; k < K; k += blockDim.x)
+    if (s_cnt[k]) atomicAdd(&counts[k], s_cnt[k]);
+}
+
+// ================================================================== (b) FP32 log-pdf
+__host__ __device__ inline int mix_cs(int D, int ldx) { return D * ldx + ldx + 4; }
+
+// Samples item*blockDim*SPT + s*blockDim + tid (s < SPT); CH components staged per
+// barrier; every broadcast float4 of L^-1 feeds SPT samples.
+template <int MAXD, int SPT>
+__device__ __forceinline__ void body_mixlogpdf_f32(const DevMixView &m, size_t N, const float *__restrict__ X,
+                                                   double *__restrict__ out, int accumulate, double add,
+                                                   float *__restrict__ lt, float *__restrict__ Qo, int CH,
+                                                   size_t item, float *sw) {
+  const int D = m.D, K = m.K, ldx = m.ldx;
+  const int CS = mix_cs(D, ldx);
+  const size_t base = item * blockDim.x * SPT + threadIdx.x;
+  float x[SPT][MAXD];
+#pragma unroll
+  for (int s = 0; s < SPT; s++) {
+    const size_t n = base + (size_t)s * blockDim.x;
+#pragma unroll
+    for (int j4 = 0; j4 < MAXD / 4; j4++) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (n < N && 4 * j4 < ldx) v = *reinterpret_cast<const float4 *>(X + n * ldx + 4 * j4);
+      x[s][4 * j4] = v.x; x[s][4 * j4 + 1] = v.y; x[s][4 * j4 + 2] = v.z; x[s][4 * j4 + 3] = v.w;
+    }
+  }
+  float mx[SPT], sm[SPT];
+#pragma unroll
+  for (int s = 0; s < SPT; s++) { mx[s] = -INFINITY; sm[s] = 0.f; }
+  const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
+  for (int kc = 0; kc < K; kc += CH) {
+    const int nk = min(CH, K - kc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nk * D * ldx; e += blockDim.x) {
+      int kk = e / (D * ldx), r = e - kk * D * ldx;
+      sw[kk * CS + r] = m.W32[(size_t)(kc + kk) * D * ldx + r];
+    }
+    for (int e = threadIdx.x; e < nk * (ldx + 4); e += blockDim.x) {
+      int kk = e / (ldx + 4), r = e - kk * (ldx + 4);
+      float v = 0.f;
+      if (r < D) v = m.b32[(size_t)(kc + kk) * D + r];
+      else if (r == ldx) v = m.lconst32[kc + kk];
+      sw[kk * CS + D * ldx + r] = v;
+    }
+    __syncthreads();
+    for (int kk = 0; kk < nk; kk++) {
+      const float *Wk = sw + kk * CS;
+      const float *bk = Wk + D * ldx;
+      const float lc = bk[ldx];
+      const int k = kc + kk;
+      if (lc == -INFINITY) {
+#pragma unroll
+        for (int s = 0; s < SPT; s++) {
+          const size_t n = base + (size_t)s * blockDim.x;
+          if (n < N) {
+            if (lt) lt[(size_t)k * N + n] = -INFINITY;
+            if (Qo) Qo[(size_t)k * N + n] = 0.f;
+          }
+        }
+        continue;
+      }
+      float q[SPT];
+#pragma unroll
+      for (int s = 0; s < SPT; s++) q[s] = 0.f;
+#pragma unroll
+      for (int i = 0; i < MAXD; i++) {
+        if (i < D) {
+          float acc[SPT];
+          const float bi = bk[i];
+#pragma unroll
+          for (int s = 0; s < SPT; s++) acc[s] = -bi;
+#pragma unroll
+          for (int j4 = 0; j4 <= i / 4; j4++) {
+            const float4 w = *reinterpret_cast<const float4 *>(Wk + i * ldx + 4 * j4);
+#pragma unroll
+            for (int s = 0; s < SPT; s++) {
+              acc[s] = fmaf(w.x, x[s][4 * j4], acc[s]);
+              acc[s] = fmaf(w.y, x[s][4 * j4 + 1], acc[s]);
+              acc[s] = fmaf(w.z, x[s][4 * j4 + 2], acc[s]);
+              acc[s] = fmaf(w.w, x[s][4 * j4 + 3], acc[s]);
+            }
+          }
+#pragma unroll
+          for (int s = 0; s < SPT; s++) q[s] = fmaf(acc[s], acc[s], q[s]);
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < SPT; s++) {
+        const float l = (m.df > 0) ? lc - hnd * log1pf(q[s] * rnu) : lc - 0.5f * q[s];
+        if (l > mx[s]) { sm[s] = sm[s] * expf(mx[s] - l) + 1.f; mx[s] = l; }
+        else sm[s] += expf(l - mx[s]);
+        const size_t n = base + (size_t)s * blockDim.x;
+        if (n < N) {
+          if (lt) lt[(size_t)k * N + n] = l;
+          if (Qo) Qo[(size_t)k * N + n] = q[s];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < SPT; s++) {
+    const size_t n = base + (size_t)s * blockDim.x;
+    if (n < N) {
+      double r = (double)mx[s] + (double)logf(sm[s]);
+      if (accumulate) out[n] += r + add;
+      else out[n] = r + add;
+    }
+  }
+}
+
+// ================================================================== (c) SN Ia
+__device__ __forceinline__ double sk_dev(double ok, double I, int &bad) {
+  if (fabs(ok) < 1e-10) return I * (1.0 + ok * I * I / 6.0);
+  if (ok > 0.0) { double s = sqrt(ok); return sinh(s * I) / s; }
+  double s = sqrt(-ok);
+  if (s * I >= PMCG_PI) { bad = 1; return 0.0; }
+  return sin(s * I) / s;
+}
+
+// One warp per sample n; the cumulative distance integral over redshift-sorted
+// supernovae is a warp prefix scan of per-interval Gauss-Legendre sums.
+// assign != 0: logpost[n] = add + logL; otherwise logpost[n] += logL.
+template <bool F32>
+__device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const double *__restrict__ X64,
+                                        const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
+                                        short *__restrict__ flg, size_t n, int assign, double add) {
+  const int lane = threadIdx.x & 31;
+  if (n >= N) return;
+  if (!flg[n]) return;
+  auto par = [&](int ip, double def) -> double {
+    if (ip < 0) return def;
+    return F32 ? (double)X32[n * ldx + ip] : X64[n * D + ip];
+  };
+  const double om = par(sn.ip_om, sn.def_om);
+  double ode, ok;
+  if (sn.ip_ode >= 0) { ode = par(sn.ip_ode, 0.0); ok = 1.0 - om - ode; }
+  else { ode = 1.0 - om; ok = 0.0; }
+  const double w0 = par(sn.ip_w0, sn.def_w0);
+  const double M = par(sn.ip_M, sn.def_M);
+  const double al = par(sn.ip_alpha, sn.def_alpha);
+  const double be = par(sn.ip_beta, sn.def_beta);
+  const double ex = 3.0 * (1.0 + w0);
+  const float omf = (float)om, okf = (float)ok, odef = (float)ode, exf = (float)ex;
+  const int G = sn.G, nsn = sn.nsn;
+  int bad = 0;
+  double carry = 0.0, chi2 = 0.0, A = 0.0, B = 0.0, C = 0.0, sl = 0.0;
+  for (int base = 0; base < nsn; base += 32) {
+    const int i = base + lane;
+    double Ii = 0.0;
+    if (i < nsn) {
+      if (F32) {
+        float acc = 0.f;
+        for (int g = 0; g < G; g++) {
+          const int q = i * G + g;
+          float e2 = omf * sn.fna3[q] + okf * sn.fna2[q] + odef * expf(exf * sn.fnla[q]);
+          if (!(e2 > 0.f)) bad = 1;
+          else acc += sn.fnw[q] * rsqrtf(e2);
+        }
+        Ii = (double)acc;
+      } else {
+        for (int g = 0; g < G; g++) {
+          const int q = i * G + g;
+          double e2 = om * sn.na3[q] + ok * sn.na2[q] + ode * exp(ex * sn.nla[q]);
+          if (!(e2 > 0.0)) bad = 1;
+          else Ii += sn.nw[q] / sqrt(e2);
+        }
+      }
+      double e2z = om * sn.za3[i] + ok * sn.za2[i] + ode * exp(ex * sn.zla[i]);
+      if (!(e2z > 0.0)) bad = 1;
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      double t = __shfl_up_sync(0xffffffffu, Ii, o);
+      if (lane >= o) Ii += t;
+    }
+    const double I = carry + Ii;
+    carry = __shfl_sync(0xffffffffu, I, 31);
+    if (i < nsn) {
+      const double zi = sn.z[i];
+      const double dm = sk_dev(ok, I, bad);
+      if (!(dm > 0.0)) bad = 1;
+      const double mu_th = 5.0 * log10((1.0 + zi) * sn.dh * fmax(dm, 1e-300)) + 25.0;
+      const double *W = sn.cov6 + (size_t)i * 6;
+      const double s2 = W[0] + al * al * W[1] + be * be * W[2] + 2.0 * al * W[3] - 2.0 * be * W[4] -
+                        2.0 * al * be * W[5] + sn.sig_int2 + sn.spv2[i];
+      if (!(s2 > 0.0)) bad = 1;
+      double d = sn.mB[i] + al * sn.x1[i] - be * sn.c[i] - mu_th;
+      const double is2 = 1.0 / s2;
+      if (sn.chi2mode == 0) { d -= M; chi2 += d * d * is2; }
+      else { A += d * d * is2; B += d * is2; C += is2; }
+      sl += log(s2);
+    }
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  chi2 = warp_sum(chi2); A = warp_sum(A); B = warp_sum(B); C = warp_sum(C); sl = warp_sum(sl);
+  if (lane == 0) {
+    if (bad) { flg[n] = 0; return; }
+    if (sn.chi2mode != 0) chi2 = A - B * B / C + log(C / (2.0 * PMCG_PI));
+    double ll = -0.5 * chi2 - (sn.add_logdet ? 0.5 * sl : 0.0);
+    if (!isfinite(ll)) flg[n] = 0;
+    else if (assign) logpost[n] = add + ll;
+    else logpost[n] += ll;
+  }
+}
+
+// ================================================================== (c) template
+constexpr int kMT = 32;
+template <typename Real>
+__host__ __device__ inline size_t tpl_smem(int P, int threads) {
+  return ((size_t)P * threads + (size_t)P * kMT + kMT) * sizeof(Real);
+}
+
+// Samples item*blockDim .. +blockDim-1; phi(theta) transposed in shared memory
+// ([P][blockDim], conflict-free), At staged kMT rows at a time and read as
+// broadcasts. assign != 0: logpost = add + logL; otherwise logpost += logL.
+template <typename Real>
+__device__ __forceinline__ void body_tpl(const TplDev &t, size_t N, const double *__restrict__ X64,
+                                         const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
+                                         const short *__restrict__ flg, size_t item, Real *sm, int assign,
+                                         double add) {
+  const int P = t.P, Dp = t.Dpar, M = t.M, B = blockDim.x;
+  Real *sphi = sm;                        // [P][B]
+  Real *sA = sphi + (size_t)P * B;        // [P][kMT]
+  Real *sd = sA + (size_t)P * kMT;        // [kMT]
+  const size_t n = item * B + threadIdx.x;
+  const bool act = n < N && flg[n];
+  {
+    Real th[64];
+    for (int i = 0; i < Dp; i++)
+      th[i] = act ? (sizeof(Real) == 8 ? (Real)X64[n * Dp + i] : (Real)X32[n * ldx + i]) : (Real)0;
+    int p = 0;
+    sphi[(p++) * B + threadIdx.x] = (Real)1;
+    for (int i = 0; i < Dp; i++) sphi[(p++) * B + threadIdx.x] = th[i];
+    for (int i = 0; i < Dp; i++)
+      for (int j = i; j < Dp; j++) sphi[(p++) * B + threadIdx.x] = th[i] * th[j];
+  }
+  Real chi2 = 0;
+  double chi2d = 0.0;
+  const Real *Asrc = (sizeof(Real) == 8) ? (const Real *)t.At : (const Real *)t.At32;
+  const Real *dsrc = (sizeof(Real) == 8) ? (const Real *)t.dt : (const Real *)t.dt32;
+  for (int m0 = 0; m0 < M; m0 += kMT) {
+    const int mt = min(kMT, M - m0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < P * kMT; e += B) {
+      int p = e / kMT, r = e - p * kMT;
+      sA[e] = (r < mt) ? Asrc[(size_t)(m0 + r) * P + p] : (Real)0;
+    }
+    for (int r = threadIdx.x; r < kMT; r += B) sd[r] = (r < mt) ? dsrc[m0 + r] : (Real)0;
+    __syncthreads();
+    for (int r0 = 0; r0 < kMT; r0 += 8) {
+      Real acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) acc[q] = sd[r0 + q];
+      for (int p = 0; p < P; p++) {
+        const Real f = sphi[p * B + threadIdx.x];
+        const Real *a = sA + p * kMT + r0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] -= a[q] * f;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) chi2 += acc[q] * acc[q];
+    }
+    chi2d += (double)chi2;
+    chi2 = 0;
+  }
+  if (act) {
+    if (assign) logpost[n] = add - 0.5 * chi2d;
+    else logpost[n] += -0.5 * chi2d;
+  }
+}
+
+// ================================================================== (d) weights
+__device__ __forceinline__ void wred_add(WRed &r, double l) {
+  if (l > r.m) {
+    double e = exp(r.m - l);  // r.m == -inf gives 0
+    r.s = r.s * e + 1.0;
+    r.t = r.t * e + l;
+    r.q = r.q * e * e + 1.0;
+    r.m = l;
+  } else {
+    double e = exp(l - r.m);
+    r.s += e;
+    r.t += e * l;
+    r.q += e * e;
+  }
+  r.n += 1.0;
+}
+
+// Block reduction of a WRed in a fixed order; thread 0 receives the result.
+__device__ __forceinline__ WRed block_wred(WRed r, WRed *s_r) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r = wred_merge(r, wred_shfl(r, o));
+  if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = r;
+  __syncthreads();
+  WRed a = s_r[0];
+  if (threadIdx.x == 0)
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge(a, s_r[w]);
+  return a;
+}
+
+// Samples tile*kTileW .. +kTileW-1: log-weights and the tile's partial record.
+// logq == nullptr means log q = 0 (re-normalising given log-weights).
+__device__ __forceinline__ void body_weights_tile(size_t N, double beta, const double *__restrict__ logpost,
+                                                  const double *__restrict__ logq, short *__restrict__ flg,
+                                                  double *__restrict__ logw, WRed *__restrict__ part, size_t tile,
+                                                  WRed *s_r) {
+  WRed r = wred_empty();
+  const size_t base = tile * kTileW;
+  for (int q = threadIdx.x; q < kTileW; q += blockDim.x) {
+    const size_t n = base + q;
+    if (n >= N) break;
+    double l = -INFINITY;
+    if (flg[n]) {
+      l = beta * logpost[n] - (logq ? logq[n] : 0.0);
+      if (!isfinite(l)) { l = -INFINITY; flg[n] = 0; }
+    }
+    logw[n] = l;
+    if (l > -INFINITY) wred_add(r, l);
+  }
+  WRed a = block_wred(r, s_r);
+  if (threadIdx.x == 0) part[tile] = a;
+}
+
+// Merge the nb tile records of one sample (strided per thread, then a fixed
+// tree) and derive logSum, evidence, perplexity and ESS.
+__device__ __forceinline__ void body_weights_final(int nb, const WRed *__restrict__ part, size_t N, DevStats *st,
+                                                   WRed *s_r) {
+  WRed a = wred_empty();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge(a, part[b]);
+  a = block_wred(a, s_r);
+  if (threadIdx.x != 0) return;
+  if (a.n == 0.0 || a.m == -INFINITY) {
+    st->status = -9011;  // PMCG_ENOWEIGHT
+    st->nok = 0.0;
+    return;
+  }
+  st->status = 0;
+  const double ls = a.m + log(a.s);
+  st->logSum = ls;
+  st->maxW = a.m;
+  st->H = ls - a.t / a.s;
+  st->sumw2 = a.q / (a.s * a.s);
+  st->nok = a.n;
+  st->ln_evidence = ls - log((double)N);
+  st->perplexity = exp(st->H) / (double)N;
+  st->ess = 1.0 / st->sumw2;
+}
+
+// ================================================================== (e) EM, mixed
+// Per-sample single-precision weight factor aw = log w - logSum - log q
+// (-inf where flg == 0): one FP64 subtraction per sample, not per component.
+__device__ __forceinline__ void body_em_factor(size_t N, const double *__restrict__ logw,
+                                               const double *__restrict__ logq, const DevStats *__restrict__ st,
+                                               float *__restrict__ aw, size_t tile) {
+  const double ls = st->logSum;
+  const size_t base = tile * kTileW;
+  for (int q = threadIdx.x; q < kTileW; q += blockDim.x) {
+    const size_t n = base + q;
+    if (n >= N) break;
+    const double l = logw[n];
+    aw[n] = (l > -INFINITY) ? (float)(l - ls - logq[n]) : -INFINITY;
+  }
+}
+
+// Staging capacity of the compacted (sample, weight) list: one full tile plus
+// one scan step of up to 256 candidates.
+constexpr int kEmBuf = kTile32 + 256;
+// A pair whose single-precision weight vt = exp(aw + lt) / itau underflows
+// (aw + lt below log FLT_MIN = -87.3) adds exactly nothing in FP32 and less
+// than 1e-38 relative in any precision: such pairs are skipped.
+constexpr float kEmLogMin = -87.0f;
+
+__host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t *tile_bytes, size_t *red_bytes) {
+  const int Dp = ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, G = threads / NB;
+  *tile_bytes = (size_t)(Dp * Dp + Dp + kTile32 * Da + kTile32 * (Dp + 1) + 3 * kEmBuf + 40) * sizeof(float);
+  *red_bytes = (size_t)G * NB * 16 * sizeof(double);
+}
+
+// Statistics of component k over sample chunk s, accumulated in the component's
+// whitened frame a = L_k^-1 (x - mu_k) (entries O(1)); a covariance of condition
+// 1e6 cannot be represented to its small eigenvalues in FP32 in the raw frame.
+//
+// The chunk is scanned 256 samples at a time; the pairs whose weight does not
+// underflow (aw + lt > kEmLogMin) are compacted, in sample order (warp ballots
+// and a block prefix), into a staging list. Every full tile of 64 listed
+// samples is then gathered (x rows, stride ldx+1), whitened with L^-1 staged
+// transposed (float4 broadcasts; warps paired over i-blocks so their triangular
+// lengths balance), and accumulated: the augmented rows [a, 1, 1/tau, 0, 0]
+// with weight vt give in the lower triangle of sum vt a a^T: S2 (whitened), S1
+// (row Dp), St (Dp,Dp) and S0 (Dp+1,Dp). Each thread owns one 4x4 block for one
+// sample group; FP32 sums are flushed into FP64 every kFlushTiles tiles. The
+// order of every sum depends only on the run's own data (deterministic).
+__device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N, int S, const float *__restrict__ X,
+                                                  const float *__restrict__ aw, const float *__restrict__ lt,
+                                                  const float *__restrict__ Qv, double *__restrict__ part, int k,
+                                                  int s, unsigned char *smem) {
+  const int D = m.D, E = em_E(D);
+  if (m.w[k] <= 0.0) return;
+  const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, nib = Dp / 4;
+  const int ldt = Dp + 1;
+  const int G = blockDim.x / NB;
+  float *sWT = reinterpret_cast<float *>(smem);   // [Dp][Dp]  (L^-1)^T
+  float *sb = sWT + Dp * Dp;                      // [Dp]      L^-1 mu
+  float *sa = sb + Dp;                            // [kTile32][Da]
+  float *sx = sa + kTile32 * Da;                  // [kTile32][ldt]
+  float *lvt = sx + kTile32 * ldt;                // [kEmBuf] listed vt
+  float *ltau = lvt + kEmBuf;                     // [kEmBuf] listed 1/tau
+  int *lidx = reinterpret_cast<int *>(ltau + kEmBuf);  // [kEmBuf] listed sample offsets
+  int *wcnt = lidx + kEmBuf;                      // [32] per-warp counts
+  const size_t chunk = (N + S - 1) / S;
+  const size_t n0 = (size_t)s * chunk, n1 = (n0 + chunk < N) ? n0 + chunk : N;
+  const float nu = (float)m.df, rnd = 1.0f / ((float)m.df + (float)D);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  for (int e = tid; e < Dp * Dp; e += blockDim.x) {
+    int i = e / Dp, j = e - i * Dp;
+    sWT[j * Dp + i] = (i < D) ? m.W32[(size_t)k * D * Dp + (size_t)i * Dp + j] : 0.f;
+  }
+  for (int i = tid; i < Dp; i += blockDim.x) sb[i] = (i < D) ? m.b32[(size_t)k * D + i] : 0.f;
+  const int blk = tid % NB, grp = tid / NB;
+  const bool active = grp < G;
+  int bi = 0;
+  while ((bi + 1) * (bi + 2) / 2 <= blk) bi++;
+  const int bj = blk - bi * (bi + 1) / 2;
+  float acc[16];
+  double acc64[16];
+#pragma unroll
+  for (int e = 0; e < 16; e++) { acc[e] = 0.f; acc64[e] = 0.0; }
+  int tiles = 0;
+
+  // Accumulate listed entries [0, nt) (nt <= kTile32).
+  auto process = [&](int nt) {
+    if (tid < kTile32) {
+      float *row = sa + tid * Da;
+      row[Dp] = 1.f;
+      row[Dp + 1] = (tid < nt) ? ltau[tid] : 1.f;
+      row[Dp + 2] = 0.f;
+      row[Dp + 3] = 0.f;
+    }
+    for (int e = tid; e < kTile32 * Dp; e += blockDim.x) {
+      const int r = e / Dp, i = e - r * Dp;
+      sx[r * ldt + i] = (r < nt) ? X[(n0 + (size_t)lidx[r]) * Dp + i] : 0.f;
+    }
+    __syncthreads();
+    for (int u = warp; u < 2 * nib; u += nwarp) {
+      const int pair = u % nib, half = u / nib;
+      const int ib = half == 0 ? pair : nib - 1 - pair;
+      const int r = half * 32 + lane;
+      float o0 = -sb[4 * ib], o1 = -sb[4 * ib + 1], o2 = -sb[4 * ib + 2], o3 = -sb[4 * ib + 3];
+      const float *xr = sx + r * ldt;
+      const int jmax = 4 * ib + 4;
+      for (int j = 0; j < jmax; j++) {
+        const float xv = xr[j];
+        const float4 w4 = *reinterpret_cast<const float4 *>(sWT + j * Dp + 4 * ib);
+        o0 = fmaf(w4.x, xv, o0); o1 = fmaf(w4.y, xv, o1); o2 = fmaf(w4.z, xv, o2); o3 = fmaf(w4.w, xv, o3);
+      }
+      float *ar = sa + r * Da + 4 * ib;
+      const bool live = r < nt;
+      ar[0] = live ? o0 : 0.f; ar[1] = live ? o1 : 0.f; ar[2] = live ? o2 : 0.f; ar[3] = live ? o3 : 0.f;
+    }
+    __syncthreads();
+    if (active) {
+      for (int q = grp; q < nt; q += G) {
+        const float w = lvt[q];
+        float4 ai = *reinterpret_cast<const float4 *>(sa + q * Da + 4 * bi);
+        const float4 aj = *reinterpret_cast<const float4 *>(sa + q * Da + 4 * bj);
+        ai.x *= w; ai.y *= w; ai.z *= w; ai.w *= w;
+        acc[0] = fmaf(ai.x, aj.x, acc[0]);   acc[1] = fmaf(ai.x, aj.y, acc[1]);
+        acc[2] = fmaf(ai.x, aj.z, acc[2]);   acc[3] = fmaf(ai.x, aj.w, acc[3]);
+        acc[4] = fmaf(ai.y, aj.x, acc[4]);   acc[5] = fmaf(ai.y, aj.y, acc[5]);
+        acc[6] = fmaf(ai.y, aj.z, acc[6]);   acc[7] = fmaf(ai.y, aj.w, acc[7]);
+        acc[8] = fmaf(ai.z, aj.x, acc[8]);   acc[9] = fmaf(ai.z, aj.y, acc[9]);
+        acc[10] = fmaf(ai.z, aj.z, acc[10]); acc[11] = fmaf(ai.z, aj.w, acc[11]);
+        acc[12] = fmaf(ai.w, aj.x, acc[12]); acc[13] = fmaf(ai.w, aj.y, acc[13]);
+        acc[14] = fmaf(ai.w, aj.z, acc[14]); acc[15] = fmaf(ai.w, aj.w, acc[15]);
+      }
+    }
+    if (++tiles == kFlushTiles) {
+      tiles = 0;
+#pragma unroll
+      for (int e = 0; e < 16; e++) { acc64[e] += (double)acc[e]; acc[e] = 0.f; }
+    }
+    __syncthreads();
+  };
+
+  int fill = 0;  // listed entries (identical in every thread)
+  for (size_t c0 = n0; c0 < n1; c0 += blockDim.x) {
+    const size_t n = c0 + tid;
+    bool act = false;
+    float vt = 0.f, it = 1.f;
+    if (n < n1) {
+      const float e = aw[n] + lt[(size_t)k * N + n];
+      if (e > kEmLogMin) {
+        act = true;
+        const float v = expf(e);
+        if (m.df > 0) it = (nu + Qv[(size_t)k * N + n]) * rnd;
+        vt = v / it;
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) wcnt[warp] = __popc(bal);
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int w = 0; w < nwarp; w++) {
+      const int c = wcnt[w];
+      off += (w < warp) ? c : 0;
+      tot += c;
+    }
+    if (act) {
+      const int pos = fill + off + __popc(bal & ((1u << lane) - 1u));
+      lidx[pos] = (int)(n - n0);
+      lvt[pos] = vt;
+      ltau[pos] = it;
+    }
+    fill += tot;
+    __syncthreads();
+    while (fill >= kTile32) {
+      process(kTile32);
+      // move the remainder (fill - kTile32 <= 256 entries) to the front
+      const int rem = fill - kTile32;
+      int ri = 0;
+      float rv = 0.f, rt = 0.f;
+      if (tid < rem) { ri = lidx[kTile32 + tid]; rv = lvt[kTile32 + tid]; rt = ltau[kTile32 + tid]; }
+      __syncthreads();
+      if (tid < rem) { lidx[tid] = ri; lvt[tid] = rv; ltau[tid] = rt; }
+      __syncthreads();
+      fill = rem;
+    }
+  }
+  if (fill > 0) process(fill);
+#pragma unroll
+  for (int e = 0; e < 16; e++) acc64[e] += (double)acc[e];
+  __syncthreads();
+  double *red = reinterpret_cast<double *>(smem);
+  if (active) {
+#pragma unroll
+    for (int e = 0; e < 16; e++) red[((size_t)grp * NB + blk) * 16 + e] = acc64[e];
+  }
+  __syncthreads();
+  double *out = part + ((size_t)k * S + s) * E;
+  if (grp == 0) {
+    for (int e = 0; e < 16; e++) {
+      double t = red[(size_t)blk * 16 + e];
+      for (int g = 1; g < G; g++) t += red[((size_t)g * NB + blk) * 16 + e];
+      const int r = 4 * bi + e / 4, c = 4 * bj + e % 4;
+      if (r < D && c <= r) out[2 + D + tri_idx(r, c)] = t;
+      else if (r == Dp && c < D) out[2 + c] = t;
+      else if (r == Dp && c == Dp) out[1] = t;
+      else if (r == Dp + 1 && c == Dp) out[0] = t;
+    }
+  }
+}
+
+// ================================================================== (e) EM finalise
+__host__ __device__ inline size_t finalize_smem(int D, int whitened) {
+  return (size_t)(em_E(D) + (whitened ? 3 : 1) * D * D) * sizeof(double);
+}
+
+// Component k: fixed-order sum of the chunk partials, new mean and covariance
+// (mapped back from the whitened frame with the old factor when whitened: mu' =
+// mu + L d, Sigma' = L Sigma_w L^T), band limit, FP64 Cholesky; the dead rule
+// buries the component (weight 0, parameters kept).
+__device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w, double *mu, double *L, size_t N,
+                                                 int S, const double *__restrict__ part,
+                                                 const int *__restrict__ counts, int band_limit, int whitened, int k,
+                                                 const DevStats *stats, double *sh, int *s_dead, double *s_piv) {
+  const int D = m.D, E = em_E(D);
+  double *st = sh;             // E
+  double *C = st + E;          // D*D
+  double *Lo = C + D * D;      // D*D old factor (whitened only)
+  double *T = Lo + D * D;      // D*D scratch (whitened only)
+  if (stats->status != 0) return;  // the weight step failed: keep the proposal
+  if (m.w[k] <= 0.0) {
+    if (threadIdx.x == 0) w[k] = 0.0;
+    return;
+  }
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    double t = 0.0;
+    for (int s = 0; s < S; s++) t += part[((size_t)k * S + s) * E + e];
+    st[e] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double S0 = st[0], St = st[1];
+    *s_dead = (counts[k] < kMinCount) || !(S0 >= 1.0 / (double)N) || !(St > 0.0) || !isfinite(S0) || !isfinite(St);
+  }
+  __syncthreads();
+  if (*s_dead) {
+    if (threadIdx.x == 0) w[k] = 0.0;
+    return;
+  }
+  const double S0 = st[0], St = st[1];
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    int i = e / D, j = e - i * D;
+    int a = i > j ? i : j, b = i > j ? j : i;
+    double di = st[2 + i] / St, dj = st[2 + j] / St;
+    C[e] = (st[2 + D + tri_idx(a, b)] - St * di * dj) / S0;
+    if (whitened) Lo[e] = (j <= i) ? m.L[(size_t)k * D * D + e] : 0.0;
+  }
+  __syncthreads();
+  if (whitened) {
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // T = Lo C
+      int i = e / D, j = e - i * D;
+      double t = 0.0;
+      for (int q = 0; q <= i; q++) t += Lo[i * D + q] * C[q * D + j];
+      T[e] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // C = T Lo^T
+      int i = e / D, j = e - i * D;
+      double t = 0.0;
+      for (int q = 0; q <= j; q++) t += T[i * D + q] * Lo[j * D + q];
+      C[e] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // symmetrise exactly
+      int i = e / D, j = e - i * D;
+      if (j < i) T[e] = 0.5 * (C[i * D + j] + C[j * D + i]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      int i = e / D, j = e - i * D;
+      if (j < i) { C[i * D + j] = T[e]; C[j * D + i] = T[e]; }
+    }
+    __syncthreads();
+  }
+  if (band_limit > 0 && band_limit < D) {
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      int i = e / D, j = e - i * D;
+      if ((i > j ? i - j : j - i) >= band_limit) C[e] = 0.0;
+    }
+    __syncthreads();
+  }
+  for (int j = 0; j < D; j++) {
+    if (threadIdx.x == 0) {
+      double d = C[j * D + j];
+      for (int q = 0; q < j; q++) d -= C[j * D + q] * C[j * D + q];
+      if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
+      *s_piv = sqrt(d);
+      C[j * D + j] = *s_piv;
+    }
+    __syncthreads();
+    for (int i = j + 1 + threadIdx.x; i < D; i += blockDim.x) {
+      double t = C[i * D + j];
+      for (int q = 0; q < j; q++) t -= C[i * D + q] * C[j * D + q];
+      C[i * D + j] = t / *s_piv;
+    }
+    __syncthreads();
+  }
+  if (*s_dead) {
+    if (threadIdx.x == 0) w[k] = 0.0;
+    return;
+  }
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    double d;
+    if (whitened) {
+      d = 0.0;
+      for (int q = 0; q <= i; q++) d += Lo[i * D + q] * (st[2 + q] / St);
+    } else {
+      d = st[2 + i] / St;
+    }
+    mu[(size_t)k * D + i] = m.mu[(size_t)k * D + i] + d;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    int i = e / D, j = e - i * D;
+    L[(size_t)k * D * D + e] = (j <= i) ? C[e] : 0.0;
+  }
+  if (threadIdx.x == 0) w[k] = S0;
+}
+
+// Renormalise the surviving weights (fixed order), count the dead, ENC.
+__device__ __forceinline__ void body_em_renorm(int K, double *w, DevStats *st) {
+  if (threadIdx.x != 0) return;
+  if (st->status != 0) return;  // the weight step failed: keep the proposal
+  double tot = 0.0;
+  for (int k = 0; k < K; k++) tot += w[k];
+  st->wsum = tot;
+  if (!(tot > 0.0) || !isfinite(tot)) {
+    st->status = -9005;  // PMCG_ENEGWEIGHT
+    st->ndead = K;
+    st->enc = 0.0;
+    return;
+  }
+  double s2 = 0.0;
+  int nd = 0;
+  for (int k = 0; k < K; k++) {
+    double v = w[k] / tot;
+    w[k] = v;
+    s2 += v * v;
+    nd += (v == 0.0);
+  }
+  st->ndead = nd;
+  st->enc = 1.0 / s2;
+}
+
+// ================================================================== mixture preparation
+__host__ __device__ inline size_t prepare_smem(int D) { return 2 * (size_t)D * D * sizeof(double); }
+
+// Component k: W = L^-1 by column substitution, b = W mu, log|L|, and the
+// single-precision copies used by the mixed kernels.
+__device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *logdetL, double *Wt, double *b,
+                                                  float *W32, float *b32, float *L32, float *mu32, int k,
+                                                  double *s) {
+  const int D = m.D, T = D * (D + 1) / 2, ldx = m.ldx;
+  double *sL = s;            // D*D
+  double *sW = s + D * D;    // D*D
+  const double *Lk = m.L + (size_t)k * D * D;
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+    sL[e] = Lk[e];
+    sW[e] = 0.0;
+  }
+  for (int e = threadIdx.x; e < D * ldx; e += blockDim.x) {  // rows padded to ldx, zero above the diagonal
+    const int i = e / ldx, j = e - i * ldx;
+    L32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)Lk[i * D + j] : 0.0f;
+  }
+  for (int i = threadIdx.x; i < D; i += blockDim.x) mu32[(size_t)k * D + i] = (float)m.mu[(size_t)k * D + i];
+  __syncthreads();
+  for (int j = threadIdx.x; j < D; j += blockDim.x) {
+    sW[j * D + j] = 1.0 / sL[j * D + j];
+    for (int i = j + 1; i < D; i++) {
+      double t = 0.0;
+      for (int q = j; q < i; q++) t += sL[i * D + q] * sW[q * D + j];
+      sW[i * D + j] = -t / sL[i * D + i];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    double t = 0.0;
+    for (int j = 0; j <= i; j++) t += sW[i * D + j] * m.mu[(size_t)k * D + j];
+    b[(size_t)k * D + i] = t;
+    b32[(size_t)k * D + i] = (float)t;
+  }
+  for (int e = threadIdx.x; e < D * ldx; e += blockDim.x) {
+    int i = e / ldx, j = e - i * ldx;
+    W32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)sW[i * D + j] : 0.0f;
+  }
+  for (int e = threadIdx.x; e < T; e += blockDim.x) {
+    int i = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+    while (tri_idx(i + 1, 0) <= e) i++;
+    while (tri_idx(i, 0) > e) i--;
+    int j = e - tri_idx(i, 0);
+    Wt[(size_t)k * T + e] = sW[i * D + j];
+  }
+  if (threadIdx.x == 0) {
+    double ld = 0.0;
+    for (int i = 0; i < D; i++) ld += log(sL[i * D + i]);
+    logdetL[k] = ld;
+  }
+}
+
+// Cumulative weights (summed in component order, as the host and the oracle
+// do) and the per-component log constants.
+__device__ __forceinline__ void body_prepare_consts(const DevMixView &m, const double *logdetL, double *cw,
+                                                    double *lconst, float *lconst32) {
+  const int K = m.K, D = m.D;
+  double cst;
+  if (m.df > 0) {
+    double nu = (double)m.df;
+    cst = lgamma(0.5 * (nu + D)) - lgamma(0.5 * nu) - 0.5 * D * log(nu * PMCG_PI);
+  } else {
+    cst = -0.5 * D * PMCG_LN2PI;
+  }
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < K; k++) { s += m.w[k]; cw[k] = s; }
+  }
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double l = (m.w[k] > 0.0) ? log(m.w[k]) + cst - logdetL[k] : -INFINITY;
+    lconst[k] = l;
+    lconst32[k] = (float)l;
+  }
+}
+
+}  // namespace pmcg

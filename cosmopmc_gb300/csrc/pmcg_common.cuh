@@ -100,7 +100,7 @@ struct DevMixView {
   const float *W32;      // [K*D*D] L^-1, row-major, zero above the diagonal
   const float *b32;      // [K*D]
   const float *lconst32; // [K]
-  const float *L32;      // [K*D*D] L, row-major (single-precision draws)
+  const float *L32;      // [K*D*ldx] L, rows padded to ldx, zero above the diagonal (single-precision draws)
   const float *mu32;     // [K*D]
 };
 

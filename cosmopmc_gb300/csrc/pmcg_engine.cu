@@ -15,8 +15,7 @@
 #include <vector>
 
 #include "../../include/pmcg.h"
-#include "pmcg_internal.h"
-#include "pmcg_kernels.h"
+#include "pmcg_engine.h"
 
 using pmcg::set_error;
 
@@ -29,61 +28,7 @@ static bool ck(cudaError_t e, error **err, int line, const char *what) {
 }
 #define CK(expr, what) ck((expr), err, __LINE__, (what))
 
-// Carves one device allocation into 256-byte aligned arrays. First pass
-// (base == nullptr) only measures.
-struct Carver {
-  char *base = nullptr;
-  size_t off = 0;
-  template <typename T>
-  T *take(size_t n) {
-    off = (off + 255) & ~(size_t)255;
-    T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
-    off += n * sizeof(T);
-    return p;
-  }
-};
-
-enum PluginType { kPluginMix = 1, kPluginSn = 2, kPluginTpl = 3 };
-struct Plugin {
-  int type = 0;
-  DevMix mix;
-  SnDev sn;
-  TplDev tpl;
-};
-
-}  // namespace pmcg
-
-struct pmcg_posterior {
-  int npar = 0;
-  double logpr = 0.0;
-  std::vector<double> min, max;
-  std::vector<pmcg::Plugin> plugins;
-};
-
-namespace pmcg {
-
-// Buffers and scratch for one sample of N points (one run or one drop-in mirror).
-struct Work {
-  int K = 0, D = 0, df = -1, prec = 0, ldx = 0, S = 0;
-  size_t N = 0;
-  cudaStream_t s = nullptr;
-  DevMix prop;
-  double *bmin = nullptr, *bmax = nullptr;
-  double *X64 = nullptr;
-  float *X32 = nullptr;
-  int *idx = nullptr, *counts = nullptr;
-  short *flg = nullptr;
-  double *logq = nullptr, *logpost = nullptr, *logw = nullptr, *wbar = nullptr;
-  double *lt64 = nullptr, *Q64 = nullptr;
-  float *lt32 = nullptr, *Q32 = nullptr, *aw32 = nullptr;
-  WRed *wpart = nullptr;
-  double *empart = nullptr;
-  DevStats *dstats = nullptr, *hstats = nullptr;
-  void *arena = nullptr;
-  int launches = 0;
-};
-
-static void work_free(Work &w) {
+void work_free(Work &w) {
   devmix_free(w.prop);
   if (w.arena) cudaFree(w.arena);
   if (w.hstats) cudaFreeHost(w.hstats);
@@ -91,36 +36,56 @@ static void work_free(Work &w) {
   w = Work();
 }
 
-static bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) {
+// Lays out the arrays of a Work in one allocation (c.base == nullptr: measure only).
+static void work_layout(Work &w, Carver &c, size_t empart_bytes) {
+  const size_t N = w.N;
+  const int K = w.K, D = w.D, prec = w.prec;
+  const bool t = w.df > 0;
+  c.off = 0;
+  w.bmin = c.take<double>(D);
+  w.bmax = c.take<double>(D);
+  w.X64 = c.take<double>(N * D);
+  w.X32 = prec ? c.take<float>(N * w.ldx) : nullptr;
+  w.idx = c.take<int>(N);
+  w.counts = c.take<int>(K);
+  w.flg = c.take<short>(N);
+  w.logq = c.take<double>(N);
+  w.logpost = c.take<double>(N);
+  w.logw = c.take<double>(N);
+  w.wbar = c.take<double>(N);
+  w.lt64 = prec ? nullptr : c.take<double>(N * K);
+  w.Q64 = (!prec && t) ? c.take<double>(N * K) : nullptr;
+  w.lt32 = prec ? c.take<float>(N * K) : nullptr;
+  w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
+  w.aw32 = prec ? c.take<float>(N) : nullptr;
+  w.wpart = c.take<WRed>(weight_tiles(N));
+  w.empart = c.take<double>(empart_bytes / sizeof(double));
+  w.dstats = c.take<DevStats>(1);
+}
+
+size_t work_bytes(int K, int D, int df, int prec, size_t N) {
+  Work w;
+  w.K = K; w.D = D; w.df = df; w.prec = prec; w.N = N; w.ldx = round4(D);
+  int S;
+  size_t empart_bytes = em_partials_size(prec, K, D, &S, N);
+  Carver c;
+  work_layout(w, c, empart_bytes);
+  // + the proposal arena (devmix_alloc)
+  const size_t T = (size_t)D * (D + 1) / 2, ldx = w.ldx;
+  size_t mix = (size_t)K * (4 + 3 * D + D * D + T) * 8 + (size_t)K * (D * ldx + D + 1 + D * ldx + D + 3) * 4;
+  return c.off + 256 + mix + 256;
+}
+
+bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) {
   if (D < 1 || D > kMaxD || K < 1 || K > kMaxK) {
     set_error(err, PMCG_EDIM, __LINE__, "unsupported shape K=%d D=%d (K<=%d, D<=%d)", K, D, kMaxK, kMaxD);
     return false;
   }
   w.K = K; w.D = D; w.df = df; w.prec = prec; w.N = N; w.ldx = round4(D);
   size_t empart_bytes = em_partials_size(prec, K, D, &w.S, N);
-  const bool t = df > 0;
   Carver c;
   for (int pass = 0; pass < 2; pass++) {
-    c.off = 0;
-    w.bmin = c.take<double>(D);
-    w.bmax = c.take<double>(D);
-    w.X64 = c.take<double>(N * D);
-    w.X32 = prec ? c.take<float>(N * w.ldx) : nullptr;
-    w.idx = c.take<int>(N);
-    w.counts = c.take<int>(K);
-    w.flg = c.take<short>(N);
-    w.logq = c.take<double>(N);
-    w.logpost = c.take<double>(N);
-    w.logw = c.take<double>(N);
-    w.wbar = c.take<double>(N);
-    w.lt64 = prec ? nullptr : c.take<double>(N * K);
-    w.Q64 = (!prec && t) ? c.take<double>(N * K) : nullptr;
-    w.lt32 = prec ? c.take<float>(N * K) : nullptr;
-    w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
-    w.aw32 = prec ? c.take<float>(N) : nullptr;
-    w.wpart = c.take<WRed>(kWeightBlocks);
-    w.empart = c.take<double>(empart_bytes / sizeof(double));
-    w.dstats = c.take<DevStats>(1);
+    work_layout(w, c, empart_bytes);
     if (pass == 0) {
       if (!CK(cudaMalloc(&w.arena, c.off + 256), "device buffers")) return false;
       c.base = (char *)w.arena;
@@ -131,7 +96,6 @@ static bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error 
   if (!CK(devmix_alloc(w.prop, K, D, df), "proposal buffers")) return false;
   return true;
 }
-
 static bool upload_box(Work &w, const double *bmin, const double *bmax, error **err) {
   if (!bmin) return true;
   return CK(cudaMemcpyAsync(w.bmin, bmin, sizeof(double) * w.D, cudaMemcpyHostToDevice, w.s), "box") &&
@@ -486,19 +450,6 @@ extern "C" double mvdens_log_pdf_void(void *g, const double *x, error **err) {
 }
 
 // ===================================================================== runs
-struct pmcg_run {
-  Work w;
-  const pmcg_posterior *post = nullptr;
-  bool box = false;
-  uint64_t seed = 0;
-  uint32_t calls = 0;
-  bool timing = false;
-  cudaEvent_t ev[PMCG_NSTAGE + 1] = {};
-  double stage_ms[PMCG_NSTAGE] = {};
-  int timed = 0;
-  int last_launches = 0;
-};
-
 extern "C" pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_posterior *post, const parabox *pb,
                                      size_t nsamples, int precision, uint64_t seed, error **err) {
   if (!proposal || !post || nsamples == 0) {

@@ -1,0 +1,83 @@
+// pmcg_engine.h — engine-internal state shared by pmcg_engine.cu (runs,
+// drop-in mirrors, posteriors) and k_batch.cu (the batch kernel). Not part of
+// the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/pmcg.h"
+#include "pmcg_internal.h"
+#include "pmcg_kernels.h"
+
+namespace pmcg {
+
+// Carves one device allocation into 256-byte aligned arrays. First pass
+// (base == nullptr) only measures.
+struct Carver {
+  char *base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  T *take(size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+enum PluginType { kPluginMix = 1, kPluginSn = 2, kPluginTpl = 3 };
+struct Plugin {
+  int type = 0;
+  DevMix mix;
+  SnDev sn;
+  TplDev tpl;
+};
+
+// Buffers and scratch for one sample of N points (one run or one drop-in mirror).
+struct Work {
+  int K = 0, D = 0, df = -1, prec = 0, ldx = 0, S = 0;
+  size_t N = 0;
+  cudaStream_t s = nullptr;
+  DevMix prop;
+  double *bmin = nullptr, *bmax = nullptr;
+  double *X64 = nullptr;
+  float *X32 = nullptr;
+  int *idx = nullptr, *counts = nullptr;
+  short *flg = nullptr;
+  double *logq = nullptr, *logpost = nullptr, *logw = nullptr, *wbar = nullptr;
+  double *lt64 = nullptr, *Q64 = nullptr;
+  float *lt32 = nullptr, *Q32 = nullptr, *aw32 = nullptr;
+  WRed *wpart = nullptr;
+  double *empart = nullptr;
+  DevStats *dstats = nullptr, *hstats = nullptr;
+  void *arena = nullptr;
+  int launches = 0;
+};
+
+bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err);
+void work_free(Work &w);
+// Device bytes work_alloc takes for this shape (admission control).
+size_t work_bytes(int K, int D, int df, int prec, size_t N);
+
+}  // namespace pmcg
+
+struct pmcg_posterior {
+  int npar = 0;
+  double logpr = 0.0;
+  std::vector<double> min, max;
+  std::vector<pmcg::Plugin> plugins;
+};
+
+struct pmcg_run {
+  pmcg::Work w;
+  const pmcg_posterior *post = nullptr;
+  bool box = false;
+  uint64_t seed = 0;
+  uint32_t calls = 0;
+  bool timing = false;
+  cudaEvent_t ev[PMCG_NSTAGE + 1] = {};
+  double stage_ms[PMCG_NSTAGE] = {};
+  int timed = 0;
+  int last_launches = 0;
+};

@@ -9,7 +9,12 @@ namespace pmcg {
 
 constexpr int kMaxD = 64;    // largest parameter dimension
 constexpr int kMaxK = 256;   // largest component count
-constexpr int kWeightBlocks = 608;  // fixed grid of the weight reduction (4 x 152 SMs)
+// Tiles of the weight reduction (one partial record per 2048 samples).
+size_t weight_tiles(size_t N);
+// Sample chunks per component of the EM statistics.
+int em_chunks(int K, size_t N);
+// Components staged per barrier by the FP32 log-pdf.
+int mix_chunk(int D, int ldx, int K);
 
 // Per-iteration scalars computed on the device (one small D2H per iteration).
 struct DevStats {

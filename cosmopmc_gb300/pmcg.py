@@ -79,7 +79,8 @@ class SnData(C.Structure):
 
 class IterStats(C.Structure):
     _fields_ = [("ln_evidence", C.c_double), ("perplexity", C.c_double), ("ess", C.c_double), ("enc", C.c_double),
-                ("logSum", C.c_double), ("maxW", C.c_double), ("nok", C.c_size_t), ("ndead", C.c_int)]
+                ("logSum", C.c_double), ("maxW", C.c_double), ("nok", C.c_size_t), ("ndead", C.c_int),
+                ("status", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -161,6 +162,13 @@ SIGNATURES = [
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
     ("pmcg_run_stage_ms", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
+    ("pmcg_batch_create", C.c_void_p, [C.c_int, C.POINTER(C.c_void_p), PErr]),
+    ("pmcg_batch_iterate", None, [C.c_void_p, _dp, C.POINTER(IterStats), PErr]),
+    ("pmcg_batch_autotune", None, [C.c_void_p, PErr]),
+    ("pmcg_batch_config", None, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int)]),
+    ("pmcg_batch_last_ms", C.c_double, [C.c_void_p]),
+    ("pmcg_batch_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_importance_weights_noalloc", None, [C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.POINTER(WeightStats), C.c_void_p, PErr]),
     ("pmcg_version", C.c_char_p, []),
@@ -477,6 +485,44 @@ class Run:
     def free(self):
         if self.p:
             load().pmcg_run_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many runs iterated by one persistent launch (pmcg_batch_*); holds the runs alive."""
+
+    def __init__(self, runs):
+        self.runs = list(runs)
+        arr = (C.c_void_p * len(self.runs))(*[r.p.value for r in self.runs])
+        self.p = C.c_void_p(call("pmcg_batch_create", len(self.runs), arr))
+
+    def iterate(self, betas=None):
+        R = len(self.runs)
+        st = (IterStats * R)()
+        b = None if betas is None else _dptr(_f64(betas))
+        call("pmcg_batch_iterate", self.p, b, st)
+        return [s.as_dict() for s in st]
+
+    def autotune(self):
+        call("pmcg_batch_autotune", self.p)
+
+    def config(self):
+        v = [C.c_int() for _ in range(4)]
+        load().pmcg_batch_config(self.p, *[C.byref(x) for x in v])
+        return dict(samples_per_thread=v[0].value, blocks_per_sm=v[1].value, grid=v[2].value, graph=v[3].value)
+
+    def last_ms(self):
+        return load().pmcg_batch_last_ms(self.p)
+
+    def free(self):
+        if self.p:
+            load().pmcg_batch_free(C.byref(self.p))
             self.p = None
 
     def __del__(self):

@@ -281,7 +281,8 @@ typedef struct {
   double logSum;
   double maxW;
   size_t nok;          /* samples with flg==1 */
-  int ndead;           /* components buried by this update */
+  int ndead;           /* components with weight 0 after this update */
+  int status;          /* 0, or the PMCG_E* code of a failed iteration (batch runs) */
 } pmcg_iter_stats;
 
 /* A run keeps its proposal, sample and scratch on the GPU. nsamples is
@@ -306,6 +307,29 @@ void pmcg_run_set_timing(pmcg_run *r, int on);
 int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage);
 /* Number of kernel launches issued by the last pmcg_run_iterate call. */
 int pmcg_run_last_launches(const pmcg_run *r);
+
+/* ------------------------------------------------------------------ *
+ * Part 2 — batched runs: one persistent launch per iteration          *
+ * ------------------------------------------------------------------ */
+/* A batch iterates many independent runs (uneven dimension, component count,
+ * sample count and likelihood) with one cooperative kernel per iteration,
+ * captured with its copies in a CUDA graph. Every run must be PMCG_MIXED with
+ * D <= 32 and a posterior with exactly one likelihood (mixture, SN Ia or
+ * template). The runs keep their state (pmcg_run_get_proposal/_sample work as
+ * usual) and give the same results as when iterated alone. The batch
+ * references the runs; free it before them. */
+typedef struct pmcg_batch pmcg_batch;
+pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err);
+/* betas [nruns] (NULL: all 1); stats [nruns] (NULL allowed). A run whose
+ * iteration fails reports stats[r].status != 0 and keeps its proposal. */
+void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *stats, error **err);
+/* Time the non-mutating stages under each candidate (samples per thread of
+ * the log-density stages, resident blocks per SM), keep the fastest and
+ * cache it for batches of the same shape. */
+void pmcg_batch_autotune(pmcg_batch *b, error **err);
+void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, int *blocks_per_sm, int *grid, int *graph);
+double pmcg_batch_last_ms(const pmcg_batch *b);
+void pmcg_batch_free(pmcg_batch **b);
 
 /* ------------------------------------------------------------------ *
  * Part 2 — importance weights without allocation                      *

@@ -1,0 +1,92 @@
+"""Batched runs (one persistent cooperative launch per iteration) against the
+same runs iterated alone: statistics and proposals must be bit-identical,
+and a failing run must not disturb the others."""
+import numpy as np
+import pytest
+
+from cosmopmc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def make_run(P, kind, D, K, N, seed):
+    if kind == "mix":
+        wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=4 if seed % 2 else -1, seed=seed, prop_hi=2.0)
+        w, mu, cov, df = wl["prop"]
+        wt, mut, covt, _ = wl["target"]
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+        target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+        post = P.Posterior(D).add_mix(target)
+        return prop, post, None
+    if kind == "sn":
+        wl = W.sn_workload(K=K, seed=seed)
+        w, mu, cov, df = wl["prop"]
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+        post = P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"])
+        return prop, post, P.Parabox(wl["bmin"], wl["bmax"])
+    if kind == "tpl":
+        wl = W.template_workload(D=D, M=64, K=K, seed=seed)
+        w, mu, cov, df = wl["prop"]
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+        post = P.Posterior(D, wl["bmin"], wl["bmax"]).add_template(wl["A"], wl["C"], wl["dobs"])
+        return prop, post, P.Parabox(wl["bmin"], wl["bmax"])
+    if kind == "dead":  # every draw falls outside the box
+        prop = P.MixMvdens.from_arrays([1.0], [[10.0, 10.0]], cov=[np.eye(2) * 0.01], df=-1).cholesky()
+        target = P.MixMvdens.from_arrays([1.0], [[0.0, 0.0]], cov=[np.eye(2)], df=-1).cholesky()
+        post = P.Posterior(2, [-1, -1], [1, 1]).add_mix(target)
+        return prop, post, P.Parabox([-1, -1], [1, 1])
+    raise ValueError(kind)
+
+
+SPECS = [("mix", 2, 1, 1000, 1), ("mix", 5, 3, 3001, 2), ("mix", 13, 7, 20000, 3), ("mix", 20, 12, 9000, 5),
+         ("sn", 6, 5, 4000, 740), ("tpl", 3, 4, 2500, 91), ("dead", 2, 1, 777, 9)]
+
+
+def test_batch_is_bit_identical_to_runs_alone(pmcg):
+    P = pmcg
+    keep, batch_runs, alone_runs = [], [], []
+    for kind, D, K, N, seed in SPECS:
+        prop, post, box = make_run(P, kind, D, K, N, seed)
+        keep.append((prop, post, box))
+        batch_runs.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+        alone_runs.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+    batch = P.Batch(batch_runs)
+    cfg = batch.config()
+    assert cfg["grid"] > 0
+    betas = [1.0, 0.5, 1.0, 0.8, 1.0, 1.0, 1.0]
+    for it in range(3):
+        bst = batch.iterate(betas)
+        for r, (spec, run) in enumerate(zip(SPECS, alone_runs)):
+            if spec[0] == "dead":
+                assert bst[r]["status"] == -9011
+                with pytest.raises(P.PmcgError):
+                    run.iterate(betas[r])
+                continue
+            ast = run.iterate(betas[r])
+            ast["status"] = 0
+            assert bst[r] == ast, (it, spec, bst[r], ast)
+            wb, mb, Lb = batch_runs[r].proposal().arrays()
+            wa, ma, La = run.proposal().arrays()
+            assert np.array_equal(wb, wa) and np.array_equal(mb, ma) and np.array_equal(Lb, La), (it, spec)
+    # the failing run kept its proposal
+    w, mu, L = batch_runs[-1].proposal().arrays()
+    assert np.array_equal(mu, [[10.0, 10.0]])
+    batch.free()
+
+
+def test_batch_autotune_keeps_results(pmcg):
+    P = pmcg
+    keep, runs_a, runs_b = [], [], []
+    for kind, D, K, N, seed in SPECS[:5]:
+        prop, post, box = make_run(P, kind, D, K, N, seed)
+        keep.append((prop, post, box))
+        runs_a.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+        runs_b.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+    a = P.Batch(runs_a)
+    b = P.Batch(runs_b)
+    b.autotune()
+    cfg = b.config()
+    assert cfg["samples_per_thread"] in (1, 2) and cfg["blocks_per_sm"] >= 1
+    for it in range(2):
+        assert a.iterate() == b.iterate()
+    assert b.last_ms() > 0.0
