@@ -44,9 +44,12 @@ __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
   const unsigned long long B = ((unsigned long long)(o.z >> 5) << 26) | (unsigned long long)(o.w >> 6);
   const float two53inv = 1.1102230246251565e-16f;  // 2^-53
-  const float oma = __ull2float_rn((1ull << 53) - A) * two53inv;  // 1 - a in (0, 1]
+  // -2 ln(1-a): from the exact small a below 1/2 (log1p), from the exact
+  // complement 1-a above, so r keeps single precision at both ends.
+  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(__ull2float_rn(A) * two53inv))
+                                      : -2.0f * logf(__ull2float_rn((1ull << 53) - A) * two53inv);
   const float b = __ull2float_rn(B) * two53inv;
-  float r = sqrtf(-2.0f * logf(oma));
+  float r = sqrtf(r2);
   float sn, cs;
   sincospif(2.0f * b, &sn, &cs);
   g0 = r * cs;
