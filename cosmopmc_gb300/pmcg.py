@@ -94,6 +94,28 @@ class WeightStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_jobs", C.c_int), ("autotune", C.c_int)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("ln_evidence", C.c_double),
+                ("perplexity", C.c_double), ("ess", C.c_double), ("enc", C.c_double), ("submit_s", C.c_double),
+                ("start_s", C.c_double), ("finish_s", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("queued", C.c_int), ("resident", C.c_int), ("peak_resident", C.c_int),
+                ("bytes_in_use", C.c_size_t), ("peak_bytes", C.c_size_t), ("budget_bytes", C.c_size_t),
+                ("epochs", C.c_longlong)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 PErr = C.POINTER(C.POINTER(Error))
 _dp = C.POINTER(C.c_double)
 LOGPDF_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, _dp, PErr)
@@ -169,6 +191,13 @@ SIGNATURES = [
                                  C.POINTER(C.c_int)]),
     ("pmcg_batch_last_ms", C.c_double, [C.c_void_p]),
     ("pmcg_batch_free", None, [C.POINTER(C.c_void_p)]),
+    ("pmcg_server_create", C.c_void_p, [C.POINTER(ServerOpts), PErr]),
+    ("pmcg_server_submit", C.c_int64, [C.c_void_p, C.POINTER(MixMvdensS), C.c_void_p, C.POINTER(ParaboxS),
+                                       C.c_size_t, C.c_int, C.c_int, C.c_double, C.c_uint64, PErr]),
+    ("pmcg_server_wait", C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(JobResult),
+                                   C.POINTER(MixMvdensS), PErr]),
+    ("pmcg_server_info", None, [C.c_void_p, C.POINTER(ServerInfo)]),
+    ("pmcg_server_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_importance_weights_noalloc", None, [C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.POINTER(WeightStats), C.c_void_p, PErr]),
     ("pmcg_version", C.c_char_p, []),
@@ -523,6 +552,47 @@ class Batch:
     def free(self):
         if self.p:
             load().pmcg_batch_free(C.byref(self.p))
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching PMC server (pmcg_server_*)."""
+
+    def __init__(self, hbm_budget_bytes=0, max_jobs=0, autotune=False):
+        o = ServerOpts(hbm_budget_bytes, max_jobs, 1 if autotune else 0)
+        self.p = C.c_void_p(call("pmcg_server_create", C.byref(o)))
+        self._keep = {}
+
+    def submit(self, proposal: MixMvdens, posterior: Posterior, nsamples, niter, seed, box=None,
+               tempering=TEMPERING_NONE, t_min=0.0):
+        jid = call("pmcg_server_submit", self.p, proposal.p, posterior.p, box.p if box is not None else None,
+                   nsamples, niter, tempering, t_min, seed)
+        self._keep[jid] = (proposal.K, proposal.D, posterior)
+        return jid
+
+    def wait(self, jid, timeout=60.0, want_proposal=False):
+        res = JobResult()
+        K, D, _ = self._keep[jid]
+        m = MixMvdens(K, D) if want_proposal else None
+        r = call("pmcg_server_wait", self.p, jid, timeout, C.byref(res), m.p if m is not None else None)
+        out = res.as_dict()
+        out["finished"] = r == 1
+        return (out, m) if want_proposal else out
+
+    def info(self):
+        i = ServerInfo()
+        load().pmcg_server_info(self.p, C.byref(i))
+        return i.as_dict()
+
+    def free(self):
+        if self.p:
+            load().pmcg_server_free(C.byref(self.p))
             self.p = None
 
     def __del__(self):

@@ -332,6 +332,47 @@ double pmcg_batch_last_ms(const pmcg_batch *b);
 void pmcg_batch_free(pmcg_batch **b);
 
 /* ------------------------------------------------------------------ *
+ * Part 2 — serving: continuous batching of PMC jobs                   *
+ * ------------------------------------------------------------------ */
+/* A server thread owns the GPU. Jobs are admitted at epoch boundaries while
+ * free slots and the device-memory budget allow (a job's footprint is the exact
+ * size of its run's buffers); every epoch runs one iteration of all resident
+ * jobs in one batch launch, so jobs that arrive while others run join the next
+ * epoch and overlap with them. A job's result depends only on its own inputs
+ * (same alone and in any mix). Served jobs: D <= 32, one likelihood. */
+typedef struct pmcg_server pmcg_server;
+typedef struct {
+  size_t hbm_budget_bytes;  /* 0: 80% of the free device memory at creation */
+  int max_jobs;             /* resident jobs at most (0: 512) */
+  int autotune;             /* tune each new batch shape (cached per shape) */
+} pmcg_server_opts;
+typedef struct {
+  int status;               /* 0 done, > 0 queued/running, < 0 PMCG_E* error */
+  int iterations;           /* iterations completed */
+  double ln_evidence, perplexity, ess, enc;  /* of the last iteration */
+  double submit_s, start_s, finish_s;        /* server clock (s) */
+} pmcg_job_result;
+typedef struct {
+  int queued, resident, peak_resident;
+  size_t bytes_in_use, peak_bytes, budget_bytes;
+  long long epochs;
+} pmcg_server_info_t;
+pmcg_server *pmcg_server_create(const pmcg_server_opts *opts, error **err);
+/* Thread-safe. The proposal and box are copied; the posterior is referenced
+ * and must outlive the job. Tempering as get_tempering_beta(tempering, iter,
+ * t_min, niter). Returns the job id (> 0), or 0 with an error. */
+int64_t pmcg_server_submit(pmcg_server *s, const mix_mvdens *proposal, const pmcg_posterior *post, const parabox *pb,
+                           size_t nsamples, int niter, int tempering, double t_min, uint64_t seed, error **err);
+/* Waits at most timeout_s: returns 1 when the job finished (res filled,
+ * final_proposal filled if not NULL and the job succeeded), 0 on timeout
+ * (PMCG_ETIMEOUT), -1 on an unknown job. */
+int pmcg_server_wait(pmcg_server *s, int64_t job, double timeout_s, pmcg_job_result *res,
+                     mix_mvdens *final_proposal, error **err);
+void pmcg_server_info(pmcg_server *s, pmcg_server_info_t *info);
+/* Stops the loop after the current epoch and frees every job. */
+void pmcg_server_free(pmcg_server **s);
+
+/* ------------------------------------------------------------------ *
  * Part 2 — importance weights without allocation                      *
  * ------------------------------------------------------------------ */
 /* No counterpart in the reference. For callers that cannot let a library

@@ -134,3 +134,13 @@ def test_weight_step_rejects_host_callbacks(pmcg):
         pmcg.call("generic_get_importance_weight_and_deduced_verb", ps.p, m.p, q, C.cast(cb, C.c_void_p), None,
                   None, 1.0, 1)
     assert e.value.code == -9006
+
+
+def test_server_and_batch_need_a_gpu(pmcg):
+    if pmcg.device_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(pmcg.PmcgError) as e:
+        pmcg.Server()
+    assert e.value.code == -9001
+    with pytest.raises(pmcg.PmcgError):
+        pmcg.call("pmcg_batch_create", 0, None)

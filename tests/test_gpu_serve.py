@@ -1,0 +1,97 @@
+"""Serving loop with continuous batching: a job's result is the same alone and in
+a mix of jobs that arrive while it runs; failures stay with their job;
+admission respects the device-memory budget; waits are bounded."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from test_gpu_batch import make_run
+
+pytestmark = pytest.mark.gpu
+
+MIX = [("mix", 3, 2, 4000, 11), ("mix", 17, 9, 30000, 12), ("sn", 6, 4, 8000, 740), ("mix", 9, 5, 15000, 13),
+       ("tpl", 3, 3, 6000, 91), ("mix", 12, 14, 25000, 14), ("mix", 20, 6, 12000, 15), ("dead", 2, 1, 500, 9),
+       ("mix", 5, 1, 2000, 16), ("mix", 31, 4, 9000, 17)]
+PROBE = ("mix", 8, 6, 20000, 123)
+
+
+def _job(P, spec, keep):
+    prop, post, box = make_run(P, *spec)
+    keep.append((prop, post, box))
+    return prop, post, box
+
+
+def test_job_result_same_alone_and_in_the_mix(pmcg):
+    P = pmcg
+    keep = []
+    prop, post, box = _job(P, PROBE, keep)
+    s1 = P.Server()
+    j = s1.submit(prop, post, PROBE[3], 6, PROBE[4], box=box, tempering=P.TEMPERING_LOG, t_min=0.05)
+    alone, prop_alone = s1.wait(j, timeout=120, want_proposal=True)
+    s1.free()
+    assert alone["finished"] and alone["status"] == 0 and alone["iterations"] == 6
+
+    s2 = P.Server(autotune=False)
+    ids = {}
+    jobs = [_job(P, spec, keep) for spec in MIX]
+
+    def feeder():
+        rng = np.random.default_rng(0)
+        for i, (spec, (pp, po, bx)) in enumerate(zip(MIX, jobs)):
+            ids[i] = s2.submit(pp, po, spec[3], 3 + i % 5, spec[4], box=bx)
+            time.sleep(float(rng.uniform(0.0, 0.01)))
+            if i == 4:  # the probe arrives while earlier jobs are on the GPU
+                ids["probe"] = s2.submit(prop, post, PROBE[3], 6, PROBE[4], box=box, tempering=P.TEMPERING_LOG,
+                                         t_min=0.05)
+
+    t = threading.Thread(target=feeder)
+    t.start()
+    t.join()
+    mixed, prop_mixed = s2.wait(ids["probe"], timeout=120, want_proposal=True)
+    results = {i: s2.wait(ids[i], timeout=120) for i in range(len(MIX))}
+    info = s2.info()
+    s2.free()
+    assert info["peak_resident"] > 1, info
+    for key in ("status", "iterations", "ln_evidence", "perplexity", "ess", "enc"):
+        assert mixed[key] == alone[key], (key, mixed[key], alone[key])
+    for a, b in zip(prop_alone.arrays(), prop_mixed.arrays()):
+        assert np.array_equal(a, b)
+    for i, spec in enumerate(MIX):
+        if spec[0] == "dead":
+            assert results[i]["status"] == -9011
+        else:
+            assert results[i]["status"] == 0 and results[i]["iterations"] == 3 + i % 5, (spec, results[i])
+
+
+def test_admission_respects_the_memory_budget(pmcg):
+    P = pmcg
+    keep = []
+    specs = [("mix", 10, 5, 40000, 20 + i) for i in range(6)]
+    jobs = [_job(P, s, keep) for s in specs]
+    # budget for about two of these jobs at once
+    probe = P.Server()
+    jid = probe.submit(jobs[0][0], jobs[0][1], 40000, 1, 1)
+    probe.wait(jid, timeout=60)
+    one = probe.info()["peak_bytes"]
+    probe.free()
+    s = P.Server(hbm_budget_bytes=int(2.5 * one))
+    ids = [s.submit(pp, po, sp[3], 4, sp[4]) for sp, (pp, po, bx) in zip(specs, jobs)]
+    res = [s.wait(i, timeout=120) for i in ids]
+    info = s.info()
+    s.free()
+    assert all(r["status"] == 0 for r in res)
+    assert info["peak_resident"] <= 2 and info["peak_bytes"] <= info["budget_bytes"], info
+
+
+def test_wait_is_bounded(pmcg):
+    P = pmcg
+    keep = []
+    prop, post, box = _job(P, ("mix", 16, 8, 400000, 31), keep)
+    s = P.Server()
+    jid = s.submit(prop, post, 400000, 40, 31)
+    with pytest.raises(P.PmcgError) as e:
+        s.wait(jid, timeout=0.001)
+    assert e.value.code == -9009
+    s.free()  # stops after the current epoch
