@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the drop-in e2e leg (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-runs measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     return ap.parse_args()
 
 
@@ -149,6 +151,133 @@ def time_run(P, run, steps, warmup, l2buf, sync, prop):
     ms, n = run.stage_ms()
     run.set_timing(False)
     return stats, ms, n, launches, wall
+
+
+def ragged_specs(R, seed=256):
+    """Batched workload: R runs, half SN-type (D=6), half Gaussian-mixture targets with
+    D ~ U{2..20}, K ~ U{1..20}, N ~ logU(1e3, 1e5)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for r in range(R):
+        N = int(round(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))))
+        K = int(rng.integers(1, 21))
+        if r % 2 == 0:
+            specs.append(("sn", 6, max(K, 2), N, 740 + r))
+        else:
+            specs.append(("mix", int(rng.integers(2, 21)), K, N, 1000 + r))
+    return specs
+
+
+def build_spec(P, W, spec, cache):
+    kind, D, K, N, seed = spec
+    if kind == "sn":
+        if "sn_post" not in cache:
+            wl = W.sn_workload()
+            cache["sn_post"] = (P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"]),
+                                P.Parabox(wl["bmin"], wl["bmax"]))
+        post, box = cache["sn_post"]
+        rng = np.random.default_rng(seed)
+        w, mu, cov, df = W.random_pos_proposal(rng, K, W.SN_BOX_MIN, W.SN_BOX_MAX)
+        return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
+    if kind == "tpl":
+        if "tpl_post" not in cache:
+            wl = W.template_workload(D=12, M=2048, K=16)
+            cache["tpl_post"] = (P.Posterior(12, wl["bmin"], wl["bmax"]).add_template(wl["A"], wl["C"], wl["dobs"]),
+                                 P.Parabox(wl["bmin"], wl["bmax"]))
+        post, box = cache["tpl_post"]
+        rng = np.random.default_rng(seed)
+        w, mu, cov, df = W.random_pos_proposal(rng, 16, -np.ones(12), np.ones(12))
+        return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
+    wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=-1, seed=seed, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+    post = P.Posterior(D).add_mix(target)
+    cache.setdefault("keep", []).append(target)
+    return prop, post, None
+
+
+def batch_bench(P, W, R=256, iters=5):
+    """256 ragged runs: one persistent launch per iteration vs the same runs one at a time."""
+    specs = ragged_specs(R)
+    cache = {}
+    built = [build_spec(P, W, s, cache) for s in specs]
+    runs_b = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    runs_s = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    total = sum(s[3] for s in specs)
+    batch = P.Batch(runs_b)
+    t0 = time.perf_counter()
+    batch.autotune()
+    tune_s = time.perf_counter() - t0
+    batch.iterate()  # warm-up
+    ms = []
+    failed = 0
+    for _ in range(iters):
+        st = batch.iterate()
+        ms.append(batch.last_ms())
+        failed += sum(1 for x in st if x["status"] != 0)
+    for r in runs_s:  # warm-up of the one-at-a-time path
+        try:
+            r.iterate()
+        except P.PmcgError:
+            pass
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        for r in runs_s:
+            try:
+                r.iterate()
+            except P.PmcgError:
+                pass
+    seq_s = (time.perf_counter() - t0) / 2
+    med = float(np.median(ms))
+    cfg = batch.config()
+    batch.free()
+    return {"workload": f"{R} runs, half SN (D=6), half GMM (D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5)",
+            "samples_per_iter": total, "value": total / (med / 1e3), "unit": UNIT, "ms_per_iter": med,
+            "one_run_at_a_time_samples_per_s": total / seq_s, "speedup_vs_one_at_a_time": (seq_s * 1e3) / med,
+            "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed,
+            "timing": "CUDA events around each graph launch (library stream), median of iterations"}
+
+
+def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4):
+    """Poisson arrivals of jobs (90% from the ragged mix, 10% template-sized), 5-10 iterations each."""
+    rng = np.random.default_rng(seed)
+    pool_specs = ragged_specs(64, seed=99)
+    cache = {}
+    pool = [(s, build_spec(P, W, s, cache)) for s in pool_specs]
+    tpl_spec = ("tpl", 12, 16, 262144, 91)
+    tpl = (tpl_spec, build_spec(P, W, tpl_spec, cache))
+    out = []
+    for rate in rates:
+        srv = P.Server()
+        n_jobs = max(8, int(rate * window_s))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+        ids = []
+        t_start = time.perf_counter()
+        for i in range(n_jobs):
+            dt = arrivals[i] - (time.perf_counter() - t_start)
+            if dt > 0:
+                time.sleep(dt)
+            spec, (pp, po, bx) = tpl if rng.uniform() < 0.1 else pool[int(rng.integers(0, len(pool)))]
+            niter = int(rng.integers(5, 11))
+            ids.append((srv.submit(pp, po, spec[3], niter, int(rng.integers(1, 1 << 30)), box=bx), spec[3], niter))
+        res = [(srv.wait(j, timeout=600), n, it) for j, n, it in ids]
+        wall = time.perf_counter() - t_start
+        info = srv.info()
+        srv.free()
+        lat = np.array([r["finish_s"] - r["submit_s"] for r, _, _ in res if r["status"] == 0])
+        samples = sum(n * it for r, n, it in res if r["status"] == 0)
+        out.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "ok": int(len(lat)),
+                    "p50_ms": float(np.percentile(lat, 50) * 1e3) if len(lat) else None,
+                    "p99_ms": float(np.percentile(lat, 99) * 1e3) if len(lat) else None,
+                    "samples_per_s": samples / wall, "peak_resident": info["peak_resident"],
+                    "epochs": info["epochs"]})
+    return {"workload": "Poisson arrivals; 90% jobs from the ragged mix, 10% template-sized (D=12, N=2^18, "
+                        "M=2048); 5-10 iterations per job; mixed precision",
+            "latency": "job submit to result (server clock)", "rates": out}
 
 
 def cpu_baseline(O, W, nsample, seed=5):
@@ -350,6 +479,11 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{reps} x {args.cpu_sample} samples of this workload "
                                           f"(oracle/pmc_oracle.c, OpenMP)"}
+    from cosmopmc_gb300 import pmcg as P
+    if not args.no_batch:
+        line["batch"] = batch_bench(P, W)
+    if not args.no_serve:
+        line["serving"] = serve_bench(P, W)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -10,29 +10,43 @@
 namespace pmcg {
 
 // ------------------------------------------------------------------ allocation
+// Every array starts on a 256-byte boundary (the single-precision factors are
+// read as float4).
+static size_t devmix_layout(int K, int D, size_t off[13]) {
+  const size_t T = (size_t)D * (D + 1) / 2, Kz = (size_t)K, ldx = (size_t)round4(D);
+  const size_t nd[8] = {Kz, Kz, Kz * D, Kz * D * D, Kz * T, Kz * D, Kz, Kz};
+  const size_t nf[5] = {Kz * D * ldx, Kz * D, Kz, Kz * D * ldx, Kz * D};
+  size_t o = 0;
+  for (int i = 0; i < 8; i++) { off[i] = o; o = (o + nd[i] * sizeof(double) + 255) & ~(size_t)255; }
+  for (int i = 0; i < 5; i++) { off[8 + i] = o; o = (o + nf[i] * sizeof(float) + 255) & ~(size_t)255; }
+  return o;
+}
+
+size_t devmix_bytes(int K, int D) {
+  size_t off[13];
+  return devmix_layout(K, D, off);
+}
+
 cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.K = K; m.D = D; m.df = df; m.ldx = round4(D);
-  const int T = D * (D + 1) / 2;
-  size_t nd = (size_t)K * (1 + 1 + D + D * D + T + D + 1 + 1);
-  size_t nf = (size_t)K * ((size_t)D * m.ldx + D + 1 + (size_t)D * m.ldx + D + 3);
-  size_t bytes = nd * sizeof(double) + nf * sizeof(float) + 256;
-  cudaError_t e = cudaMalloc(&m.arena, bytes);
+  size_t off[13];
+  const size_t o = devmix_layout(K, D, off);
+  cudaError_t e = cudaMalloc(&m.arena, o);
   if (e != cudaSuccess) { m.arena = nullptr; return e; }
-  double *p = (double *)m.arena;
-  m.w = p; p += K;
-  m.cw = p; p += K;
-  m.mu = p; p += (size_t)K * D;
-  m.L = p; p += (size_t)K * D * D;
-  m.Wt = p; p += (size_t)K * T;
-  m.b = p; p += (size_t)K * D;
-  m.logdetL = p; p += K;
-  m.lconst = p; p += K;
-  float *f = (float *)p;
-  m.W32 = f; f += (size_t)K * D * m.ldx;
-  m.b32 = f; f += (size_t)K * D;
-  m.lconst32 = f; f += K;
-  m.L32 = f; f += (size_t)K * D * m.ldx;
-  m.mu32 = f;
+  char *a = (char *)m.arena;
+  m.w = (double *)(a + off[0]);
+  m.cw = (double *)(a + off[1]);
+  m.mu = (double *)(a + off[2]);
+  m.L = (double *)(a + off[3]);
+  m.Wt = (double *)(a + off[4]);
+  m.b = (double *)(a + off[5]);
+  m.logdetL = (double *)(a + off[6]);
+  m.lconst = (double *)(a + off[7]);
+  m.W32 = (float *)(a + off[8]);
+  m.b32 = (float *)(a + off[9]);
+  m.lconst32 = (float *)(a + off[10]);
+  m.L32 = (float *)(a + off[11]);
+  m.mu32 = (float *)(a + off[12]);
   return cudaSuccess;
 }
 

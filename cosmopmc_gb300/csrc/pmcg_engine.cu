@@ -70,10 +70,7 @@ size_t work_bytes(int K, int D, int df, int prec, size_t N) {
   size_t empart_bytes = em_partials_size(prec, K, D, &S, N);
   Carver c;
   work_layout(w, c, empart_bytes);
-  // + the proposal arena (devmix_alloc)
-  const size_t T = (size_t)D * (D + 1) / 2, ldx = w.ldx;
-  size_t mix = (size_t)K * (4 + 3 * D + D * D + T) * 8 + (size_t)K * (D * ldx + D + 1 + D * ldx + D + 3) * 4;
-  return c.off + 256 + mix + 256;
+  return c.off + 256 + devmix_bytes(K, D);  // + the proposal arena
 }
 
 bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) {

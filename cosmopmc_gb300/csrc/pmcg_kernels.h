@@ -42,6 +42,7 @@ struct DevMix {
 };
 
 cudaError_t devmix_alloc(DevMix &m, int K, int D, int df);
+size_t devmix_bytes(int K, int D);
 void devmix_free(DevMix &m);
 // Upload w, mu, L (host, FP64) and derive L^-1, L^-1 mu, constants, cumulative weights.
 cudaError_t devmix_upload(DevMix &m, const double *w, const double *mu, const double *L, cudaStream_t s);
