@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the drop-in e2e leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-runs measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
+                    help="single-precision log-densities on tcgen05 (1) or CUDA cores (0); default: library setting")
     return ap.parse_args()
 
 
@@ -154,8 +156,8 @@ def time_run(P, run, steps, warmup, l2buf, sync, prop):
 
 
 def ragged_specs(R, seed=256):
-    """Batched workload: R runs, half SN-type (D=6), half Gaussian-mixture targets with
-    D ~ U{2..20}, K ~ U{1..20}, N ~ logU(1e3, 1e5)."""
+    """Batched workload: R runs, half SN-type (D=6, 740 supernovae, Fisher-matrix start),
+    half Gaussian-mixture targets with D ~ U{2..20}, K ~ U{1..20}, N ~ logU(1e3, 1e5)."""
     rng = np.random.default_rng(seed)
     specs = []
     for r in range(R):
@@ -175,9 +177,10 @@ def build_spec(P, W, spec, cache):
             wl = W.sn_workload()
             cache["sn_post"] = (P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"]),
                                 P.Parabox(wl["bmin"], wl["bmax"]))
+            cache["sn_fisher"] = W.sn_fisher(wl["sn"], W.SN_TRUTH)
         post, box = cache["sn_post"]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.random_pos_proposal(rng, K, W.SN_BOX_MIN, W.SN_BOX_MAX)
+        w, mu, cov, df = W.fisher_proposal(rng, K, W.SN_TRUTH, cache["sn_fisher"], W.SN_BOX_MIN, W.SN_BOX_MAX)
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     if kind == "tpl":
         if "tpl_post" not in cache:
@@ -349,6 +352,8 @@ def main():
     from cosmopmc_gb300 import workloads as W
 
     P.load()
+    if args.tensor_cores is not None:
+        P.set_tensor_cores(args.tensor_cores)
     N = args.nsamples
     prop, target, post = build_workload(P, W, N)
     l2buf = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2

@@ -11,25 +11,28 @@ namespace pmcg {
 
 // ------------------------------------------------------------------ allocation
 // Every array starts on a 256-byte boundary (the single-precision factors are
-// read as float4).
-static size_t devmix_layout(int K, int D, size_t off[13]) {
+// read as float4, the tensor-core image by bulk copies). The tensor-core image
+// of L^-1 (slot 13) exists for D <= 32 only.
+static size_t devmix_layout(int K, int D, size_t off[14]) {
   const size_t T = (size_t)D * (D + 1) / 2, Kz = (size_t)K, ldx = (size_t)round4(D);
   const size_t nd[8] = {Kz, Kz, Kz * D, Kz * D * D, Kz * T, Kz * D, Kz, Kz};
   const size_t nf[5] = {Kz * D * ldx, Kz * D, Kz, Kz * D * ldx, Kz * D};
   size_t o = 0;
   for (int i = 0; i < 8; i++) { off[i] = o; o = (o + nd[i] * sizeof(double) + 255) & ~(size_t)255; }
   for (int i = 0; i < 5; i++) { off[8 + i] = o; o = (o + nf[i] * sizeof(float) + 255) & ~(size_t)255; }
+  off[13] = o;
+  if (D <= 32) o += umma_bimage_bytes(K);
   return o;
 }
 
 size_t devmix_bytes(int K, int D) {
-  size_t off[13];
+  size_t off[14];
   return devmix_layout(K, D, off);
 }
 
 cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.K = K; m.D = D; m.df = df; m.ldx = round4(D);
-  size_t off[13];
+  size_t off[14];
   const size_t o = devmix_layout(K, D, off);
   cudaError_t e = cudaMalloc(&m.arena, o);
   if (e != cudaSuccess) { m.arena = nullptr; return e; }
@@ -47,6 +50,7 @@ cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.lconst32 = (float *)(a + off[10]);
   m.L32 = (float *)(a + off[11]);
   m.mu32 = (float *)(a + off[12]);
+  m.bimg = (D <= 32) ? (unsigned char *)(a + off[13]) : nullptr;
   return cudaSuccess;
 }
 
@@ -72,7 +76,9 @@ cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mix_prepare_consts_kernel<<<1, 256, 0, s>>>(v, m.logdetL, m.cw, m.lconst, m.lconst32);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !m.bimg) return e;
+  return launch_umma_bimage(v, m.bimg, s);
 }
 
 cudaError_t devmix_upload(DevMix &m, const double *w, const double *mu, const double *L, cudaStream_t s) {

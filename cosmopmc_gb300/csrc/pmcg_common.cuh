@@ -102,6 +102,7 @@ struct DevMixView {
   const float *lconst32; // [K]
   const float *L32;      // [K*D*ldx] L, rows padded to ldx, zero above the diagonal (single-precision draws)
   const float *mu32;     // [K*D]
+  const unsigned char *bimg;  // tensor-core operand image of L^-1 (D <= 32), or null
 };
 
 #define PMCG_CUDA_OK(expr) ((expr) == cudaSuccess)

@@ -90,6 +90,7 @@ bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) 
   }
   if (!CK(cudaMallocHost(&w.hstats, sizeof(DevStats)), "pinned stats")) return false;
   if (!CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking), "stream")) return false;
+  if (!CK(cudaMemsetAsync(w.dstats, 0, sizeof(DevStats), w.s), "stats")) return false;
   if (!CK(devmix_alloc(w.prop, K, D, df), "proposal buffers")) return false;
   return true;
 }
@@ -107,8 +108,18 @@ static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **
             "draw kernel");
 }
 
+// Single-precision mixture log-density on the tensor cores (tcgen05) when the
+// switch is on and the mixture carries an operand image (D <= 32).
+static bool use_tensor_cores(const Work &w, const DevMix &m) {
+  return w.prec == 1 && g_use_tensor_cores && m.bimg != nullptr && m.D <= 32;
+}
+
 static bool stage_logq(Work &w, error **err) {
   w.launches += 1;
+  if (use_tensor_cores(w, w.prop))
+    return CK(launch_umma_logq(w.prop.view(), w.prop.bimg, w.N, w.X32, w.logq, 0, 0.0, w.lt32, w.Q32,
+                               &w.dstats->tc_err, w.s),
+              "tensor-core mixture log-pdf kernel");
   return CK(launch_mixlogpdf(w.prec, w.prop.view(), w.N, w.X64, w.X32, w.logq, 0, 0.0, w.lt64, w.Q64, w.lt32,
                              w.Q32, w.s),
             "mixture log-pdf kernel");
@@ -124,9 +135,14 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
   for (const Plugin &pl : p->plugins) {
     w.launches += 1;
     if (pl.type == kPluginMix) {
-      if (!CK(launch_mixlogpdf(w.prec, pl.mix.view(), w.N, w.X64, w.X32, w.logpost, 1, 0.0, nullptr, nullptr,
-                               nullptr, nullptr, w.s),
-              "target mixture kernel"))
+      if (use_tensor_cores(w, pl.mix)) {
+        if (!CK(launch_umma_logq(pl.mix.view(), pl.mix.bimg, w.N, w.X32, w.logpost, 1, 0.0, nullptr, nullptr,
+                                 &w.dstats->tc_err, w.s),
+                "tensor-core target mixture kernel"))
+          return false;
+      } else if (!CK(launch_mixlogpdf(w.prec, pl.mix.view(), w.N, w.X64, w.X32, w.logpost, 1, 0.0, nullptr,
+                                      nullptr, nullptr, nullptr, w.s),
+                     "target mixture kernel"))
         return false;
     } else if (pl.type == kPluginSn) {
       if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "SN kernel"))
@@ -157,6 +173,10 @@ static bool fetch_stats(Work &w, error **err) {
   if (!CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "stats") ||
       !CK(cudaStreamSynchronize(w.s), "iteration"))
     return false;
+  if (w.hstats->tc_err != 0) {
+    set_error(err, PMCG_ETIMEOUT, __LINE__, "tensor-core log-density: a pipeline wait expired");
+    return false;
+  }
   if (w.hstats->status != 0) {
     set_error(err, w.hstats->status, __LINE__,
               w.hstats->status == PMCG_ENOWEIGHT ? "every sample has zero weight" : "all component weights are zero");
@@ -423,7 +443,10 @@ extern "C" void pmcg_mix_log_pdf_batch(const mix_mvdens *m, size_t N, const doub
       ok = CK(cudaMemcpyAsync(lt, w.lt64, 8 * (size_t)m->ncomp * N, cudaMemcpyDeviceToHost, w.s), "lt");
     }
   }
-  ok = ok && CK(cudaStreamSynchronize(w.s), "mixture log-pdf");
+  ok = ok && CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "status") &&
+       CK(cudaStreamSynchronize(w.s), "mixture log-pdf");
+  if (ok && w.hstats->tc_err != 0)
+    set_error(err, PMCG_ETIMEOUT, __LINE__, "tensor-core log-density: a pipeline wait expired");
   work_free(w);
 }
 
@@ -705,6 +728,12 @@ static bool sync_weights(SimMirror *m, const pmc_simu *psim, error **err) {
 }  // namespace pmcg
 
 extern "C" void pmcg_set_dropin_precision(int precision) { g_dropin_precision = precision ? PMCG_MIXED : PMCG_FP64; }
+
+extern "C" int pmcg_set_tensor_cores(int on) {
+  const int prev = g_use_tensor_cores;
+  g_use_tensor_cores = on ? 1 : 0;
+  return prev;
+}
 
 extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {
   SimMirror *m = find_mirror(psim);

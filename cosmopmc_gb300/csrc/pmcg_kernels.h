@@ -23,6 +23,7 @@ struct DevStats {
   double wsum;      // sum of updated weights before renormalisation
   int ndead;        // components with weight 0 after the update
   int status;       // 0 ok, else a PMCG_E* code
+  int tc_err;       // set by the tensor-core log-density when one of its waits expired
 };
 
 // Device-resident mixture; one allocation, carved into the arrays below.
@@ -31,15 +32,24 @@ struct DevMix {
   double *w = nullptr, *cw = nullptr, *mu = nullptr, *L = nullptr, *Wt = nullptr, *b = nullptr;
   double *logdetL = nullptr, *lconst = nullptr;
   float *W32 = nullptr, *b32 = nullptr, *lconst32 = nullptr, *L32 = nullptr, *mu32 = nullptr;
+  unsigned char *bimg = nullptr;  // tensor-core operand image (D <= 32)
   void *arena = nullptr;
   DevMixView view() const {
     DevMixView v;
     v.K = K; v.D = D; v.df = df; v.ldx = ldx;
     v.w = w; v.cw = cw; v.mu = mu; v.L = L; v.Wt = Wt; v.b = b; v.lconst = lconst;
-    v.W32 = W32; v.b32 = b32; v.lconst32 = lconst32; v.L32 = L32; v.mu32 = mu32;
+    v.W32 = W32; v.b32 = b32; v.lconst32 = lconst32; v.L32 = L32; v.mu32 = mu32; v.bimg = bimg;
     return v;
   }
 };
+
+// Tensor-core (tcgen05) proposal log-density, D <= 32 (k_umma.cu).
+size_t umma_bimage_bytes(int K);
+cudaError_t launch_umma_bimage(const DevMixView &m, unsigned char *img, cudaStream_t s);
+cudaError_t launch_umma_logq(const DevMixView &m, const unsigned char *bimg, size_t N, const float *X, double *out,
+                             int accumulate, double add, float *lt, float *Qo, int *errflag, cudaStream_t s);
+// Process-wide switch for the tensor-core log-density (set by pmcg_set_tensor_cores).
+extern int g_use_tensor_cores;
 
 cudaError_t devmix_alloc(DevMix &m, int K, int D, int df);
 size_t devmix_bytes(int K, int D);

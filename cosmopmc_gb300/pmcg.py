@@ -165,6 +165,7 @@ SIGNATURES = [
     ("get_tempering_beta", C.c_double, [C.c_int, C.c_int, C.c_double, C.c_int, PErr]),
     ("pmcg_simu_host_modified", None, [C.POINTER(PmcSimuS)]),
     ("pmcg_set_dropin_precision", None, [C.c_int]),
+    ("pmcg_set_tensor_cores", C.c_int, [C.c_int]),
     ("pmcg_posterior_alloc", C.c_void_p, [C.c_int, _dp, _dp, PErr]),
     ("pmcg_posterior_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_posterior_add_mixmvdens", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
@@ -644,6 +645,13 @@ def get_tempering_beta(kind, it, tmin, nmax):
 
 def set_dropin_precision(prec):
     load().pmcg_set_dropin_precision(prec)
+
+
+def set_tensor_cores(on):
+    """Switch the single-precision mixture log-density (D <= 32) between the
+    tcgen05 tensor-core kernel and the CUDA-core kernel; returns the previous
+    setting."""
+    return load().pmcg_set_tensor_cores(1 if on else 0)
 
 
 def device_count():

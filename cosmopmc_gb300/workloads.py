@@ -99,10 +99,68 @@ def sn_data(nsn=740, seed=740, chi2mode=0, quad_nodes=4, sig_mB=0.15):
                 def_om=0.3, def_w0=-1.0, def_M=-19.3, def_alpha=0.0, def_beta=0.0)
 
 
-def sn_workload(nsn=740, K=10, seed=740, chi2mode=0):
+def _sn_model_mag(sn, theta):
+    """m_B model of every supernova at theta = (Om, Ode, w0, M, alpha, beta), vectorised over z."""
+    om, ode, w0, M, al, be = theta
+    z = sn["z"]
+    xg, wg = np.polynomial.legendre.leggauss(8)
+    nsub = 64
+    t = np.linspace(0.0, 1.0, nsub + 1)
+    e = z[:, None] * t[None, :]
+    hw, c = 0.5 * (e[:, 1:] - e[:, :-1]), 0.5 * (e[:, 1:] + e[:, :-1])
+    an = 1.0 + c[:, :, None] + hw[:, :, None] * xg[None, None, :]
+    ok = 1.0 - om - ode
+    f = 1.0 / np.sqrt(om * an ** 3 + ok * an ** 2 + ode * an ** (3 * (1 + w0)))
+    I = np.sum(hw[:, :, None] * wg[None, None, :] * f, axis=(1, 2))
+    if abs(ok) < 1e-10:
+        dm = I
+    elif ok > 0:
+        dm = np.sinh(np.sqrt(ok) * I) / np.sqrt(ok)
+    else:
+        dm = np.sin(np.sqrt(-ok) * I) / np.sqrt(-ok)
+    dl = (1 + z) * C_KMS / (100 * sn["h"]) * dm
+    return 5 * np.log10(dl) + 25 + M - al * sn["x1"] + be * sn["c"]
+
+
+def sn_fisher(sn, theta, rel_step=1e-4):
+    """Fisher matrix J^T S^-1 J of the SN chi^2 (diagonal m_B errors) at theta, central differences."""
+    theta = np.asarray(theta, float)
+    sig2 = sn["cov6"][:, 0] + sn["sig_int"] ** 2
+    J = np.empty((len(sn["z"]), len(theta)))
+    for i in range(len(theta)):
+        h = rel_step * max(1.0, abs(theta[i]))
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += h
+        tm[i] -= h
+        J[:, i] = (_sn_model_mag(sn, tp) - _sn_model_mag(sn, tm)) / (2 * h)
+    return J.T @ (J / sig2[:, None])
+
+
+def fisher_proposal(rng, K, theta0, F, bmin, bmax, fshift=1.0, frescale=2.0, df=-1):
+    """Initial proposal from a Fisher matrix (the reference's Fisher start): every
+    component has covariance frescale * F^-1 and a mean shifted from theta0 by
+    fshift * F^-1/2 xi, xi ~ N(0, I), clipped into the box; equal weights."""
+    Cf = np.linalg.inv(F)
+    Cf = 0.5 * (Cf + Cf.T)
+    L = np.linalg.cholesky(Cf)
+    bmin, bmax = np.asarray(bmin, float), np.asarray(bmax, float)
+    mu = theta0[None, :] + fshift * (rng.standard_normal((K, len(theta0))) @ L.T)
+    mu = np.clip(mu, bmin + 1e-3 * (bmax - bmin), bmax - 1e-3 * (bmax - bmin))
+    covs = np.repeat((frescale * Cf)[None], K, axis=0)
+    return np.full(K, 1.0 / K), mu, covs, df
+
+
+def sn_workload(nsn=740, K=10, seed=740, chi2mode=0, init="random"):
+    """SN Ia run. init="random": the random-position proposal of the box;
+    init="fisher": components around the truth with the Fisher covariance
+    (a healthy run from the first iteration)."""
     sn = sn_data(nsn, seed, chi2mode)
     rng = np.random.default_rng(seed + 1)
-    w, mu, covs, df = random_pos_proposal(rng, K, SN_BOX_MIN, SN_BOX_MAX)
+    if init == "fisher":
+        F = sn_fisher(sn, SN_TRUTH)
+        w, mu, covs, df = fisher_proposal(rng, K, SN_TRUTH, F, SN_BOX_MIN, SN_BOX_MAX)
+    else:
+        w, mu, covs, df = random_pos_proposal(rng, K, SN_BOX_MIN, SN_BOX_MAX)
     return dict(sn=sn, bmin=SN_BOX_MIN.copy(), bmax=SN_BOX_MAX.copy(), prop=(w, mu, covs, df))
 
 

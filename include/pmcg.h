@@ -203,6 +203,12 @@ void pmcg_simu_host_modified(pmc_simu *psim);
  * plain FP64 path) or PMCG_MIXED. */
 void pmcg_set_dropin_precision(int precision);
 
+/* Single-precision (PMCG_MIXED) mixture log-densities with D <= 32 on the
+ * tensor cores: tcgen05 TF32 products in three-term split form, TMEM
+ * accumulators (1 = on, 0 = the CUDA-core kernel). Returns the previous
+ * setting. No counterpart in the reference (a GPU execution choice). */
+int pmcg_set_tensor_cores(int on);
+
 /* ------------------------------------------------------------------ *
  * Part 2 — device posterior plugins (the batched counterpart of the  *
  * per-point func_likeli_t of wrappers/include/init_wrappers.h:15-42). *
