@@ -1,38 +1,53 @@
-// k_umma.cu — (b) proposal log-density on the 5th-generation tensor cores.
+// k_umma.cu — (b) mixture log-density on the 5th-generation tensor cores.
 //
 // Y = X L^-1^T for every (sample, component): a [N x 32] x [32 x K*32] product,
 // followed per (sample, component) by y - L^-1 mu, Q = |y|^2, the Gaussian or
-// Student-t log-density and an online log-sum-exp over components.
+// Student-t log-density and an online log-sum-exp over components. Same
+// result contract as the CUDA-core kernel (body_mixlogpdf_f32).
 //
-//  * tcgen05.mma kind::tf32, issued by one thread, accumulators in TMEM.
-//    Single-precision accuracy with three TF32 products (3xTF32 split):
-//    x = x_hi + x_lo, W = W_hi + W_lo, xW ~ x_hi W_hi + x_hi W_lo + x_lo W_hi.
-//  * CTA = 256 threads, persistent (one per SM), tiles of 256 samples = two
-//    M=128 accumulators; components in groups of 4 (N = 128 columns each).
-//  * A (samples) is staged by the threads (split into hi/lo) into the 128-byte
-//    swizzled K-major layout; B (L^-1 rows, hi/lo) is pre-swizzled once per
-//    proposal into that layout in global memory and streamed per group with
-//    cp.async.bulk into a double buffer (mbarrier complete_tx).
-//  * TMEM: 512 columns = two buffers of (2 tiles x 128 columns); the MMAs of
-//    group g+1 run while the 8 warps read group g (tcgen05.ld 32x32b) and
-//    evaluate the densities.
-//  * Every mbarrier wait is bounded: on expiry the kernel sets an error flag,
-//    stops issuing work, drains and frees its TMEM and returns.
+//  * tcgen05.mma kind::tf32, accumulators in TMEM. Single-precision accuracy
+//    from three TF32 products (three-term split): x = x_hi + x_lo,
+//    W = W_hi + W_lo, xW ~ x_hi W_hi + x_hi W_lo + x_lo W_hi.
+//  * L^-1 is lower triangular: the operand rows are ordered by 8-row block
+//    (n = block*32 + component*8 + row), so K-step s only multiplies the rows
+//    of blocks >= s (N = 32 (KS - s), KS = ceil(D/8)): 10 of 16 block
+//    products for D = 32.
+//  * CTA = 9 warps, persistent (one per SM). Warp 8 is the producer: one
+//    thread streams the operand image of each group of 4 components
+//    (cp.async.bulk into a 3-stage ring, mbarrier complete_tx) and issues the
+//    MMAs. Warps 0-7 stage the samples (TF32 hi/lo, 128-byte swizzle), read
+//    the accumulators (tcgen05.ld 32x32b) and evaluate the densities.
+//  * Tiles of 256 samples = two M=128 accumulators; TMEM holds two buffers of
+//    (2 x 128 columns), so the MMAs of group g+1 run while group g is read.
+//  * Every mbarrier wait is bounded (about one second): on expiry the CTA
+//    raises an abort flag that every other wait observes, sets the error
+//    flag, lets its copies and MMAs in flight land (bounded) and frees TMEM.
 #include "pmcg_bodies.cuh"
 
 namespace pmcg {
 
-constexpr int kUmTile = 256;                 // samples per CTA tile
-constexpr int kUmGC = 4;                     // components per group (N = 128)
-constexpr int kUmHalf = 128 * 128;           // bytes of one 128-row x 32-float operand (16 KB)
-constexpr int kUmGroupBytes = 2 * kUmHalf;   // B image of one group: hi + lo (32 KB)
-constexpr int kUmSmemA = 4 * kUmHalf;        // two tiles x (hi, lo)
-constexpr int kUmSmemB = 2 * kUmGroupBytes;  // double buffer
-constexpr int kUmSmem = kUmSmemA + kUmSmemB + 1024 + 128;  // + 1024 alignment slack + barriers
+constexpr int kUmTile = 256;                  // samples per CTA tile
+constexpr int kUmGC = 4;                      // components per group (128 operand rows)
+constexpr int kUmHalf = 128 * 128;            // bytes of one 128-row x 32-float operand (16 KB)
+constexpr int kUmCopyBytes = 2 * kUmHalf;     // streamed per group: hi + lo (32 KB)
+constexpr int kUmGroupStride = 33 * 1024;     // image stride per group: hi, lo, b[128], lc[4]
+constexpr int kUmStages = 3;                  // operand ring
+constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
+constexpr int kUmSmemB = kUmStages * kUmCopyBytes;
+constexpr int kUmThreads = 288;               // 8 epilogue warps + 1 producer warp
+constexpr int kUmEpi = 256;
 constexpr long long kUmWaitLimit = 1ll << 26;   // iteration cap of one wait
 constexpr uint64_t kUmWaitNs = 1000000000ull;   // wall-time bound of one wait (1 s)
 
-size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupBytes; }
+// Barriers: bfull[3], bempty[3], mfull[2], tfree[2], afull
+constexpr int kUmBars = 2 * kUmStages + 5;
+
+size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupStride; }
+
+static size_t umma_smem_bytes(int K) {
+  const int G = (K + kUmGC - 1) / kUmGC;
+  return (size_t)kUmSmemA + kUmSmemB + 1024 + (size_t)G * 132 * sizeof(float) + kUmBars * 8 + 16;
+}
 
 // Byte offset of element (row, col) (col < 32 floats) in a 128-byte-swizzled,
 // K-major operand: 8-row atoms of 1024 bytes, 16-byte chunk c of row r stored
@@ -47,20 +62,29 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-// ------------------------------------------------------------------ B image
-// Group g, component c (k = 4g + c), row i, column j: W_k[i][j] split into
-// TF32 hi and lo, zero for padding rows / columns / components.
+// ------------------------------------------------------------------ operand image
+// Group g, component c (k = 4g + c), row i = 8 rb + r, column j: operand row
+// n = 32 rb + 8 c + r holds W_k[i][:] split into TF32 hi and lo (zero for
+// padding rows / columns / components); then b[n] = (L^-1 mu)_k[i] and the
+// four log-constants (-inf for padding components).
 __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
   const int g = blockIdx.x, D = m.D, K = m.K, ldx = m.ldx;
-  unsigned char *hi = img + (size_t)g * kUmGroupBytes, *lo = hi + kUmHalf;
+  unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmHalf;
+  float *bimg = reinterpret_cast<float *>(hi + kUmCopyBytes);
   for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
-    const int n = e >> 5, j = e & 31, c = n >> 5, i = n & 31, k = g * kUmGC + c;
+    const int n = e >> 5, j = e & 31;
+    const int rb = n >> 5, c = (n >> 3) & 3, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
     float w = 0.f;
     if (k < K && i < D && j < D) w = m.W32[(size_t)k * D * ldx + (size_t)i * ldx + j];
     const float h = tf32_round(w);
     const float l = tf32_round(w - h);
     *reinterpret_cast<float *>(hi + sw128_off(n, j)) = h;
     *reinterpret_cast<float *>(lo + sw128_off(n, j)) = l;
+    if (j == 0) bimg[n] = (k < K && i < D) ? m.b32[(size_t)k * D + i] : 0.f;
+  }
+  if (threadIdx.x < kUmGC) {
+    const int k = g * kUmGC + threadIdx.x;
+    bimg[128 + threadIdx.x] = (k < K) ? m.lconst32[k] : -INFINITY;
   }
 }
 
@@ -77,31 +101,52 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
-// Parity wait on an mbarrier, bounded by about one second of wall time (and an
-// iteration cap); false when the bound ran out.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Parity wait bounded by about one second of wall time (and an iteration
+// cap). Gives up early when another role of the CTA raised the abort flag;
+// raises it on expiry. Returns false when the CTA is aborting.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
   uint64_t t0 = 0;
   for (long long it = 0; it < kUmWaitLimit; it++) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((it & 255) == 0) {
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 63) == 0) {
+      if (*abort) return false;
       const uint64_t t = global_ns();
       if (it == 0) t0 = t;
-      else if (t - t0 > kUmWaitNs) return false;
+      else if (t - t0 > kUmWaitNs) break;
     }
+  }
+  *abort = 1;
+  return false;
+}
+
+// Bounded wait that ignores the abort flag (draining after an abort).
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = global_ns();
+  for (long long it = 0; it < kUmWaitLimit; it++) {
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 63) == 0 && global_ns() - t0 > kUmWaitNs) return false;
   }
   return false;
 }
@@ -125,23 +170,27 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor: D f32, A/B tf32, both K-major, M=128, N=128.
-constexpr uint32_t kUmIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// Instruction descriptor: D f32, A/B tf32, both K-major, M=128, N = n.
+__device__ __forceinline__ uint32_t um_idesc(uint32_t n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
 
-__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(kUmIdesc), "r"(accumulate));
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// 32 consecutive TMEM columns of this warp's 32 lanes (no wait).
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float *v) {
+  uint32_t *r = reinterpret_cast<uint32_t *>(v);
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
       "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -151,37 +200,57 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
         "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ------------------------------------------------------------------ kernel
 template <bool STUDENT>
-__global__ void __launch_bounds__(256, 1) umma_logq_kernel(DevMixView m, const unsigned char *__restrict__ bimg,
-                                                           size_t N, const float *__restrict__ X,
-                                                           double *__restrict__ out, int accumulate, double add,
-                                                           float *__restrict__ lt, float *__restrict__ Qo,
-                                                           int *__restrict__ errflag) {
+__global__ void __launch_bounds__(kUmThreads, 1)
+    umma_logq_kernel(DevMixView m, const unsigned char *__restrict__ bimg, size_t N, const float *__restrict__ X,
+                     double *__restrict__ out, int accumulate, double add, float *__restrict__ lt,
+                     float *__restrict__ Qo, int *__restrict__ errflag) {
   extern __shared__ __align__(1024) unsigned char um_raw[];
   // 1024-byte aligned operand base (swizzle atoms)
   unsigned char *base = um_raw + ((1024 - (smem_u32(um_raw) & 1023)) & 1023);
-  unsigned char *sA = base;                       // [tile 0 hi][tile 0 lo][tile 1 hi][tile 1 lo]
-  unsigned char *sB = base + kUmSmemA;            // [buffer 0][buffer 1], each hi + lo
-  uint64_t *bars = reinterpret_cast<uint64_t *>(sB + kUmSmemB);  // 0,1: B loaded; 2,3: MMA done
-  uint32_t *tmem_hold = reinterpret_cast<uint32_t *>(bars + 4);
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned char *sA = base;                          // [acc 0 hi][acc 0 lo][acc 1 hi][acc 1 lo]
+  unsigned char *sB = base + kUmSmemA;               // ring of kUmStages x (hi, lo)
   const int D = m.D, K = m.K, ldx = m.ldx;
   const int G = (K + kUmGC - 1) / kUmGC;
+  const int KS = (D + 7) >> 3;                       // K-steps of 8 (and 8-row blocks)
+  float *s_b = reinterpret_cast<float *>(sB + kUmSmemB);          // [G][128] b, then [G][4] lc
+  float *s_lc = s_b + (size_t)G * 128;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(s_lc + (size_t)G * 4);
+  uint32_t *tmem_hold = reinterpret_cast<uint32_t *>(bars + kUmBars);
+  __shared__ int s_abort;
+  volatile int *abort = &s_abort;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const size_t ntiles = (N + kUmTile - 1) / kUmTile;
-  const uint32_t barB0 = smem_u32(&bars[0]), barB1 = smem_u32(&bars[1]);
-  const uint32_t barM0 = smem_u32(&bars[2]), barM1 = smem_u32(&bars[3]);
+  const int my_tiles = (int)((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
+  const int items = my_tiles * G;
+
+  // barrier addresses: bfull(s) = bfull0 + 8 s, bempty(s) = bempty0 + 8 s, ...
+  const uint32_t bfull0 = smem_u32(&bars[0]), bempty0 = smem_u32(&bars[kUmStages]);
+  const uint32_t mfull0 = smem_u32(&bars[2 * kUmStages]), tfree0 = smem_u32(&bars[2 * kUmStages + 2]);
+  const uint32_t afull = smem_u32(&bars[2 * kUmStages + 4]);
   const uint32_t sA_u = smem_u32(sA), sB_u = smem_u32(sB);
 
   if (tid == 0) {
-    mbar_init(barB0, 1); mbar_init(barB1, 1); mbar_init(barM0, 1); mbar_init(barM1, 1);
+    s_abort = 0;
+#pragma unroll
+    for (int s = 0; s < kUmStages; s++) { mbar_init(bfull0 + 8 * s, 1); mbar_init(bempty0 + 8 * s, 1); }
+    mbar_init(mfull0, 1); mbar_init(mfull0 + 8, 1);
+    mbar_init(tfree0, kUmEpi); mbar_init(tfree0 + 8, kUmEpi);
+    mbar_init(afull, kUmEpi);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // resident b and log-constants of every group
+  for (int e = tid; e < G * 132; e += blockDim.x) {
+    const int g = e / 132, o = e - g * 132;
+    const float v = *reinterpret_cast<const float *>(bimg + (size_t)g * kUmGroupStride + kUmCopyBytes + o * 4);
+    if (o < 128) s_b[g * 128 + o] = v;
+    else s_lc[g * 4 + (o - 128)] = v;
   }
   if (warp == 0) {
     __syncwarp();
@@ -194,136 +263,172 @@ __global__ void __launch_bounds__(256, 1) umma_logq_kernel(DevMixView m, const u
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_hold;
 
-  // Phase bookkeeping. Loads (B buffers) and MMA commits are issued by thread 0
-  // only; at most one of each is outstanding per barrier, so a parity wait on
-  // the count of completed phases is unambiguous.
-  uint32_t issB[2] = {0, 0}, doneB[2] = {0, 0};   // thread 0
-  uint32_t issM[2] = {0, 0}, doneM[2] = {0, 0};   // issM: thread 0; doneM: every thread
-  const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
-  const int mt = warp >> 2;                      // accumulator (sample half) this warp reads
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-
-  auto load_group = [&](int g) {
-    const int buf = g & 1;
-    bulk_load(sB_u + (uint32_t)buf * kUmGroupBytes, bimg + (size_t)g * kUmGroupBytes, kUmGroupBytes,
-              buf ? barB1 : barB0);
-    issB[buf]++;
-  };
-  // Thread 0: wait for the B image of group g, then issue its 24 MMAs (two
-  // tiles x three split products x four K steps of 8) and commit them.
-  auto issue_group = [&](int g) -> bool {
-    const int buf = g & 1;
-    if (!mbar_wait(buf ? barB1 : barB0, doneB[buf] & 1)) return false;
-    doneB[buf]++;
-    const uint32_t bB = sB_u + (uint32_t)buf * kUmGroupBytes;
-    asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == kUmEpi / 32) {
+    // ================================================================ producer
+    if (lane == 0) {
+      int issued_loads = 0, last_commit = -1;
+      auto load = [&](int q) {
+        const int st = q % kUmStages, g = q % G;
+        bulk_load(sB_u + (uint32_t)st * kUmCopyBytes, bimg + (size_t)g * kUmGroupStride, kUmCopyBytes,
+                  bfull0 + 8 * st);
+        issued_loads++;
+      };
+      for (int q = 0; q < kUmStages && q < items; q++) load(q);
+      bool ok = true;
+      for (int q = 0; q < items && ok; q++) {
+        const int g = q % G, st = q % kUmStages, ab = q & 1;
+        if (g == 0 && !mbar_wait(afull, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
+        if (!mbar_wait(bfull0 + 8 * st, (uint32_t)((q / kUmStages) & 1), abort)) { ok = false; break; }
+        if (q >= 2 && !mbar_wait(tfree0 + 8 * ab, (uint32_t)(((q - 2) >> 1) & 1), abort)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t bH = sB_u + (uint32_t)st * kUmCopyBytes;
 #pragma unroll
-    for (int t = 0; t < 2; t++) {
-      const uint32_t d = tmem + (uint32_t)buf * 256 + t * 128;
-      const uint32_t aH = sA_u + (2 * t) * kUmHalf, aL = sA_u + (2 * t + 1) * kUmHalf;
-#pragma unroll
-      for (int ks = 0; ks < 4; ks++) {
-        const uint32_t ko = ks * 32;
-        umma_tf32(d, sw128_desc(aH + ko), sw128_desc(bB + ko), ks > 0);
-        umma_tf32(d, sw128_desc(aH + ko), sw128_desc(bB + kUmHalf + ko), 1);
-        umma_tf32(d, sw128_desc(aL + ko), sw128_desc(bB + ko), 1);
-      }
-    }
-    umma_commit(buf ? barM1 : barM0);
-    issM[buf]++;
-    return true;
-  };
-
-  bool aborted = false;  // uniform over the CTA
-  bool pabort = false;   // thread 0: a B-image wait expired
-  for (size_t tile = blockIdx.x; tile < ntiles && !aborted; tile += gridDim.x) {
-    const size_t n0 = tile * kUmTile;
-    // ---- stage A: 256 rows x 8 chunks of 4 floats, split into TF32 hi / lo;
-    // columns >= D (row padding) and rows >= N are zero
-    for (int e = tid; e < kUmTile * 8; e += blockDim.x) {
-      const int s = e >> 3, c = e & 7;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (n0 + s < N && c * 4 < D) {
-        v = *reinterpret_cast<const float4 *>(X + (n0 + s) * ldx + c * 4);
-        if (c * 4 + 1 >= D) v.y = 0.f;
-        if (c * 4 + 2 >= D) v.z = 0.f;
-        if (c * 4 + 3 >= D) v.w = 0.f;
-      }
-      const int t = s >> 7, r = s & 127;
-      const uint32_t off = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
-      float4 h, l;
-      h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
-      l.x = tf32_round(v.x - h.x); l.y = tf32_round(v.y - h.y); l.z = tf32_round(v.z - h.z); l.w = tf32_round(v.w - h.w);
-      *reinterpret_cast<float4 *>(sA + (2 * t) * kUmHalf + off) = h;
-      *reinterpret_cast<float4 *>(sA + (2 * t + 1) * kUmHalf + off) = l;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-      load_group(0);
-      if (G > 1) load_group(1);
-      if (!issue_group(0)) pabort = true;
-    }
-    float mx = -INFINITY, sm = 0.f;
-    const size_t n = n0 + (size_t)mt * 128 + (warp & 3) * 32 + lane;
-    for (int g = 0; g < G; g++) {
-      const int buf = g & 1;
-      // thread 0 issues group g+1 into the other TMEM buffer before the epilogue of g
-      if (tid == 0 && g + 1 < G && !pabort && !issue_group(g + 1)) pabort = true;
-      const bool ok = mbar_wait(buf ? barM1 : barM0, doneM[buf] & 1);
-      if (ok) doneM[buf]++;
-      if (__syncthreads_or(!ok || pabort)) {
-        aborted = true;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      __syncwarp();  // tcgen05.ld is warp-collective
-#pragma unroll
-      for (int c = 0; c < kUmGC; c++) {
-        const int k = g * kUmGC + c;
-        float v[32];
-        tmem_ld32(tmem + lane_base + (uint32_t)(buf * 256 + mt * 128 + c * 32), v);
-        if (k >= K) continue;
-        const float lc = m.lconst32[k];
-        float q = 0.f;
-        const float *bk = m.b32 + (size_t)k * D;
-#pragma unroll
-        for (int i = 0; i < 32; i++) {
-          if (i < D) {
-            const float y = v[i] - __ldg(&bk[i]);
-            q = fmaf(y, y, q);
+        for (int t = 0; t < 2; t++) {
+          const uint32_t d0 = tmem + (uint32_t)ab * 256 + (uint32_t)t * 128;
+          const uint32_t aH = sA_u + (uint32_t)(2 * t) * kUmHalf, aL = aH + kUmHalf;
+          for (int ks = 0; ks < KS; ks++) {
+            const uint32_t idesc = um_idesc((uint32_t)(32 * (KS - ks)));
+            const uint32_t d = d0 + (uint32_t)(32 * ks);
+            const uint32_t bo = (uint32_t)(ks * 4096 + ks * 32), ao = (uint32_t)(ks * 32);
+            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bH + bo), idesc, ks > 0);
+            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bH + kUmHalf + bo), idesc, 1);
+            umma_tf32(d, sw128_desc(aL + ao), sw128_desc(bH + bo), idesc, 1);
           }
         }
-        float l;
-        if (lc == -INFINITY) l = -INFINITY;
-        else l = STUDENT ? lc - hnd * log1pf(q * rnu) : lc - 0.5f * q;
-        if (l > mx) { sm = sm * expf(mx - l) + 1.f; mx = l; }
-        else if (l > -INFINITY) sm += expf(l - mx);
-        if (n < N && lt) {
-          lt[(size_t)k * N + n] = l;
-          if (Qo) Qo[(size_t)k * N + n] = (lc == -INFINITY) ? 0.f : q;
+        umma_commit(mfull0 + 8 * ab);
+        umma_commit(bempty0 + 8 * st);
+        last_commit = q;
+        // refill the stage of item q-1 once its MMAs have read it
+        if (q >= 1 && q - 1 + kUmStages < items) {
+          const int p = q - 1;
+          if (!mbar_wait(bempty0 + 8 * (p % kUmStages), (uint32_t)((p / kUmStages) & 1), abort)) { ok = false; break; }
+          load(p + kUmStages);
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();  // TMEM buffer and B buffer of group g are free again
-      if (tid == 0 && g + 2 < G) load_group(g + 2);
+      if (!ok) atomicExch(errflag, 1);
+      // Let the MMAs and copies still in flight land before shared memory and
+      // TMEM are released (both complete at once on the normal path; after an
+      // abort of either role the waits are bounded).
+      if (last_commit >= 0)
+        mbar_drain(bempty0 + 8 * (last_commit % kUmStages), (uint32_t)((last_commit / kUmStages) & 1));
+      for (int q = last_commit + 1; q < issued_loads; q++)
+        mbar_drain(bfull0 + 8 * (q % kUmStages), (uint32_t)((q / kUmStages) & 1));
     }
-    if (aborted) break;
-    if (n < N) {
-      const double r = (double)mx + (double)logf(sm);
-      if (accumulate) out[n] += r + add;
-      else out[n] = r;
+  } else {
+    // ================================================================ epilogue
+    const int mt = warp >> 2;                                // accumulator this warp reads
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
+    float4 xr[8];
+    auto fetch = [&](size_t tile) {
+      const size_t n0 = tile * kUmTile;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int s = (tid >> 3) + 32 * j, c = tid & 7;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n0 + s < N && c * 4 < D) {
+          v = __ldg(reinterpret_cast<const float4 *>(X + (n0 + s) * ldx + c * 4));
+          if (c * 4 + 1 >= D) v.y = 0.f;
+          if (c * 4 + 2 >= D) v.z = 0.f;
+          if (c * 4 + 3 >= D) v.w = 0.f;
+        }
+        xr[j] = v;
+      }
+    };
+    auto stage = [&]() {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int s = (tid >> 3) + 32 * j, c = tid & 7;
+        const int t = s >> 7, r = s & 127;
+        const uint32_t off = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+        const float4 v = xr[j];
+        float4 h, l;
+        h.x = tf32_round(v.x); h.y = tf32_round(v.y); h.z = tf32_round(v.z); h.w = tf32_round(v.w);
+        l.x = tf32_round(v.x - h.x); l.y = tf32_round(v.y - h.y);
+        l.z = tf32_round(v.z - h.z); l.w = tf32_round(v.w - h.w);
+        *reinterpret_cast<float4 *>(sA + (2 * t) * kUmHalf + off) = h;
+        *reinterpret_cast<float4 *>(sA + (2 * t + 1) * kUmHalf + off) = l;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(afull);
+    };
+
+    bool ok = true;
+    fetch(blockIdx.x);
+    stage();
+    for (int i = 0; i < my_tiles && ok; i++) {
+      const size_t tile = blockIdx.x + (size_t)i * gridDim.x;
+      const size_t n = tile * kUmTile + (size_t)mt * 128 + (warp & 3) * 32 + lane;
+      if (i + 1 < my_tiles) fetch(tile + gridDim.x);   // next tile's samples, in flight during this one
+      float mx = -INFINITY, sm = 0.f;
+      for (int g = 0; g < G; g++) {
+        const int q = i * G + g, ab = q & 1;
+        if (!mbar_wait(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncwarp();
+        // accumulators of row blocks 0-1, then 2-3 (64 registers at a time)
+        const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128);
+        const float *bg = s_b + g * 128;
+        float qc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+          float v[2][32];
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+            if (2 * half + h < KS) tmem_ld32_nowait(tcol + (uint32_t)((2 * half + h) * 32), v[h]);
+          tmem_ld_wait();
+          if (half == 1) {
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(tfree0 + 8 * ab);                   // TMEM buffer free for group g+2
+            // the last group's MMAs are done with A: stage the next tile before the math
+            if (g == G - 1 && i + 1 < my_tiles) stage();
+          }
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int rb = 2 * half + h;
+            if (rb < KS) {
+#pragma unroll
+              for (int c = 0; c < 4; c++) {
+                const float4 b0 = *reinterpret_cast<const float4 *>(bg + rb * 32 + c * 8);
+                const float4 b1 = *reinterpret_cast<const float4 *>(bg + rb * 32 + c * 8 + 4);
+                const float *vv = &v[h][c * 8];
+                float y;
+                y = vv[0] - b0.x; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[1] - b0.y; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[2] - b0.z; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[3] - b0.w; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[4] - b1.x; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[5] - b1.y; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[6] - b1.z; qc[c] = fmaf(y, y, qc[c]);
+                y = vv[7] - b1.w; qc[c] = fmaf(y, y, qc[c]);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int k = g * kUmGC + c;
+          if (k >= K) break;
+          const float lc = s_lc[g * 4 + c];
+          float l;
+          if (lc == -INFINITY) l = -INFINITY;
+          else l = STUDENT ? lc - hnd * log1pf(qc[c] * rnu) : lc - 0.5f * qc[c];
+          if (l > mx) { sm = sm * expf(mx - l) + 1.f; mx = l; }
+          else if (l > -INFINITY) sm += expf(l - mx);
+          if (n < N && lt) {
+            lt[(size_t)k * N + n] = l;
+            if (Qo) Qo[(size_t)k * N + n] = (lc == -INFINITY) ? 0.f : qc[c];
+          }
+        }
+      }
+      if (!ok) break;
+      if (n < N) {
+        const double r = (double)mx + (double)logf(sm);
+        if (accumulate) out[n] += r + add;
+        else out[n] = r;
+      }
     }
-    __syncthreads();  // A is rewritten by the next tile
-  }
-  if (aborted && tid == 0) {
-    atomicExch(errflag, 1);
-    // let every copy and MMA still in flight land (bounded) before the
-    // shared memory and TMEM are released
-    for (int b = 0; b < 2; b++) {
-      while (doneB[b] < issB[b] && mbar_wait(b ? barB1 : barB0, doneB[b] & 1)) doneB[b]++;
-      while (doneM[b] < issM[b] && mbar_wait(b ? barM1 : barM0, doneM[b] & 1)) doneM[b]++;
-    }
+    if (!ok) atomicExch(errflag, 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -337,23 +442,26 @@ int g_use_tensor_cores = 0;
 
 cudaError_t launch_umma_logq(const DevMixView &m, const unsigned char *bimg, size_t N, const float *X, double *out,
                              int accumulate, double add, float *lt, float *Qo, int *errflag, cudaStream_t s) {
-  if (m.D > 32 || N == 0) return cudaErrorInvalidValue;
-  int dev = 0, sms = 0;
+  if (m.D > 32 || m.K < 1 || N == 0 || !bimg) return cudaErrorInvalidValue;
+  const size_t smem = umma_smem_bytes(m.K);
+  int dev = 0, sms = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > (size_t)maxsm) return cudaErrorInvalidValue;
   const size_t ntiles = (N + kUmTile - 1) / kUmTile;
   const unsigned grid = (unsigned)(ntiles < (size_t)sms ? ntiles : (size_t)sms);
   cudaError_t e;
   if (m.df > 0) {
-    if ((e = cudaFuncSetAttribute(umma_logq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmSmem)) !=
+    if ((e = cudaFuncSetAttribute(umma_logq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
       return e;
-    umma_logq_kernel<true><<<grid, 256, kUmSmem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
+    umma_logq_kernel<true><<<grid, kUmThreads, smem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
   } else {
-    if ((e = cudaFuncSetAttribute(umma_logq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmSmem)) !=
+    if ((e = cudaFuncSetAttribute(umma_logq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
       return e;
-    umma_logq_kernel<false><<<grid, 256, kUmSmem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
+    umma_logq_kernel<false><<<grid, kUmThreads, smem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
   }
   return cudaGetLastError();
 }
