@@ -12,11 +12,17 @@
 //    (n = block*32 + component*8 + row), so K-step s only multiplies the rows
 //    of blocks >= s (N = 32 (KS - s), KS = ceil(D/8)): 10 of 16 block
 //    products for D = 32.
-//  * CTA = 9 warps, persistent (one per SM). Warp 8 is the producer: one
+//  * The shift -L^-1 mu is folded into the product: it is stored (hi, lo) in
+//    the never-read upper-triangle blocks of the operand image and added by
+//    one more K-step against a constant operand of ones, so the accumulators
+//    hold y = L^-1 (x - mu) and the epilogue only forms |y|^2.
+//  * CTA = 17 warps, persistent (one per SM). Warp 16 is the producer: one
 //    thread streams the operand image of each group of 4 components
 //    (cp.async.bulk into a 3-stage ring, mbarrier complete_tx) and issues the
-//    MMAs. Warps 0-7 stage the samples (TF32 hi/lo, 128-byte swizzle), read
-//    the accumulators (tcgen05.ld 32x32b) and evaluate the densities.
+//    MMAs. Warps 0-15 stage the samples (TF32 hi/lo, 128-byte swizzle), read
+//    the accumulators (tcgen05.ld 32x32b; two warps per TMEM lane quarter,
+//    two components each) and evaluate the densities; the two halves of each
+//    sample's log-sum-exp are merged through shared memory.
 //  * Tiles of 256 samples = two M=128 accumulators; TMEM holds two buffers of
 //    (2 x 128 columns), so the MMAs of group g+1 run while group g is read.
 //  * Every mbarrier wait is bounded (about one second): on expiry the CTA
@@ -30,23 +36,25 @@ constexpr int kUmTile = 256;                  // samples per CTA tile
 constexpr int kUmGC = 4;                      // components per group (128 operand rows)
 constexpr int kUmHalf = 128 * 128;            // bytes of one 128-row x 32-float operand (16 KB)
 constexpr int kUmCopyBytes = 2 * kUmHalf;     // streamed per group: hi + lo (32 KB)
-constexpr int kUmGroupStride = 33 * 1024;     // image stride per group: hi, lo, b[128], lc[4]
+constexpr int kUmGroupStride = 33 * 1024;     // image stride per group: hi, lo, lc[4]
 constexpr int kUmStages = 3;                  // operand ring
 constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
+constexpr int kUmSmemOnes = kUmHalf;          // constant operand of the shift K-step
 constexpr int kUmSmemB = kUmStages * kUmCopyBytes;
-constexpr int kUmThreads = 288;               // 8 epilogue warps + 1 producer warp
-constexpr int kUmEpi = 256;
+constexpr int kUmEpi = 512;                   // 16 epilogue warps
+constexpr int kUmThreads = kUmEpi + 32;       // + 1 producer warp
 constexpr long long kUmWaitLimit = 1ll << 26;   // iteration cap of one wait
 constexpr uint64_t kUmWaitNs = 1000000000ull;   // wall-time bound of one wait (1 s)
 
-// Barriers: bfull[3], bempty[3], mfull[2], tfree[2], afull
-constexpr int kUmBars = 2 * kUmStages + 5;
+// Barriers: bfull[3], bempty[3], mfull[2], tfree[2], afull, merged[2], read[2]
+constexpr int kUmBars = 2 * kUmStages + 9;
 
 size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupStride; }
 
 static size_t umma_smem_bytes(int K) {
   const int G = (K + kUmGC - 1) / kUmGC;
-  return (size_t)kUmSmemA + kUmSmemB + 1024 + (size_t)G * 132 * sizeof(float) + kUmBars * 8 + 16;
+  return (size_t)kUmSmemA + kUmSmemOnes + kUmSmemB + 1024 + 2 * 256 * 2 * sizeof(float) +
+         (size_t)G * 4 * sizeof(float) + kUmBars * 8 + 16;
 }
 
 // Byte offset of element (row, col) (col < 32 floats) in a 128-byte-swizzled,
@@ -65,26 +73,41 @@ __device__ __forceinline__ float tf32_round(float x) {
 // ------------------------------------------------------------------ operand image
 // Group g, component c (k = 4g + c), row i = 8 rb + r, column j: operand row
 // n = 32 rb + 8 c + r holds W_k[i][:] split into TF32 hi and lo (zero for
-// padding rows / columns / components); then b[n] = (L^-1 mu)_k[i] and the
-// four log-constants (-inf for padding components).
+// padding rows / columns / components). The shift s_n = -(L^-1 mu)_k[i],
+// split into TF32 (hi, lo), sits in columns 24, 25 of rows that no K-step
+// reads there: rows n < 32 min(KS, 3) of the hi image (upper triangle, or
+// unused when KS <= 3) and, for KS = 4, rows 96..127 in rows 0..31 of the lo
+// image. After the operands: the four log-constants (-inf for padding).
 __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
   const int g = blockIdx.x, D = m.D, K = m.K, ldx = m.ldx;
+  const int KS = (D + 7) >> 3;
   unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmHalf;
-  float *bimg = reinterpret_cast<float *>(hi + kUmCopyBytes);
   for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
     const int n = e >> 5, j = e & 31;
     const int rb = n >> 5, c = (n >> 3) & 3, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
     float w = 0.f;
     if (k < K && i < D && j < D) w = m.W32[(size_t)k * D * ldx + (size_t)i * ldx + j];
-    const float h = tf32_round(w);
-    const float l = tf32_round(w - h);
+    float h = tf32_round(w);
+    float l = tf32_round(w - h);
+    // shift entries (the slots are zero in the factor)
+    if (j == 24 || j == 25) {
+      const int nh = n;                                   // hi image slot -> operand row nh
+      const int nl = (KS == 4 && n < 32) ? n + 96 : -1;   // lo image slot -> operand row nl
+      auto shift = [&](int row, float &hv) {
+        const int rrb = row >> 5, rc = (row >> 3) & 3, ri = rrb * 8 + (row & 7), rk = g * kUmGC + rc;
+        const float sv = (rk < K && ri < D) ? -m.b32[(size_t)rk * D + ri] : 0.f;
+        const float sh = tf32_round(sv);
+        hv = (j == 24) ? sh : tf32_round(sv - sh);
+      };
+      if (nh < 32 * (KS < 3 ? KS : 3)) shift(nh, h);
+      if (nl >= 0) shift(nl, l);
+    }
     *reinterpret_cast<float *>(hi + sw128_off(n, j)) = h;
     *reinterpret_cast<float *>(lo + sw128_off(n, j)) = l;
-    if (j == 0) bimg[n] = (k < K && i < D) ? m.b32[(size_t)k * D + i] : 0.f;
   }
   if (threadIdx.x < kUmGC) {
     const int k = g * kUmGC + threadIdx.x;
-    bimg[128 + threadIdx.x] = (k < K) ? m.lconst32[k] : -INFINITY;
+    reinterpret_cast<float *>(hi + kUmCopyBytes)[threadIdx.x] = (k < K) ? m.lconst32[k] : -INFINITY;
   }
 }
 
@@ -188,25 +211,34 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// 32 consecutive TMEM columns of this warp's 32 lanes (no wait).
-__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float *v) {
+// 16 consecutive TMEM columns of this warp's 32 lanes (no wait).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float *v) {
   uint32_t *r = reinterpret_cast<uint32_t *>(v);
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
+}
+
+// acc += (a, b)^2 elementwise on a packed pair (one f32x2 FMA).
+__device__ __forceinline__ void sq2_acc(unsigned long long &acc, float a, float b) {
+  asm("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1, %2};\n\tfma.rn.f32x2 %0, t, t, %0;\n\t}"
+      : "+l"(acc)
+      : "f"(a), "f"(b));
+}
+__device__ __forceinline__ float sum2(unsigned long long acc) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(acc));
+  return a + b;
 }
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ------------------------------------------------------------------ kernel
 template <bool STUDENT>
-__global__ void __launch_bounds__(kUmThreads, 1)
+__global__ void __maxnreg__(120)
     umma_logq_kernel(DevMixView m, const unsigned char *__restrict__ bimg, size_t N, const float *__restrict__ X,
                      double *__restrict__ out, int accumulate, double add, float *__restrict__ lt,
                      float *__restrict__ Qo, int *__restrict__ errflag) {
@@ -214,12 +246,13 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // 1024-byte aligned operand base (swizzle atoms)
   unsigned char *base = um_raw + ((1024 - (smem_u32(um_raw) & 1023)) & 1023);
   unsigned char *sA = base;                          // [acc 0 hi][acc 0 lo][acc 1 hi][acc 1 lo]
-  unsigned char *sB = base + kUmSmemA;               // ring of kUmStages x (hi, lo)
+  unsigned char *sOnes = sA + kUmSmemA;              // rows of (col 24, col 25) = (1, 1)
+  unsigned char *sB = sOnes + kUmSmemOnes;           // ring of kUmStages x (hi, lo)
+  float *s_merge = reinterpret_cast<float *>(sB + kUmSmemB);     // [2][256][2] (max, sum) of half 1
   const int D = m.D, K = m.K, ldx = m.ldx;
   const int G = (K + kUmGC - 1) / kUmGC;
   const int KS = (D + 7) >> 3;                       // K-steps of 8 (and 8-row blocks)
-  float *s_b = reinterpret_cast<float *>(sB + kUmSmemB);          // [G][128] b, then [G][4] lc
-  float *s_lc = s_b + (size_t)G * 128;
+  float *s_lc = s_merge + 2 * 256 * 2;               // [G][4]
   uint64_t *bars = reinterpret_cast<uint64_t *>(s_lc + (size_t)G * 4);
   uint32_t *tmem_hold = reinterpret_cast<uint32_t *>(bars + kUmBars);
   __shared__ int s_abort;
@@ -234,7 +267,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   const uint32_t bfull0 = smem_u32(&bars[0]), bempty0 = smem_u32(&bars[kUmStages]);
   const uint32_t mfull0 = smem_u32(&bars[2 * kUmStages]), tfree0 = smem_u32(&bars[2 * kUmStages + 2]);
   const uint32_t afull = smem_u32(&bars[2 * kUmStages + 4]);
-  const uint32_t sA_u = smem_u32(sA), sB_u = smem_u32(sB);
+  const uint32_t merged0 = smem_u32(&bars[2 * kUmStages + 5]), read0 = smem_u32(&bars[2 * kUmStages + 7]);
+  const uint32_t sA_u = smem_u32(sA), sOnes_u = smem_u32(sOnes), sB_u = smem_u32(sB);
 
   if (tid == 0) {
     s_abort = 0;
@@ -243,15 +277,18 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     mbar_init(mfull0, 1); mbar_init(mfull0 + 8, 1);
     mbar_init(tfree0, kUmEpi); mbar_init(tfree0 + 8, kUmEpi);
     mbar_init(afull, kUmEpi);
+    mbar_init(merged0, kUmEpi / 2); mbar_init(merged0 + 8, kUmEpi / 2);
+    mbar_init(read0, kUmEpi / 2); mbar_init(read0 + 8, kUmEpi / 2);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // resident b and log-constants of every group
-  for (int e = tid; e < G * 132; e += blockDim.x) {
-    const int g = e / 132, o = e - g * 132;
-    const float v = *reinterpret_cast<const float *>(bimg + (size_t)g * kUmGroupStride + kUmCopyBytes + o * 4);
-    if (o < 128) s_b[g * 128 + o] = v;
-    else s_lc[g * 4 + (o - 128)] = v;
+  // constant operand of the shift K-step and the log-constants of every group
+  for (int e = tid; e < 128 * 32; e += blockDim.x) {
+    const int r = e >> 5, j = e & 31;
+    *reinterpret_cast<float *>(sOnes + sw128_off(r, j)) = (j == 24 || j == 25) ? 1.f : 0.f;
   }
+  for (int e = tid; e < G * 4; e += blockDim.x)
+    s_lc[e] = *reinterpret_cast<const float *>(bimg + (size_t)(e >> 2) * kUmGroupStride + kUmCopyBytes + (e & 3) * 4);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 0) {
     __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_hold)),
@@ -275,13 +312,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       };
       for (int q = 0; q < kUmStages && q < items; q++) load(q);
       bool ok = true;
+      const uint64_t ones_desc = sw128_desc(sOnes_u + 96);          // columns 24..31 of the ones operand
       for (int q = 0; q < items && ok; q++) {
         const int g = q % G, st = q % kUmStages, ab = q & 1;
         if (g == 0 && !mbar_wait(afull, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
         if (!mbar_wait(bfull0 + 8 * st, (uint32_t)((q / kUmStages) & 1), abort)) { ok = false; break; }
         if (q >= 2 && !mbar_wait(tfree0 + 8 * ab, (uint32_t)(((q - 2) >> 1) & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t bH = sB_u + (uint32_t)st * kUmCopyBytes;
+        const uint32_t bH = sB_u + (uint32_t)st * kUmCopyBytes, bL = bH + kUmHalf;
 #pragma unroll
         for (int t = 0; t < 2; t++) {
           const uint32_t d0 = tmem + (uint32_t)ab * 256 + (uint32_t)t * 128;
@@ -291,9 +329,13 @@ __global__ void __launch_bounds__(kUmThreads, 1)
             const uint32_t d = d0 + (uint32_t)(32 * ks);
             const uint32_t bo = (uint32_t)(ks * 4096 + ks * 32), ao = (uint32_t)(ks * 32);
             umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bH + bo), idesc, ks > 0);
-            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bH + kUmHalf + bo), idesc, 1);
+            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bL + bo), idesc, 1);
             umma_tf32(d, sw128_desc(aL + ao), sw128_desc(bH + bo), idesc, 1);
           }
+          // shift K-step: rows < 32 min(KS, 3) from the hi image, rows 96..127 from the lo image
+          const int nh = 32 * (KS < 3 ? KS : 3);
+          umma_tf32(d0, ones_desc, sw128_desc(bH + 96), um_idesc((uint32_t)nh), 1);
+          if (KS == 4) umma_tf32(d0 + 96, ones_desc, sw128_desc(bL + 96), um_idesc(32), 1);
         }
         umma_commit(mfull0 + 8 * ab);
         umma_commit(bempty0 + 8 * st);
@@ -301,7 +343,10 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         // refill the stage of item q-1 once its MMAs have read it
         if (q >= 1 && q - 1 + kUmStages < items) {
           const int p = q - 1;
-          if (!mbar_wait(bempty0 + 8 * (p % kUmStages), (uint32_t)((p / kUmStages) & 1), abort)) { ok = false; break; }
+          if (!mbar_wait(bempty0 + 8 * (p % kUmStages), (uint32_t)((p / kUmStages) & 1), abort)) {
+            ok = false;
+            break;
+          }
           load(p + kUmStages);
         }
       }
@@ -316,15 +361,17 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     }
   } else {
     // ================================================================ epilogue
-    const int mt = warp >> 2;                                // accumulator this warp reads
-    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    // warp w: TMEM lane quarter w&3 of accumulator (w>>2)&1, components 2h, 2h+1 (h = w>>3)
+    const int quarter = warp & 3, mt = (warp >> 2) & 1, hh = warp >> 3;
+    const int srow = mt * 128 + quarter * 32 + lane;         // sample row within the tile
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
-    float4 xr[8];
+    float4 xr[4];
     auto fetch = [&](size_t tile) {
       const size_t n0 = tile * kUmTile;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int s = (tid >> 3) + 32 * j, c = tid & 7;
+      for (int j = 0; j < 4; j++) {
+        const int s = (tid >> 3) + 64 * j, c = tid & 7;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (n0 + s < N && c * 4 < D) {
           v = __ldg(reinterpret_cast<const float4 *>(X + (n0 + s) * ldx + c * 4));
@@ -337,8 +384,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     };
     auto stage = [&]() {
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int s = (tid >> 3) + 32 * j, c = tid & 7;
+      for (int j = 0; j < 4; j++) {
+        const int s = (tid >> 3) + 64 * j, c = tid & 7;
         const int t = s >> 7, r = s & 127;
         const uint32_t off = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
         const float4 v = xr[j];
@@ -358,7 +405,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     stage();
     for (int i = 0; i < my_tiles && ok; i++) {
       const size_t tile = blockIdx.x + (size_t)i * gridDim.x;
-      const size_t n = tile * kUmTile + (size_t)mt * 128 + (warp & 3) * 32 + lane;
+      const size_t n = tile * kUmTile + srow;
       if (i + 1 < my_tiles) fetch(tile + gridDim.x);   // next tile's samples, in flight during this one
       float mx = -INFINITY, sm = 0.f;
       for (int g = 0; g < G; g++) {
@@ -366,66 +413,66 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         if (!mbar_wait(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         __syncwarp();
-        // accumulators of row blocks 0-1, then 2-3 (64 registers at a time)
-        const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128);
-        const float *bg = s_b + g * 128;
-        float qc[4] = {0.f, 0.f, 0.f, 0.f};
+        // y of components 2h (columns 32 rb + 16 h + 0..7) and 2h+1 (+ 8..15)
+        float v[4][16];
+        const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128 + hh * 16);
 #pragma unroll
-        for (int half = 0; half < 2; half++) {
-          float v[2][32];
+        for (int rb = 0; rb < 4; rb++)
+          if (rb < KS) tmem_ld16_nowait(tcol + (uint32_t)(rb * 32), v[rb]);
+        tmem_ld_wait();
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive(tfree0 + 8 * ab);                       // TMEM buffer free for group g+2
+        // the last group's MMAs are done with A: stage the next tile before the math
+        if (g == G - 1 && i + 1 < my_tiles) stage();
+        unsigned long long q2[2] = {0ull, 0ull};
 #pragma unroll
-          for (int h = 0; h < 2; h++)
-            if (2 * half + h < KS) tmem_ld32_nowait(tcol + (uint32_t)((2 * half + h) * 32), v[h]);
-          tmem_ld_wait();
-          if (half == 1) {
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(tfree0 + 8 * ab);                   // TMEM buffer free for group g+2
-            // the last group's MMAs are done with A: stage the next tile before the math
-            if (g == G - 1 && i + 1 < my_tiles) stage();
-          }
+        for (int rb = 0; rb < 4; rb++) {
+          if (rb < KS) {
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int rb = 2 * half + h;
-            if (rb < KS) {
-#pragma unroll
-              for (int c = 0; c < 4; c++) {
-                const float4 b0 = *reinterpret_cast<const float4 *>(bg + rb * 32 + c * 8);
-                const float4 b1 = *reinterpret_cast<const float4 *>(bg + rb * 32 + c * 8 + 4);
-                const float *vv = &v[h][c * 8];
-                float y;
-                y = vv[0] - b0.x; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[1] - b0.y; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[2] - b0.z; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[3] - b0.w; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[4] - b1.x; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[5] - b1.y; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[6] - b1.z; qc[c] = fmaf(y, y, qc[c]);
-                y = vv[7] - b1.w; qc[c] = fmaf(y, y, qc[c]);
-              }
+            for (int e = 0; e < 8; e += 2) {
+              sq2_acc(q2[0], v[rb][e], v[rb][e + 1]);
+              sq2_acc(q2[1], v[rb][8 + e], v[rb][9 + e]);
             }
           }
         }
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int k = g * kUmGC + c;
+        for (int cc = 0; cc < 2; cc++) {
+          const int c = 2 * hh + cc, k = g * kUmGC + c;
           if (k >= K) break;
+          const float qv = sum2(q2[cc]);
           const float lc = s_lc[g * 4 + c];
           float l;
           if (lc == -INFINITY) l = -INFINITY;
-          else l = STUDENT ? lc - hnd * log1pf(qc[c] * rnu) : lc - 0.5f * qc[c];
+          else l = STUDENT ? lc - hnd * log1pf(qv * rnu) : lc - 0.5f * qv;
           if (l > mx) { sm = sm * expf(mx - l) + 1.f; mx = l; }
           else if (l > -INFINITY) sm += expf(l - mx);
           if (n < N && lt) {
             lt[(size_t)k * N + n] = l;
-            if (Qo) Qo[(size_t)k * N + n] = (lc == -INFINITY) ? 0.f : qc[c];
+            if (Qo) Qo[(size_t)k * N + n] = (lc == -INFINITY) ? 0.f : qv;
           }
         }
       }
       if (!ok) break;
-      if (n < N) {
-        const double r = (double)mx + (double)logf(sm);
-        if (accumulate) out[n] += r + add;
-        else out[n] = r;
+      // merge the two halves of the sample's log-sum-exp (double-buffered by tile parity)
+      const int mb = i & 1;
+      float *slot = s_merge + (mb * 256 + srow) * 2;
+      if (hh == 1) {
+        if (i >= 2 && !mbar_wait(read0 + 8 * mb, (uint32_t)(((i - 2) >> 1) & 1), abort)) { ok = false; break; }
+        slot[0] = mx;
+        slot[1] = sm;
+        mbar_arrive(merged0 + 8 * mb);
+      } else {
+        if (!mbar_wait(merged0 + 8 * mb, (uint32_t)((i >> 1) & 1), abort)) { ok = false; break; }
+        const float m2 = slot[0], s2 = slot[1];
+        mbar_arrive(read0 + 8 * mb);
+        float mm = fmaxf(mx, m2), ss;
+        if (mm == -INFINITY) ss = 0.f;
+        else ss = (mx == -INFINITY ? 0.f : sm * expf(mx - mm)) + (m2 == -INFINITY ? 0.f : s2 * expf(m2 - mm));
+        if (n < N) {
+          const double r = (double)mm + (double)logf(ss);
+          if (accumulate) out[n] += r + add;
+          else out[n] = r;
+        }
       }
     }
     if (!ok) atomicExch(errflag, 1);
@@ -452,6 +499,11 @@ cudaError_t launch_umma_logq(const DevMixView &m, const unsigned char *bimg, siz
   const size_t ntiles = (N + kUmTile - 1) / kUmTile;
   const unsigned grid = (unsigned)(ntiles < (size_t)sms ? ntiles : (size_t)sms);
   cudaError_t e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, m.df > 0 ? (const void *)umma_logq_kernel<true>
+                                                : (const void *)umma_logq_kernel<false>)) != cudaSuccess)
+    return e;
+  if (fa.maxThreadsPerBlock < kUmThreads) return cudaErrorLaunchOutOfResources;
   if (m.df > 0) {
     if ((e = cudaFuncSetAttribute(umma_logq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
