@@ -238,7 +238,7 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 
 // ------------------------------------------------------------------ kernel
 template <bool STUDENT>
-__global__ void __maxnreg__(120)
+__global__ void __launch_bounds__(kUmThreads, 1)
     umma_logq_kernel(DevMixView m, const unsigned char *__restrict__ bimg, size_t N, const float *__restrict__ X,
                      double *__restrict__ out, int accumulate, double add, float *__restrict__ lt,
                      float *__restrict__ Qo, int *__restrict__ errflag) {
@@ -413,25 +413,31 @@ __global__ void __maxnreg__(120)
         if (!mbar_wait(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         __syncwarp();
-        // y of components 2h (columns 32 rb + 16 h + 0..7) and 2h+1 (+ 8..15)
-        float v[4][16];
+        // y of components 2h (columns 32 rb + 16 h + 0..7) and 2h+1 (+ 8..15),
+        // row blocks 0-1 then 2-3 (32 registers at a time)
         const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128 + hh * 16);
-#pragma unroll
-        for (int rb = 0; rb < 4; rb++)
-          if (rb < KS) tmem_ld16_nowait(tcol + (uint32_t)(rb * 32), v[rb]);
-        tmem_ld_wait();
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        mbar_arrive(tfree0 + 8 * ab);                       // TMEM buffer free for group g+2
-        // the last group's MMAs are done with A: stage the next tile before the math
-        if (g == G - 1 && i + 1 < my_tiles) stage();
         unsigned long long q2[2] = {0ull, 0ull};
 #pragma unroll
-        for (int rb = 0; rb < 4; rb++) {
-          if (rb < KS) {
+        for (int half = 0; half < 2; half++) {
+          float v[2][16];
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              sq2_acc(q2[0], v[rb][e], v[rb][e + 1]);
-              sq2_acc(q2[1], v[rb][8 + e], v[rb][9 + e]);
+          for (int h = 0; h < 2; h++)
+            if (2 * half + h < KS) tmem_ld16_nowait(tcol + (uint32_t)((2 * half + h) * 32), v[h]);
+          tmem_ld_wait();
+          if (half == 1) {
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(tfree0 + 8 * ab);                   // TMEM buffer free for group g+2
+            // the last group's MMAs are done with A: stage the next tile before the math
+            if (g == G - 1 && i + 1 < my_tiles) stage();
+          }
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            if (2 * half + h < KS) {
+#pragma unroll
+              for (int e = 0; e < 8; e += 2) {
+                sq2_acc(q2[0], v[h][e], v[h][e + 1]);
+                sq2_acc(q2[1], v[h][8 + e], v[h][9 + e]);
+              }
             }
           }
         }
