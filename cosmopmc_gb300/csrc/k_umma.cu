@@ -207,6 +207,44 @@ __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
+// Descriptor of base + off bytes from the descriptor of base (off < 256 KB -
+// base, a multiple of 16): only the start-address field changes.
+__device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t off) { return d + (uint64_t)(off >> 4); }
+
+// The MMAs of one group for both accumulators: K-steps of the triangular
+// product (three split terms each), then the shift K-step. Consecutive MMAs
+// alternate between the two accumulators.
+template <int KS>
+__device__ __forceinline__ void issue_group(uint32_t d0, uint64_t a0, uint64_t b0, uint64_t ones) {
+#pragma unroll
+  for (int ks = 0; ks < KS; ks++) {
+    const uint32_t idesc = um_idesc((uint32_t)(32 * (KS - ks)));
+    const uint32_t bo = (uint32_t)(ks * 4096 + ks * 32), ao = (uint32_t)(ks * 32);
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const uint64_t aH = desc_add(a0, (uint32_t)(2 * t) * kUmHalf + ao);
+      umma_tf32(d0 + t * 128 + 32 * ks, aH, desc_add(b0, bo), idesc, ks > 0);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const uint64_t aH = desc_add(a0, (uint32_t)(2 * t) * kUmHalf + ao);
+      umma_tf32(d0 + t * 128 + 32 * ks, aH, desc_add(b0, kUmHalf + bo), idesc, 1);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const uint64_t aL = desc_add(a0, (uint32_t)(2 * t + 1) * kUmHalf + ao);
+      umma_tf32(d0 + t * 128 + 32 * ks, aL, desc_add(b0, bo), idesc, 1);
+    }
+  }
+  // shift K-step: rows < 32 min(KS, 3) from the hi image, rows 96..127 from the lo image
+  constexpr int nh = 32 * (KS < 3 ? KS : 3);
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
+    umma_tf32(d0 + t * 128, ones, desc_add(b0, 96), um_idesc((uint32_t)nh), 1);
+    if (KS == 4) umma_tf32(d0 + t * 128 + 96, ones, desc_add(b0, kUmHalf + 96), um_idesc(32), 1);
+  }
+}
+
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -237,7 +275,7 @@ __device__ __forceinline__ float sum2(unsigned long long acc) {
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ------------------------------------------------------------------ kernel
-template <bool STUDENT>
+template <bool STUDENT, int KS>
 __global__ void __launch_bounds__(kUmThreads, 1)
     umma_logq_kernel(DevMixView m, const unsigned char *__restrict__ bimg, size_t N, const float *__restrict__ X,
                      double *__restrict__ out, int accumulate, double add, float *__restrict__ lt,
@@ -251,7 +289,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   float *s_merge = reinterpret_cast<float *>(sB + kUmSmemB);     // [2][256][2] (max, sum) of half 1
   const int D = m.D, K = m.K, ldx = m.ldx;
   const int G = (K + kUmGC - 1) / kUmGC;
-  const int KS = (D + 7) >> 3;                       // K-steps of 8 (and 8-row blocks)
+  // KS = ceil(D / 8): K-steps of 8 (and 8-row blocks)
   float *s_lc = s_merge + 2 * 256 * 2;               // [G][4]
   uint64_t *bars = reinterpret_cast<uint64_t *>(s_lc + (size_t)G * 4);
   uint32_t *tmem_hold = reinterpret_cast<uint32_t *>(bars + kUmBars);
@@ -313,30 +351,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       for (int q = 0; q < kUmStages && q < items; q++) load(q);
       bool ok = true;
       const uint64_t ones_desc = sw128_desc(sOnes_u + 96);          // columns 24..31 of the ones operand
+      const uint64_t a_desc = sw128_desc(sA_u), b_desc = sw128_desc(sB_u);
       for (int q = 0; q < items && ok; q++) {
         const int g = q % G, st = q % kUmStages, ab = q & 1;
         if (g == 0 && !mbar_wait(afull, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
         if (!mbar_wait(bfull0 + 8 * st, (uint32_t)((q / kUmStages) & 1), abort)) { ok = false; break; }
         if (q >= 2 && !mbar_wait(tfree0 + 8 * ab, (uint32_t)(((q - 2) >> 1) & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t bH = sB_u + (uint32_t)st * kUmCopyBytes, bL = bH + kUmHalf;
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-          const uint32_t d0 = tmem + (uint32_t)ab * 256 + (uint32_t)t * 128;
-          const uint32_t aH = sA_u + (uint32_t)(2 * t) * kUmHalf, aL = aH + kUmHalf;
-          for (int ks = 0; ks < KS; ks++) {
-            const uint32_t idesc = um_idesc((uint32_t)(32 * (KS - ks)));
-            const uint32_t d = d0 + (uint32_t)(32 * ks);
-            const uint32_t bo = (uint32_t)(ks * 4096 + ks * 32), ao = (uint32_t)(ks * 32);
-            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bH + bo), idesc, ks > 0);
-            umma_tf32(d, sw128_desc(aH + ao), sw128_desc(bL + bo), idesc, 1);
-            umma_tf32(d, sw128_desc(aL + ao), sw128_desc(bH + bo), idesc, 1);
-          }
-          // shift K-step: rows < 32 min(KS, 3) from the hi image, rows 96..127 from the lo image
-          const int nh = 32 * (KS < 3 ? KS : 3);
-          umma_tf32(d0, ones_desc, sw128_desc(bH + 96), um_idesc((uint32_t)nh), 1);
-          if (KS == 4) umma_tf32(d0 + 96, ones_desc, sw128_desc(bL + 96), um_idesc(32), 1);
-        }
+        issue_group<KS>(tmem + (uint32_t)ab * 256, a_desc, desc_add(b_desc, (uint32_t)st * kUmCopyBytes), ones_desc);
         umma_commit(mfull0 + 8 * ab);
         umma_commit(bempty0 + 8 * st);
         last_commit = q;
@@ -504,23 +526,27 @@ cudaError_t launch_umma_logq(const DevMixView &m, const unsigned char *bimg, siz
   if (smem > (size_t)maxsm) return cudaErrorInvalidValue;
   const size_t ntiles = (N + kUmTile - 1) / kUmTile;
   const unsigned grid = (unsigned)(ntiles < (size_t)sms ? ntiles : (size_t)sms);
-  cudaError_t e;
-  cudaFuncAttributes fa;
-  if ((e = cudaFuncGetAttributes(&fa, m.df > 0 ? (const void *)umma_logq_kernel<true>
-                                                : (const void *)umma_logq_kernel<false>)) != cudaSuccess)
-    return e;
-  if (fa.maxThreadsPerBlock < kUmThreads) return cudaErrorLaunchOutOfResources;
-  if (m.df > 0) {
-    if ((e = cudaFuncSetAttribute(umma_logq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-      return e;
-    umma_logq_kernel<true><<<grid, kUmThreads, smem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
-  } else {
-    if ((e = cudaFuncSetAttribute(umma_logq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-      return e;
-    umma_logq_kernel<false><<<grid, kUmThreads, smem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo, errflag);
+  const int KS = (m.D + 7) >> 3;
+  cudaError_t e = cudaSuccess;
+#define PMCG_UMMA(ST, KSV)                                                                                    \
+  {                                                                                                           \
+    cudaFuncAttributes fa;                                                                                    \
+    if ((e = cudaFuncGetAttributes(&fa, (const void *)umma_logq_kernel<ST, KSV>)) != cudaSuccess) return e;   \
+    if (fa.maxThreadsPerBlock < kUmThreads) return cudaErrorLaunchOutOfResources;                             \
+    if ((e = cudaFuncSetAttribute(umma_logq_kernel<ST, KSV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                  (int)smem)) != cudaSuccess)                                                 \
+      return e;                                                                                               \
+    umma_logq_kernel<ST, KSV><<<grid, kUmThreads, smem, s>>>(m, bimg, N, X, out, accumulate, add, lt, Qo,       \
+                                                             errflag);                                        \
   }
+  if (m.df > 0) {
+    if (KS == 1) PMCG_UMMA(true, 1) else if (KS == 2) PMCG_UMMA(true, 2) else if (KS == 3) PMCG_UMMA(true, 3)
+    else PMCG_UMMA(true, 4)
+  } else {
+    if (KS == 1) PMCG_UMMA(false, 1) else if (KS == 2) PMCG_UMMA(false, 2) else if (KS == 3) PMCG_UMMA(false, 3)
+    else PMCG_UMMA(false, 4)
+  }
+#undef PMCG_UMMA
   return cudaGetLastError();
 }
 
