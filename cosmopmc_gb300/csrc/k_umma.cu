@@ -18,7 +18,7 @@
 //    hold y = L^-1 (x - mu) and the epilogue only forms |y|^2.
 //  * CTA = 17 warps, persistent (one per SM). Warp 16 is the producer: one
 //    thread streams the operand image of each group of 4 components
-//    (cp.async.bulk into a 3-stage ring, mbarrier complete_tx) and issues the
+//    (cp.async.bulk into a 4-stage ring, mbarrier complete_tx) and issues the
 //    MMAs. Warps 0-15 stage the samples (TF32 hi/lo, 128-byte swizzle), read
 //    the accumulators (tcgen05.ld 32x32b; two warps per TMEM lane quarter,
 //    two components each) and evaluate the densities; the two halves of each
@@ -37,7 +37,7 @@ constexpr int kUmGC = 4;                      // components per group (128 opera
 constexpr int kUmHalf = 128 * 128;            // bytes of one 128-row x 32-float operand (16 KB)
 constexpr int kUmCopyBytes = 2 * kUmHalf;     // streamed per group: hi + lo (32 KB)
 constexpr int kUmGroupStride = 33 * 1024;     // image stride per group: hi, lo, lc[4]
-constexpr int kUmStages = 3;                  // operand ring
+constexpr int kUmStages = 4;                  // operand ring
 constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
 constexpr int kUmSmemOnes = kUmHalf;          // constant operand of the shift K-step
 constexpr int kUmSmemB = kUmStages * kUmCopyBytes;
@@ -46,7 +46,7 @@ constexpr int kUmThreads = kUmEpi + 32;       // + 1 producer warp
 constexpr long long kUmWaitLimit = 1ll << 26;   // iteration cap of one wait
 constexpr uint64_t kUmWaitNs = 1000000000ull;   // wall-time bound of one wait (1 s)
 
-// Barriers: bfull[3], bempty[3], mfull[2], tfree[2], afull, merged[2], read[2]
+// Barriers: bfull[4], bempty[4], mfull[2], tfree[2], afull, merged[2], read[2]
 constexpr int kUmBars = 2 * kUmStages + 9;
 
 size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupStride; }
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
                   bfull0 + 8 * st);
         issued_loads++;
       };
-      for (int q = 0; q < kUmStages && q < items; q++) load(q);
+      for (int q = 0; q < 2 && q < items; q++) load(q);
       bool ok = true;
       const uint64_t ones_desc = sw128_desc(sOnes_u + 96);          // columns 24..31 of the ones operand
       const uint64_t a_desc = sw128_desc(sA_u), b_desc = sw128_desc(sB_u);
@@ -362,14 +362,15 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         umma_commit(mfull0 + 8 * ab);
         umma_commit(bempty0 + 8 * st);
         last_commit = q;
-        // refill the stage of item q-1 once its MMAs have read it
-        if (q >= 1 && q - 1 + kUmStages < items) {
-          const int p = q - 1;
-          if (!mbar_wait(bempty0 + 8 * (p % kUmStages), (uint32_t)((p / kUmStages) & 1), abort)) {
+        // Load group q+2 into the stage of item q-2, whose MMAs are complete:
+        // the epilogue released its accumulators (tfree, waited above) only
+        // after they had landed. The stage of item q-1 may still be read.
+        if (q + 2 < items) {
+          if (q >= 2 && !mbar_wait(bempty0 + 8 * ((q - 2) % kUmStages), (uint32_t)(((q - 2) / kUmStages) & 1), abort)) {
             ok = false;
             break;
           }
-          load(p + kUmStages);
+          load(q + 2);
         }
       }
       if (!ok) atomicExch(errflag, 1);
