@@ -612,6 +612,28 @@ extern "C" int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage) {
   return r->timed;
 }
 
+extern "C" double pmcg_run_time_stage(pmcg_run *r, int stage, int reps, error **err) {
+  Work &w = r->w;
+  if ((stage != 1 && stage != 2) || reps < 1 || r->calls == 0) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_time_stage: stage 1 or 2 of a run that has iterated, reps >= 1");
+    return -1.0;
+  }
+  bool ok = true;
+  if (!CK(cudaEventRecord(r->ev[0], w.s), "event")) return -1.0;
+  for (int i = 0; i < reps && ok; i++) ok = (stage == 1) ? stage_logq(w, err) : stage_logpost(w, r->post, err);
+  if (!ok || !CK(cudaEventRecord(r->ev[1], w.s), "event") ||
+      !CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "status") ||
+      !CK(cudaStreamSynchronize(w.s), "stage timing"))
+    return -1.0;
+  if (w.hstats->tc_err != 0) {
+    set_error(err, PMCG_ETIMEOUT, __LINE__, "tensor-core log-density: a pipeline wait expired");
+    return -1.0;
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+  return (double)ms / reps;
+}
+
 extern "C" int pmcg_run_last_launches(const pmcg_run *r) { return r->last_launches; }
 
 extern "C" int pmcg_device_count(void) {

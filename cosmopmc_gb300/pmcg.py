@@ -185,6 +185,7 @@ SIGNATURES = [
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
     ("pmcg_run_stage_ms", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
+    ("pmcg_run_time_stage", C.c_double, [C.c_void_p, C.c_int, C.c_int, PErr]),
     ("pmcg_batch_create", C.c_void_p, [C.c_int, C.POINTER(C.c_void_p), PErr]),
     ("pmcg_batch_iterate", None, [C.c_void_p, _dp, C.POINTER(IterStats), PErr]),
     ("pmcg_batch_autotune", None, [C.c_void_p, PErr]),
@@ -511,6 +512,10 @@ class Run:
 
     def last_launches(self):
         return load().pmcg_run_last_launches(self.p)
+
+    def time_stage(self, stage, reps=10):
+        """Mean ms of re-evaluating stage 1 (log q) or 2 (log posterior) of the current sample."""
+        return call("pmcg_run_time_stage", self.p, stage, reps)
 
     def free(self):
         if self.p:

@@ -311,6 +311,11 @@ void pmcg_run_free(pmcg_run **r);
 #define PMCG_NSTAGE 5
 void pmcg_run_set_timing(pmcg_run *r, int on);
 int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage);
+/* Re-evaluates stage 1 (proposal log-density) or 2 (log-posterior) of the
+ * run's current sample reps times on the run's stream and returns the mean
+ * milliseconds per evaluation (CUDA events); the results are unchanged. The
+ * run must have iterated once. No counterpart in the reference (profiling). */
+double pmcg_run_time_stage(pmcg_run *r, int stage, int reps, error **err);
 /* Number of kernel launches issued by the last pmcg_run_iterate call. */
 int pmcg_run_last_launches(const pmcg_run *r);
 
