@@ -148,15 +148,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 
 // Parity wait bounded by about one second of wall time (and an iteration
 // cap). Gives up early when another role of the CTA raised the abort flag;
-// raises it on expiry. Returns false when the CTA is aborting.
+// raises it on expiry. Returns false when the CTA is aborting. The clock and
+// the flag are only consulted every 256 polls, off the fast path.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
   uint64_t t0 = 0;
-  for (long long it = 0; it < kUmWaitLimit; it++) {
+  for (long long it = 1; it <= kUmWaitLimit; it++) {
     if (mbar_try(bar, parity)) return true;
-    if ((it & 63) == 0) {
+    if ((it & 255) == 0) {
       if (*abort) return false;
       const uint64_t t = global_ns();
-      if (it == 0) t0 = t;
+      if (it == 256) t0 = t;
       else if (t - t0 > kUmWaitNs) break;
     }
   }
@@ -166,12 +167,31 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
 
 // Bounded wait that ignores the abort flag (draining after an abort).
 __device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
-  const uint64_t t0 = global_ns();
-  for (long long it = 0; it < kUmWaitLimit; it++) {
+  uint64_t t0 = 0;
+  for (long long it = 1; it <= kUmWaitLimit; it++) {
     if (mbar_try(bar, parity)) return true;
-    if ((it & 63) == 0 && global_ns() - t0 > kUmWaitNs) return false;
+    if ((it & 255) == 0) {
+      const uint64_t t = global_ns();
+      if (it == 256) t0 = t;
+      else if (t - t0 > kUmWaitNs) return false;
+    }
   }
   return false;
+}
+
+// Warp-level forms: one lane polls (keeps the shared-memory traffic of
+// waiting warps off the tensor cores' operand reads) and the warp proceeds
+// together; one arrival per warp after __syncwarp.
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive_warp(uint32_t bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
 }
 
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
@@ -313,10 +333,11 @@ __global__ void __launch_bounds__(kUmThreads, 1)
 #pragma unroll
     for (int s = 0; s < kUmStages; s++) { mbar_init(bfull0 + 8 * s, 1); mbar_init(bempty0 + 8 * s, 1); }
     mbar_init(mfull0, 1); mbar_init(mfull0 + 8, 1);
-    mbar_init(tfree0, kUmEpi); mbar_init(tfree0 + 8, kUmEpi);
-    mbar_init(afull, kUmEpi);
-    mbar_init(merged0, kUmEpi / 2); mbar_init(merged0 + 8, kUmEpi / 2);
-    mbar_init(read0, kUmEpi / 2); mbar_init(read0 + 8, kUmEpi / 2);
+    // epilogue barriers count warps (one arrival per warp)
+    mbar_init(tfree0, kUmEpi / 32); mbar_init(tfree0 + 8, kUmEpi / 32);
+    mbar_init(afull, kUmEpi / 32);
+    mbar_init(merged0, kUmEpi / 64); mbar_init(merged0 + 8, kUmEpi / 64);
+    mbar_init(read0, kUmEpi / 64); mbar_init(read0 + 8, kUmEpi / 64);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // constant operand of the shift K-step and the log-constants of every group
@@ -420,7 +441,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         *reinterpret_cast<float4 *>(sA + (2 * t + 1) * kUmHalf + off) = l;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(afull);
+      mbar_arrive_warp(afull);
     };
 
     bool ok = true;
@@ -433,9 +454,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       float mx = -INFINITY, sm = 0.f;
       for (int g = 0; g < G; g++) {
         const int q = i * G + g, ab = q & 1;
-        if (!mbar_wait(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
+        if (!mbar_wait_warp(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        __syncwarp();
         // y of components 2h (columns 32 rb + 16 h + 0..7) and 2h+1 (+ 8..15),
         // row blocks 0-1 then 2-3 (32 registers at a time)
         const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128 + hh * 16);
@@ -449,7 +469,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
           tmem_ld_wait();
           if (half == 1) {
             asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(tfree0 + 8 * ab);                   // TMEM buffer free for group g+2
+            mbar_arrive_warp(tfree0 + 8 * ab);              // TMEM buffer free for group g+2
             // the last group's MMAs are done with A: stage the next tile before the math
             if (g == G - 1 && i + 1 < my_tiles) stage();
           }
@@ -486,14 +506,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       const int mb = i & 1;
       float *slot = s_merge + (mb * 256 + srow) * 2;
       if (hh == 1) {
-        if (i >= 2 && !mbar_wait(read0 + 8 * mb, (uint32_t)(((i - 2) >> 1) & 1), abort)) { ok = false; break; }
+        if (i >= 2 && !mbar_wait_warp(read0 + 8 * mb, (uint32_t)(((i - 2) >> 1) & 1), abort)) { ok = false; break; }
         slot[0] = mx;
         slot[1] = sm;
-        mbar_arrive(merged0 + 8 * mb);
+        mbar_arrive_warp(merged0 + 8 * mb);
       } else {
-        if (!mbar_wait(merged0 + 8 * mb, (uint32_t)((i >> 1) & 1), abort)) { ok = false; break; }
+        if (!mbar_wait_warp(merged0 + 8 * mb, (uint32_t)((i >> 1) & 1), abort)) { ok = false; break; }
         const float m2 = slot[0], s2 = slot[1];
-        mbar_arrive(read0 + 8 * mb);
+        mbar_arrive_warp(read0 + 8 * mb);
         float mm = fmaxf(mx, m2), ss;
         if (mm == -INFINITY) ss = 0.f;
         else ss = (mx == -INFINITY ? 0.f : sm * expf(mx - mm)) + (m2 == -INFINITY ? 0.f : s2 * expf(m2 - mm));
