@@ -108,11 +108,29 @@ __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t 
                                                            const float *__restrict__ aw,
                                                            const float *__restrict__ lt,
                                                            const float *__restrict__ Qv,
-                                                           double *__restrict__ part) {
+                                                           double *__restrict__ part,
+                                                           const uint32_t *__restrict__ mask) {
   extern __shared__ float4 smf4[];
   // component-fastest grid: the blocks of one sample chunk run together and share it in L2
-  body_em_stats_f32(m, N, S, X, aw, lt, Qv, part, blockIdx.x, blockIdx.y, reinterpret_cast<unsigned char *>(smf4));
+  body_em_stats_f32(m, N, S, X, aw, lt, Qv, part, blockIdx.x, blockIdx.y, reinterpret_cast<unsigned char *>(smf4),
+                    mask);
 }
+
+// One bit per (component, sample): aw[n] + lt[k][n] > kEmLogMin, the listing
+// test of the EM statistics. A streaming pass over lt (warp ballots, no atomics).
+__global__ void __launch_bounds__(256) em_mask_kernel(size_t N, int K, const float *__restrict__ aw,
+                                                      const float *__restrict__ lt, uint32_t *__restrict__ mask) {
+  const size_t W = (N + 31) / 32;
+  const int k = blockIdx.y;
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < W * 32; n += (size_t)gridDim.x * blockDim.x) {
+    bool act = false;
+    if (n < N) act = aw[n] + lt[(size_t)k * N + n] > kEmLogMin;
+    const unsigned bal = __ballot_sync(0xffffffffu, act);
+    if ((threadIdx.x & 31) == 0) mask[(size_t)k * W + n / 32] = bal;
+  }
+}
+
+size_t em_mask_words(int K, size_t N) { return (size_t)K * ((N + 31) / 32); }
 
 __global__ void em_weight_factor_kernel(size_t N, const double *__restrict__ logw, const double *__restrict__ logq,
                                         const DevStats *__restrict__ st, float *__restrict__ aw) {
@@ -149,7 +167,7 @@ size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N) {
 cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, const float *X32,
                       const double *logw, const double *logq, const double *lt64, const double *Q64,
                       const float *lt32, const float *Q32, const int *counts, double *partials, int S,
-                      DevStats *st, int band_limit, float *aw32, cudaStream_t s) {
+                      DevStats *st, int band_limit, float *aw32, uint32_t *emmask, cudaStream_t s) {
   DevMixView v = m.view();
   const int D = m.D, E = em_E(D);
   cudaError_t e;
@@ -169,7 +187,14 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
       e = cudaFuncSetAttribute(em_stats_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    em_stats_f32_kernel<<<dim3(m.K, S), 256, smem, s>>>(v, N, S, X32, aw32, lt32, Q32, partials);
+    if (emmask) {
+      const size_t W = (N + 31) / 32;
+      size_t gx = (W * 32 + 255) / 256;
+      if (gx > 1216) gx = 1216;
+      em_mask_kernel<<<dim3((unsigned)gx, m.K), 256, 0, s>>>(N, m.K, aw32, lt32, emmask);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    em_stats_f32_kernel<<<dim3(m.K, S), 256, smem, s>>>(v, N, S, X32, aw32, lt32, Q32, partials, emmask);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int whitened = precision != 0;

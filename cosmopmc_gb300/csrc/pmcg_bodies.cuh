@@ -584,10 +584,13 @@ __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t 
 // (row Dp), St (Dp,Dp) and S0 (Dp+1,Dp). Each thread owns one 4x4 block for one
 // sample group; FP32 sums are flushed into FP64 every kFlushTiles tiles. The
 // order of every sum depends only on the run's own data (deterministic).
+// mask (optional): bit j of word mask[k * W + w] set iff sample 32 w + j is
+// listed for component k (em_mask_kernel). With a mask the block walks 32-sample
+// words instead of testing every sample; the list and every sum are identical.
 __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N, int S, const float *__restrict__ X,
                                                   const float *__restrict__ aw, const float *__restrict__ lt,
                                                   const float *__restrict__ Qv, double *__restrict__ part, int k,
-                                                  int s, unsigned char *smem) {
+                                                  int s, unsigned char *smem, const uint32_t *__restrict__ mask = nullptr) {
   const int D = m.D, E = em_E(D);
   if (m.w[k] <= 0.0) return;
   const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, nib = Dp / 4;
@@ -677,6 +680,76 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   };
 
   int fill = 0;  // listed entries (identical in every thread)
+  // Process full tiles and move the remainder (fill - kTile32 <= 256 entries) to the front.
+  auto drain = [&]() {
+    while (fill >= kTile32) {
+      process(kTile32);
+      const int rem = fill - kTile32;
+      int ri = 0;
+      float rv = 0.f, rt = 0.f;
+      if (tid < rem) { ri = lidx[kTile32 + tid]; rv = lvt[kTile32 + tid]; rt = ltau[kTile32 + tid]; }
+      __syncthreads();
+      if (tid < rem) { lidx[tid] = ri; lvt[tid] = rv; ltau[tid] = rt; }
+      __syncthreads();
+      fill = rem;
+    }
+  };
+  if (mask != nullptr) {
+    const size_t W = (N + 31) / 32;
+    const size_t wbeg = n0 / 32, wend = (n1 + 31) / 32;
+    for (size_t wb = wbeg; wb < wend && n0 < n1; wb += blockDim.x) {
+      const size_t wi = wb + tid;
+      uint32_t bits = 0u;
+      if (wi < wend) {
+        bits = mask[(size_t)k * W + wi];
+        const size_t base = wi * 32;
+        if (base < n0) bits &= ~0u << (unsigned)(n0 - base);
+        if (base + 32 > n1) bits &= (1u << (unsigned)(n1 - base)) - 1u;
+      }
+      const int c = __popc(bits);
+      int incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (lane == 31) wcnt[warp] = incl;
+      __syncthreads();
+      int off = 0, tot = 0;
+      for (int w = 0; w < nwarp; w++) {
+        const int cw = wcnt[w];
+        off += (w < warp) ? cw : 0;
+        tot += cw;
+      }
+      const int pos = off + incl - c;   // position of this word's first entry in this pass
+      // emit in rounds that fit the list buffer, processing full tiles in between
+      for (int done = 0; done < tot;) {
+        const int take = min(kEmBuf - fill, tot - done);
+        uint32_t b = bits;
+        int p = pos;
+        while (b) {
+          const int j = __ffs(b) - 1;
+          b &= b - 1u;
+          if (p >= done && p < done + take) {
+            const size_t n = wi * 32 + j;
+            const float e = aw[n] + lt[(size_t)k * N + n];
+            const float v = expf(e);
+            const float it = (m.df > 0) ? (nu + Qv[(size_t)k * N + n]) * rnd : 1.f;
+            const int q = fill + p - done;
+            lidx[q] = (int)(n - n0);
+            lvt[q] = v / it;
+            ltau[q] = it;
+          }
+          p++;
+        }
+        fill += take;
+        done += take;
+        __syncthreads();
+        drain();
+      }
+      __syncthreads();  // wcnt is rewritten by the next pass
+    }
+  } else
   for (size_t c0 = n0; c0 < n1; c0 += blockDim.x) {
     const size_t n = c0 + tid;
     bool act = false;
@@ -707,18 +780,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
     }
     fill += tot;
     __syncthreads();
-    while (fill >= kTile32) {
-      process(kTile32);
-      // move the remainder (fill - kTile32 <= 256 entries) to the front
-      const int rem = fill - kTile32;
-      int ri = 0;
-      float rv = 0.f, rt = 0.f;
-      if (tid < rem) { ri = lidx[kTile32 + tid]; rv = lvt[kTile32 + tid]; rt = ltau[kTile32 + tid]; }
-      __syncthreads();
-      if (tid < rem) { lidx[tid] = ri; lvt[tid] = rv; ltau[tid] = rt; }
-      __syncthreads();
-      fill = rem;
-    }
+    drain();
   }
   if (fill > 0) process(fill);
 #pragma unroll

@@ -58,6 +58,7 @@ static void work_layout(Work &w, Carver &c, size_t empart_bytes) {
   w.lt32 = prec ? c.take<float>(N * K) : nullptr;
   w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
   w.aw32 = prec ? c.take<float>(N) : nullptr;
+  w.emmask = prec ? c.take<uint32_t>(em_mask_words(K, N)) : nullptr;
   w.wpart = c.take<WRed>(weight_tiles(N));
   w.empart = c.take<double>(empart_bytes / sizeof(double));
   w.dstats = c.take<DevStats>(1);
@@ -163,9 +164,10 @@ static bool stage_weights(Work &w, double beta, bool with_logq, error **err) {
 }
 
 static bool stage_em(Work &w, error **err) {
-  w.launches += w.prec ? 6 : 5;
+  // FP64: stats, finalize, renorm, 2 prepare; mixed: + weight factor, listing bits; + operand image (D <= 32)
+  w.launches += (w.prec ? 7 : 5) + (w.prop.bimg ? 1 : 0);
   return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
-                      w.empart, w.S, w.dstats, w.D, w.aw32, w.s),
+                      w.empart, w.S, w.dstats, w.D, w.aw32, w.emmask, w.s),
             "EM kernels");
 }
 

@@ -48,6 +48,7 @@ struct Work {
   double *logq = nullptr, *logpost = nullptr, *logw = nullptr, *wbar = nullptr;
   double *lt64 = nullptr, *Q64 = nullptr;
   float *lt32 = nullptr, *Q32 = nullptr, *aw32 = nullptr;
+  uint32_t *emmask = nullptr;  // EM listing bits (mixed path)
   WRed *wpart = nullptr;
   double *empart = nullptr;
   DevStats *dstats = nullptr, *hstats = nullptr;

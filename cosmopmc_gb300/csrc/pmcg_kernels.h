@@ -79,10 +79,13 @@ cudaError_t launch_weights(size_t N, double beta, const double *logpost, const d
 
 // (e) EM statistics, finalisation (Cholesky on the device) and renormalisation.
 size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);
+// emmask (mixed path, optional): em_mask_words(K, N) words of scratch for the
+// listing bits; null keeps the per-sample test inside the statistics kernel.
+size_t em_mask_words(int K, size_t N);
 cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, const float *X32,
                       const double *logw, const double *logq, const double *lt64, const double *Q64,
                       const float *lt32, const float *Q32, const int *counts, double *partials, int S,
-                      DevStats *st, int band_limit, float *aw32, cudaStream_t s);
+                      DevStats *st, int band_limit, float *aw32, uint32_t *emmask, cudaStream_t s);
 
 // Convert the mixed-precision sample to FP64 row-major.
 cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
