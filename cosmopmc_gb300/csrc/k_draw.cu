@@ -56,6 +56,130 @@ cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t s
 #undef PMCG_DRAW
 }
 
+// ------------------------------------------------------------------ grouped draw
+// Single-precision draws in three passes, so that the threads of a warp share
+// one component's factor (broadcast reads) instead of gathering a different
+// component's rows each: (1) component of every sample and the counts,
+// (2) samples bucketed by component, (3) normals and transform in bucket
+// order, rows written to the sample's own position. Every value equals the
+// one-pass kernel's (same counters, same operations).
+
+// Component k = min{k : u < C_k} (binary search; C is non-decreasing), else
+// the last component with positive weight.
+__device__ __forceinline__ int pick_component(const double *s_cw, const double *w, int K, double u) {
+  int lo = 0, hi = K;  // first index with u < C
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (u < s_cw[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  if (lo < K) return lo;
+  for (int j = K - 1; j >= 0; j--)
+    if (w[j] > 0.0) return j;
+  return 0;
+}
+
+__global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t N, uint32_t key0, uint32_t key1,
+                                                        uint32_t call, int *__restrict__ idx,
+                                                        int *__restrict__ counts) {
+  extern __shared__ double s_cw[];
+  int *s_cnt = reinterpret_cast<int *>(s_cw + m.K);
+  for (int k = threadIdx.x; k < m.K; k += blockDim.x) { s_cw[k] = m.cw[k]; s_cnt[k] = 0; }
+  __syncthreads();
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < N) {
+    P4 c = {0u, (uint32_t)n, (uint32_t)(n >> 32), call};
+    P4 o = philox4x32_10(c, key0, key1);
+    const int k = pick_component(s_cw, m.w, m.K, u53(o.x, o.y));
+    idx[n] = k;
+    atomicAdd(&s_cnt[k], 1);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m.K; k += blockDim.x)
+    if (s_cnt[k]) atomicAdd(&counts[k], s_cnt[k]);
+}
+
+// perm[off_k + r] = n, off_k = sum of the counts below k; r from a block-local
+// rank plus one reservation per (block, component).
+__global__ void __launch_bounds__(256) draw_bucket_kernel(size_t N, int K, const int *__restrict__ idx,
+                                                          const int *__restrict__ counts, int *__restrict__ cursor,
+                                                          int *__restrict__ perm) {
+  extern __shared__ int s_i[];
+  int *s_off = s_i, *s_hist = s_i + K, *s_base = s_i + 2 * K;
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int k = 0; k < K; k++) { s_off[k] = o; o += counts[k]; }
+  }
+  for (int k = threadIdx.x; k < K; k += blockDim.x) s_hist[k] = 0;
+  __syncthreads();
+  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int k = 0, r = 0;
+  if (n < N) {
+    k = idx[n];
+    r = atomicAdd(&s_hist[k], 1);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < K; j += blockDim.x)
+    if (s_hist[j]) s_base[j] = s_off[j] + atomicAdd(&cursor[j], s_hist[j]);
+  __syncthreads();
+  if (n < N) perm[s_base[k] + r] = (int)n;
+}
+
+template <int MAXD>
+__global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t N, uint32_t key0, uint32_t key1,
+                                                         uint32_t call, const double *__restrict__ bmin,
+                                                         const double *__restrict__ bmax,
+                                                         const int *__restrict__ perm, const int *__restrict__ idx,
+                                                         float *__restrict__ X32, short *__restrict__ flg) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  const size_t n = (size_t)perm[p];
+  const int k = idx[n], D = m.D, ldx = m.ldx, df = m.df;
+  float z[MAXD];
+  float c2;
+  draw_normals<MAXD, float>(D, df > 0 ? df : 0, (uint32_t)n, (uint32_t)(n >> 32), call, key0, key1, z, c2);
+  const float sc = (df > 0) ? (float)sqrt((double)df / (double)c2) : 1.f;
+  float x[MAXD];
+  const int in = draw_transform_f32<MAXD>(m, k, z, sc, bmin, bmax, x, 1);
+  float *row = X32 + n * ldx;
+#pragma unroll
+  for (int j4 = 0; j4 < MAXD / 4; j4++) {
+    if (4 * j4 < ldx) {
+      float4 v;
+      v.x = (4 * j4 < D) ? x[4 * j4] : 0.f;
+      v.y = (4 * j4 + 1 < D) ? x[4 * j4 + 1] : 0.f;
+      v.z = (4 * j4 + 2 < D) ? x[4 * j4 + 2] : 0.f;
+      v.w = (4 * j4 + 3 < D) ? x[4 * j4 + 3] : 0.f;
+      *reinterpret_cast<float4 *>(row + 4 * j4) = v;
+    }
+  }
+  flg[n] = (short)in;
+}
+
+cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
+                                const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
+                                int *cursor, cudaStream_t s) {
+  if (m.D < 1 || m.D > kMaxD || m.K < 1 || m.K > kMaxK) return cudaErrorInvalidValue;
+  if (N == 0) return cudaSuccess;
+  if (N > (size_t)INT32_MAX) return cudaErrorInvalidValue;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * m.K, s)) != cudaSuccess) return e;
+  const unsigned g256 = (unsigned)((N + 255) / 256);
+  draw_pick_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(m, N, k0, k1, call, idx, counts);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  draw_bucket_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(N, m.K, idx, counts, cursor, perm);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const unsigned g128 = (unsigned)((N + 127) / 128);
+#define PMCG_APPLY(MD) draw_apply_kernel<MD><<<g128, 128, 0, s>>>(m, N, k0, k1, call, bmin, bmax, perm, idx, X32, flg)
+  if (m.ldx <= 8) PMCG_APPLY(8);
+  else if (m.ldx <= 16) PMCG_APPLY(16);
+  else if (m.ldx <= 32) PMCG_APPLY(32);
+  else PMCG_APPLY(64);
+#undef PMCG_APPLY
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ helpers
 __global__ void x32_to_x64_kernel(size_t N, int D, int ldx, const float *__restrict__ X32, double *__restrict__ X64) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

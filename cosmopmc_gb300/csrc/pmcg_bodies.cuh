@@ -63,6 +63,72 @@ __host__ __device__ inline size_t draw_smem(int K, int ldo, int threads) {
   return align16((size_t)K * 8 + (size_t)K * 4) + (size_t)threads * (ldo + 1) * sizeof(Real);
 }
 
+// Normals of sample n (counter {1+m, n, call}) into z[0..D), zero above; the
+// sum of squares of the nu extra normals into c2 (Student-t), else c2 = 0.
+template <int MAXD, typename Real>
+__device__ __forceinline__ void draw_normals(int D, int nu, uint32_t nlo, uint32_t nhi, uint32_t call, uint32_t key0,
+                                             uint32_t key1, Real (&z)[MAXD], Real &c2) {
+  c2 = (Real)0;
+#pragma unroll
+  for (int mm = 0; mm < MAXD / 2; mm++) {
+    if (2 * mm < D) {
+      P4 c = {1u + (uint32_t)mm, nlo, nhi, call};
+      P4 o = philox4x32_10(c, key0, key1);
+      Real g0, g1;
+      box_muller<Real>(o, g0, g1);
+      z[2 * mm] = g0;
+      if (2 * mm + 1 < D) {
+        z[2 * mm + 1] = g1;
+      } else {
+        z[2 * mm + 1] = (Real)0;
+        if (nu > 0) c2 += g1 * g1;
+      }
+    } else {
+      z[2 * mm] = (Real)0;
+      z[2 * mm + 1] = (Real)0;
+    }
+  }
+  const int jstart = (D % 2 == 0) ? D : D + 1;
+  for (int j = jstart; j < D + nu; j += 2) {
+    P4 c = {1u + (uint32_t)(j / 2), nlo, nhi, call};
+    P4 o = philox4x32_10(c, key0, key1);
+    Real g0, g1;
+    box_muller<Real>(o, g0, g1);
+    c2 += g0 * g0;
+    if (j + 1 < D + nu) c2 += g1 * g1;
+  }
+}
+
+// x = mu_k + sc L_k z in single precision (L32 rows padded to ldx with zeros
+// above the diagonal: float4 reads); returns 0 when a coordinate leaves the box.
+template <int MAXD>
+__device__ __forceinline__ int draw_transform_f32(const DevMixView &m, int k, const float (&z)[MAXD], float sc,
+                                                  const double *__restrict__ bmin, const double *__restrict__ bmax,
+                                                  float *xo, int xstride) {
+  const int D = m.D, ldx = m.ldx;
+  const float *Lk = m.L32 + (size_t)k * D * ldx;
+  const float *mk = m.mu32 + (size_t)k * D;
+  int in = 1;
+#pragma unroll
+  for (int i = 0; i < MAXD; i++) {
+    if (i < D) {
+      float acc = 0.f;
+#pragma unroll
+      for (int j4 = 0; j4 <= i / 4; j4++) {
+        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4));
+        acc = fmaf(l4.x, z[4 * j4], acc);
+        acc = fmaf(l4.y, z[4 * j4 + 1], acc);
+        acc = fmaf(l4.z, z[4 * j4 + 2], acc);
+        acc = fmaf(l4.w, z[4 * j4 + 3], acc);
+      }
+      const float xi = __ldg(&mk[i]) + sc * acc;
+      xo[i * xstride] = xi;
+      if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
+    }
+  }
+  return in;
+}
+
 // Samples n0 .. n0+blockDim-1: one thread per sample, rows staged in shared
 // memory and written with coalesced stores. Component k = min{k : u < C_k}.
 template <int MAXD, typename Real>
@@ -105,34 +171,7 @@ __device__ __forceinline__ void body_draw(const DevMixView &m, size_t N, uint32_
       for (int i = 0; i < MAXD; i++) z[i] = (i < D) ? (Real)pre_z[n * D + i] : (Real)0;
       c2 = pre_chi2 ? (Real)pre_chi2[n] : (Real)1;
     } else {
-#pragma unroll
-      for (int mm = 0; mm < MAXD / 2; mm++) {
-        if (2 * mm < D) {
-          P4 c = {1u + (uint32_t)mm, nlo, nhi, call};
-          P4 o = philox4x32_10(c, key0, key1);
-          Real g0, g1;
-          box_muller<Real>(o, g0, g1);
-          z[2 * mm] = g0;
-          if (2 * mm + 1 < D) {
-            z[2 * mm + 1] = g1;
-          } else {
-            z[2 * mm + 1] = (Real)0;
-            if (nu > 0) c2 += g1 * g1;
-          }
-        } else {
-          z[2 * mm] = (Real)0;
-          z[2 * mm + 1] = (Real)0;
-        }
-      }
-      const int jstart = (D % 2 == 0) ? D : D + 1;
-      for (int j = jstart; j < D + nu; j += 2) {
-        P4 c = {1u + (uint32_t)(j / 2), nlo, nhi, call};
-        P4 o = philox4x32_10(c, key0, key1);
-        Real g0, g1;
-        box_muller<Real>(o, g0, g1);
-        c2 += g0 * g0;
-        if (j + 1 < D + nu) c2 += g1 * g1;
-      }
+      draw_normals<MAXD, Real>(D, nu, nlo, nhi, call, key0, key1, z, c2);
     }
     const Real sc = (df > 0) ? (Real)sqrt((double)df / (double)c2) : (Real)1;
     const int lds = ldo + 1;
@@ -152,27 +191,10 @@ __device__ __forceinline__ void body_draw(const DevMixView &m, size_t N, uint32_
         }
       }
     } else {
-      // L32 rows padded to ldx with zeros above the diagonal: float4 reads.
-      const int ldx = m.ldx;
-      const float *Lk = m.L32 + (size_t)k * D * ldx;
-      const float *mk = m.mu32 + (size_t)k * D;
+      float zf[MAXD];
 #pragma unroll
-      for (int i = 0; i < MAXD; i++) {
-        if (i < D) {
-          float acc = 0.f;
-#pragma unroll
-          for (int j4 = 0; j4 <= i / 4; j4++) {
-            const float4 l4 = __ldg(reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4));
-            acc = fmaf(l4.x, (float)z[4 * j4], acc);
-            acc = fmaf(l4.y, (float)z[4 * j4 + 1], acc);
-            acc = fmaf(l4.z, (float)z[4 * j4 + 2], acc);
-            acc = fmaf(l4.w, (float)z[4 * j4 + 3], acc);
-          }
-          const float xi = __ldg(&mk[i]) + (float)sc * acc;
-          s_x[threadIdx.x * lds + i] = (Real)xi;
-          if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
-        }
-      }
+      for (int i = 0; i < MAXD; i++) zf[i] = (float)z[i];
+      in = draw_transform_f32<MAXD>(m, k, zf, (float)sc, bmin, bmax, reinterpret_cast<float *>(s_x) + threadIdx.x * lds, 1);
     }
     for (int i = D; i < ldo; i++) s_x[threadIdx.x * lds + i] = (Real)0;
     idx[n] = k;

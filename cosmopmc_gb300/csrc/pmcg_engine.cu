@@ -59,6 +59,8 @@ static void work_layout(Work &w, Carver &c, size_t empart_bytes) {
   w.Q32 = (prec && t) ? c.take<float>(N * K) : nullptr;
   w.aw32 = prec ? c.take<float>(N) : nullptr;
   w.emmask = prec ? c.take<uint32_t>(em_mask_words(K, N)) : nullptr;
+  w.perm = prec ? c.take<int>(N) : nullptr;
+  w.cursor = prec ? c.take<int>(K) : nullptr;
   w.wpart = c.take<WRed>(weight_tiles(N));
   w.empart = c.take<double>(empart_bytes / sizeof(double));
   w.dstats = c.take<DevStats>(1);
@@ -103,6 +105,12 @@ static bool upload_box(Work &w, const double *bmin, const double *bmax, error **
 
 static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **err) {
   if (!CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts")) return false;
+  if (w.prec == 1) {
+    w.launches += 3;
+    return CK(launch_draw_grouped(w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
+                                  w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor, w.s),
+              "draw kernels");
+  }
   w.launches += 1;
   return CK(launch_draw(w.prec, w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
                         nullptr, nullptr, nullptr, w.X64, w.X32, w.idx, w.flg, w.counts, w.s),

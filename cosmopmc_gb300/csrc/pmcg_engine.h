@@ -49,6 +49,7 @@ struct Work {
   double *lt64 = nullptr, *Q64 = nullptr;
   float *lt32 = nullptr, *Q32 = nullptr, *aw32 = nullptr;
   uint32_t *emmask = nullptr;  // EM listing bits (mixed path)
+  int *perm = nullptr, *cursor = nullptr;  // draws bucketed by component (mixed path)
   WRed *wpart = nullptr;
   double *empart = nullptr;
   DevStats *dstats = nullptr, *hstats = nullptr;

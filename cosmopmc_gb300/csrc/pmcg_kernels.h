@@ -67,6 +67,13 @@ cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t s
                         const double *pre_chi2, double *X64, float *X32, int *idx, short *flg, int *counts,
                         cudaStream_t s);
 
+// (a) single-precision draws in component order (three launches; counts must
+// start at zero). perm: N ints, cursor: K ints of scratch. Same values as
+// launch_draw(precision 1) without pre-drawn variates.
+cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
+                                const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
+                                int *cursor, cudaStream_t s);
+
 // (b) mixture log-pdf of N points. out[n] = LSE (accumulate=0) or out[n] += LSE + add (accumulate=1).
 // lt/Q optional, [K x N].
 cudaError_t launch_mixlogpdf(int precision, const DevMixView &m, size_t N, const double *X64, const float *X32,
