@@ -121,7 +121,7 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
       break;
     }
     case kBWeights:
-      body_weights_tile(d.N, dy.beta, d.logpost, d.logq, d.flg, d.logw, d.wpart, li, s_r);
+      body_weights_tile<true>(d.N, dy.beta, d.logpost, d.logq, d.flg, d.logw, d.wpart, li, s_r);
       break;
     case kBWFinal:
       body_weights_final((int)((d.N + kTileW - 1) / kTileW), d.wpart, d.N, d.st, s_r);

@@ -116,17 +116,31 @@ __global__ void __launch_bounds__(256) em_stats_f32_kernel(DevMixView m, size_t 
                     mask);
 }
 
-// One bit per (component, sample): aw[n] + lt[k][n] > kEmLogMin, the listing
-// test of the EM statistics. A streaming pass over lt (warp ballots, no atomics).
-__global__ void __launch_bounds__(256) em_mask_kernel(size_t N, int K, const float *__restrict__ aw,
-                                                      const float *__restrict__ lt, uint32_t *__restrict__ mask) {
+// The weight factor aw (as body_em_factor) and one bit per (component,
+// sample): aw[n] + lt[k][n] > kEmLogMin, the listing test of the EM
+// statistics. One streaming pass over lt (warp ballots, no atomics); each
+// thread keeps its sample's factor in a register across the components.
+__global__ void __launch_bounds__(256) em_factor_mask_kernel(size_t N, int K, const double *__restrict__ logw,
+                                                             const double *__restrict__ logq,
+                                                             const DevStats *__restrict__ st, float *__restrict__ aw,
+                                                             const float *__restrict__ lt,
+                                                             uint32_t *__restrict__ mask) {
+  const double ls = st->logSum;
   const size_t W = (N + 31) / 32;
-  const int k = blockIdx.y;
   for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < W * 32; n += (size_t)gridDim.x * blockDim.x) {
-    bool act = false;
-    if (n < N) act = aw[n] + lt[(size_t)k * N + n] > kEmLogMin;
-    const unsigned bal = __ballot_sync(0xffffffffu, act);
-    if ((threadIdx.x & 31) == 0) mask[(size_t)k * W + n / 32] = bal;
+    float a = -INFINITY;
+    if (n < N) {
+      const double l = logw[n];
+      a = (l > -INFINITY) ? (float)(l - ls - logq[n]) : -INFINITY;
+      aw[n] = a;
+    }
+    const size_t wd = n / 32;
+#pragma unroll 8
+    for (int k = 0; k < K; k++) {
+      const bool act = (n < N) && (a + lt[(size_t)k * N + n] > kEmLogMin);
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if ((threadIdx.x & 31) == 0) mask[(size_t)k * W + wd] = bal;
+    }
   }
 }
 
@@ -178,7 +192,14 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
   } else {
     const int Da = m.ldx + 4, nb = Da / 4, NB = nb * (nb + 1) / 2;
     if (NB > 256) return cudaErrorInvalidValue;
-    em_weight_factor_kernel<<<(unsigned)((N + kTileW - 1) / kTileW), 256, 0, s>>>(N, logw, logq, st, aw32);
+    if (emmask) {
+      const size_t W = (N + 31) / 32;
+      size_t gx = (W * 32 + 255) / 256;
+      if (gx > 2432) gx = 2432;
+      em_factor_mask_kernel<<<(unsigned)gx, 256, 0, s>>>(N, m.K, logw, logq, st, aw32, lt32, emmask);
+    } else {
+      em_weight_factor_kernel<<<(unsigned)((N + kTileW - 1) / kTileW), 256, 0, s>>>(N, logw, logq, st, aw32);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     size_t tb, rb;
     em32_layout(D, m.ldx, 256, &tb, &rb);
@@ -186,13 +207,6 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
     if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(em_stats_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
-    }
-    if (emmask) {
-      const size_t W = (N + 31) / 32;
-      size_t gx = (W * 32 + 255) / 256;
-      if (gx > 1216) gx = 1216;
-      em_mask_kernel<<<dim3((unsigned)gx, m.K), 256, 0, s>>>(N, m.K, aw32, lt32, emmask);
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     em_stats_f32_kernel<<<dim3(m.K, S), 256, smem, s>>>(v, N, S, X32, aw32, lt32, Q32, partials, emmask);
   }

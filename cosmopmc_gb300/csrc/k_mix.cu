@@ -72,8 +72,14 @@ __global__ void mix_prepare_consts_kernel(DevMixView m, const double *logdetL, d
 
 cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   DevMixView v = m.view();
-  mix_prepare_comp_kernel<<<m.K, 64, prepare_smem(m.D), s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
-  cudaError_t e = cudaGetLastError();
+  const size_t smem = prepare_smem(m.D);
+  cudaError_t e;
+  if (smem > 48 * 1024 &&
+      (e = cudaFuncSetAttribute(mix_prepare_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess)
+    return e;
+  mix_prepare_comp_kernel<<<m.K, 64, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mix_prepare_consts_kernel<<<1, 256, 0, s>>>(v, m.logdetL, m.cw, m.lconst, m.lconst32);
   e = cudaGetLastError();

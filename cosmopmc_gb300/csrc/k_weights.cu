@@ -15,11 +15,12 @@ namespace pmcg {
 
 size_t weight_tiles(size_t N) { return N == 0 ? 1 : (N + kTileW - 1) / kTileW; }
 
+template <bool FAST>
 __global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, const double *__restrict__ logpost,
                                                       const double *__restrict__ logq, short *__restrict__ flg,
                                                       double *__restrict__ logw, WRed *__restrict__ partials) {
   __shared__ WRed s_r[8];
-  body_weights_tile(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
+  body_weights_tile<FAST>(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
 }
 
 __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *__restrict__ partials, size_t N,
@@ -29,9 +30,10 @@ __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *
 }
 
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
-                           double *logw, WRed *partials, DevStats *st, cudaStream_t s) {
+                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast) {
   const unsigned nb = (unsigned)weight_tiles(N);
-  weights_kernel<<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
+  if (fast) weights_kernel<true><<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
+  else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   weights_final_kernel<<<1, 256, 0, s>>>((int)nb, partials, N, st);

@@ -486,15 +486,23 @@ __device__ __forceinline__ void body_tpl(const TplDev &t, size_t N, const double
 }
 
 // ================================================================== (d) weights
+// FAST (single-precision runs): each factor e^{x}, x <= 0, is evaluated in
+// single precision (relative error ~1e-7, below the FP32 log-densities it
+// weighs); the sums stay FP64. Otherwise everything is FP64.
+template <bool FAST>
+__device__ __forceinline__ double wexp(double x) {
+  return FAST ? (double)expf((float)x) : exp(x);
+}
+template <bool FAST = false>
 __device__ __forceinline__ void wred_add(WRed &r, double l) {
   if (l > r.m) {
-    double e = exp(r.m - l);  // r.m == -inf gives 0
+    double e = wexp<FAST>(r.m - l);  // r.m == -inf gives 0
     r.s = r.s * e + 1.0;
     r.t = r.t * e + l;
     r.q = r.q * e * e + 1.0;
     r.m = l;
   } else {
-    double e = exp(l - r.m);
+    double e = wexp<FAST>(l - r.m);
     r.s += e;
     r.t += e * l;
     r.q += e * e;
@@ -516,6 +524,7 @@ __device__ __forceinline__ WRed block_wred(WRed r, WRed *s_r) {
 
 // Samples tile*kTileW .. +kTileW-1: log-weights and the tile's partial record.
 // logq == nullptr means log q = 0 (re-normalising given log-weights).
+template <bool FAST = false>
 __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const double *__restrict__ logpost,
                                                   const double *__restrict__ logq, short *__restrict__ flg,
                                                   double *__restrict__ logw, WRed *__restrict__ part, size_t tile,
@@ -531,7 +540,7 @@ __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const d
       if (!isfinite(l)) { l = -INFINITY; flg[n] = 0; }
     }
     logw[n] = l;
-    if (l > -INFINITY) wred_add(r, l);
+    if (l > -INFINITY) wred_add<FAST>(r, l);
   }
   WRed a = block_wred(r, s_r);
   if (threadIdx.x == 0) part[tile] = a;
@@ -830,7 +839,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
 
 // ================================================================== (e) EM finalise
 __host__ __device__ inline size_t finalize_smem(int D, int whitened) {
-  return (size_t)(em_E(D) + (whitened ? 3 : 1) * D * D) * sizeof(double);
+  return (size_t)(em_E(D) + (whitened ? 3 : 1) * D * D + D) * sizeof(double);
 }
 
 // Component k: fixed-order sum of the chunk partials, new mean and covariance
@@ -845,7 +854,7 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   double *st = sh;             // E
   double *C = st + E;          // D*D
   double *Lo = C + D * D;      // D*D old factor (whitened only)
-  double *T = Lo + D * D;      // D*D scratch (whitened only)
+  double *T = Lo + D * D;      // D*D scratch (whitened only); then D: mean shift
   if (stats->status != 0) return;  // the weight step failed: keep the proposal
   if (m.w[k] <= 0.0) {
     if (threadIdx.x == 0) w[k] = 0.0;
@@ -867,11 +876,15 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     return;
   }
   const double S0 = st[0], St = st[1];
+  // the weighted mean shift d = S1 / St (D divisions in parallel) and 1 / S0
+  double *dm = whitened ? T + D * D : C + D * D;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) dm[i] = st[2 + i] / St;
+  __syncthreads();
+  const double rS0 = 1.0 / S0;
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
     int i = e / D, j = e - i * D;
     int a = i > j ? i : j, b = i > j ? j : i;
-    double di = st[2 + i] / St, dj = st[2 + j] / St;
-    C[e] = (st[2 + D + tri_idx(a, b)] - St * di * dj) / S0;
+    C[e] = (st[2 + D + tri_idx(a, b)] - St * dm[i] * dm[j]) * rS0;
     if (whitened) Lo[e] = (j <= i) ? m.L[(size_t)k * D * D + e] : 0.0;
   }
   __syncthreads();
@@ -917,10 +930,11 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
       C[j * D + j] = *s_piv;
     }
     __syncthreads();
+    const double rp = 1.0 / *s_piv;
     for (int i = j + 1 + threadIdx.x; i < D; i += blockDim.x) {
       double t = C[i * D + j];
       for (int q = 0; q < j; q++) t -= C[i * D + q] * C[j * D + q];
-      C[i * D + j] = t / *s_piv;
+      C[i * D + j] = t * rp;
     }
     __syncthreads();
   }
@@ -932,9 +946,9 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     double d;
     if (whitened) {
       d = 0.0;
-      for (int q = 0; q <= i; q++) d += Lo[i * D + q] * (st[2 + q] / St);
+      for (int q = 0; q <= i; q++) d += Lo[i * D + q] * dm[q];
     } else {
-      d = st[2 + i] / St;
+      d = dm[i];
     }
     mu[(size_t)k * D + i] = m.mu[(size_t)k * D + i] + d;
   }
@@ -948,31 +962,46 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
 
 // Renormalise the surviving weights (fixed order), count the dead, ENC.
 __device__ __forceinline__ void body_em_renorm(int K, double *w, DevStats *st) {
-  if (threadIdx.x != 0) return;
+  // one warp: the total in component order by lane 0, the divisions in
+  // parallel (FP64 division is long-latency), fixed-tree sums of squares
+  if (threadIdx.x >= 32) return;
   if (st->status != 0) return;  // the weight step failed: keep the proposal
-  double tot = 0.0;
-  for (int k = 0; k < K; k++) tot += w[k];
-  st->wsum = tot;
+  __shared__ double s_tot;
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int k = 0; k < K; k++) tot += w[k];
+    s_tot = tot;
+    st->wsum = tot;
+  }
+  __syncwarp();
+  const double tot = s_tot;
   if (!(tot > 0.0) || !isfinite(tot)) {
-    st->status = -9005;  // PMCG_ENEGWEIGHT
-    st->ndead = K;
-    st->enc = 0.0;
+    if (threadIdx.x == 0) {
+      st->status = -9005;  // PMCG_ENEGWEIGHT
+      st->ndead = K;
+      st->enc = 0.0;
+    }
     return;
   }
   double s2 = 0.0;
   int nd = 0;
-  for (int k = 0; k < K; k++) {
-    double v = w[k] / tot;
+  for (int k = threadIdx.x; k < K; k += 32) {
+    const double v = w[k] / tot;
     w[k] = v;
     s2 += v * v;
     nd += (v == 0.0);
   }
-  st->ndead = nd;
-  st->enc = 1.0 / s2;
+  s2 = warp_sum(s2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nd += __shfl_down_sync(0xffffffffu, nd, o);
+  if (threadIdx.x == 0) {
+    st->ndead = nd;
+    st->enc = 1.0 / s2;
+  }
 }
 
 // ================================================================== mixture preparation
-__host__ __device__ inline size_t prepare_smem(int D) { return 2 * (size_t)D * D * sizeof(double); }
+__host__ __device__ inline size_t prepare_smem(int D) { return (2 * (size_t)D * D + 2 * (size_t)D) * sizeof(double); }
 
 // Component k: W = L^-1 by column substitution, b = W mu, log|L|, and the
 // single-precision copies used by the mixed kernels.
@@ -992,13 +1021,19 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
     L32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)Lk[i * D + j] : 0.0f;
   }
   for (int i = threadIdx.x; i < D; i += blockDim.x) mu32[(size_t)k * D + i] = (float)m.mu[(size_t)k * D + i];
+  double *sR = sW + D * D;   // D: 1 / L_ii
+  double *sG = sR + D;       // D: log L_ii
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    sR[i] = 1.0 / Lk[i * D + i];
+    sG[i] = log(Lk[i * D + i]);
+  }
   __syncthreads();
   for (int j = threadIdx.x; j < D; j += blockDim.x) {
-    sW[j * D + j] = 1.0 / sL[j * D + j];
+    sW[j * D + j] = sR[j];
     for (int i = j + 1; i < D; i++) {
       double t = 0.0;
       for (int q = j; q < i; q++) t += sL[i * D + q] * sW[q * D + j];
-      sW[i * D + j] = -t / sL[i * D + i];
+      sW[i * D + j] = -t * sR[i];
     }
   }
   __syncthreads();
@@ -1021,7 +1056,7 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
   }
   if (threadIdx.x == 0) {
     double ld = 0.0;
-    for (int i = 0; i < D; i++) ld += log(sL[i * D + i]);
+    for (int i = 0; i < D; i++) ld += sG[i];
     logdetL[k] = ld;
   }
 }

@@ -167,13 +167,13 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
 static bool stage_weights(Work &w, double beta, bool with_logq, error **err) {
   w.launches += 2;
   return CK(launch_weights(w.N, beta, w.logpost, with_logq ? w.logq : nullptr, w.flg, w.logw, w.wpart, w.dstats,
-                           w.s),
+                           w.s, w.prec == 1),
             "weight kernels");
 }
 
 static bool stage_em(Work &w, error **err) {
-  // FP64: stats, finalize, renorm, 2 prepare; mixed: + weight factor, listing bits; + operand image (D <= 32)
-  w.launches += (w.prec ? 7 : 5) + (w.prop.bimg ? 1 : 0);
+  // FP64: stats, finalize, renorm, 2 prepare; mixed: + weight factor with listing bits; + operand image (D <= 32)
+  w.launches += (w.prec ? 6 : 5) + (w.prop.bimg ? 1 : 0);
   return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
                       w.empart, w.S, w.dstats, w.D, w.aw32, w.emmask, w.s),
             "EM kernels");

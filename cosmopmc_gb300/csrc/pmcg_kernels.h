@@ -80,9 +80,10 @@ cudaError_t launch_mixlogpdf(int precision, const DevMixView &m, size_t N, const
                              double *out, int accumulate, double add, double *lt64, double *Q64, float *lt32,
                              float *Q32, cudaStream_t s);
 
-// (d) weights + reduction; writes logw and the scalars of DevStats.
+// (d) weights + reduction; writes logw and the scalars of DevStats. fast: the
+// per-sample factors e^{l-m} in single precision (single-precision runs).
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
-                           double *logw, WRed *partials, DevStats *st, cudaStream_t s);
+                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast = 0);
 
 // (e) EM statistics, finalisation (Cholesky on the device) and renormalisation.
 size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);
