@@ -1,30 +1,31 @@
 // k_umma.cu — (b) mixture log-density on the 5th-generation tensor cores.
 //
 // Y = X L^-1^T for every (sample, component): a [N x 32] x [32 x K*32] product,
-// followed per (sample, component) by y - L^-1 mu, Q = |y|^2, the Gaussian or
+// followed per (sample, component) by Q = |L^-1 (x - mu)|^2, the Gaussian or
 // Student-t log-density and an online log-sum-exp over components. Same
 // result contract as the CUDA-core kernel (body_mixlogpdf_f32).
 //
 //  * tcgen05.mma kind::tf32, accumulators in TMEM. Single-precision accuracy
 //    from three TF32 products (three-term split): x = x_hi + x_lo,
 //    W = W_hi + W_lo, xW ~ x_hi W_hi + x_hi W_lo + x_lo W_hi.
+//  * Components in groups of 8: N = 256 operand rows per MMA (an MMA has a
+//    fixed issue cost, so each should be as wide as the instruction allows).
 //  * L^-1 is lower triangular: the operand rows are ordered by 8-row block
-//    (n = block*32 + component*8 + row), so K-step s only multiplies the rows
-//    of blocks >= s (N = 32 (KS - s), KS = ceil(D/8)): 10 of 16 block
+//    (n = block*64 + component*8 + row), so K-step s only multiplies the rows
+//    of blocks >= s (N = 64 (KS - s), KS = ceil(D/8)): 10 of 16 block
 //    products for D = 32.
 //  * The shift -L^-1 mu is folded into the product: it is stored (hi, lo) in
 //    the never-read upper-triangle blocks of the operand image and added by
 //    one more K-step against a constant operand of ones, so the accumulators
 //    hold y = L^-1 (x - mu) and the epilogue only forms |y|^2.
-//  * CTA = 17 warps, persistent (one per SM). Warp 16 is the producer: one
-//    thread streams the operand image of each group of 4 components
-//    (cp.async.bulk into a 4-stage ring, mbarrier complete_tx) and issues the
-//    MMAs. Warps 0-15 stage the samples (TF32 hi/lo, 128-byte swizzle), read
-//    the accumulators (tcgen05.ld 32x32b; two warps per TMEM lane quarter,
-//    two components each) and evaluate the densities; the two halves of each
-//    sample's log-sum-exp are merged through shared memory.
-//  * Tiles of 256 samples = two M=128 accumulators; TMEM holds two buffers of
-//    (2 x 128 columns), so the MMAs of group g+1 run while group g is read.
+//  * CTA = 9 warps, persistent (one per SM); tiles of 256 samples = two
+//    M=128 accumulators of 256 TMEM columns each. Warp 8 is the producer: one
+//    thread streams the operand image of each group (cp.async.bulk into a
+//    2-stage ring, mbarrier complete_tx) and issues the MMAs, accumulator 0
+//    then 1. Warps 0-7 stage the samples (TF32 hi/lo, 128-byte swizzle), read
+//    the accumulators (tcgen05.ld 32x32b; 4 warps per accumulator, one sample
+//    and all eight components per thread) and evaluate the densities: while
+//    one accumulator is read, the MMAs of the other run.
 //  * Every mbarrier wait is bounded (about one second): on expiry the CTA
 //    raises an abort flag that every other wait observes, sets the error
 //    flag, lets its copies and MMAs in flight land (bounded) and frees TMEM.
@@ -33,28 +34,28 @@
 namespace pmcg {
 
 constexpr int kUmTile = 256;                  // samples per CTA tile
-constexpr int kUmGC = 4;                      // components per group (128 operand rows)
+constexpr int kUmGC = 8;                      // components per group (256 operand rows)
 constexpr int kUmHalf = 128 * 128;            // bytes of one 128-row x 32-float operand (16 KB)
-constexpr int kUmCopyBytes = 2 * kUmHalf;     // streamed per group: hi + lo (32 KB)
-constexpr int kUmGroupStride = 33 * 1024;     // image stride per group: hi, lo, lc[4]
-constexpr int kUmStages = 4;                  // operand ring
+constexpr int kUmOpBytes = 2 * kUmHalf;       // one 256-row operand (32 KB)
+constexpr int kUmCopyBytes = 2 * kUmOpBytes;  // streamed per group: hi + lo (64 KB)
+constexpr int kUmGroupStride = kUmCopyBytes + 1024;  // image stride per group: hi, lo, lc[8]
+constexpr int kUmStages = 2;                  // operand ring
 constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
 constexpr int kUmSmemOnes = kUmHalf;          // constant operand of the shift K-step
 constexpr int kUmSmemB = kUmStages * kUmCopyBytes;
-constexpr int kUmEpi = 512;                   // 16 epilogue warps
+constexpr int kUmEpi = 256;                   // 8 epilogue warps
 constexpr int kUmThreads = kUmEpi + 32;       // + 1 producer warp
 constexpr long long kUmWaitLimit = 1ll << 26;   // iteration cap of one wait
 constexpr uint64_t kUmWaitNs = 1000000000ull;   // wall-time bound of one wait (1 s)
 
-// Barriers: bfull[4], bempty[4], mfull[2], tfree[2], afull, merged[2], read[2]
-constexpr int kUmBars = 2 * kUmStages + 9;
+// Barriers: bfull[2], bempty[2], mfull[2], tfree[2], afull
+constexpr int kUmBars = 2 * kUmStages + 5;
 
 size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupStride; }
 
 static size_t umma_smem_bytes(int K) {
   const int G = (K + kUmGC - 1) / kUmGC;
-  return (size_t)kUmSmemA + kUmSmemOnes + kUmSmemB + 1024 + 2 * 256 * 2 * sizeof(float) +
-         (size_t)G * 4 * sizeof(float) + kUmBars * 8 + 16;
+  return (size_t)kUmSmemA + kUmSmemOnes + kUmSmemB + 1024 + (size_t)G * kUmGC * sizeof(float) + kUmBars * 8 + 16;
 }
 
 // Byte offset of element (row, col) (col < 32 floats) in a 128-byte-swizzled,
@@ -71,35 +72,35 @@ __device__ __forceinline__ float tf32_round(float x) {
 }
 
 // ------------------------------------------------------------------ operand image
-// Group g, component c (k = 4g + c), row i = 8 rb + r, column j: operand row
-// n = 32 rb + 8 c + r holds W_k[i][:] split into TF32 hi and lo (zero for
+// Group g, component c (k = 8g + c), row i = 8 rb + r, column j: operand row
+// n = 64 rb + 8 c + r holds W_k[i][:] split into TF32 hi and lo (zero for
 // padding rows / columns / components). The shift s_n = -(L^-1 mu)_k[i],
 // split into TF32 (hi, lo), sits in columns 24, 25 of rows that no K-step
-// reads there: rows n < 32 min(KS, 3) of the hi image (upper triangle, or
-// unused when KS <= 3) and, for KS = 4, rows 96..127 in rows 0..31 of the lo
-// image. After the operands: the four log-constants (-inf for padding).
+// reads there: rows n < 64 min(KS, 3) of the hi operand (upper triangle, or
+// unused when KS <= 3) and, for KS = 4, rows 192..255 in rows 0..63 of the lo
+// operand. After the operands: the eight log-constants (-inf for padding).
 __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
   const int g = blockIdx.x, D = m.D, K = m.K, ldx = m.ldx;
   const int KS = (D + 7) >> 3;
-  unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmHalf;
-  for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
+  unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmOpBytes;
+  for (int e = threadIdx.x; e < 256 * 32; e += blockDim.x) {
     const int n = e >> 5, j = e & 31;
-    const int rb = n >> 5, c = (n >> 3) & 3, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
+    const int rb = n >> 6, c = (n >> 3) & 7, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
     float w = 0.f;
     if (k < K && i < D && j < D) w = m.W32[(size_t)k * D * ldx + (size_t)i * ldx + j];
     float h = tf32_round(w);
     float l = tf32_round(w - h);
     // shift entries (the slots are zero in the factor)
     if (j == 24 || j == 25) {
-      const int nh = n;                                   // hi image slot -> operand row nh
-      const int nl = (KS == 4 && n < 32) ? n + 96 : -1;   // lo image slot -> operand row nl
+      const int nh = n;                                   // hi slot -> operand row nh
+      const int nl = (KS == 4 && n < 64) ? n + 192 : -1;  // lo slot -> operand row nl
       auto shift = [&](int row, float &hv) {
-        const int rrb = row >> 5, rc = (row >> 3) & 3, ri = rrb * 8 + (row & 7), rk = g * kUmGC + rc;
+        const int rrb = row >> 6, rc = (row >> 3) & 7, ri = rrb * 8 + (row & 7), rk = g * kUmGC + rc;
         const float sv = (rk < K && ri < D) ? -m.b32[(size_t)rk * D + ri] : 0.f;
         const float sh = tf32_round(sv);
         hv = (j == 24) ? sh : tf32_round(sv - sh);
       };
-      if (nh < 32 * (KS < 3 ? KS : 3)) shift(nh, h);
+      if (nh < 64 * (KS < 3 ? KS : 3)) shift(nh, h);
       if (nl >= 0) shift(nl, l);
     }
     *reinterpret_cast<float *>(hi + sw128_off(n, j)) = h;
@@ -231,52 +232,41 @@ __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64
 // base, a multiple of 16): only the start-address field changes.
 __device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t off) { return d + (uint64_t)(off >> 4); }
 
-// The MMAs of one group for both accumulators: K-steps of the triangular
-// product (three split terms each), then the shift K-step. Consecutive MMAs
-// alternate between the two accumulators.
+// The MMAs of one group for one accumulator (A at a0: hi, then lo 16 KB on;
+// B at b0: hi operand, lo 32 KB on): K-steps of the triangular product (three
+// split terms each), then the shift K-step.
 template <int KS>
-__device__ __forceinline__ void issue_group(uint32_t d0, uint64_t a0, uint64_t b0, uint64_t ones) {
+__device__ __forceinline__ void issue_group(uint32_t d, uint64_t a0, uint64_t b0, uint64_t ones) {
 #pragma unroll
   for (int ks = 0; ks < KS; ks++) {
-    const uint32_t idesc = um_idesc((uint32_t)(32 * (KS - ks)));
-    const uint32_t bo = (uint32_t)(ks * 4096 + ks * 32), ao = (uint32_t)(ks * 32);
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-      const uint64_t aH = desc_add(a0, (uint32_t)(2 * t) * kUmHalf + ao);
-      umma_tf32(d0 + t * 128 + 32 * ks, aH, desc_add(b0, bo), idesc, ks > 0);
-    }
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-      const uint64_t aH = desc_add(a0, (uint32_t)(2 * t) * kUmHalf + ao);
-      umma_tf32(d0 + t * 128 + 32 * ks, aH, desc_add(b0, kUmHalf + bo), idesc, 1);
-    }
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-      const uint64_t aL = desc_add(a0, (uint32_t)(2 * t + 1) * kUmHalf + ao);
-      umma_tf32(d0 + t * 128 + 32 * ks, aL, desc_add(b0, bo), idesc, 1);
-    }
+    const uint32_t idesc = um_idesc((uint32_t)(64 * (KS - ks)));
+    const uint32_t bo = (uint32_t)(ks * 8192 + ks * 32), ao = (uint32_t)(ks * 32);
+    const uint32_t dd = d + (uint32_t)(64 * ks);
+    umma_tf32(dd, desc_add(a0, ao), desc_add(b0, bo), idesc, ks > 0);
+    umma_tf32(dd, desc_add(a0, ao), desc_add(b0, kUmOpBytes + bo), idesc, 1);
+    umma_tf32(dd, desc_add(a0, kUmHalf + ao), desc_add(b0, bo), idesc, 1);
   }
-  // shift K-step: rows < 32 min(KS, 3) from the hi image, rows 96..127 from the lo image
-  constexpr int nh = 32 * (KS < 3 ? KS : 3);
-#pragma unroll
-  for (int t = 0; t < 2; t++) {
-    umma_tf32(d0 + t * 128, ones, desc_add(b0, 96), um_idesc((uint32_t)nh), 1);
-    if (KS == 4) umma_tf32(d0 + t * 128 + 96, ones, desc_add(b0, kUmHalf + 96), um_idesc(32), 1);
-  }
+  // shift K-step: rows < 64 min(KS, 3) from the hi operand, rows 192..255 from the lo operand
+  constexpr int nh = 64 * (KS < 3 ? KS : 3);
+  umma_tf32(d, ones, desc_add(b0, 96), um_idesc((uint32_t)nh), 1);
+  if (KS == 4) umma_tf32(d + 192, ones, desc_add(b0, kUmOpBytes + 96), um_idesc(64), 1);
 }
 
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// 16 consecutive TMEM columns of this warp's 32 lanes (no wait).
-__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float *v) {
+// 32 consecutive TMEM columns of this warp's 32 lanes (no wait).
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float *v) {
   uint32_t *r = reinterpret_cast<uint32_t *>(v);
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
 
@@ -306,12 +296,11 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   unsigned char *sA = base;                          // [acc 0 hi][acc 0 lo][acc 1 hi][acc 1 lo]
   unsigned char *sOnes = sA + kUmSmemA;              // rows of (col 24, col 25) = (1, 1)
   unsigned char *sB = sOnes + kUmSmemOnes;           // ring of kUmStages x (hi, lo)
-  float *s_merge = reinterpret_cast<float *>(sB + kUmSmemB);     // [2][256][2] (max, sum) of half 1
   const int D = m.D, K = m.K, ldx = m.ldx;
   const int G = (K + kUmGC - 1) / kUmGC;
   // KS = ceil(D / 8): K-steps of 8 (and 8-row blocks)
-  float *s_lc = s_merge + 2 * 256 * 2;               // [G][4]
-  uint64_t *bars = reinterpret_cast<uint64_t *>(s_lc + (size_t)G * 4);
+  float *s_lc = reinterpret_cast<float *>(sB + kUmSmemB);        // [G][8]
+  uint64_t *bars = reinterpret_cast<uint64_t *>(s_lc + (size_t)G * kUmGC);
   uint32_t *tmem_hold = reinterpret_cast<uint32_t *>(bars + kUmBars);
   __shared__ int s_abort;
   volatile int *abort = &s_abort;
@@ -321,11 +310,10 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   const int my_tiles = (int)((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
   const int items = my_tiles * G;
 
-  // barrier addresses: bfull(s) = bfull0 + 8 s, bempty(s) = bempty0 + 8 s, ...
+  // barrier addresses: bfull(s) = bfull0 + 8 s, mfull(t) = mfull0 + 8 t, ...
   const uint32_t bfull0 = smem_u32(&bars[0]), bempty0 = smem_u32(&bars[kUmStages]);
   const uint32_t mfull0 = smem_u32(&bars[2 * kUmStages]), tfree0 = smem_u32(&bars[2 * kUmStages + 2]);
   const uint32_t afull = smem_u32(&bars[2 * kUmStages + 4]);
-  const uint32_t merged0 = smem_u32(&bars[2 * kUmStages + 5]), read0 = smem_u32(&bars[2 * kUmStages + 7]);
   const uint32_t sA_u = smem_u32(sA), sOnes_u = smem_u32(sOnes), sB_u = smem_u32(sB);
 
   if (tid == 0) {
@@ -334,10 +322,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     for (int s = 0; s < kUmStages; s++) { mbar_init(bfull0 + 8 * s, 1); mbar_init(bempty0 + 8 * s, 1); }
     mbar_init(mfull0, 1); mbar_init(mfull0 + 8, 1);
     // epilogue barriers count warps (one arrival per warp)
-    mbar_init(tfree0, kUmEpi / 32); mbar_init(tfree0 + 8, kUmEpi / 32);
+    mbar_init(tfree0, kUmEpi / 64); mbar_init(tfree0 + 8, kUmEpi / 64);
     mbar_init(afull, kUmEpi / 32);
-    mbar_init(merged0, kUmEpi / 64); mbar_init(merged0 + 8, kUmEpi / 64);
-    mbar_init(read0, kUmEpi / 64); mbar_init(read0 + 8, kUmEpi / 64);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // constant operand of the shift K-step and the log-constants of every group
@@ -345,8 +331,9 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int r = e >> 5, j = e & 31;
     *reinterpret_cast<float *>(sOnes + sw128_off(r, j)) = (j == 24 || j == 25) ? 1.f : 0.f;
   }
-  for (int e = tid; e < G * 4; e += blockDim.x)
-    s_lc[e] = *reinterpret_cast<const float *>(bimg + (size_t)(e >> 2) * kUmGroupStride + kUmCopyBytes + (e & 3) * 4);
+  for (int e = tid; e < G * kUmGC; e += blockDim.x)
+    s_lc[e] = *reinterpret_cast<const float *>(bimg + (size_t)(e / kUmGC) * kUmGroupStride + kUmCopyBytes +
+                                               (e % kUmGC) * 4);
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 0) {
     __syncwarp();
@@ -369,29 +356,35 @@ __global__ void __launch_bounds__(kUmThreads, 1)
                   bfull0 + 8 * st);
         issued_loads++;
       };
-      for (int q = 0; q < 2 && q < items; q++) load(q);
+      for (int q = 0; q < kUmStages && q < items; q++) load(q);
       bool ok = true;
       const uint64_t ones_desc = sw128_desc(sOnes_u + 96);          // columns 24..31 of the ones operand
       const uint64_t a_desc = sw128_desc(sA_u), b_desc = sw128_desc(sB_u);
       for (int q = 0; q < items && ok; q++) {
-        const int g = q % G, st = q % kUmStages, ab = q & 1;
+        const int g = q % G, st = q % kUmStages;
         if (g == 0 && !mbar_wait(afull, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
         if (!mbar_wait(bfull0 + 8 * st, (uint32_t)((q / kUmStages) & 1), abort)) { ok = false; break; }
-        if (q >= 2 && !mbar_wait(tfree0 + 8 * ab, (uint32_t)(((q - 2) >> 1) & 1), abort)) { ok = false; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        issue_group<KS>(tmem + (uint32_t)ab * 256, a_desc, desc_add(b_desc, (uint32_t)st * kUmCopyBytes), ones_desc);
-        umma_commit(mfull0 + 8 * ab);
+        const uint64_t bd = desc_add(b_desc, (uint32_t)st * kUmCopyBytes);
+#pragma unroll 1
+        for (int t = 0; t < 2; t++) {
+          // accumulator t was read for item q-1
+          if (q >= 1 && !mbar_wait(tfree0 + 8 * t, (uint32_t)((q - 1) & 1), abort)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          issue_group<KS>(tmem + (uint32_t)t * 256, desc_add(a_desc, (uint32_t)(2 * t) * kUmHalf), bd, ones_desc);
+          umma_commit(mfull0 + 8 * t);
+        }
+        if (!ok) break;
         umma_commit(bempty0 + 8 * st);
         last_commit = q;
-        // Load group q+2 into the stage of item q-2, whose MMAs are complete:
-        // the epilogue released its accumulators (tfree, waited above) only
-        // after they had landed. The stage of item q-1 may still be read.
-        if (q + 2 < items) {
-          if (q >= 2 && !mbar_wait(bempty0 + 8 * ((q - 2) % kUmStages), (uint32_t)(((q - 2) / kUmStages) & 1), abort)) {
+        // Load group q+1 into the stage of item q-1, whose MMAs are complete: the
+        // epilogue released its accumulators (tfree, waited above) only after
+        // they had landed.
+        if (q >= 1 && q + 1 < items) {
+          if (!mbar_wait(bempty0 + 8 * ((q - 1) % kUmStages), (uint32_t)(((q - 1) / kUmStages) & 1), abort)) {
             ok = false;
             break;
           }
-          load(q + 2);
+          load(q + 1);
         }
       }
       if (!ok) atomicExch(errflag, 1);
@@ -405,17 +398,17 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     }
   } else {
     // ================================================================ epilogue
-    // warp w: TMEM lane quarter w&3 of accumulator (w>>2)&1, components 2h, 2h+1 (h = w>>3)
-    const int quarter = warp & 3, mt = (warp >> 2) & 1, hh = warp >> 3;
-    const int srow = mt * 128 + quarter * 32 + lane;         // sample row within the tile
+    // warp w: TMEM lane quarter w&3 of accumulator t = w>>2; one sample, all eight components
+    const int quarter = warp & 3, ta = warp >> 2;
+    const int srow = ta * 128 + quarter * 32 + lane;         // sample row within the tile
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
-    float4 xr[4];
+    float4 xr[8];
     auto fetch = [&](size_t tile) {
       const size_t n0 = tile * kUmTile;
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int s = (tid >> 3) + 64 * j, c = tid & 7;
+      for (int j = 0; j < 8; j++) {
+        const int s = (tid >> 3) + 32 * j, c = tid & 7;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (n0 + s < N && c * 4 < D) {
           v = __ldg(reinterpret_cast<const float4 *>(X + (n0 + s) * ldx + c * 4));
@@ -428,8 +421,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     };
     auto stage = [&]() {
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int s = (tid >> 3) + 64 * j, c = tid & 7;
+      for (int j = 0; j < 8; j++) {
+        const int s = (tid >> 3) + 32 * j, c = tid & 7;
         const int t = s >> 7, r = s & 127;
         const uint32_t off = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
         const float4 v = xr[j];
@@ -453,43 +446,41 @@ __global__ void __launch_bounds__(kUmThreads, 1)
       if (i + 1 < my_tiles) fetch(tile + gridDim.x);   // next tile's samples, in flight during this one
       float mx = -INFINITY, sm = 0.f;
       for (int g = 0; g < G; g++) {
-        const int q = i * G + g, ab = q & 1;
-        if (!mbar_wait_warp(mfull0 + 8 * ab, (uint32_t)((q >> 1) & 1), abort)) { ok = false; break; }
+        const int q = i * G + g;
+        if (!mbar_wait_warp(mfull0 + 8 * ta, (uint32_t)(q & 1), abort)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        // y of components 2h (columns 32 rb + 16 h + 0..7) and 2h+1 (+ 8..15),
-        // row blocks 0-1 then 2-3 (32 registers at a time)
-        const uint32_t tcol = tmem + lane_base + (uint32_t)(ab * 256 + mt * 128 + hh * 16);
-        unsigned long long q2[2] = {0ull, 0ull};
+        // y of component c, row block rb: columns 64 rb + 8 c + r (32 columns = 4 components per load)
+        const uint32_t tcol = tmem + lane_base + (uint32_t)(ta * 256);
+        unsigned long long q2[8];
 #pragma unroll
-        for (int half = 0; half < 2; half++) {
-          float v[2][16];
+        for (int c = 0; c < 8; c++) q2[c] = 0ull;
 #pragma unroll
-          for (int h = 0; h < 2; h++)
-            if (2 * half + h < KS) tmem_ld16_nowait(tcol + (uint32_t)((2 * half + h) * 32), v[h]);
-          tmem_ld_wait();
-          if (half == 1) {
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive_warp(tfree0 + 8 * ab);              // TMEM buffer free for group g+2
-            // the last group's MMAs are done with A: stage the next tile before the math
-            if (g == G - 1 && i + 1 < my_tiles) stage();
-          }
+        for (int rb = 0; rb < KS; rb++) {
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            if (2 * half + h < KS) {
+          for (int hc = 0; hc < 2; hc++) {
+            float v[32];
+            tmem_ld32_nowait(tcol + (uint32_t)(rb * 64 + hc * 32), v);
+            tmem_ld_wait();
 #pragma unroll
-              for (int e = 0; e < 8; e += 2) {
-                sq2_acc(q2[0], v[h][e], v[h][e + 1]);
-                sq2_acc(q2[1], v[h][8 + e], v[h][9 + e]);
-              }
+            for (int c = 0; c < 4; c++) {
+#pragma unroll
+              for (int e = 0; e < 8; e += 2) sq2_acc(q2[hc * 4 + c], v[c * 8 + e], v[c * 8 + e + 1]);
             }
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive_warp(tfree0 + 8 * ta);                  // accumulator free for the next group
+        if (g == G - 1 && i + 1 < my_tiles) {
+          // every MMA reading A (accumulator 1's are issued last) is done: stage the next tile
+          if (ta == 0 && !mbar_wait_warp(mfull0 + 8, (uint32_t)(q & 1), abort)) { ok = false; break; }
+          stage();
+        }
 #pragma unroll
-        for (int cc = 0; cc < 2; cc++) {
-          const int c = 2 * hh + cc, k = g * kUmGC + c;
+        for (int c = 0; c < 8; c++) {
+          const int k = g * kUmGC + c;
           if (k >= K) break;
-          const float qv = sum2(q2[cc]);
-          const float lc = s_lc[g * 4 + c];
+          const float qv = sum2(q2[c]);
+          const float lc = s_lc[g * kUmGC + c];
           float l;
           if (lc == -INFINITY) l = -INFINITY;
           else l = STUDENT ? lc - hnd * log1pf(qv * rnu) : lc - 0.5f * qv;
@@ -502,26 +493,10 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         }
       }
       if (!ok) break;
-      // merge the two halves of the sample's log-sum-exp (double-buffered by tile parity)
-      const int mb = i & 1;
-      float *slot = s_merge + (mb * 256 + srow) * 2;
-      if (hh == 1) {
-        if (i >= 2 && !mbar_wait_warp(read0 + 8 * mb, (uint32_t)(((i - 2) >> 1) & 1), abort)) { ok = false; break; }
-        slot[0] = mx;
-        slot[1] = sm;
-        mbar_arrive_warp(merged0 + 8 * mb);
-      } else {
-        if (!mbar_wait_warp(merged0 + 8 * mb, (uint32_t)((i >> 1) & 1), abort)) { ok = false; break; }
-        const float m2 = slot[0], s2 = slot[1];
-        mbar_arrive_warp(read0 + 8 * mb);
-        float mm = fmaxf(mx, m2), ss;
-        if (mm == -INFINITY) ss = 0.f;
-        else ss = (mx == -INFINITY ? 0.f : sm * expf(mx - mm)) + (m2 == -INFINITY ? 0.f : s2 * expf(m2 - mm));
-        if (n < N) {
-          const double r = (double)mm + (double)logf(ss);
-          if (accumulate) out[n] += r + add;
-          else out[n] = r;
-        }
+      if (n < N) {
+        const double r = (double)mx + (double)logf(sm);
+        if (accumulate) out[n] += r + add;
+        else out[n] = r;
       }
     }
     if (!ok) atomicExch(errflag, 1);
