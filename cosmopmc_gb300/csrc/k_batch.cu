@@ -388,6 +388,11 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
             BCK(cudaMallocHost(&b->h_stats, sizeof(DevStats) * nruns), "stats") &&
             BCK(cudaMemcpy(b->d_desc, b->hdesc.data(), sizeof(BatchDesc) * nruns, cudaMemcpyHostToDevice),
                 "descriptors");
+  // The batch's draws add to the counts, which its preparation stage zeroes
+  // after each iteration: start from zero (a fresh run's counts are
+  // uninitialised; a run iterated alone holds that iteration's counts).
+  for (int r = 0; ok && r < nruns; r++)
+    ok = BCK(cudaMemsetAsync(runs[r]->w.counts, 0, sizeof(int) * runs[r]->w.K, runs[r]->w.s), "counts");
   // the runs' own streams may still have work queued (proposal uploads)
   for (int r = 0; ok && r < nruns; r++) ok = BCK(cudaStreamSynchronize(runs[r]->w.s), "run stream");
   // a tuned configuration for this shape, if any

@@ -93,7 +93,9 @@ bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) 
   }
   if (!CK(cudaMallocHost(&w.hstats, sizeof(DevStats)), "pinned stats")) return false;
   if (!CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking), "stream")) return false;
-  if (!CK(cudaMemsetAsync(w.dstats, 0, sizeof(DevStats), w.s), "stats")) return false;
+  if (!CK(cudaMemsetAsync(w.dstats, 0, sizeof(DevStats), w.s), "stats") ||
+      !CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * K, w.s), "counts"))
+    return false;
   if (!CK(devmix_alloc(w.prop, K, D, df), "proposal buffers")) return false;
   return true;
 }
