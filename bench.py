@@ -36,6 +36,12 @@ UNIT = "samples/s"
 WORKLOAD = "mixture microbench: D=32, K=64 Student-t nu=3 (cond 1e6), 16-comp Gaussian-mixture target, N=2^20"
 
 
+# DRAM traffic of one launch of the tensor-core proposal log-density at the
+# mixture workload (N = 2^20), from the ncu capture summarised in
+# profiles/umma_logq_mixture.md (None until captured).
+UMMA_TRAFFIC_BYTES = None
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,29 +444,39 @@ def main():
 
 def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches, stage_ms, nt, clocks, W):
     K, D = 64, 32
-    # ---------------- roofline of the dominant kernel (FP32 CUDA-core contraction)
+    # ---------------- roofline of the dominant kernel
+    from cosmopmc_gb300 import pmcg as P
+    tc = P.set_tensor_cores(True)
+    P.set_tensor_cores(tc)
     stage_names = ["draw", "logq", "logpost", "weights", "em"]
     per_stage = {nm: v / nt for nm, v in zip(stage_names, stage_ms)}
-    top = max(per_stage, key=per_stage.get)
-    tri = D * (D + 1) // 2
-    flops = {"logq": N * K * (2 * tri + 2 * D), "logpost": N * 16 * (2 * tri + 2 * D),
-             "em": N * K * (D * D + 3 * D)}
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * (sm_mhz * 1e6) / 1e12
-    if top in flops:
-        achieved = flops[top] / (per_stage[top] / 1000.0) / 1e12
-        roof = {"bound": "fp32", "kernel": {"logq": "mixlogpdf_f32_kernel", "logpost": "mixlogpdf_f32_kernel",
-                                           "em": "em_stats_f32_kernel"}[top],
-                "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                "traffic": None, "stage_ms": per_stage,
-                "peak_note": "FP32 CUDA-core peak derived from 152 SMs x 128 lanes x 2 x median SM clock under load"}
+    # algorithmic flops of the proposal log-density: per (sample, component) the
+    # triangular product L^-1 (x - mu) (D (D+1) / 2 multiply-adds) and |y|^2 (D)
+    flops = N * K * (D * (D + 1) + 2 * D)
+    t_ms = per_stage["logq"]
+    achieved = flops / (t_ms / 1000.0) / 1e12
+    if tc:
+        bf16 = peaks.get("bf16_tflops")
+        peak = bf16 / 2.0 if bf16 else 1900.0 / 2.0
+        roof = {"bound": "tensor", "kernel": "umma_logq_kernel (tcgen05 kind::tf32, three-term split)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                # DRAM bytes per launch at this workload from the ncu capture in profiles/ (lt and Q writes dominate)
+                "traffic": UMMA_TRAFFIC_BYTES, "stage_ms": per_stage,
+                "peak_note": ("dense TF32 = half the measured cuBLAS bf16 burst rate of MEASURED_PEAKS.json"
+                              if bf16 else "dense TF32 = half the fallback bf16 1.9 PFLOP/s"),
+                "flops_note": "algorithmic FP32 flops D(D+1)+2D per (sample, component); the tensor cores "
+                              "execute 3x that (TF32 split) on the lower triangle"}
     else:
-        roof = {"bound": "hbm", "stage_ms": per_stage}
+        fp32_peak = 152 * 128 * 2 * (sm_mhz * 1e6) / 1e12
+        roof = {"bound": "fp32", "kernel": "mixlogpdf_f32_kernel", "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None, "stage_ms": per_stage,
+                "peak_note": "FP32 CUDA-core peak derived from 152 SMs x 128 lanes x 2 x median SM clock under load"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -484,7 +500,6 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{reps} x {args.cpu_sample} samples of this workload "
                                           f"(oracle/pmc_oracle.c, OpenMP)"}
-    from cosmopmc_gb300 import pmcg as P
     if not args.no_batch:
         line["batch"] = batch_bench(P, W)
     if not args.no_serve:

@@ -509,7 +509,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   }
 }
 
-int g_use_tensor_cores = 0;
+// On by default: validated against the CUDA-core kernel and the FP64 oracle.
+int g_use_tensor_cores = 1;
 
 cudaError_t launch_umma_logq(const DevMixView &m, const unsigned char *bimg, size_t N, const float *X, double *out,
                              int accumulate, double add, float *lt, float *Qo, int *errflag, cudaStream_t s) {

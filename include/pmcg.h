@@ -205,8 +205,10 @@ void pmcg_set_dropin_precision(int precision);
 
 /* Single-precision (PMCG_MIXED) mixture log-densities with D <= 32 on the
  * tensor cores: tcgen05 TF32 products in three-term split form, TMEM
- * accumulators (1 = on, 0 = the CUDA-core kernel). Returns the previous
- * setting. No counterpart in the reference (a GPU execution choice). */
+ * accumulators (1 = on, the default; 0 = the CUDA-core kernel). Batched runs
+ * (pmcg_batch_*, the serving loop) always use the CUDA-core kernel, so a run
+ * alone reproduces its batched results bit for bit with 0. Returns the
+ * previous setting. No counterpart in the reference (a GPU execution choice). */
 int pmcg_set_tensor_cores(int on);
 
 /* ------------------------------------------------------------------ *

@@ -9,6 +9,15 @@ from cosmopmc_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _cuda_core_log_density(pmcg):
+    """Batched runs evaluate log q on the CUDA cores; runs alone match them bit
+    for bit with the same kernel."""
+    prev = pmcg.set_tensor_cores(False)
+    yield
+    pmcg.set_tensor_cores(prev)
+
+
 def make_run(P, kind, D, K, N, seed):
     if kind == "mix":
         wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=4 if seed % 2 else -1, seed=seed, prop_hi=2.0)
