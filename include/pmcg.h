@@ -329,8 +329,9 @@ int pmcg_run_last_launches(const pmcg_run *r);
  * captured with its copies in a CUDA graph. Every run must be PMCG_MIXED with
  * D <= 32 and a posterior with exactly one likelihood (mixture, SN Ia or
  * template). The runs keep their state (pmcg_run_get_proposal/_sample work as
- * usual) and give the same results as when iterated alone. The batch
- * references the runs; free it before them. */
+ * usual) and give the same results as when iterated alone with the
+ * CUDA-core log-density (pmcg_set_tensor_cores(0)). The batch references the
+ * runs; free it before them. */
 typedef struct pmcg_batch pmcg_batch;
 pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err);
 /* betas [nruns] (NULL: all 1); stats [nruns] (NULL allowed). A run whose
