@@ -124,7 +124,7 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
       body_weights_tile<true>(d.N, dy.beta, d.logpost, d.logq, d.flg, d.logw, d.wpart, li, s_r);
       break;
     case kBWFinal:
-      body_weights_final((int)((d.N + kTileW - 1) / kTileW), d.wpart, d.N, d.st, s_r);
+      body_weights_final<true>((int)((d.N + kTileW - 1) / kTileW), d.wpart, d.N, d.st, s_r);
       break;
     case kBFactor:
       body_em_factor(d.N, d.logw, d.logq, d.st, d.aw32, li);

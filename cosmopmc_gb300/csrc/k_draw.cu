@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t N,
   float z[MAXD];
   float c2;
   draw_normals<MAXD, float>(D, df > 0 ? df : 0, (uint32_t)n, (uint32_t)(n >> 32), call, key0, key1, z, c2);
-  const float sc = (df > 0) ? (float)sqrt((double)df / (double)c2) : 1.f;
+  const float sc = (df > 0) ? student_scale<float>(df, c2) : 1.f;
   float x[MAXD];
   const int in = draw_transform_f32<MAXD>(m, k, z, sc, bmin, bmax, x, 1);
   float *row = X32 + n * ldx;

@@ -134,12 +134,19 @@ __global__ void __launch_bounds__(256) em_factor_mask_kernel(size_t N, int K, co
       a = (l > -INFINITY) ? (float)(l - ls - logq[n]) : -INFINITY;
       aw[n] = a;
     }
-    const size_t wd = n / 32;
-#pragma unroll 8
-    for (int k = 0; k < K; k++) {
-      const bool act = (n < N) && (a + lt[(size_t)k * N + n] > kEmLogMin);
-      const unsigned bal = __ballot_sync(0xffffffffu, act);
-      if ((threadIdx.x & 31) == 0) mask[(size_t)k * W + wd] = bal;
+    const size_t wd = n / 32, nl = n < N ? n : N - 1;  // padding lanes read a valid sample
+    for (int k0 = 0; k0 < K; k0 += 8) {
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = (k0 + j < K) ? __ldg(&lt[(size_t)(k0 + j) * N + nl]) : 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if (k0 + j < K) {
+          const bool act = (n < N) && (a + v[j] > kEmLogMin);
+          const unsigned bal = __ballot_sync(0xffffffffu, act);
+          if ((threadIdx.x & 31) == 0) mask[(size_t)(k0 + j) * W + wd] = bal;
+        }
+      }
     }
   }
 }
@@ -217,7 +224,7 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
     e = cudaFuncSetAttribute(em_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
     if (e != cudaSuccess) return e;
   }
-  em_finalize_kernel<<<m.K, 128, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit, whitened, st);
+  em_finalize_kernel<<<m.K, 256, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit, whitened, st);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   em_renorm_kernel<<<1, 32, 0, s>>>(m.K, m.w, st);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

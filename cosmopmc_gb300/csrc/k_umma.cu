@@ -83,8 +83,9 @@ __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
   const int g = blockIdx.x, D = m.D, K = m.K, ldx = m.ldx;
   const int KS = (D + 7) >> 3;
   unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmOpBytes;
-  for (int e = threadIdx.x; e < 256 * 32; e += blockDim.x) {
-    const int n = e >> 5, j = e & 31;
+  // block (g, y) writes operand rows 32 y .. 32 y + 31
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    const int n = blockIdx.y * 32 + (e >> 5), j = e & 31;
     const int rb = n >> 6, c = (n >> 3) & 7, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
     float w = 0.f;
     if (k < K && i < D && j < D) w = m.W32[(size_t)k * D * ldx + (size_t)i * ldx + j];
@@ -106,7 +107,7 @@ __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
     *reinterpret_cast<float *>(hi + sw128_off(n, j)) = h;
     *reinterpret_cast<float *>(lo + sw128_off(n, j)) = l;
   }
-  if (threadIdx.x < kUmGC) {
+  if (blockIdx.y == 0 && threadIdx.x < kUmGC) {
     const int k = g * kUmGC + threadIdx.x;
     reinterpret_cast<float *>(hi + kUmCopyBytes)[threadIdx.x] = (k < K) ? m.lconst32[k] : -INFINITY;
   }
@@ -114,7 +115,7 @@ __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
 
 cudaError_t launch_umma_bimage(const DevMixView &m, unsigned char *img, cudaStream_t s) {
   const int G = (m.K + kUmGC - 1) / kUmGC;
-  umma_bimage_kernel<<<G, 256, 0, s>>>(m, img);
+  umma_bimage_kernel<<<dim3(G, 8), 256, 0, s>>>(m, img);
   return cudaGetLastError();
 }
 

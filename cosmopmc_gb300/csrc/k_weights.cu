@@ -23,10 +23,11 @@ __global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, con
   body_weights_tile<FAST>(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
 }
 
+template <bool FAST>
 __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *__restrict__ partials, size_t N,
                                                             DevStats *st) {
   __shared__ WRed s_r[8];
-  body_weights_final(nb, partials, N, st, s_r);
+  body_weights_final<FAST>(nb, partials, N, st, s_r);
 }
 
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
@@ -36,7 +37,8 @@ cudaError_t launch_weights(size_t N, double beta, const double *logpost, const d
   else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  weights_final_kernel<<<1, 256, 0, s>>>((int)nb, partials, N, st);
+  if (fast) weights_final_kernel<true><<<1, 256, 0, s>>>((int)nb, partials, N, st);
+  else weights_final_kernel<false><<<1, 256, 0, s>>>((int)nb, partials, N, st);
   return cudaGetLastError();
 }
 

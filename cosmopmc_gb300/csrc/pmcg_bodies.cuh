@@ -39,6 +39,21 @@ __device__ __forceinline__ void box_muller<double>(P4 o, double &g0, double &g1)
   g0 = r * cs;
   g1 = r * sn;
 }
+// An integer A < 2^53 rounded to the nearest float (ties to even) with integer
+// operations only: the same value as __ull2float_rn, without the 64-bit
+// conversion unit (slow on GB300).
+__device__ __forceinline__ float u53_to_float_rn(unsigned long long A) {
+  if (A < (1ull << 24)) return __uint2float_rn((unsigned)A);  // exact
+  const int p = 63 - __clzll((long long)A);  // top bit, 24..52
+  const int sh = p - 23;
+  unsigned long long m = A >> sh;           // 24 significant bits
+  const unsigned long long rem = A & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (m & 1ull))) m++;
+  int e = p;
+  if (m == (1ull << 24)) { m >>= 1; e++; }
+  return __uint_as_float(((unsigned)(e + 127) << 23) | ((unsigned)m & 0x7FFFFFu));
+}
+
 template <>
 __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
@@ -46,9 +61,9 @@ __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const float two53inv = 1.1102230246251565e-16f;  // 2^-53
   // -2 ln(1-a): from the exact small a below 1/2 (log1p), from the exact
   // complement 1-a above, so r keeps single precision at both ends.
-  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(__ull2float_rn(A) * two53inv))
-                                      : -2.0f * logf(__ull2float_rn((1ull << 53) - A) * two53inv);
-  const float b = __ull2float_rn(B) * two53inv;
+  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(u53_to_float_rn(A) * two53inv))
+                                      : -2.0f * logf(u53_to_float_rn((1ull << 53) - A) * two53inv);
+  const float b = u53_to_float_rn(B) * two53inv;
   float r = sqrtf(r2);
   float sn, cs;
   sincospif(2.0f * b, &sn, &cs);
@@ -97,6 +112,14 @@ __device__ __forceinline__ void draw_normals(int D, int nu, uint32_t nlo, uint32
     c2 += g0 * g0;
     if (j + 1 < D + nu) c2 += g1 * g1;
   }
+}
+
+// Student-t scale sqrt(nu / chi2): FP64 in the FP64 path, single precision
+// (correctly rounded division and square root) in the mixed path.
+template <typename Real>
+__device__ __forceinline__ Real student_scale(int df, Real c2) {
+  if (sizeof(Real) == 8) return (Real)sqrt((double)df / (double)c2);
+  return (Real)sqrtf((float)df / (float)c2);
 }
 
 // x = mu_k + sc L_k z in single precision (L32 rows padded to ldx with zeros
@@ -173,7 +196,7 @@ __device__ __forceinline__ void body_draw(const DevMixView &m, size_t N, uint32_
     } else {
       draw_normals<MAXD, Real>(D, nu, nlo, nhi, call, key0, key1, z, c2);
     }
-    const Real sc = (df > 0) ? (Real)sqrt((double)df / (double)c2) : (Real)1;
+    const Real sc = (df > 0) ? student_scale<Real>(df, c2) : (Real)1;
     const int lds = ldo + 1;
     int in = 1;
     if (sizeof(Real) == 8) {
@@ -511,14 +534,15 @@ __device__ __forceinline__ void wred_add(WRed &r, double l) {
 }
 
 // Block reduction of a WRed in a fixed order; thread 0 receives the result.
+template <bool FAST = false>
 __device__ __forceinline__ WRed block_wred(WRed r, WRed *s_r) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) r = wred_merge(r, wred_shfl(r, o));
+  for (int o = 16; o > 0; o >>= 1) r = wred_merge<FAST>(r, wred_shfl(r, o));
   if ((threadIdx.x & 31) == 0) s_r[threadIdx.x >> 5] = r;
   __syncthreads();
   WRed a = s_r[0];
   if (threadIdx.x == 0)
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge(a, s_r[w]);
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = wred_merge<FAST>(a, s_r[w]);
   return a;
 }
 
@@ -542,17 +566,18 @@ __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const d
     logw[n] = l;
     if (l > -INFINITY) wred_add<FAST>(r, l);
   }
-  WRed a = block_wred(r, s_r);
+  WRed a = block_wred<FAST>(r, s_r);
   if (threadIdx.x == 0) part[tile] = a;
 }
 
 // Merge the nb tile records of one sample (strided per thread, then a fixed
 // tree) and derive logSum, evidence, perplexity and ESS.
+template <bool FAST = false>
 __device__ __forceinline__ void body_weights_final(int nb, const WRed *__restrict__ part, size_t N, DevStats *st,
                                                    WRed *s_r) {
   WRed a = wred_empty();
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge(a, part[b]);
-  a = block_wred(a, s_r);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge<FAST>(a, part[b]);
+  a = block_wred<FAST>(a, s_r);
   if (threadIdx.x != 0) return;
   if (a.n == 0.0 || a.m == -INFINITY) {
     st->status = -9011;  // PMCG_ENOWEIGHT
@@ -921,20 +946,24 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     }
     __syncthreads();
   }
+  // right-looking Cholesky of the lower triangle: pivot, scale the column by the
+  // reciprocal pivot, rank-1 update of the trailing triangle (short FP64 chains)
   for (int j = 0; j < D; j++) {
     if (threadIdx.x == 0) {
       double d = C[j * D + j];
-      for (int q = 0; q < j; q++) d -= C[j * D + q] * C[j * D + q];
       if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
-      *s_piv = sqrt(d);
-      C[j * D + j] = *s_piv;
+      const double pv = sqrt(d);
+      C[j * D + j] = pv;
+      *s_piv = 1.0 / pv;
     }
     __syncthreads();
-    const double rp = 1.0 / *s_piv;
-    for (int i = j + 1 + threadIdx.x; i < D; i += blockDim.x) {
-      double t = C[i * D + j];
-      for (int q = 0; q < j; q++) t -= C[i * D + q] * C[j * D + q];
-      C[i * D + j] = t * rp;
+    const double rp = *s_piv;
+    for (int i = j + 1 + threadIdx.x; i < D; i += blockDim.x) C[i * D + j] *= rp;
+    __syncthreads();
+    const int n1 = D - j - 1;
+    for (int e = threadIdx.x; e < n1 * n1; e += blockDim.x) {
+      const int i = j + 1 + e / n1, c = j + 1 + e % n1;
+      if (c <= i) C[i * D + c] = fma(-C[i * D + j], C[c * D + j], C[i * D + c]);
     }
     __syncthreads();
   }
@@ -1028,15 +1057,21 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
     sG[i] = log(Lk[i * D + i]);
   }
   __syncthreads();
-  for (int j = threadIdx.x; j < D; j += blockDim.x) {
-    sW[j * D + j] = sR[j];
-    for (int i = j + 1; i < D; i++) {
-      double t = 0.0;
-      for (int q = j; q < i; q++) t += sL[i * D + q] * sW[q * D + j];
-      sW[i * D + j] = -t * sR[i];
-    }
-  }
+  // L W = I by right-looking forward substitution: row q of W is final once
+  // scaled by 1/L_qq; then every later row subtracts L_iq W_q. Each sum runs in
+  // the same order as a column substitution would (terms q = j .. i-1).
+  for (int i = threadIdx.x; i < D; i += blockDim.x) sW[i * D + i] = 1.0;
   __syncthreads();
+  for (int q = 0; q < D; q++) {
+    for (int j = threadIdx.x; j <= q; j += blockDim.x) sW[q * D + j] *= sR[q];
+    __syncthreads();
+    const int nr = D - q - 1, nc = q + 1;
+    for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
+      const int i = q + 1 + e / nc, j = e % nc;
+      sW[i * D + j] = fma(-sL[i * D + q], sW[q * D + j], sW[i * D + j]);
+    }
+    __syncthreads();
+  }
   for (int i = threadIdx.x; i < D; i += blockDim.x) {
     double t = 0.0;
     for (int j = 0; j <= i; j++) t += sW[i * D + j] * m.mu[(size_t)k * D + j];
@@ -1048,7 +1083,7 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
     W32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)sW[i * D + j] : 0.0f;
   }
   for (int e = threadIdx.x; e < T; e += blockDim.x) {
-    int i = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+    int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);  // corrected below
     while (tri_idx(i + 1, 0) <= e) i++;
     while (tri_idx(i, 0) > e) i--;
     int j = e - tri_idx(i, 0);

@@ -51,12 +51,16 @@ struct WRed {
   double n;
 };
 __device__ __forceinline__ WRed wred_empty() { WRed r; r.m = -INFINITY; r.s = r.t = r.q = 0.0; r.n = 0.0; return r; }
+// FAST: the two rescaling factors e^{m_a - m}, e^{m_b - m} in single precision
+// (single-precision runs); otherwise FP64.
+template <bool FAST = false>
 __device__ __forceinline__ WRed wred_merge(WRed a, WRed b) {
   if (b.m == -INFINITY) { a.n += b.n; return a; }
   if (a.m == -INFINITY) { b.n += a.n; return b; }
   WRed r;
   r.m = fmax(a.m, b.m);
-  double ea = exp(a.m - r.m), eb = exp(b.m - r.m);
+  double ea = FAST ? (double)expf((float)(a.m - r.m)) : exp(a.m - r.m);
+  double eb = FAST ? (double)expf((float)(b.m - r.m)) : exp(b.m - r.m);
   r.s = a.s * ea + b.s * eb;
   r.t = a.t * ea + b.t * eb;
   r.q = a.q * ea * ea + b.q * eb * eb;
