@@ -39,21 +39,6 @@ __device__ __forceinline__ void box_muller<double>(P4 o, double &g0, double &g1)
   g0 = r * cs;
   g1 = r * sn;
 }
-// An integer A < 2^53 rounded to the nearest float (ties to even) with integer
-// operations only: the same value as __ull2float_rn, without the 64-bit
-// conversion unit (slow on GB300).
-__device__ __forceinline__ float u53_to_float_rn(unsigned long long A) {
-  if (A < (1ull << 24)) return __uint2float_rn((unsigned)A);  // exact
-  const int p = 63 - __clzll((long long)A);  // top bit, 24..52
-  const int sh = p - 23;
-  unsigned long long m = A >> sh;           // 24 significant bits
-  const unsigned long long rem = A & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-  if (rem > half || (rem == half && (m & 1ull))) m++;
-  int e = p;
-  if (m == (1ull << 24)) { m >>= 1; e++; }
-  return __uint_as_float(((unsigned)(e + 127) << 23) | ((unsigned)m & 0x7FFFFFu));
-}
-
 template <>
 __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
@@ -61,9 +46,9 @@ __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const float two53inv = 1.1102230246251565e-16f;  // 2^-53
   // -2 ln(1-a): from the exact small a below 1/2 (log1p), from the exact
   // complement 1-a above, so r keeps single precision at both ends.
-  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(u53_to_float_rn(A) * two53inv))
-                                      : -2.0f * logf(u53_to_float_rn((1ull << 53) - A) * two53inv);
-  const float b = u53_to_float_rn(B) * two53inv;
+  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(__ull2float_rn(A) * two53inv))
+                                      : -2.0f * logf(__ull2float_rn((1ull << 53) - A) * two53inv);
+  const float b = __ull2float_rn(B) * two53inv;
   float r = sqrtf(r2);
   float sn, cs;
   sincospif(2.0f * b, &sn, &cs);
