@@ -24,9 +24,11 @@ __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t
 
 // ================================================================== (a) draw
 // Box-Muller pair from one Philox block. FP64 path: two 53-bit uniforms (the
-// oracle's mapping). FP32 path: the same 53-bit integers, 1-a and b, rounded
-// once to float (integer conversions, no FP64 arithmetic), so its normals equal
-// the FP64 ones to single precision, tails included.
+// oracle's mapping). FP32 path: the same 53-bit integers, 1-a and b, converted
+// to float from two 32-bit halves (within one unit of the last place of the
+// correctly rounded value; 32-bit conversions avoid the 64-bit conversion
+// unit, slow on GB300), so its normals equal the FP64 ones to single
+// precision, tails included.
 template <typename Real>
 __device__ __forceinline__ void box_muller(P4 o, Real &g0, Real &g1);
 
@@ -39,16 +41,21 @@ __device__ __forceinline__ void box_muller<double>(P4 o, double &g0, double &g1)
   g0 = r * cs;
   g1 = r * sn;
 }
+// An integer below 2^53 as float from its high (>= 2^26) and low 26-bit parts.
+__device__ __forceinline__ float u53_to_float(unsigned long long A) {
+  return fmaf(__uint2float_rn((unsigned)(A >> 26)), 67108864.0f, __uint2float_rn((unsigned)(A & 0x3FFFFFFull)));
+}
+
 template <>
 __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
-  const unsigned long long B = ((unsigned long long)(o.z >> 5) << 26) | (unsigned long long)(o.w >> 6);
   const float two53inv = 1.1102230246251565e-16f;  // 2^-53
   // -2 ln(1-a): from the exact small a below 1/2 (log1p), from the exact
   // complement 1-a above, so r keeps single precision at both ends.
-  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(__ull2float_rn(A) * two53inv))
-                                      : -2.0f * logf(__ull2float_rn((1ull << 53) - A) * two53inv);
-  const float b = __ull2float_rn(B) * two53inv;
+  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(u53_to_float(A) * two53inv))
+                                      : -2.0f * logf(u53_to_float((1ull << 53) - A) * two53inv);
+  // b = B / 2^53 with B = (z >> 5) 2^26 + (w >> 6): z / 2^32 to single precision
+  const float b = __uint2float_rn(o.z) * 2.3283064365386963e-10f;  // 2^-32
   float r = sqrtf(r2);
   float sn, cs;
   sincospif(2.0f * b, &sn, &cs);
