@@ -170,9 +170,9 @@ __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *
 __global__ void em_renorm_kernel(int K, double *w, DevStats *st) { body_em_renorm(K, w, st); }
 
 int em_chunks(int K, size_t N) {
-  // about 16 statistics blocks per SM (8 waves of 2 resident blocks): the
-  // blocks are latency-bound, so more and shorter ones balance better
-  int S = (16 * 152 + K - 1) / K;
+  // about 8 statistics blocks per SM (4 waves of 2 resident blocks); measured
+  // against 2 and 16 per SM at the mixture workload
+  int S = (8 * 152 + K - 1) / K;
   size_t maxS = (N + 2047) / 2048;
   if (maxS < 1) maxS = 1;
   if ((size_t)S > maxS) S = (int)maxS;
