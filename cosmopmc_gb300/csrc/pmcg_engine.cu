@@ -667,7 +667,14 @@ struct SimMirror {
   bool lt_valid = false;   // logq/lt/Q valid for (X, snapshot proposal)
   bool w_valid = false;    // logw and the device statistics valid
   std::vector<double> snap_w, snap_mu, snap_L;
+  double *mom = nullptr;   // scratch of the weighted moments (allocated on first use)
 };
+
+static void mirror_delete(SimMirror *m) {
+  work_free(m->w);
+  if (m->mom) cudaFree(m->mom);
+  delete m;
+}
 
 static std::mutex g_mu;
 static std::unordered_map<const pmc_simu *, SimMirror *> g_sims;
@@ -677,15 +684,13 @@ static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error *
   SimMirror *&m = g_sims[psim];
   const int prec = g_dropin_precision;
   if (m && (m->w.K != K || m->w.D != D || m->w.df != df || m->w.N != psim->nsamples || m->w.prec != prec)) {
-    work_free(m->w);
-    delete m;
+    mirror_delete(m);
     m = nullptr;
   }
   if (!m) {
     m = new SimMirror();
     if (!work_alloc(m->w, K, D, df, prec, psim->nsamples, err)) {
-      work_free(m->w);
-      delete m;
+      mirror_delete(m);
       m = nullptr;
       g_sims.erase(psim);
       return nullptr;
@@ -712,8 +717,7 @@ void forget_simu(const pmc_simu *p) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_sims.find(p);
   if (it == g_sims.end()) return;
-  work_free(it->second->w);
-  delete it->second;
+  mirror_delete(it->second);
   g_sims.erase(it);
 }
 
@@ -849,6 +853,79 @@ extern "C" double normalize_importance_weight(pmc_simu *psim, error **err) {
   psim->logSum = w.hstats->logSum;
   psim->maxW = w.hstats->maxW;
   return psim->logSum;
+}
+
+// Replaces every sample's weight by its log-posterior, as exec/importance_sample.c:26-91
+// does point by point: flg = 1, or 0 outside the posterior's prior box or on a
+// likelihood error; isLog = 1; maxW. Returns the number of counted samples.
+extern "C" size_t importance_sample(pmc_simu *psim, const pmcg_posterior *post, int quiet, error **err) {
+  (void)quiet;
+  if (!psim || !post || psim->nsamples == 0) {
+    set_error(err, PMCG_EARG, __LINE__, "importance_sample: null sample or posterior");
+    return 0;
+  }
+  if (post->npar != psim->ndim) {
+    set_error(err, PMCG_EDIM, __LINE__, "posterior has %d parameters, the sample %d", post->npar, psim->ndim);
+    return 0;
+  }
+  const int D = psim->ndim;
+  const bool box = !post->min.empty();
+  for (size_t n = 0; n < psim->nsamples; n++) {
+    short in = 1;
+    if (box)
+      for (int i = 0; i < D; i++) {
+        const double x = psim->X[n * D + i];
+        if (!(x >= post->min[i] && x <= post->max[i])) { in = 0; break; }
+      }
+    psim->flg[n] = in;
+  }
+  pmcg_simu_host_modified(psim);
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return 0;
+  Work &w = m->w;
+  bool ok = sync_sample(m, psim, err) && stage_logpost(w, post, err) &&
+            CK(cudaMemcpyAsync(psim->weights, w.logpost, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "log posterior") &&
+            CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
+            CK(cudaStreamSynchronize(w.s), "importance sample");
+  if (!ok) return 0;
+  m->lt_valid = m->w_valid = false;
+  size_t count = 0;
+  double mw = -INFINITY;
+  for (size_t n = 0; n < psim->nsamples; n++) {
+    if (!psim->flg[n] || !std::isfinite(psim->weights[n])) { psim->flg[n] = 0; continue; }
+    count++;
+    if (psim->weights[n] > mw) mw = psim->weights[n];
+  }
+  psim->isLog = 1;
+  psim->maxW = mw;
+  psim->nok = count;
+  m->x_valid = false;  // flags were rewritten on the host
+  return count;
+}
+
+// Weighted mean [ndim] and covariance [ndim x ndim] of the sample with its
+// (normalised) weights, on the device (the means and covariances of the
+// reference's post-processing, exec/exec_helper.c:63-349).
+extern "C" void pmcg_weighted_moments(pmc_simu *psim, double *mean, double *cov, error **err) {
+  if (!psim || !mean || !cov) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_weighted_moments: null argument");
+    return;
+  }
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return;
+  Work &w = m->w;
+  const int D = w.D;
+  if (!sync_sample(m, psim, err) || !sync_weights(m, psim, err)) return;
+  if (!m->mom && !CK(cudaMalloc(&m->mom, sizeof(double) * (moments_scratch_doubles(D) + D + (size_t)D * D)),
+                     "moments scratch"))
+    return;
+  double *dmean = m->mom + moments_scratch_doubles(D), *dcov = dmean + D;
+  bool ok = CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise") &&
+            CK(launch_moments(w.N, D, w.X64, w.wbar, w.flg, m->mom, dmean, dcov, w.s), "moments") &&
+            CK(cudaMemcpyAsync(mean, dmean, sizeof(double) * D, cudaMemcpyDeviceToHost, w.s), "mean") &&
+            CK(cudaMemcpyAsync(cov, dcov, sizeof(double) * D * D, cudaMemcpyDeviceToHost, w.s), "covariance") &&
+            CK(cudaStreamSynchronize(w.s), "moments");
+  (void)ok;
 }
 
 extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err) {

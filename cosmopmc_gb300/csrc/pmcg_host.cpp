@@ -4,6 +4,7 @@
 // touches a per-sample computation; the hot path is in pmcg_engine.cu.
 #include "../../include/pmcg.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdlib>
@@ -375,6 +376,113 @@ extern "C" void pmc_simu_realloc(pmc_simu *p, size_t nsamples, error **err) {
   }
   p->nsamples = nsamples;
   pmcg_simu_host_modified(p);
+}
+
+// ------------------------------------------------------------------ sample files
+// The CosmoPMC sample file (exec/exec_helper.c:351-427): a header ("# npar =
+// .., n_ded = ..", column titles, parameter names) and one row per counted
+// sample: the unnormalised log-weight, minus the component index, the
+// parameters and the deduced parameters, each "%16.9g".
+extern "C" void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const char *const *par_names,
+                                       double norm, error **err) {
+  (void)norm;
+  FILE *f = fopen(name, "w");
+  if (!f) {
+    set_error(err, PMCG_EIO, __LINE__, "cannot open %s for writing", name);
+    return;
+  }
+  const int D = psim->ndim, Dd = psim->n_ded > 0 ? psim->n_ded : 0;
+  fprintf(f, "# npar = %d, n_ded = %d\n", D, Dd);
+  fprintf(f, "#         weight            chi2");
+  for (int i = 0; i < D; i++) fprintf(f, "        param[%d]", i);
+  for (int i = 0; i < Dd; i++) fprintf(f, "    param_ded[%d]", i);
+  fprintf(f, "\n#                               ");
+  for (int i = 0; i < D; i++) {
+    if (par_names && par_names[i]) fprintf(f, "%16s", par_names[i]);
+    else fprintf(f, "%16s", "p");
+  }
+  fprintf(f, "\n");
+  const double lognorm = psim->logSum;
+  for (size_t n = 0; n < psim->nsamples; n++) {
+    if (psim->flg[n] == 0) continue;
+    double logw = psim->weights[n];
+    if (!psim->isLog) logw = std::log(logw);
+    logw += lognorm;  // back to the unnormalised log-weight
+    fprintf(f, "%16.9g%16.9g", logw, -(double)psim->indices[n]);
+    for (int i = 0; i < D; i++) fprintf(f, "%16.9g", psim->X[n * D + i]);
+    for (int i = 0; i < Dd; i++) fprintf(f, "%16.9g", psim->X_ded[n * Dd + i]);
+    fprintf(f, "\n");
+  }
+  if (fclose(f) != 0) set_error(err, PMCG_EIO, __LINE__, "write error on %s", name);
+}
+
+// Reads a sample file written as above (at most nsamples rows; comment lines
+// start with '#'). The weights come back normalised (isLog = 0) with logSum
+// and maxW of the file's unnormalised log-weights, every row counted (flg = 1)
+// and the component index restored from the second column. proposal, when
+// given, must match npar; clipping (nclipw > 0) is not provided.
+extern "C" pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, const mix_mvdens *proposal,
+                                        int nclipw, error **err) {
+  if (!f || npar < 1 || nsamples == 0) {
+    set_error(err, PMCG_EARG, __LINE__, "pmc_simu_from_file: invalid arguments");
+    return nullptr;
+  }
+  if (nclipw > 0) {
+    set_error(err, PMCG_EUNSUPPORTED, __LINE__, "pmc_simu_from_file: weight clipping (nclipw = %d) is not provided",
+              nclipw);
+    return nullptr;
+  }
+  if (proposal && proposal->ndim != npar) {
+    set_error(err, PMCG_EDIM, __LINE__, "proposal has %d parameters, the sample %d", proposal->ndim, npar);
+    return nullptr;
+  }
+  const int Dd = n_ded > 0 ? n_ded : 0, ncol = 2 + npar + Dd;
+  pmc_simu *p = pmc_simu_init_plus_ded(nsamples, npar, Dd, err);
+  if (!p) return nullptr;
+  std::vector<double> row((size_t)ncol);
+  size_t n = 0;
+  char line[65536];
+  while (n < nsamples && fgets(line, sizeof line, f)) {
+    const char *c = line;
+    while (*c == ' ' || *c == '\t') c++;
+    if (*c == '#' || *c == '\n' || *c == '\0') continue;
+    int got = 0;
+    char *end = nullptr;
+    for (; got < ncol; got++) {
+      row[got] = strtod(c, &end);
+      if (end == c) break;
+      c = end;
+    }
+    if (got != ncol) {
+      set_error(err, PMCG_EIO, __LINE__, "sample file row %zu: %d of %d columns", n + 1, got, ncol);
+      pmc_simu_free(&p);
+      return nullptr;
+    }
+    p->weights[n] = row[0];
+    p->indices[n] = (int)std::lround(-row[1]);
+    for (int i = 0; i < npar; i++) p->X[n * npar + i] = row[2 + i];
+    for (int i = 0; i < Dd; i++) p->X_ded[n * Dd + i] = row[2 + npar + i];
+    p->flg[n] = 1;
+    n++;
+  }
+  if (n == 0) {
+    set_error(err, PMCG_EIO, __LINE__, "sample file holds no sample");
+    pmc_simu_free(&p);
+    return nullptr;
+  }
+  p->nsamples = n;
+  double mx = -INFINITY;
+  for (size_t i = 0; i < n; i++) mx = std::max(mx, p->weights[i]);
+  double s = 0.0;
+  for (size_t i = 0; i < n; i++) s += std::exp(p->weights[i] - mx);
+  const double ls = mx + std::log(s);
+  for (size_t i = 0; i < n; i++) p->weights[i] = std::exp(p->weights[i] - ls);
+  p->isLog = 0;
+  p->logSum = ls;
+  p->maxW = mx;
+  p->nok = n;
+  pmcg_simu_host_modified(p);
+  return p;
 }
 
 extern "C" void pmc_simu_free(pmc_simu **p) {

@@ -95,6 +95,13 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
                       const float *lt32, const float *Q32, const int *counts, double *partials, int S,
                       DevStats *st, int band_limit, float *aw32, uint32_t *emmask, cudaStream_t s);
 
+// (f) Weighted mean [D] and covariance [D x D] (device outputs) of X [N x D]
+// with normalised weights wbar (flg == 0 excluded); scratch of
+// moments_scratch_doubles(D) doubles.
+size_t moments_scratch_doubles(int D);
+cudaError_t launch_moments(size_t N, int D, const double *X, const double *wbar, const short *flg, double *scratch,
+                           double *mean_out, double *cov_out, cudaStream_t s);
+
 // Convert the mixed-precision sample to FP64 row-major.
 cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
 // Normalised weights wbar = exp(logw - logSum) (0 where flg == 0).

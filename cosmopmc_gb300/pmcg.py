@@ -142,6 +142,11 @@ SIGNATURES = [
     ("mix_mvdens_dump", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
     ("mix_mvdens_dwnp", C.POINTER(MixMvdensS), [C.c_void_p, PErr]),
     ("mix_mvdens_print", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
+    ("out_pmc_simu_cosmo_pmc", None, [C.c_char_p, C.POINTER(PmcSimuS), C.POINTER(C.c_char_p), C.c_double, PErr]),
+    ("pmc_simu_from_file", C.POINTER(PmcSimuS), [C.c_void_p, C.c_size_t, C.c_int, C.c_int,
+                                                   C.POINTER(MixMvdensS), C.c_int, PErr]),
+    ("importance_sample", C.c_size_t, [C.POINTER(PmcSimuS), C.c_void_p, C.c_int, PErr]),
+    ("pmcg_weighted_moments", None, [C.POINTER(PmcSimuS), _dp, _dp, PErr]),
     ("effective_number_of_components", C.c_double, [C.POINTER(MixMvdensS), PErr]),
     ("init_parabox", C.POINTER(ParaboxS), [C.c_int, PErr]),
     ("add_slab", None, [C.POINTER(ParaboxS), C.c_int, C.c_double, C.c_double, PErr]),
@@ -249,6 +254,19 @@ def call(name, *args):
     r = getattr(load(), name)(*args, e.ref)
     e.check()
     return r
+
+
+_LIBC = None
+
+
+def _libc():
+    global _LIBC
+    if _LIBC is None:
+        _LIBC = C.CDLL(None)
+        _LIBC.fopen.restype = C.c_void_p
+        _LIBC.fopen.argtypes = [C.c_char_p, C.c_char_p]
+        _LIBC.fclose.argtypes = [C.c_void_p]
+    return _LIBC
 
 
 def _dptr(a):
@@ -378,6 +396,37 @@ class PmcSimu:
 
     def host_modified(self):
         load().pmcg_simu_host_modified(self.p)
+
+    def write(self, path, par_names=None):
+        """CosmoPMC sample file (out_pmc_simu_cosmo_pmc)."""
+        names = None
+        if par_names is not None:
+            names = (C.c_char_p * len(par_names))(*[n.encode() for n in par_names])
+        call("out_pmc_simu_cosmo_pmc", str(path).encode(), self.p, names, 0.0)
+
+    @classmethod
+    def read(cls, path, nsamples, ndim, n_ded=0):
+        """pmc_simu_from_file: normalised weights (isLog = 0), logSum, indices."""
+        f = _libc().fopen(str(path).encode(), b"r")
+        if not f:
+            raise OSError(f"cannot open {path}")
+        try:
+            p = call("pmc_simu_from_file", f, nsamples, ndim, n_ded, None, 0)
+        finally:
+            _libc().fclose(f)
+        obj = cls.__new__(cls)
+        obj.p = p
+        return obj
+
+    def importance_sample(self, post, quiet=1):
+        """Weights := log-posterior of each sample (importance_sample)."""
+        return call("importance_sample", self.p, post.p, quiet)
+
+    def weighted_moments(self):
+        D = self.s.ndim
+        mean, cov = np.empty(D), np.empty((D, D))
+        call("pmcg_weighted_moments", self.p, _dptr(mean), _dptr(cov))
+        return mean, cov
 
     def free(self):
         if self.p:

@@ -139,6 +139,18 @@ typedef struct {
 
 pmc_simu *pmc_simu_init_mpi(size_t nsamples, int ndim, int n_ded, error **err);     /* cosmo_pmc.c:633 */
 pmc_simu *pmc_simu_init_plus_ded(size_t nsamples, int ndim, int n_ded, error **err);/* cosmo_pmc.c:429 */
+/* Sample files (exec/exec_helper.c:351-427): writes the counted samples as
+ * "unnormalised log-weight, -component, parameters, deduced parameters"
+ * (%16.9g) under the CosmoPMC header; par_names may be NULL. norm is unused
+ * (kept for the reference's signature). */
+void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const char *const *par_names, double norm,
+                            error **err);                                           /* cosmo_pmc.c:431 */
+/* Reads such a file (at most nsamples rows; exec/importance_sample.c:198,
+ * exec/cosmo_pmc.c:416): weights normalised (isLog = 0, logSum, maxW of the
+ * file's log-weights), flg = 1, indices from the second column. proposal
+ * (optional) must match npar; nclipw > 0 is rejected (clipping not provided). */
+pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, const mix_mvdens *proposal, int nclipw,
+                             error **err);
 void pmc_simu_realloc(pmc_simu *psim, size_t nsamples, error **err);                /* cosmo_pmc.c:313 */
 void pmc_simu_free(pmc_simu **psim);                                                /* cosmo_pmc.c:738 */
 
@@ -199,6 +211,19 @@ double get_tempering_beta(int tempering, int iter, double t_min, int nmax, error
  * device copy is re-uploaded before the next weight step). */
 void pmcg_simu_host_modified(pmc_simu *psim);
 
+/* Importance sampling of an existing sample with another posterior
+ * (exec/importance_sample.c:26-91): every sample's weight becomes its
+ * log-posterior, evaluated on the device; flg = 0 outside the posterior's
+ * prior box or on a likelihood error; isLog = 1, maxW set. Returns the number
+ * of counted samples. The reference takes a config_base; here the posterior
+ * is a pmcg_posterior. */
+typedef struct pmcg_posterior pmcg_posterior;
+size_t importance_sample(pmc_simu *psim, const pmcg_posterior *post, int quiet, error **err);
+/* Weighted mean [ndim] and covariance [ndim x ndim] of the sample with its
+ * weights (normalised on the device; log or linear, as psim->isLog says), as
+ * the reference's post-processing computes them (exec/exec_helper.c:63-349). */
+void pmcg_weighted_moments(pmc_simu *psim, double *mean, double *cov, error **err);
+
 /* Precision of the drop-in entry points above: PMCG_FP64 (default, the
  * plain FP64 path) or PMCG_MIXED. */
 void pmcg_set_dropin_precision(int precision);
@@ -215,7 +240,6 @@ int pmcg_set_tensor_cores(int on);
  * Part 2 — device posterior plugins (the batched counterpart of the  *
  * per-point func_likeli_t of wrappers/include/init_wrappers.h:15-42). *
  * ------------------------------------------------------------------ */
-typedef struct pmcg_posterior pmcg_posterior;
 
 /* Flat box prior: logpr_default = -sum log(max-min) added once per point
  * (wrappers/src/param.c:124-129, 988-1003). */

@@ -144,3 +144,43 @@ def test_server_and_batch_need_a_gpu(pmcg):
     assert e.value.code == -9001
     with pytest.raises(pmcg.PmcgError):
         pmcg.call("pmcg_batch_create", 0, None)
+
+
+def test_sample_file_roundtrip(pmcg, tmp_path):
+    """out_pmc_simu_cosmo_pmc / pmc_simu_from_file (exec/exec_helper.c:351-427 layout):
+    counted rows only, unnormalised log-weight back from the normalised weights."""
+    rng = np.random.default_rng(3)
+    N, D = 50, 4
+    ps = pmcg.PmcSimu(N, D)
+    X = rng.normal(size=(N, D))
+    logw = rng.normal(size=N) * 3
+    flg = np.ones(N, dtype=np.int16)
+    flg[[3, 17]] = 0
+    ps.X[:] = X
+    ps.flg[:] = flg
+    ps.indices[:] = rng.integers(0, 7, N)
+    mx = logw[flg == 1].max()
+    ls = mx + np.log(np.sum(np.exp(logw[flg == 1] - mx)))
+    ps.weights[:] = np.exp(logw - ls)        # normalised, as after normalize_importance_weight
+    ps.s.isLog = 0
+    ps.s.logSum = ls
+    path = tmp_path / "pmcsim"
+    ps.write(path, [f"p{i}" for i in range(D)])
+    text = path.read_text().splitlines()
+    assert text[0] == "# npar = 4, n_ded = 0" and len([t for t in text if not t.startswith("#")]) == N - 2
+    back = pmcg.PmcSimu.read(path, 1000, D)
+    keep = flg == 1
+    assert back.N == N - 2 and back.s.isLog == 0
+    np.testing.assert_allclose(back.X, X[keep], rtol=1e-8, atol=1e-8)
+    np.testing.assert_array_equal(back.indices, ps.indices[keep])
+    np.testing.assert_allclose(back.s.logSum, ls, rtol=1e-8)
+    np.testing.assert_allclose(back.weights, np.exp(logw[keep] - ls), rtol=1e-7)
+    assert np.all(back.flg == 1)
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    f = libc.fopen(str(path).encode(), b"r")
+    with pytest.raises(pmcg.PmcgError):
+        pmcg.call("pmc_simu_from_file", f, 100, D, 0, None, 2)  # weight clipping is not provided
+    libc.fclose(f)

@@ -1,0 +1,99 @@
+"""Importance sampling of an existing sample with another posterior
+(exec/importance_sample.c) and device weighted moments, through the C ABI,
+against the FP64 oracle and numpy."""
+import numpy as np
+import pytest
+
+from cosmopmc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_importance_sample_sn_matches_oracle(pmcg, oracle):
+    """Weights := log posterior (flat box prior + SN likelihood); flg = 0 outside the
+    box and on a loitering cosmology."""
+    wl = W.sn_workload(nsn=120)
+    sn = wl["sn"]
+    post = pmcg.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(sn)
+    rng = np.random.default_rng(8)
+    N = 3001
+    X = rng.uniform(wl["bmin"], wl["bmax"], (N, 6))
+    X[0] = [0.0, 1.5, -3.0, -19.1, 0.1, 3.0]   # loitering
+    X[1, 0] = wl["bmax"][0] + 0.5              # outside the box
+    ps = pmcg.PmcSimu(N, 6)
+    ps.X[:] = X
+    ps.host_modified()
+    count = ps.importance_sample(post)
+    ref, ok = oracle.sn_loglike(sn, X)
+    inside = np.all((X >= wl["bmin"]) & (X <= wl["bmax"]), axis=1)
+    good = (ok == 1) & inside
+    np.testing.assert_array_equal(ps.flg == 1, good)
+    assert count == good.sum() and ps.s.isLog == 1
+    logpr = -np.sum(np.log(wl["bmax"] - wl["bmin"]))
+    np.testing.assert_allclose(ps.weights[good], ref[good] + logpr, rtol=1e-11, atol=1e-8)
+    assert ps.s.maxW == pytest.approx(np.max(ref[good] + logpr), rel=1e-12)
+
+
+def test_importance_reweighting_from_a_sample_file(pmcg, oracle, tmp_path):
+    """A PMC sample written to file, read back, re-weighted by a second likelihood
+    (the importance_sample flow): combined weights = old * new, as the reference
+    combines them (exec/importance_sample.c:265-284)."""
+    D, K = 4, 3
+    wl = W.mixture_workload(D=D, K=K, Kt=1, nu=-1, seed=21, prop_hi=1.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = pmcg.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    target = pmcg.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+    post = pmcg.Posterior(D).add_mix(target)
+    N = 20000
+    ps = pmcg.PmcSimu(N, D)
+    rng = pmcg.Rng(5)
+    pmcg.simulate_mix_mvdens(ps, prop, rng, None)
+    pmcg.importance_weights(ps, prop, post, 1.0)
+    pmcg.normalize_importance_weight(ps)
+    path = tmp_path / "pmcsim"
+    ps.write(path)
+    back = pmcg.PmcSimu.read(path, N, D)
+    old_logw = np.log(back.weights) + back.s.logSum
+    # a second, independent likelihood: a broad Gaussian around the target's mean
+    mu2 = mut[0] + 0.5
+    second = pmcg.MixMvdens.from_arrays([1.0], mu2[None, :], cov=[np.eye(D) * 4.0], df=-1).cholesky()
+    post2 = pmcg.Posterior(D).add_mix(second)
+    count = back.importance_sample(post2)
+    assert count == back.N
+    om = oracle.Mix(np.array([1.0]), mu2[None, :], cov=np.eye(D)[None] * 4.0, df=-1)
+    ref = oracle.mix_logpdf(om, back.X)
+    np.testing.assert_allclose(back.weights, ref, rtol=1e-11, atol=1e-9)
+    # combined log-weights and their normalisation
+    comb = old_logw + back.weights
+    back.weights[:] = comb
+    back.host_modified()
+    pmcg.normalize_importance_weight(back)
+    m = comb.max()
+    np.testing.assert_allclose(back.s.logSum, m + np.log(np.sum(np.exp(comb - m))), rtol=1e-10)
+
+
+@pytest.mark.parametrize("D", [1, 6, 32, 64])
+def test_weighted_moments_match_numpy(pmcg, D):
+    rng = np.random.default_rng(D)
+    N = 70001
+    ps = pmcg.PmcSimu(N, D)
+    X = rng.normal(0, 3, (N, D)) + rng.normal(0, 10, D)[None, :]
+    logw = rng.normal(0, 2, N)
+    flg = (rng.uniform(size=N) > 0.05).astype(np.int16)
+    ps.X[:] = X
+    ps.weights[:] = logw
+    ps.flg[:] = flg
+    ps.s.isLog = 1
+    ps.host_modified()
+    mean, cov = ps.weighted_moments()
+    k = flg == 1
+    wb = np.exp(logw[k] - logw[k].max())
+    wb /= wb.sum()
+    m_ref = wb @ X[k]
+    d = X[k] - m_ref
+    c_ref = (wb[:, None] * d).T @ d
+    np.testing.assert_allclose(mean, m_ref, rtol=1e-9, atol=1e-9)
+    sig = np.sqrt(np.diag(c_ref))
+    assert np.max(np.abs(cov - c_ref) / np.outer(sig, sig)) < 1e-5
+    np.testing.assert_array_equal(cov, cov.T)
