@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the drop-in e2e leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-runs measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-likelihoods", action="store_true", help="skip the SN and template measurements")
     ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
                     help="single-precision log-densities on tcgen05 (1) or CUDA cores (0); default: library setting")
     return ap.parse_args()
@@ -160,6 +161,37 @@ def time_run(P, run, steps, warmup, l2buf, sync, prop):
     ms, n = run.stage_ms()
     run.set_timing(False)
     return stats, ms, n, launches, wall
+
+
+def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
+    """The other likelihoods at their configuration sizes: SN Ia (D=6, K=10, 740
+    supernovae, Fisher start; N = 10^4 as configured and N = 2^18) and the dense
+    template (D=12, K=16, M=2048, N = 2^18); mixed precision vs FP64, same seeds."""
+    out = {}
+    wl = W.sn_workload(K=10, init="fisher")
+    w, mu, cov, df = wl["prop"]
+    sn_prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    sn_post = P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"])
+    sn_box = P.Parabox(wl["bmin"], wl["bmax"])
+    tw = W.template_workload(D=12, M=2048, K=16)
+    w, mu, cov, df = tw["prop"]
+    tpl_prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    tpl_post = P.Posterior(12, tw["bmin"], tw["bmax"]).add_template(tw["A"], tw["C"], tw["dobs"])
+    tpl_box = P.Parabox(tw["bmin"], tw["bmax"])
+    cases = [("sn_N1e4", sn_prop, sn_post, sn_box, 10000), ("sn_N2e18", sn_prop, sn_post, sn_box, 1 << 18),
+             ("template_N2e18", tpl_prop, tpl_post, tpl_box, 1 << 18)]
+    for name, prop, post, box, N in cases:
+        rec = {"N": N}
+        for prec, tag in ((P.MIXED, "mixed"), (P.FP64, "fp64")):
+            run = P.Run(prop, post, N, precision=prec, seed=11, box=box)
+            st, ms, nt, _, _ = time_run(P, run, steps, warmup, l2buf, sync, prop)
+            step = sum(ms) / nt
+            rec[tag] = {"samples_per_s": N / (step / 1e3), "ms_per_step": step, "ln_evidence": st["ln_evidence"],
+                        "stage_ms": [v / nt for v in ms]}
+            run.free()
+        rec["speedup_mixed_vs_fp64"] = rec["mixed"]["samples_per_s"] / rec["fp64"]["samples_per_s"]
+        out[name] = rec
+    return out
 
 
 def ragged_specs(R, seed=256):
@@ -501,6 +533,11 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{reps} x {args.cpu_sample} samples of this workload "
                                           f"(oracle/pmc_oracle.c, OpenMP)"}
+    if not args.no_likelihoods:
+        import torch
+        l2 = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")
+        line["likelihoods"] = likelihood_bench(P, W, l2, torch.cuda.synchronize)
+        del l2
     if not args.no_batch:
         line["batch"] = batch_bench(P, W)
     if not args.no_serve:
