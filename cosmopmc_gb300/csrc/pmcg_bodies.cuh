@@ -348,6 +348,93 @@ __device__ __forceinline__ double sk_dev(double ok, double I, int &bad) {
   return sin(s * I) / s;
 }
 
+__device__ __forceinline__ float sk_f(float ok, float I, int &bad) {
+  if (fabsf(ok) < 1e-7f) return I * (1.f + ok * I * I * (1.f / 6.f));
+  if (ok > 0.f) { const float s = sqrtf(ok); return sinhf(s * I) / s; }
+  const float s = sqrtf(-ok);
+  if (s * I >= 3.14159265f) { bad = 1; return 0.f; }
+  return sinf(s * I) / s;
+}
+
+// Single-precision SN body (one warp per sample): the node sums, the distance,
+// the residual and its weight in FP32, with every residual taken relative to
+// the reference model (d = dref + alpha x1 - beta c - (M - M_ref)
+// - 5 log10(D_M / D_M,ref)), so no O(20 mag) quantities are differenced in
+// single precision; the cumulative distance integral and the sums over
+// supernovae (per-lane partials of at most ceil(nsn/32) terms) in FP64. The
+// marginalised mode uses residuals without M, shift-invariant in
+// A - B^2/C.
+__device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const float *__restrict__ X32, int ldx,
+                                            double *__restrict__ logpost, short *__restrict__ flg, size_t n,
+                                            int assign, double add) {
+  const int lane = threadIdx.x & 31;
+  if (n >= N) return;
+  if (!flg[n]) return;
+  auto par = [&](int ip, double def) -> double { return ip < 0 ? def : (double)X32[n * ldx + ip]; };
+  const double om = par(sn.ip_om, sn.def_om);
+  double ode, ok;
+  if (sn.ip_ode >= 0) { ode = par(sn.ip_ode, 0.0); ok = 1.0 - om - ode; }
+  else { ode = 1.0 - om; ok = 0.0; }
+  const float omf = (float)om, okf = (float)ok, odef = (float)ode;
+  const float exf = (float)(3.0 * (1.0 + par(sn.ip_w0, sn.def_w0)));
+  const float dMf = (float)(par(sn.ip_M, sn.def_M) - sn.mref);
+  const float al = (float)par(sn.ip_alpha, sn.def_alpha), be = (float)par(sn.ip_beta, sn.def_beta);
+  const float sig2 = (float)sn.sig_int2;
+  const int G = sn.G, nsn = sn.nsn;
+  int bad = 0;
+  double carry = 0.0;
+  float chi2 = 0.f, A = 0.f, B = 0.f, Cs = 0.f, sl = 0.f;
+  for (int base = 0; base < nsn; base += 32) {
+    const int i = base + lane;
+    double Ii = 0.0;
+    if (i < nsn) {
+      float acc = 0.f;
+      for (int g = 0; g < G; g++) {
+        const int q = i * G + g;
+        const float e2 = omf * sn.fna3[q] + okf * sn.fna2[q] + odef * expf(exf * sn.fnla[q]);
+        if (!(e2 > 0.f)) bad = 1;
+        else acc += sn.fnw[q] * rsqrtf(e2);
+      }
+      Ii = (double)acc;
+      const float e2z = omf * sn.fza3[i] + okf * sn.fza2[i] + odef * expf(exf * sn.fzla[i]);
+      if (!(e2z > 0.f)) bad = 1;
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, Ii, o);
+      if (lane >= o) Ii += t;
+    }
+    const double I = carry + Ii;
+    carry = __shfl_sync(0xffffffffu, I, 31);
+    if (i < nsn) {
+      const float dm = sk_f(okf, (float)I, bad);
+      if (!(dm > 0.f)) bad = 1;
+      const float dmu = 5.f * log10f(fmaxf(dm, 1e-30f) / sn.fdmref[i]);
+      const float *W = sn.fcov6 + (size_t)i * 6;
+      const float s2 = W[0] + al * al * W[1] + be * be * W[2] + 2.f * al * W[3] - 2.f * be * W[4] -
+                       2.f * al * be * W[5] + sig2 + sn.fspv2[i];
+      if (!(s2 > 0.f)) bad = 1;
+      const float d = sn.fdref[i] + al * sn.fx1[i] - be * sn.fc[i] - dmu;
+      const float is2 = 1.f / s2;
+      if (sn.chi2mode == 0) { const float dd = d - dMf; chi2 = fmaf(dd * dd, is2, chi2); }
+      else { A = fmaf(d * d, is2, A); B = fmaf(d, is2, B); Cs += is2; }
+      if (sn.add_logdet) sl += logf(s2);
+    }
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  double c2 = warp_sum((double)chi2);
+  const double Ad = warp_sum((double)A), Bd = warp_sum((double)B), Cd = warp_sum((double)Cs),
+               sld = warp_sum((double)sl);
+  if (lane == 0) {
+    if (bad) { flg[n] = 0; return; }
+    if (sn.chi2mode != 0) c2 = Ad - Bd * Bd / Cd + log(Cd / (2.0 * PMCG_PI));
+    const double ll = -0.5 * c2 - (sn.add_logdet ? 0.5 * sld : 0.0);
+    if (!isfinite(ll)) flg[n] = 0;
+    else if (assign) logpost[n] = add + ll;
+    else logpost[n] += ll;
+  }
+}
+
 // One warp per sample n; the cumulative distance integral over redshift-sorted
 // supernovae is a warp prefix scan of per-interval Gauss-Legendre sums.
 // assign != 0: logpost[n] = add + logL; otherwise logpost[n] += logL.
@@ -355,6 +442,10 @@ template <bool F32>
 __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const double *__restrict__ X64,
                                         const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
                                         short *__restrict__ flg, size_t n, int assign, double add) {
+  if (F32) {
+    body_sn_f32(sn, N, X32, ldx, logpost, flg, n, assign, add);
+    return;
+  }
   const int lane = threadIdx.x & 31;
   if (n >= N) return;
   if (!flg[n]) return;

@@ -120,6 +120,13 @@ struct SnDev {
   double *na2 = nullptr, *na3 = nullptr, *nla = nullptr, *nw = nullptr;
   double *za2 = nullptr, *za3 = nullptr, *zla = nullptr;  // at the SN redshifts
   float *fna2 = nullptr, *fna3 = nullptr, *fnla = nullptr, *fnw = nullptr;
+  // single-precision path: residuals relative to a reference model (flat
+  // LambdaCDM 0.3/0.7, M = -19.3, alpha = beta = 0) so every per-supernova
+  // quantity stays O(1): dref = m_B - mu_ref - M_ref, dmref = D_M of the
+  // reference (same quadrature), and float copies of the data
+  float *fdref = nullptr, *fdmref = nullptr, *fx1 = nullptr, *fc = nullptr, *fcov6 = nullptr, *fspv2 = nullptr;
+  float *fza2 = nullptr, *fza3 = nullptr, *fzla = nullptr;
+  double mref = -19.3;
   void *arena = nullptr;
 };
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
