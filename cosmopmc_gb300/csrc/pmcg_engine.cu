@@ -411,11 +411,39 @@ extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const 
   pl.type = kPluginTpl;
   TplDev &t = pl.tpl;
   t.M = M; t.P = P; t.Dpar = D;
+  // Gram form of the single-precision path: G = At^T At, b = At^T dt, c0 = dt.dt (FP64)
+  const bool gram = P <= kGramMaxP && D <= 16;
+  const int Pp = (P + 3) & ~3;
+  std::vector<float> G32, b32;
+  if (gram) {
+    std::vector<double> Gm((size_t)P * P, 0.0), bv(P, 0.0);
+    double c0 = 0.0;
+    for (int i = 0; i < M; i++) {
+      const double *a = &At[(size_t)i * P];
+      for (int p1 = 0; p1 < P; p1++) {
+        const double ap = a[p1];
+        bv[p1] += ap * dt[i];
+        for (int p2 = 0; p2 <= p1; p2++) Gm[(size_t)p1 * P + p2] += ap * a[p2];
+      }
+      c0 += dt[i] * dt[i];
+    }
+    G32.assign((size_t)Pp * Pp, 0.f);
+    b32.assign(Pp, 0.f);
+    for (int p1 = 0; p1 < P; p1++) {
+      b32[p1] = (float)bv[p1];
+      for (int p2 = 0; p2 <= p1; p2++) {
+        G32[(size_t)p1 * Pp + p2] = (float)Gm[(size_t)p1 * P + p2];
+        G32[(size_t)p2 * Pp + p1] = (float)Gm[(size_t)p1 * P + p2];
+      }
+    }
+    t.c0 = c0;
+  }
   Carver cv;
   for (int pass = 0; pass < 2; pass++) {
     cv.off = 0;
     t.At = cv.take<double>((size_t)M * P); t.dt = cv.take<double>(M);
     t.At32 = cv.take<float>((size_t)M * P); t.dt32 = cv.take<float>(M);
+    if (gram) { t.G32 = cv.take<float>((size_t)Pp * Pp); t.b32 = cv.take<float>(Pp); }
     if (pass == 0) {
       if (!CK(cudaMalloc(&t.arena, cv.off + 256), "template buffers")) return;
       cv.base = (char *)t.arena;
@@ -426,6 +454,9 @@ extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const 
             CK(cudaMemcpy(t.dt, dt.data(), 8 * dt.size(), cudaMemcpyHostToDevice), "template upload") &&
             CK(cudaMemcpy(t.At32, At32.data(), 4 * At32.size(), cudaMemcpyHostToDevice), "template upload") &&
             CK(cudaMemcpy(t.dt32, dt32.data(), 4 * dt32.size(), cudaMemcpyHostToDevice), "template upload");
+  if (ok && gram)
+    ok = CK(cudaMemcpy(t.G32, G32.data(), 4 * G32.size(), cudaMemcpyHostToDevice), "template upload") &&
+         CK(cudaMemcpy(t.b32, b32.data(), 4 * b32.size(), cudaMemcpyHostToDevice), "template upload");
   if (!ok) { cudaFree(t.arena); return; }
   p->plugins.push_back(pl);
 }

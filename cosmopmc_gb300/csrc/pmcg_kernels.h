@@ -137,8 +137,14 @@ struct TplDev {
   int M = 0, P = 0, Dpar = 0;
   double *At = nullptr, *dt = nullptr;   // [M x P], [M]
   float *At32 = nullptr, *dt32 = nullptr;
+  // Gram form of the single-precision path (P <= kGramMaxP): chi2 = c0 - 2 phi.b
+  // + phi^T G phi with G = At^T At ([Pp x Pp], Pp = P rounded up to 4), b = At^T dt,
+  // c0 = dt.dt (computed in FP64 at set-up)
+  float *G32 = nullptr, *b32 = nullptr;
+  double c0 = 0.0;
   void *arena = nullptr;
 };
+constexpr int kGramMaxP = 96;
 cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X64, const float *X32, int ldx,
                        double *logpost, const short *flg, cudaStream_t s);
 
