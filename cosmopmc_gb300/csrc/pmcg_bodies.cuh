@@ -435,90 +435,6 @@ __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const flo
   }
 }
 
-// Lane-blocked single-precision SN body (nsn <= 32 kSnMaxKb): lane l owns the
-// kb consecutive sorted supernovae l kb .. l kb + kb - 1, so the cumulative
-// distance integral is a per-lane running sum of at most kb FP32 interval sums
-// plus one FP64 exclusive scan of the 32 lane totals per sample (instead of one
-// FP64 scan step per 32 supernovae); the per-supernova work is as in
-// body_sn_f32. Padding positions carry weight 0.
-__device__ __forceinline__ void body_sn_f32_blocked(const SnDev &sn, size_t N, const float *__restrict__ X32,
-                                                    int ldx, double *__restrict__ logpost, short *__restrict__ flg,
-                                                    size_t n, int assign, double add) {
-  const int lane = threadIdx.x & 31;
-  if (n >= N) return;
-  if (!flg[n]) return;
-  auto par = [&](int ip, double def) -> double { return ip < 0 ? def : (double)X32[n * ldx + ip]; };
-  const double om = par(sn.ip_om, sn.def_om);
-  double ode, ok;
-  if (sn.ip_ode >= 0) { ode = par(sn.ip_ode, 0.0); ok = 1.0 - om - ode; }
-  else { ode = 1.0 - om; ok = 0.0; }
-  const float omf = (float)om, okf = (float)ok, odef = (float)ode;
-  const float exf = (float)(3.0 * (1.0 + par(sn.ip_w0, sn.def_w0)));
-  const float dMf = (float)(par(sn.ip_M, sn.def_M) - sn.mref);
-  const float al = (float)par(sn.ip_alpha, sn.def_alpha), be = (float)par(sn.ip_beta, sn.def_beta);
-  const float sig2 = (float)sn.sig_int2;
-  const int G = sn.G, kb = sn.kb, np = 32 * kb;
-  int bad = 0;
-  float cum[kSnMaxKb];
-  float local = 0.f;
-#pragma unroll
-  for (int k = 0; k < kSnMaxKb; k++) {
-    if (k < kb) {
-      const int pos = k * 32 + lane;
-      float acc = 0.f;
-      for (int g = 0; g < G; g++) {
-        const int q = g * np + pos;
-        const float e2 = omf * sn.bna3[q] + okf * sn.bna2[q] + odef * expf(exf * sn.bnla[q]);
-        if (!(e2 > 0.f)) bad = 1;
-        else acc += sn.bnw[q] * rsqrtf(e2);
-      }
-      const float e2z = omf * sn.bza3[pos] + okf * sn.bza2[pos] + odef * expf(exf * sn.bzla[pos]);
-      if (!(e2z > 0.f)) bad = 1;
-      local += acc;
-      cum[k] = local;
-    }
-  }
-  double incl = (double)local;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const float off = (float)(incl - (double)local);
-  float chi2 = 0.f, A = 0.f, B = 0.f, Cs = 0.f, sl = 0.f;
-#pragma unroll
-  for (int k = 0; k < kSnMaxKb; k++) {
-    if (k < kb) {
-      const int pos = k * 32 + lane;
-      const float v = sn.bvalid[pos];
-      const float dm = sk_f(okf, off + cum[k], bad);
-      if (!(dm > 0.f)) bad = 1;
-      const float dmu = 5.f * log10f(fmaxf(dm, 1e-30f) / sn.bdmref[pos]);
-      const float s2 = sn.bcov6[pos] + al * al * sn.bcov6[np + pos] + be * be * sn.bcov6[2 * np + pos] +
-                       2.f * al * sn.bcov6[3 * np + pos] - 2.f * be * sn.bcov6[4 * np + pos] -
-                       2.f * al * be * sn.bcov6[5 * np + pos] + sig2 + sn.bspv2[pos];
-      if (!(s2 > 0.f)) bad = 1;
-      const float d = sn.bdref[pos] + al * sn.bx1[pos] - be * sn.bc[pos] - dmu;
-      const float is2 = v / s2;
-      if (sn.chi2mode == 0) { const float dd = d - dMf; chi2 = fmaf(dd * dd, is2, chi2); }
-      else { A = fmaf(d * d, is2, A); B = fmaf(d, is2, B); Cs += is2; }
-      if (sn.add_logdet) sl = fmaf(v, logf(s2), sl);
-    }
-  }
-  bad = __any_sync(0xffffffffu, bad);
-  double c2 = warp_sum((double)chi2);
-  const double Ad = warp_sum((double)A), Bd = warp_sum((double)B), Cd = warp_sum((double)Cs),
-               sld = warp_sum((double)sl);
-  if (lane == 0) {
-    if (bad) { flg[n] = 0; return; }
-    if (sn.chi2mode != 0) c2 = Ad - Bd * Bd / Cd + log(Cd / (2.0 * PMCG_PI));
-    const double ll = -0.5 * c2 - (sn.add_logdet ? 0.5 * sld : 0.0);
-    if (!isfinite(ll)) flg[n] = 0;
-    else if (assign) logpost[n] = add + ll;
-    else logpost[n] += ll;
-  }
-}
-
 // One warp per sample n; the cumulative distance integral over redshift-sorted
 // supernovae is a warp prefix scan of per-interval Gauss-Legendre sums.
 // assign != 0: logpost[n] = add + logL; otherwise logpost[n] += logL.
@@ -527,8 +443,7 @@ __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const 
                                         const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
                                         short *__restrict__ flg, size_t n, int assign, double add) {
   if (F32) {
-    if (sn.kb > 0) body_sn_f32_blocked(sn, N, X32, ldx, logpost, flg, n, assign, add);
-    else body_sn_f32(sn, N, X32, ldx, logpost, flg, n, assign, add);
+    body_sn_f32(sn, N, X32, ldx, logpost, flg, n, assign, add);
     return;
   }
   const int lane = threadIdx.x & 31;

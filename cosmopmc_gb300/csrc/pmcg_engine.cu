@@ -327,8 +327,6 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
   s.def_beta = sd->def_beta;
   s.dh = ckms / (100.0 * sd->h);
   s.sig_int2 = sd->sig_int * sd->sig_int;
-  const int kb = (n + 31) / 32 <= kSnMaxKb ? (n + 31) / 32 : 0;
-  s.kb = kb;
   Carver cv;
   for (int pass = 0; pass < 2; pass++) {
     cv.off = 0;
@@ -342,15 +340,6 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
     s.fdref = cv.take<float>(n); s.fdmref = cv.take<float>(n); s.fx1 = cv.take<float>(n); s.fc = cv.take<float>(n);
     s.fcov6 = cv.take<float>(6 * (size_t)n); s.fspv2 = cv.take<float>(n);
     s.fza2 = cv.take<float>(n); s.fza3 = cv.take<float>(n); s.fzla = cv.take<float>(n);
-    if (kb > 0) {
-      const size_t np = 32 * (size_t)kb;
-      s.bna2 = cv.take<float>(np * G); s.bna3 = cv.take<float>(np * G); s.bnla = cv.take<float>(np * G);
-      s.bnw = cv.take<float>(np * G);
-      s.bdref = cv.take<float>(np); s.bdmref = cv.take<float>(np); s.bx1 = cv.take<float>(np); s.bc = cv.take<float>(np);
-      s.bcov6 = cv.take<float>(6 * np); s.bspv2 = cv.take<float>(np);
-      s.bza2 = cv.take<float>(np); s.bza3 = cv.take<float>(np); s.bzla = cv.take<float>(np);
-      s.bvalid = cv.take<float>(np);
-    }
     if (pass == 0) {
       if (!CK(cudaMalloc(&s.arena, cv.off + 256), "SN buffers")) return;
       cv.base = (char *)s.arena;
@@ -390,32 +379,6 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
             up(s.fcov6, fcv.data(), 24 * (size_t)n) && up(s.fspv2, fsp.data(), 4 * (size_t)n) &&
             up(s.fza2, fz2.data(), 4 * (size_t)n) && up(s.fza3, fz3.data(), 4 * (size_t)n) &&
             up(s.fzla, fzl.data(), 4 * (size_t)n);
-  if (ok && kb > 0) {
-    // lane-blocked layout: position k * 32 + l <-> sorted index l * kb + k
-    const size_t np = 32 * (size_t)kb;
-    std::vector<float> b2(np * G, 1.f), b3(np * G, 1.f), bl(np * G, 0.f), bw(np * G, 0.f);
-    std::vector<float> bdr(np, 0.f), bdm(np, 1.f), bx(np, 0.f), bcc(np, 0.f), bcv(6 * np, 0.f), bsp(np, 0.f);
-    std::vector<float> bz2(np, 1.f), bz3(np, 1.f), bzl(np, 0.f), bva(np, 0.f);
-    for (int l = 0; l < 32; l++)
-      for (int k = 0; k < kb; k++) {
-        const size_t pos = (size_t)k * 32 + l;
-        const int i = l * kb + k;
-        if (i >= n) { bcv[pos] = 1.f; continue; }
-        for (int g = 0; g < G; g++) {
-          const size_t q = (size_t)i * G + g, d = (size_t)g * np + pos;
-          b2[d] = f2[q]; b3[d] = f3[q]; bl[d] = fl[q]; bw[d] = fw[q];
-        }
-        bdr[pos] = fdr[i]; bdm[pos] = fdm[i]; bx[pos] = fx[i]; bcc[pos] = fcc[i]; bsp[pos] = fsp[i];
-        for (int c6 = 0; c6 < 6; c6++) bcv[(size_t)c6 * np + pos] = fcv[6 * (size_t)i + c6];
-        bz2[pos] = fz2[i]; bz3[pos] = fz3[i]; bzl[pos] = fzl[i]; bva[pos] = 1.f;
-      }
-    ok = up(s.bna2, b2.data(), 4 * b2.size()) && up(s.bna3, b3.data(), 4 * b3.size()) &&
-         up(s.bnla, bl.data(), 4 * bl.size()) && up(s.bnw, bw.data(), 4 * bw.size()) &&
-         up(s.bdref, bdr.data(), 4 * np) && up(s.bdmref, bdm.data(), 4 * np) && up(s.bx1, bx.data(), 4 * np) &&
-         up(s.bc, bcc.data(), 4 * np) && up(s.bcov6, bcv.data(), 4 * bcv.size()) && up(s.bspv2, bsp.data(), 4 * np) &&
-         up(s.bza2, bz2.data(), 4 * np) && up(s.bza3, bz3.data(), 4 * np) && up(s.bzla, bzl.data(), 4 * np) &&
-         up(s.bvalid, bva.data(), 4 * np);
-  }
   if (!ok) { cudaFree(s.arena); return; }
   p->plugins.push_back(pl);
 }

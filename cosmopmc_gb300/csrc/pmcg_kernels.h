@@ -127,16 +127,8 @@ struct SnDev {
   float *fdref = nullptr, *fdmref = nullptr, *fx1 = nullptr, *fc = nullptr, *fcov6 = nullptr, *fspv2 = nullptr;
   float *fza2 = nullptr, *fza3 = nullptr, *fzla = nullptr;
   double mref = -19.3;
-  // lane-blocked copies (nsn <= 32 kSnMaxKb): lane l of a warp owns the kb
-  // consecutive sorted supernovae l kb .. l kb + kb - 1, stored at k * 32 + l
-  // (node arrays [G][32 kb]); padding positions have bvalid = 0
-  int kb = 0;
-  float *bna2 = nullptr, *bna3 = nullptr, *bnla = nullptr, *bnw = nullptr;
-  float *bdref = nullptr, *bdmref = nullptr, *bx1 = nullptr, *bc = nullptr, *bcov6 = nullptr, *bspv2 = nullptr;
-  float *bza2 = nullptr, *bza3 = nullptr, *bzla = nullptr, *bvalid = nullptr;
   void *arena = nullptr;
 };
-constexpr int kSnMaxKb = 48;  // lane-blocked layout up to 1536 supernovae
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
                       int ldx, double *logpost, short *flg, cudaStream_t s);
 
