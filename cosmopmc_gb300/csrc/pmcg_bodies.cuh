@@ -356,13 +356,89 @@ __device__ __forceinline__ float sk_f(float ok, float I, int &bad) {
   return sinf(s * I) / s;
 }
 
+// Error-free sum of two floats (Knuth's TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) += v for a float-float pair (about 44 significant bits).
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float vhi, float vlo) {
+  float s, e;
+  two_sum_f(hi, vhi, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, vlo));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+// Warp tree sum of one float per lane, carried as float-float; lane 0 holds the
+// result.
+__device__ __forceinline__ void warp_sum_ff(float v, float &hi, float &lo) {
+  hi = v; lo = 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    ff_add(hi, lo, h2, l2);
+  }
+}
+
+// PTX approximate transcendental and reciprocal instructions (MUFU): ex2,
+// lg2 and rcp with relative error of order 2^-22, used where a few 1e-7 of
+// relative error per supernova is far below the single-precision tolerance.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Transverse comoving distance S_k(I) = sinh(sqrt(Ok) I)/sqrt(Ok) (Ok > 0),
+// I (Ok = 0), sin(sqrt(-Ok) I)/sqrt(-Ok) (Ok < 0). All three are the one power
+// series I * sum_j u^j / (2j+1)! in u = Ok I^2; for |u| <= 4 eight terms leave
+// a truncation below 2e-10 relative (4^8/17!), evaluated by Horner's rule
+// without branches. Larger |u| takes the closed forms; the sine branch
+// reaches its first zero (a closed universe's antipode) at u = -pi^2.
+__device__ __forceinline__ float sk_series_f(float ok, float I, int &bad) {
+  const float u = ok * I * I;
+  if (fabsf(u) <= 4.f) {
+    float p = 1.f / 1307674368000.f;              // 1/15!
+    p = fmaf(p, u, 1.f / 6227020800.f);           // 1/13!
+    p = fmaf(p, u, 1.f / 39916800.f);             // 1/11!
+    p = fmaf(p, u, 1.f / 362880.f);               // 1/9!
+    p = fmaf(p, u, 1.f / 5040.f);                 // 1/7!
+    p = fmaf(p, u, 1.f / 120.f);                  // 1/5!
+    p = fmaf(p, u, 1.f / 6.f);                    // 1/3!
+    p = fmaf(p, u, 1.f);
+    return I * p;
+  }
+  return sk_f(ok, I, bad);
+}
+
 // Single-precision SN body (one warp per sample): the node sums, the distance,
 // the residual and its weight in FP32, with every residual taken relative to
 // the reference model (d = dref + alpha x1 - beta c - (M - M_ref)
 // - 5 log10(D_M / D_M,ref)), so no O(20 mag) quantities are differenced in
-// single precision; the cumulative distance integral and the sums over
-// supernovae (per-lane partials of at most ceil(nsn/32) terms) in FP64. The
-// marginalised mode uses residuals without M, shift-invariant in
+// single precision. The cumulative distance integral is a warp scan in FP32
+// inside each block of 32 supernovae plus a float-float carry across blocks
+// (its rounding does not accumulate over the survey), and the sums over
+// supernovae are per-lane FP32 partials reduced across the warp in
+// float-float; only the final combination runs in FP64 (GB300 issues FP64 at
+// a small fraction of the FP32 rate). Node and supernova data are float4
+// planes indexed by supernova, so each warp load is 512 contiguous bytes.
+// The marginalised mode uses residuals without M, shift-invariant in
 // A - B^2/C.
 __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const float *__restrict__ X32, int ldx,
                                             double *__restrict__ logpost, short *__restrict__ flg, size_t n,
@@ -370,65 +446,73 @@ __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const flo
   const int lane = threadIdx.x & 31;
   if (n >= N) return;
   if (!flg[n]) return;
-  auto par = [&](int ip, double def) -> double { return ip < 0 ? def : (double)X32[n * ldx + ip]; };
-  const double om = par(sn.ip_om, sn.def_om);
-  double ode, ok;
-  if (sn.ip_ode >= 0) { ode = par(sn.ip_ode, 0.0); ok = 1.0 - om - ode; }
-  else { ode = 1.0 - om; ok = 0.0; }
-  const float omf = (float)om, okf = (float)ok, odef = (float)ode;
-  const float exf = (float)(3.0 * (1.0 + par(sn.ip_w0, sn.def_w0)));
-  const float dMf = (float)(par(sn.ip_M, sn.def_M) - sn.mref);
-  const float al = (float)par(sn.ip_alpha, sn.def_alpha), be = (float)par(sn.ip_beta, sn.def_beta);
-  const float sig2 = (float)sn.sig_int2;
+  auto par = [&](int ip, float def) -> float { return ip < 0 ? def : X32[n * ldx + ip]; };
+  const float omf = par(sn.ip_om, sn.fdef_om);
+  float odef, okf;
+  if (sn.ip_ode >= 0) { odef = par(sn.ip_ode, 0.f); okf = (1.f - omf) - odef; }
+  else { odef = 1.f - omf; okf = 0.f; }
+  const float exf = 3.f * (1.f + par(sn.ip_w0, sn.fdef_w0));
+  const float dMf = par(sn.ip_M, sn.fdef_M) - sn.mref;
+  const float al = par(sn.ip_alpha, sn.fdef_alpha), be = par(sn.ip_beta, sn.fdef_beta);
+  const float a2 = al * al, b2 = be * be, ab = al * be;
   const int G = sn.G, nsn = sn.nsn;
+  const float4 *__restrict__ node = sn.fnode;
+  const float4 *__restrict__ p0 = sn.fsn, *__restrict__ p1 = sn.fsn + nsn, *__restrict__ p2 = sn.fsn + 2 * nsn;
+  const float k5 = 1.50514997831990598f;  // 5 log10(2): 5 log10(x) = k5 log2(x)
   int bad = 0;
-  double carry = 0.0;
+  float chi = 0.f, clo = 0.f;  // carry of the distance integral (float-float)
   float chi2 = 0.f, A = 0.f, B = 0.f, Cs = 0.f, sl = 0.f;
   for (int base = 0; base < nsn; base += 32) {
     const int i = base + lane;
-    double Ii = 0.0;
+    float p = 0.f;
+    float4 q0, q1, q2;
     if (i < nsn) {
-      float acc = 0.f;
       for (int g = 0; g < G; g++) {
-        const int q = i * G + g;
-        const float e2 = omf * sn.fna3[q] + okf * sn.fna2[q] + odef * expf(exf * sn.fnla[q]);
-        if (!(e2 > 0.f)) bad = 1;
-        else acc += sn.fnw[q] * rsqrtf(e2);
+        const float4 nd = node[(size_t)g * nsn + i];
+        const float e2 = fmaf(omf, nd.x, fmaf(okf, nd.y, odef * ex2_approx(exf * nd.z)));
+        bad |= !(e2 > 0.f);
+        p = fmaf(nd.w, rsqrt_approx(e2), p);
       }
-      Ii = (double)acc;
-      const float e2z = omf * sn.fza3[i] + okf * sn.fza2[i] + odef * expf(exf * sn.fzla[i]);
-      if (!(e2z > 0.f)) bad = 1;
+      q0 = p0[i]; q1 = p1[i]; q2 = p2[i];
+      const float e2z = fmaf(omf, q2.z, fmaf(okf, q2.w, odef * ex2_approx(exf * sn.fzl2[i])));
+      bad |= !(e2z > 0.f);
     }
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, Ii, o);
-      if (lane >= o) Ii += t;
+      const float t = __shfl_up_sync(0xffffffffu, p, o);
+      if (lane >= o) p += t;
     }
-    const double I = carry + Ii;
-    carry = __shfl_sync(0xffffffffu, I, 31);
+    float Is, Ie;
+    two_sum_f(chi, p, Is, Ie);
+    const float I = Is + (Ie + clo);
+    ff_add(chi, clo, __shfl_sync(0xffffffffu, p, 31), 0.f);
     if (i < nsn) {
-      const float dm = sk_f(okf, (float)I, bad);
-      if (!(dm > 0.f)) bad = 1;
-      const float dmu = 5.f * log10f(fmaxf(dm, 1e-30f) / sn.fdmref[i]);
-      const float *W = sn.fcov6 + (size_t)i * 6;
-      const float s2 = W[0] + al * al * W[1] + be * be * W[2] + 2.f * al * W[3] - 2.f * be * W[4] -
-                       2.f * al * be * W[5] + sig2 + sn.fspv2[i];
-      if (!(s2 > 0.f)) bad = 1;
-      const float d = sn.fdref[i] + al * sn.fx1[i] - be * sn.fc[i] - dmu;
-      const float is2 = 1.f / s2;
+      const float dm = sk_series_f(okf, I, bad);
+      bad |= !(dm > 0.f);
+      const float dmu = k5 * lg2_approx(fmaxf(dm, 1e-30f) * q0.w);
+      const float s2 = fmaf(ab, q2.y, fmaf(be, q2.x, fmaf(al, q1.w, fmaf(b2, q1.z, fmaf(a2, q1.y, q1.x)))));
+      bad |= !(s2 > 0.f);
+      const float d = fmaf(al, q0.y, fmaf(-be, q0.z, q0.x)) - dmu;
+      const float is2 = rcp_approx(s2);
       if (sn.chi2mode == 0) { const float dd = d - dMf; chi2 = fmaf(dd * dd, is2, chi2); }
       else { A = fmaf(d * d, is2, A); B = fmaf(d, is2, B); Cs += is2; }
-      if (sn.add_logdet) sl += logf(s2);
+      if (sn.add_logdet) sl += lg2_approx(s2);
     }
   }
   bad = __any_sync(0xffffffffu, bad);
-  double c2 = warp_sum((double)chi2);
-  const double Ad = warp_sum((double)A), Bd = warp_sum((double)B), Cd = warp_sum((double)Cs),
-               sld = warp_sum((double)sl);
+  float h0, l0, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
+  if (sn.chi2mode == 0) warp_sum_ff(chi2, h0, l0);
+  else { warp_sum_ff(A, h0, l0); warp_sum_ff(B, h1, l1); warp_sum_ff(Cs, h2, l2); }
+  if (sn.add_logdet) warp_sum_ff(sl, h3, l3);
   if (lane == 0) {
     if (bad) { flg[n] = 0; return; }
-    if (sn.chi2mode != 0) c2 = Ad - Bd * Bd / Cd + log(Cd / (2.0 * PMCG_PI));
-    const double ll = -0.5 * c2 - (sn.add_logdet ? 0.5 * sld : 0.0);
+    double c2 = (double)h0 + (double)l0;
+    if (sn.chi2mode != 0) {
+      const double Bd = (double)h1 + (double)l1, Cd = (double)h2 + (double)l2;
+      c2 = c2 - Bd * Bd / Cd + log(Cd / (2.0 * PMCG_PI));
+    }
+    // sum of log2 s^2 over supernovae, times ln 2
+    const double ll = -0.5 * c2 - (sn.add_logdet ? 0.5 * 0.69314718055994531 * ((double)h3 + (double)l3) : 0.0);
     if (!isfinite(ll)) flg[n] = 0;
     else if (assign) logpost[n] = add + ll;
     else logpost[n] += ll;
@@ -462,7 +546,6 @@ __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const 
   const double al = par(sn.ip_alpha, sn.def_alpha);
   const double be = par(sn.ip_beta, sn.def_beta);
   const double ex = 3.0 * (1.0 + w0);
-  const float omf = (float)om, okf = (float)ok, odef = (float)ode, exf = (float)ex;
   const int G = sn.G, nsn = sn.nsn;
   int bad = 0;
   double carry = 0.0, chi2 = 0.0, A = 0.0, B = 0.0, C = 0.0, sl = 0.0;
@@ -470,22 +553,11 @@ __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const 
     const int i = base + lane;
     double Ii = 0.0;
     if (i < nsn) {
-      if (F32) {
-        float acc = 0.f;
-        for (int g = 0; g < G; g++) {
-          const int q = i * G + g;
-          float e2 = omf * sn.fna3[q] + okf * sn.fna2[q] + odef * expf(exf * sn.fnla[q]);
-          if (!(e2 > 0.f)) bad = 1;
-          else acc += sn.fnw[q] * rsqrtf(e2);
-        }
-        Ii = (double)acc;
-      } else {
-        for (int g = 0; g < G; g++) {
-          const int q = i * G + g;
-          double e2 = om * sn.na3[q] + ok * sn.na2[q] + ode * exp(ex * sn.nla[q]);
-          if (!(e2 > 0.0)) bad = 1;
-          else Ii += sn.nw[q] / sqrt(e2);
-        }
+      for (int g = 0; g < G; g++) {
+        const int q = i * G + g;
+        double e2 = om * sn.na3[q] + ok * sn.na2[q] + ode * exp(ex * sn.nla[q]);
+        if (!(e2 > 0.0)) bad = 1;
+        else Ii += sn.nw[q] / sqrt(e2);
       }
       double e2z = om * sn.za3[i] + ok * sn.za2[i] + ode * exp(ex * sn.zla[i]);
       if (!(e2z > 0.0)) bad = 1;

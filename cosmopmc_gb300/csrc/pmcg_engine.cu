@@ -327,6 +327,8 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
   s.def_beta = sd->def_beta;
   s.dh = ckms / (100.0 * sd->h);
   s.sig_int2 = sd->sig_int * sd->sig_int;
+  s.fdef_om = (float)s.def_om; s.fdef_w0 = (float)s.def_w0; s.fdef_M = (float)s.def_M;
+  s.fdef_alpha = (float)s.def_alpha; s.fdef_beta = (float)s.def_beta;
   Carver cv;
   for (int pass = 0; pass < 2; pass++) {
     cv.off = 0;
@@ -335,11 +337,7 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
     s.za2 = cv.take<double>(n); s.za3 = cv.take<double>(n); s.zla = cv.take<double>(n);
     s.na2 = cv.take<double>((size_t)n * G); s.na3 = cv.take<double>((size_t)n * G);
     s.nla = cv.take<double>((size_t)n * G); s.nw = cv.take<double>((size_t)n * G);
-    s.fna2 = cv.take<float>((size_t)n * G); s.fna3 = cv.take<float>((size_t)n * G);
-    s.fnla = cv.take<float>((size_t)n * G); s.fnw = cv.take<float>((size_t)n * G);
-    s.fdref = cv.take<float>(n); s.fdmref = cv.take<float>(n); s.fx1 = cv.take<float>(n); s.fc = cv.take<float>(n);
-    s.fcov6 = cv.take<float>(6 * (size_t)n); s.fspv2 = cv.take<float>(n);
-    s.fza2 = cv.take<float>(n); s.fza3 = cv.take<float>(n); s.fzla = cv.take<float>(n);
+    s.fnode = cv.take<float4>((size_t)n * G); s.fsn = cv.take<float4>(3 * (size_t)n); s.fzl2 = cv.take<float>(n);
     if (pass == 0) {
       if (!CK(cudaMalloc(&s.arena, cv.off + 256), "SN buffers")) return;
       cv.base = (char *)s.arena;
@@ -348,37 +346,34 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
   auto up = [&](void *dst, const void *src, size_t bytes) {
     return CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "SN upload");
   };
-  auto tof = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
-  std::vector<float> f2 = tof(na2), f3 = tof(na3), fl = tof(nla), fw = tof(nw);
   // reference model of the single-precision path (flat LambdaCDM 0.3/0.7, the
   // same nodes): D_M,ref and the reference residual m_B - mu_ref - M_ref
-  std::vector<double> dref(n), dmref(n);
+  const double il2 = 1.0 / std::log(2.0);
+  std::vector<float4> fnode((size_t)n * G), fsn(3 * (size_t)n);
+  std::vector<float> fzl2(n);
   {
     double I = 0.0;
     for (int t = 0; t < n; t++) {
       for (int g = 0; g < G; g++) {
         const size_t q = (size_t)t * G + g;
         I += nw[q] / std::sqrt(0.3 * na3[q] + 0.7);
+        fnode[(size_t)g * n + t] = make_float4((float)na3[q], (float)na2[q], (float)(nla[q] * il2), (float)nw[q]);
       }
-      dmref[t] = I;
       const double mu_ref = 5.0 * std::log10((1.0 + z[t]) * s.dh * I) + 25.0;
-      dref[t] = mB[t] - mu_ref - s.mref;
+      const double *W = &cov6[6 * (size_t)t];
+      fsn[t] = make_float4((float)(mB[t] - mu_ref - (double)s.mref), (float)x1[t], (float)c[t], (float)(1.0 / I));
+      fsn[n + t] = make_float4((float)(W[0] + s.sig_int2 + spv2[t]), (float)W[1], (float)W[2], (float)(2.0 * W[3]));
+      fsn[2 * (size_t)n + t] = make_float4((float)(-2.0 * W[4]), (float)(-2.0 * W[5]), (float)za3[t], (float)za2[t]);
+      fzl2[t] = (float)(zla[t] * il2);
     }
   }
-  std::vector<float> fdr = tof(dref), fdm = tof(dmref), fx = tof(x1), fcc = tof(c), fcv = tof(cov6), fsp = tof(spv2),
-                     fz2 = tof(za2), fz3 = tof(za3), fzl = tof(zla);
   bool ok = up(s.z, z.data(), 8 * n) && up(s.spv2, spv2.data(), 8 * n) && up(s.mB, mB.data(), 8 * n) &&
             up(s.x1, x1.data(), 8 * n) && up(s.c, c.data(), 8 * n) && up(s.cov6, cov6.data(), 48 * (size_t)n) &&
             up(s.za2, za2.data(), 8 * n) && up(s.za3, za3.data(), 8 * n) && up(s.zla, zla.data(), 8 * n) &&
             up(s.na2, na2.data(), 8 * na2.size()) && up(s.na3, na3.data(), 8 * na3.size()) &&
             up(s.nla, nla.data(), 8 * nla.size()) && up(s.nw, nw.data(), 8 * nw.size()) &&
-            up(s.fna2, f2.data(), 4 * f2.size()) && up(s.fna3, f3.data(), 4 * f3.size()) &&
-            up(s.fnla, fl.data(), 4 * fl.size()) && up(s.fnw, fw.data(), 4 * fw.size()) &&
-            up(s.fdref, fdr.data(), 4 * (size_t)n) && up(s.fdmref, fdm.data(), 4 * (size_t)n) &&
-            up(s.fx1, fx.data(), 4 * (size_t)n) && up(s.fc, fcc.data(), 4 * (size_t)n) &&
-            up(s.fcov6, fcv.data(), 24 * (size_t)n) && up(s.fspv2, fsp.data(), 4 * (size_t)n) &&
-            up(s.fza2, fz2.data(), 4 * (size_t)n) && up(s.fza3, fz3.data(), 4 * (size_t)n) &&
-            up(s.fzla, fzl.data(), 4 * (size_t)n);
+            up(s.fnode, fnode.data(), sizeof(float4) * fnode.size()) &&
+            up(s.fsn, fsn.data(), sizeof(float4) * fsn.size()) && up(s.fzl2, fzl2.data(), 4 * (size_t)n);
   if (!ok) { cudaFree(s.arena); return; }
   p->plugins.push_back(pl);
 }

@@ -119,14 +119,21 @@ struct SnDev {
   double *z = nullptr, *spv2 = nullptr, *mB = nullptr, *x1 = nullptr, *c = nullptr, *cov6 = nullptr;
   double *na2 = nullptr, *na3 = nullptr, *nla = nullptr, *nw = nullptr;
   double *za2 = nullptr, *za3 = nullptr, *zla = nullptr;  // at the SN redshifts
-  float *fna2 = nullptr, *fna3 = nullptr, *fnla = nullptr, *fnw = nullptr;
   // single-precision path: residuals relative to a reference model (flat
-  // LambdaCDM 0.3/0.7, M = -19.3, alpha = beta = 0) so every per-supernova
-  // quantity stays O(1): dref = m_B - mu_ref - M_ref, dmref = D_M of the
-  // reference (same quadrature), and float copies of the data
-  float *fdref = nullptr, *fdmref = nullptr, *fx1 = nullptr, *fc = nullptr, *fcov6 = nullptr, *fspv2 = nullptr;
-  float *fza2 = nullptr, *fza3 = nullptr, *fzla = nullptr;
-  double mref = -19.3;
+  // LambdaCDM 0.3/0.7, M = M_ref, alpha = beta = 0) so every per-supernova
+  // quantity stays O(1). Nodes as float4 (a^3, a^2, log2 a, weight x
+  // half-interval), node-major [G x nsn] so a warp reads 32 consecutive
+  // supernovae; per supernova three float4 planes [3 x nsn]:
+  //   0: dref = m_B - mu_ref - M_ref, x1, c, 1 / D_M,ref (same quadrature)
+  //   1: cov_mm + sig_int^2 + sig_pv^2, cov_x1x1, cov_cc, 2 cov_mx1
+  //   2: -2 cov_mc, -2 cov_x1c, (1+z)^3, (1+z)^2
+  // and log2(1+z) [nsn]
+  float4 *fnode = nullptr, *fsn = nullptr;
+  float *fzl2 = nullptr;
+  // reference magnitude (a float value, so the set-up in FP64 and the body in
+  // FP32 subtract the same number) and float copies of the scalars
+  float mref = -19.3f;
+  float fdef_om = 0.3f, fdef_w0 = -1.0f, fdef_M = -19.3f, fdef_alpha = 0.0f, fdef_beta = 0.0f;
   void *arena = nullptr;
 };
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
