@@ -79,15 +79,17 @@ __device__ __forceinline__ int pick_component(const double *s_cw, const double *
   return 0;
 }
 
-__global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t N, uint32_t key0, uint32_t key1,
-                                                        uint32_t call, int *__restrict__ idx,
-                                                        int *__restrict__ counts) {
+// Samples [n0, n1): component index, per-component counts (and, when ccounts
+// is given, the counts of this range alone).
+__global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t n0, size_t n1, uint32_t key0,
+                                                        uint32_t key1, uint32_t call, int *__restrict__ idx,
+                                                        int *__restrict__ counts, int *__restrict__ ccounts) {
   extern __shared__ double s_cw[];
   int *s_cnt = reinterpret_cast<int *>(s_cw + m.K);
   for (int k = threadIdx.x; k < m.K; k += blockDim.x) { s_cw[k] = m.cw[k]; s_cnt[k] = 0; }
   __syncthreads();
-  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n < N) {
+  const size_t n = n0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < n1) {
     P4 c = {0u, (uint32_t)n, (uint32_t)(n >> 32), call};
     P4 o = philox4x32_10(c, key0, key1);
     const int k = pick_component(s_cw, m.w, m.K, u53(o.x, o.y));
@@ -96,12 +98,16 @@ __global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t N, 
   }
   __syncthreads();
   for (int k = threadIdx.x; k < m.K; k += blockDim.x)
-    if (s_cnt[k]) atomicAdd(&counts[k], s_cnt[k]);
+    if (s_cnt[k]) {
+      atomicAdd(&counts[k], s_cnt[k]);
+      if (ccounts) atomicAdd(&ccounts[k], s_cnt[k]);
+    }
 }
 
-// perm[off_k + r] = n, off_k = sum of the counts below k; r from a block-local
-// rank plus one reservation per (block, component).
-__global__ void __launch_bounds__(256) draw_bucket_kernel(size_t N, int K, const int *__restrict__ idx,
+// Samples [n0, n1) bucketed by component: perm[off_k + r] = n with off_k the
+// sum of the range's counts below k and r a block-local rank plus one
+// reservation per (block, component); perm is indexed from the range start.
+__global__ void __launch_bounds__(256) draw_bucket_kernel(size_t n0, size_t n1, int K, const int *__restrict__ idx,
                                                           const int *__restrict__ counts, int *__restrict__ cursor,
                                                           int *__restrict__ perm) {
   extern __shared__ int s_i[];
@@ -112,9 +118,9 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t N, int K, const
   }
   for (int k = threadIdx.x; k < K; k += blockDim.x) s_hist[k] = 0;
   __syncthreads();
-  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = n0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   int k = 0, r = 0;
-  if (n < N) {
+  if (n < n1) {
     k = idx[n];
     r = atomicAdd(&s_hist[k], 1);
   }
@@ -122,17 +128,18 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t N, int K, const
   for (int j = threadIdx.x; j < K; j += blockDim.x)
     if (s_hist[j]) s_base[j] = s_off[j] + atomicAdd(&cursor[j], s_hist[j]);
   __syncthreads();
-  if (n < N) perm[s_base[k] + r] = (int)n;
+  if (n < n1) perm[s_base[k] + r] = (int)n;
 }
 
+// The cnt samples listed in perm (absolute sample indices), in list order.
 template <int MAXD>
-__global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t N, uint32_t key0, uint32_t key1,
+__global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cnt, uint32_t key0, uint32_t key1,
                                                          uint32_t call, const double *__restrict__ bmin,
                                                          const double *__restrict__ bmax,
                                                          const int *__restrict__ perm, const int *__restrict__ idx,
                                                          float *__restrict__ X32, short *__restrict__ flg) {
   const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= N) return;
+  if (p >= cnt) return;
   const size_t n = (size_t)perm[p];
   const int k = idx[n], D = m.D, ldx = m.ldx, df = m.df;
   float z[MAXD];
@@ -156,28 +163,39 @@ __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t N,
   flg[n] = (short)in;
 }
 
-cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
-                                const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
-                                int *cursor, cudaStream_t s) {
+cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, size_t n1, uint64_t seed,
+                                      uint32_t call, const double *bmin, const double *bmax, float *X32, int *idx,
+                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s) {
   if (m.D < 1 || m.D > kMaxD || m.K < 1 || m.K > kMaxK) return cudaErrorInvalidValue;
-  if (N == 0) return cudaSuccess;
-  if (N > (size_t)INT32_MAX) return cudaErrorInvalidValue;
+  if (N > (size_t)INT32_MAX || n0 > n1 || n1 > N) return cudaErrorInvalidValue;
+  if (n1 == n0) return cudaSuccess;
+  const bool whole = (n0 == 0 && n1 == N);
+  int *ccounts = whole ? nullptr : cursor + m.K;  // the range's own counts (bucket offsets)
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const size_t cnt = n1 - n0;
   cudaError_t e;
-  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * m.K, s)) != cudaSuccess) return e;
-  const unsigned g256 = (unsigned)((N + 255) / 256);
-  draw_pick_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(m, N, k0, k1, call, idx, counts);
+  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * m.K * (whole ? 1 : 2), s)) != cudaSuccess) return e;
+  const unsigned g256 = (unsigned)((cnt + 255) / 256);
+  draw_pick_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(m, n0, n1, k0, k1, call, idx, counts, ccounts);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  draw_bucket_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(N, m.K, idx, counts, cursor, perm);
+  draw_bucket_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(n0, n1, m.K, idx, whole ? counts : ccounts, cursor,
+                                                          perm + n0);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  const unsigned g128 = (unsigned)((N + 127) / 128);
-#define PMCG_APPLY(MD) draw_apply_kernel<MD><<<g128, 128, 0, s>>>(m, N, k0, k1, call, bmin, bmax, perm, idx, X32, flg)
+  const unsigned g128 = (unsigned)((cnt + 127) / 128);
+#define PMCG_APPLY(MD) \
+  draw_apply_kernel<MD><<<g128, 128, 0, s>>>(m, cnt, k0, k1, call, bmin, bmax, perm + n0, idx, X32, flg)
   if (m.ldx <= 8) PMCG_APPLY(8);
   else if (m.ldx <= 16) PMCG_APPLY(16);
   else if (m.ldx <= 32) PMCG_APPLY(32);
   else PMCG_APPLY(64);
 #undef PMCG_APPLY
   return cudaGetLastError();
+}
+
+cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
+                                const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
+                                int *cursor, cudaStream_t s) {
+  return launch_draw_grouped_range(m, N, 0, N, seed, call, bmin, bmax, X32, idx, flg, counts, perm, cursor, s);
 }
 
 // ------------------------------------------------------------------ helpers

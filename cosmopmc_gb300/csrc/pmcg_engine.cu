@@ -60,7 +60,7 @@ static void work_layout(Work &w, Carver &c, size_t empart_bytes) {
   w.aw32 = prec ? c.take<float>(N) : nullptr;
   w.emmask = prec ? c.take<uint32_t>(em_mask_words(K, N)) : nullptr;
   w.perm = prec ? c.take<int>(N) : nullptr;
-  w.cursor = prec ? c.take<int>(K) : nullptr;
+  w.cursor = prec ? c.take<int>(2 * (size_t)K) : nullptr;
   w.wpart = c.take<WRed>(weight_tiles(N));
   w.empart = c.take<double>(empart_bytes / sizeof(double));
   w.dstats = c.take<DevStats>(1);
@@ -712,8 +712,13 @@ namespace pmcg {
 
 static int g_dropin_precision = PMCG_FP64;
 
+// Ranges of the drop-in draw copied to the host while the next range draws.
+constexpr int kDrawChunks = 8;
+
 struct SimMirror {
   Work w;
+  cudaStream_t cs = nullptr;             // device-to-host copies of the sample
+  cudaEvent_t ev[kDrawChunks] = {};      // range drawn and converted
   bool x_valid = false;    // device X/flg/indices/counts match the host sample
   bool lt_valid = false;   // logq/lt/Q valid for (X, snapshot proposal)
   bool w_valid = false;    // logw and the device statistics valid
@@ -722,6 +727,10 @@ struct SimMirror {
 };
 
 static void mirror_delete(SimMirror *m) {
+  if (m->cs) cudaStreamSynchronize(m->cs);
+  for (cudaEvent_t &e : m->ev)
+    if (e) cudaEventDestroy(e);
+  if (m->cs) cudaStreamDestroy(m->cs);
   work_free(m->w);
   if (m->mom) cudaFree(m->mom);
   delete m;
@@ -740,7 +749,10 @@ static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error *
   }
   if (!m) {
     m = new SimMirror();
-    if (!work_alloc(m->w, K, D, df, prec, psim->nsamples, err)) {
+    bool ok = work_alloc(m->w, K, D, df, prec, psim->nsamples, err) &&
+              CK(cudaStreamCreateWithFlags(&m->cs, cudaStreamNonBlocking), "copy stream");
+    for (cudaEvent_t &e : m->ev) ok = ok && CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    if (!ok) {
       mirror_delete(m);
       m = nullptr;
       g_sims.erase(psim);
@@ -840,19 +852,46 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
   Work &w = m->w;
   if (!sync_proposal(m, proposal, err)) return 0;
   if (pb && !upload_box(w, pb->min, pb->max, err)) return 0;
-  bool ok = stage_draw(w, pb != nullptr, rng->seed, rng->calls, err);
-  if (ok && w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
-  ok = ok && CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, w.s), "X") &&
-       CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, w.s), "indices") &&
+  // The host-bound FP64 sample is the largest transfer of the drop-in step: in
+  // the single-precision path the draw runs in kDrawChunks sample ranges, each
+  // converted and copied to the host (copy stream) while the next one draws;
+  // the flags follow the last range and are counted while X is in flight.
+  const int C = (w.prec && w.N >= (size_t)kDrawChunks * 4096) ? kDrawChunks : 1;
+  const bool box = pb != nullptr;
+  bool ok = true;
+  if (w.prec == 1 && C > 1) {
+    w.launches += 3 * C;
+    ok = CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts");
+    for (int c = 0; ok && c < C; c++) {
+      const size_t n0 = w.N * c / C, n1 = w.N * (c + 1) / C;
+      ok = CK(launch_draw_grouped_range(w.prop.view(), w.N, n0, n1, rng->seed, rng->calls, box ? w.bmin : nullptr,
+                                        box ? w.bmax : nullptr, w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor,
+                                        w.s),
+              "draw kernels") &&
+           CK(launch_x32_to_x64(n1 - n0, w.D, w.ldx, w.X32 + n0 * w.ldx, w.X64 + n0 * w.D, w.s), "convert") &&
+           CK(cudaEventRecord(m->ev[c], w.s), "event") && CK(cudaStreamWaitEvent(m->cs, m->ev[c], 0), "wait") &&
+           CK(cudaMemcpyAsync(psim->X + n0 * w.D, w.X64 + n0 * w.D, 8 * (n1 - n0) * w.D, cudaMemcpyDeviceToHost,
+                              m->cs),
+              "X");
+    }
+  } else {
+    ok = stage_draw(w, box, rng->seed, rng->calls, err);
+    if (ok && w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
+    ok = ok && CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, w.s), "X");
+  }
+  ok = ok && CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, w.s), "indices") &&
        CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
        CK(cudaStreamSynchronize(w.s), "draw");
+  size_t nok = 0;
+  if (ok)
+    for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
+  const bool copied = CK(cudaStreamSynchronize(m->cs), "sample copy");  // even after a failure
+  ok = ok && copied;
   rng->calls++;
   if (!ok) return 0;
   m->x_valid = true;
   m->lt_valid = false;
   m->w_valid = false;
-  size_t nok = 0;
-  for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
   psim->isLog = 1;
   return nok;
 }

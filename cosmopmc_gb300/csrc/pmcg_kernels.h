@@ -68,11 +68,17 @@ cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t s
                         cudaStream_t s);
 
 // (a) single-precision draws in component order (three launches; counts must
-// start at zero). perm: N ints, cursor: K ints of scratch. Same values as
+// start at zero). perm: N ints, cursor: 2K ints of scratch. Same values as
 // launch_draw(precision 1) without pre-drawn variates.
 cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
                                 const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
                                 int *cursor, cudaStream_t s);
+// The samples [n0, n1) of an N-point draw alone (values depend only on the
+// sample index, so ranges drawn in any order give the whole draw); counts
+// accumulate over ranges.
+cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, size_t n1, uint64_t seed,
+                                      uint32_t call, const double *bmin, const double *bmax, float *X32, int *idx,
+                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s);
 
 // (b) mixture log-pdf of N points. out[n] = LSE (accumulate=0) or out[n] += LSE + add (accumulate=1).
 // lt/Q optional, [K x N].

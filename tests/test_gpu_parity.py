@@ -77,6 +77,35 @@ def test_draw_indices_bit_exact(pmcg, oracle, prec, shape):
     assert rng.calls == 1
 
 
+def test_dropin_ranged_draw_equals_single_pass(pmcg, oracle):
+    """The single-precision drop-in draw runs in sample ranges whose host copies
+    overlap the next range's draw: the sample equals the engine's single-pass
+    draw of the same seed bit for bit, indices equal the oracle's (N not a
+    multiple of the range count, a box that rejects some samples)."""
+    K, D, df = 64, 32, 3
+    w, mu, cov, _ = small_mixture(K, D, df, seed=12)
+    m = make_mix(pmcg, w, mu, cov, df)
+    N = 100003
+    bmin, bmax = mu.min(0) - 30.0, mu.max(0) + 30.0   # rejects part of the Student-t tails
+    pmcg.set_dropin_precision(1)
+    ps = pmcg.PmcSimu(N, D)
+    rng = pmcg.Rng(4321)
+    nok = pmcg.simulate_mix_mvdens(ps, m, rng, pmcg.Parabox(bmin, bmax))
+    run = pmcg.Run(m, pmcg.Posterior(D, bmin, bmax).add_mix(m), N, precision=1, seed=4321,
+                   box=pmcg.Parabox(bmin, bmax))
+    run.iterate(1.0)
+    ref = run.sample()
+    np.testing.assert_array_equal(ps.X, ref.X)
+    np.testing.assert_array_equal(ps.indices, ref.indices)
+    np.testing.assert_array_equal(ps.flg, ref.flg)
+    assert nok == int(np.sum(ps.flg != 0)) and 0 < nok < N
+    om = oracle_mix(oracle, m)
+    u, z, chi2 = oracle.randoms(4321, 0, N, D, df)
+    _, idx, _, _ = oracle.draw(om, u, z, chi2, bmin, bmax)
+    np.testing.assert_array_equal(ps.indices, idx)
+    run.free()
+
+
 # ----------------------------------------------------------------- (b) mixture log-pdf
 @pytest.mark.parametrize("tag", ["gauss", "t"])
 def test_mix_logpdf_golden(pmcg, tag):
