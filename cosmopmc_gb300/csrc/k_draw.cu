@@ -132,22 +132,41 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t n0, size_t n1, 
 }
 
 // The cnt samples listed in perm (absolute sample indices), in list order.
+// perm lists samples by component, so a block's samples nearly always share
+// one: the rows of L_k and mu_k of the block's first sample are staged in
+// shared memory (loads issued before the normals, so their latency overlaps
+// the generator) and warps whose samples all belong to it read them there;
+// any other warp reads its components from global memory.
 template <int MAXD>
 __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cnt, uint32_t key0, uint32_t key1,
                                                          uint32_t call, const double *__restrict__ bmin,
                                                          const double *__restrict__ bmax,
                                                          const int *__restrict__ perm, const int *__restrict__ idx,
                                                          float *__restrict__ X32, short *__restrict__ flg) {
-  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= cnt) return;
-  const size_t n = (size_t)perm[p];
-  const int k = idx[n], D = m.D, ldx = m.ldx, df = m.df;
+  __shared__ __align__(16) float sL[MAXD * MAXD + MAXD];
+  const int D = m.D, ldx = m.ldx, df = m.df;
+  const size_t p0 = (size_t)blockIdx.x * blockDim.x;  // < cnt: the grid covers cnt exactly
+  const size_t p = p0 + threadIdx.x;
+  const int kb = idx[perm[p0]];
+  {
+    const float4 *src = reinterpret_cast<const float4 *>(m.L32 + (size_t)kb * D * ldx);
+    float4 *dst = reinterpret_cast<float4 *>(sL);
+    for (int e = threadIdx.x; e < D * ldx / 4; e += blockDim.x) dst[e] = __ldg(src + e);
+    for (int e = threadIdx.x; e < D; e += blockDim.x) sL[MAXD * MAXD + e] = __ldg(m.mu32 + (size_t)kb * D + e);
+  }
+  const bool live = p < cnt;
+  const size_t n = live ? (size_t)perm[p] : 0;
+  const int k = live ? idx[n] : kb;
   float z[MAXD];
-  float c2;
-  draw_normals<MAXD, float>(D, df > 0 ? df : 0, (uint32_t)n, (uint32_t)(n >> 32), call, key0, key1, z, c2);
+  float c2 = 0.f;
+  if (live) draw_normals<MAXD, float>(D, df > 0 ? df : 0, (uint32_t)n, (uint32_t)(n >> 32), call, key0, key1, z, c2);
+  __syncthreads();
+  const bool staged = __all_sync(0xffffffffu, k == kb);
+  if (!live) return;
   const float sc = (df > 0) ? student_scale<float>(df, c2) : 1.f;
   float x[MAXD];
-  const int in = draw_transform_f32<MAXD>(m, k, z, sc, bmin, bmax, x, 1);
+  const int in = staged ? draw_transform_rows<MAXD, true>(D, ldx, sL, sL + MAXD * MAXD, z, sc, bmin, bmax, x, 1)
+                        : draw_transform_f32<MAXD>(m, k, z, sc, bmin, bmax, x, 1);
   float *row = X32 + n * ldx;
 #pragma unroll
   for (int j4 = 0; j4 < MAXD / 4; j4++) {

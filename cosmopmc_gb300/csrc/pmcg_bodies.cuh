@@ -51,9 +51,17 @@ __device__ __forceinline__ void box_muller<float>(P4 o, float &g0, float &g1) {
   const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
   const float two53inv = 1.1102230246251565e-16f;  // 2^-53
   // -2 ln(1-a): from the exact small a below 1/2 (log1p), from the exact
-  // complement 1-a above, so r keeps single precision at both ends.
-  const float r2 = (A < (1ull << 52)) ? -2.0f * log1pf(-(u53_to_float(A) * two53inv))
-                                      : -2.0f * logf(u53_to_float((1ull << 53) - A) * two53inv);
+  // complement c = 1-a <= 1/2 above, so r keeps single precision at both ends.
+  // There |log2 c| >= 1, so the MUFU log2 (absolute error near 2^-22) is
+  // within a few 1e-7 relative.
+  float r2;
+  if (A < (1ull << 52)) {
+    r2 = -2.0f * log1pf(-(u53_to_float(A) * two53inv));
+  } else {
+    float l2;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l2) : "f"(u53_to_float((1ull << 53) - A) * two53inv));
+    r2 = -1.3862943611198906f * l2;  // -2 ln 2
+  }
   // b = B / 2^53 with B = (z >> 5) 2^26 + (w >> 6): z / 2^32 to single precision
   const float b = __uint2float_rn(o.z) * 2.3283064365386963e-10f;  // 2^-32
   float r = sqrtf(r2);
@@ -114,15 +122,14 @@ __device__ __forceinline__ Real student_scale(int df, Real c2) {
   return (Real)sqrtf((float)df / (float)c2);
 }
 
-// x = mu_k + sc L_k z in single precision (L32 rows padded to ldx with zeros
-// above the diagonal: float4 reads); returns 0 when a coordinate leaves the box.
-template <int MAXD>
-__device__ __forceinline__ int draw_transform_f32(const DevMixView &m, int k, const float (&z)[MAXD], float sc,
-                                                  const double *__restrict__ bmin, const double *__restrict__ bmax,
-                                                  float *xo, int xstride) {
-  const int D = m.D, ldx = m.ldx;
-  const float *Lk = m.L32 + (size_t)k * D * ldx;
-  const float *mk = m.mu32 + (size_t)k * D;
+// x = mu_k + sc L_k z in single precision from the rows of L_k (stride ldx,
+// zero above the diagonal: float4 reads) and mu_k; SHARED: the rows are staged
+// in shared memory (plain loads), otherwise read-only global loads. Returns 0
+// when a coordinate leaves the box.
+template <int MAXD, bool SHARED>
+__device__ __forceinline__ int draw_transform_rows(int D, int ldx, const float *Lk, const float *mk,
+                                                   const float (&z)[MAXD], float sc, const double *__restrict__ bmin,
+                                                   const double *__restrict__ bmax, float *xo, int xstride) {
   int in = 1;
 #pragma unroll
   for (int i = 0; i < MAXD; i++) {
@@ -130,18 +137,26 @@ __device__ __forceinline__ int draw_transform_f32(const DevMixView &m, int k, co
       float acc = 0.f;
 #pragma unroll
       for (int j4 = 0; j4 <= i / 4; j4++) {
-        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4));
+        const float4 *q = reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4);
+        const float4 l4 = SHARED ? *q : __ldg(q);
         acc = fmaf(l4.x, z[4 * j4], acc);
         acc = fmaf(l4.y, z[4 * j4 + 1], acc);
         acc = fmaf(l4.z, z[4 * j4 + 2], acc);
         acc = fmaf(l4.w, z[4 * j4 + 3], acc);
       }
-      const float xi = __ldg(&mk[i]) + sc * acc;
+      const float xi = (SHARED ? mk[i] : __ldg(&mk[i])) + sc * acc;
       xo[i * xstride] = xi;
       if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
     }
   }
   return in;
+}
+template <int MAXD>
+__device__ __forceinline__ int draw_transform_f32(const DevMixView &m, int k, const float (&z)[MAXD], float sc,
+                                                  const double *__restrict__ bmin, const double *__restrict__ bmax,
+                                                  float *xo, int xstride) {
+  return draw_transform_rows<MAXD, false>(m.D, m.ldx, m.L32 + (size_t)k * m.D * m.ldx, m.mu32 + (size_t)k * m.D, z,
+                                          sc, bmin, bmax, xo, xstride);
 }
 
 // Samples n0 .. n0+blockDim-1: one thread per sample, rows staged in shared
