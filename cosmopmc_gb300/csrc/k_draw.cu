@@ -64,13 +64,16 @@ cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t s
 // order, rows written to the sample's own position. Every value equals the
 // one-pass kernel's (same counters, same operations).
 
-// Component k = min{k : u < C_k} (binary search; C is non-decreasing), else
-// the last component with positive weight.
-__device__ __forceinline__ int pick_component(const double *s_cw, const double *w, int K, double u) {
-  int lo = 0, hi = K;  // first index with u < C
+// Component k = min{k : u < C_k} (C non-decreasing), else the last component
+// with positive weight. With u = A 2^-53 for the 53-bit integer A of the
+// uniform, u < C_k <=> A < T_k = ceil(C_k 2^53) (C_k 2^53 is exact), so the
+// binary search compares integers: the same pick as the FP64 comparison.
+__device__ __forceinline__ int pick_component(const unsigned long long *s_T, const double *w, int K,
+                                              unsigned long long A) {
+  int lo = 0, hi = K;  // first index with A < T
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if (u < s_cw[mid]) hi = mid;
+    if (A < s_T[mid]) hi = mid;
     else lo = mid + 1;
   }
   if (lo < K) return lo;
@@ -79,22 +82,35 @@ __device__ __forceinline__ int pick_component(const double *s_cw, const double *
   return 0;
 }
 
+// Samples per block of the pick and bucket passes (kPickPer per thread): few
+// blocks, so few global count / cursor atomics per component.
+constexpr int kPickPer = 8;
+constexpr int kPickBlock = 256 * kPickPer;
+
 // Samples [n0, n1): component index, per-component counts (and, when ccounts
 // is given, the counts of this range alone).
 __global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t n0, size_t n1, uint32_t key0,
                                                         uint32_t key1, uint32_t call, int *__restrict__ idx,
                                                         int *__restrict__ counts, int *__restrict__ ccounts) {
-  extern __shared__ double s_cw[];
-  int *s_cnt = reinterpret_cast<int *>(s_cw + m.K);
-  for (int k = threadIdx.x; k < m.K; k += blockDim.x) { s_cw[k] = m.cw[k]; s_cnt[k] = 0; }
+  extern __shared__ unsigned long long s_T[];
+  int *s_cnt = reinterpret_cast<int *>(s_T + m.K);
+  for (int k = threadIdx.x; k < m.K; k += blockDim.x) {
+    s_T[k] = (unsigned long long)ceil(m.cw[k] * 9007199254740992.0);
+    s_cnt[k] = 0;
+  }
   __syncthreads();
-  const size_t n = n0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n < n1) {
-    P4 c = {0u, (uint32_t)n, (uint32_t)(n >> 32), call};
-    P4 o = philox4x32_10(c, key0, key1);
-    const int k = pick_component(s_cw, m.w, m.K, u53(o.x, o.y));
-    idx[n] = k;
-    atomicAdd(&s_cnt[k], 1);
+  const size_t b0 = n0 + (size_t)blockIdx.x * kPickBlock + threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < kPickPer; j++) {
+    const size_t n = b0 + (size_t)j * 256;
+    if (n < n1) {
+      P4 c = {0u, (uint32_t)n, (uint32_t)(n >> 32), call};
+      P4 o = philox4x32_10(c, key0, key1);
+      const unsigned long long A = ((unsigned long long)(o.x >> 5) << 26) | (unsigned long long)(o.y >> 6);
+      const int k = pick_component(s_T, m.w, m.K, A);
+      idx[n] = k;
+      atomicAdd(&s_cnt[k], 1);
+    }
   }
   __syncthreads();
   for (int k = threadIdx.x; k < m.K; k += blockDim.x)
@@ -118,17 +134,26 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t n0, size_t n1, 
   }
   for (int k = threadIdx.x; k < K; k += blockDim.x) s_hist[k] = 0;
   __syncthreads();
-  const size_t n = n0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int k = 0, r = 0;
-  if (n < n1) {
-    k = idx[n];
-    r = atomicAdd(&s_hist[k], 1);
+  const size_t b0 = n0 + (size_t)blockIdx.x * kPickBlock + threadIdx.x;
+  int kk[kPickPer], rr[kPickPer];
+#pragma unroll
+  for (int j = 0; j < kPickPer; j++) {
+    const size_t n = b0 + (size_t)j * 256;
+    kk[j] = 0; rr[j] = 0;
+    if (n < n1) {
+      kk[j] = idx[n];
+      rr[j] = atomicAdd(&s_hist[kk[j]], 1);
+    }
   }
   __syncthreads();
   for (int j = threadIdx.x; j < K; j += blockDim.x)
     if (s_hist[j]) s_base[j] = s_off[j] + atomicAdd(&cursor[j], s_hist[j]);
   __syncthreads();
-  if (n < n1) perm[s_base[k] + r] = (int)n;
+#pragma unroll
+  for (int j = 0; j < kPickPer; j++) {
+    const size_t n = b0 + (size_t)j * 256;
+    if (n < n1) perm[s_base[kk[j]] + rr[j]] = (int)n;
+  }
 }
 
 // The cnt samples listed in perm (absolute sample indices), in list order.
@@ -194,11 +219,11 @@ cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, 
   const size_t cnt = n1 - n0;
   cudaError_t e;
   if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * m.K * (whole ? 1 : 2), s)) != cudaSuccess) return e;
-  const unsigned g256 = (unsigned)((cnt + 255) / 256);
-  draw_pick_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(m, n0, n1, k0, k1, call, idx, counts, ccounts);
+  const unsigned gp = (unsigned)((cnt + kPickBlock - 1) / kPickBlock);
+  draw_pick_kernel<<<gp, 256, (size_t)m.K * 12, s>>>(m, n0, n1, k0, k1, call, idx, counts, ccounts);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  draw_bucket_kernel<<<g256, 256, (size_t)m.K * 12, s>>>(n0, n1, m.K, idx, whole ? counts : ccounts, cursor,
-                                                          perm + n0);
+  draw_bucket_kernel<<<gp, 256, (size_t)m.K * 12, s>>>(n0, n1, m.K, idx, whole ? counts : ccounts, cursor,
+                                                        perm + n0);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const unsigned g128 = (unsigned)((cnt + 127) / 128);
 #define PMCG_APPLY(MD) \

@@ -135,18 +135,23 @@ __global__ void __launch_bounds__(256) em_factor_mask_kernel(size_t N, int K, co
       aw[n] = a;
     }
     const size_t wd = n / 32, nl = n < N ? n : N - 1;  // padding lanes read a valid sample
-    for (int k0 = 0; k0 < K; k0 += 8) {
-      float v[8];
+    const float *lp = lt + nl;
+    uint32_t *mp = mask + wd;
+#pragma unroll 1
+    for (int k0 = 0; k0 < K; k0 += 16) {  // 16 loads in flight per thread
+      float v[16];
 #pragma unroll
-      for (int j = 0; j < 8; j++) v[j] = (k0 + j < K) ? __ldg(&lt[(size_t)(k0 + j) * N + nl]) : 0.f;
+      for (int j = 0; j < 16; j++) v[j] = (k0 + j < K) ? __ldg(lp + (size_t)j * N) : 0.f;
+      lp += (size_t)16 * N;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
+      for (int j = 0; j < 16; j++) {
         if (k0 + j < K) {
           const bool act = (n < N) && (a + v[j] > kEmLogMin);
           const unsigned bal = __ballot_sync(0xffffffffu, act);
-          if ((threadIdx.x & 31) == 0) mask[(size_t)(k0 + j) * W + wd] = bal;
+          if ((threadIdx.x & 31) == 0) mp[(size_t)j * W] = bal;
         }
       }
+      mp += (size_t)16 * W;
     }
   }
 }

@@ -786,15 +786,97 @@ __device__ __forceinline__ WRed block_wred(WRed r, WRed *s_r) {
   return a;
 }
 
+// Order-preserving 64-bit key of a double (larger key <=> larger value; every
+// key of a non-NaN value is above 0).
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_value(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
 // Samples tile*kTileW .. +kTileW-1: log-weights and the tile's partial record.
 // logq == nullptr means log q = 0 (re-normalising given log-weights).
+// FAST (single-precision runs, 256 threads, 8 samples per thread): the tile
+// maximum m first (integer compare of order keys), then e = exp(l - m) in
+// single precision with per-thread FP32 partials of s, q and sum e (l - m) over
+// the thread's 8 samples, summed across threads in FP64 (GB300 issues FP64 at
+// a small fraction of the FP32 rate: about 6 FP64 operations per sample
+// instead of a rescaling merge per sample). Otherwise the FP64 online record.
 template <bool FAST = false>
 __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const double *__restrict__ logpost,
                                                   const double *__restrict__ logq, short *__restrict__ flg,
                                                   double *__restrict__ logw, WRed *__restrict__ part, size_t tile,
                                                   WRed *s_r) {
-  WRed r = wred_empty();
   const size_t base = tile * kTileW;
+  if constexpr (FAST) {
+    constexpr int PER = kTileW / 256;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double l[PER];
+    unsigned long long mk = 0ull;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const size_t n = base + threadIdx.x + (size_t)j * 256;
+      double v = -INFINITY;
+      if (n < N) {
+        if (flg[n]) {
+          v = beta * logpost[n] - (logq ? logq[n] : 0.0);
+          if (!isfinite(v)) { v = -INFINITY; flg[n] = 0; }
+        }
+        logw[n] = v;
+      }
+      l[j] = v;
+      if (v > -INFINITY) mk = (dkey(v) > mk) ? dkey(v) : mk;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, mk, o);
+      mk = (t > mk) ? t : mk;
+    }
+    unsigned long long *s_key = reinterpret_cast<unsigned long long *>(s_r);   // [8]
+    double *s_sum = reinterpret_cast<double *>(s_r) + 8;                      // [8][4]
+    if (lane == 0) s_key[warp] = mk;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < 8; w++) mk = (s_key[w] > mk) ? s_key[w] : mk;
+    const double m = mk ? dkey_value(mk) : -INFINITY;
+    float fs = 0.f, ft = 0.f, fq = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      if (l[j] > -INFINITY) {
+        const float d = (float)(l[j] - m);
+        const float e = expf(d);
+        fs += e;
+        ft = fmaf(e, d, ft);
+        fq = fmaf(e, e, fq);
+        cnt++;
+      }
+    }
+    double ds = fs, dt = ft, dq = fq;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ds += __shfl_down_sync(0xffffffffu, ds, o);
+      dt += __shfl_down_sync(0xffffffffu, dt, o);
+      dq += __shfl_down_sync(0xffffffffu, dq, o);
+      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+      s_sum[4 * warp] = ds; s_sum[4 * warp + 1] = dt; s_sum[4 * warp + 2] = dq; s_sum[4 * warp + 3] = (double)cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      WRed r = wred_empty();
+      double S = 0.0, T = 0.0, Q = 0.0, C = 0.0;
+      for (int w = 0; w < 8; w++) { S += s_sum[4 * w]; T += s_sum[4 * w + 1]; Q += s_sum[4 * w + 2]; C += s_sum[4 * w + 3]; }
+      if (mk) { r.m = m; r.s = S; r.t = T + m * S; r.q = Q; }
+      r.n = C;
+      part[tile] = r;
+    }
+    return;
+  }
+  WRed r = wred_empty();
   for (int q = threadIdx.x; q < kTileW; q += blockDim.x) {
     const size_t n = base + q;
     if (n >= N) break;
