@@ -1235,7 +1235,13 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     if (whitened) Lo[e] = (j <= i) ? m.L[(size_t)k * D * D + e] : 0.0;
   }
   __syncthreads();
-  if (whitened) {
+  // Whitened frame without a band limit: Sigma' = Lo C Lo^T and L' = Lo chol(C)
+  // is its Cholesky factor (a product of lower-triangular factors with positive
+  // diagonals), so the well-conditioned C is factorised and one triangular
+  // product (D^3/6 multiply-adds) replaces the two dense ones (D^3).
+  const bool banded = band_limit > 0 && band_limit < D;
+  const bool via_lo = whitened && !banded;
+  if (whitened && banded) {
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // T = Lo C
       int i = e / D, j = e - i * D;
       double t = 0.0;
@@ -1261,7 +1267,7 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     }
     __syncthreads();
   }
-  if (band_limit > 0 && band_limit < D) {
+  if (banded) {
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
       int i = e / D, j = e - i * D;
       if ((i > j ? i - j : j - i) >= band_limit) C[e] = 0.0;
@@ -1306,7 +1312,15 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   __syncthreads();
   for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
     int i = e / D, j = e - i * D;
-    L[(size_t)k * D * D + e] = (j <= i) ? C[e] : 0.0;
+    double v = 0.0;
+    if (j <= i) {
+      if (via_lo) {
+        for (int q = j; q <= i; q++) v = fma(Lo[i * D + q], C[q * D + j], v);
+      } else {
+        v = C[e];
+      }
+    }
+    L[(size_t)k * D * D + e] = v;
   }
   if (threadIdx.x == 0) w[k] = S0;
 }
