@@ -77,7 +77,7 @@ __device__ __forceinline__ int find_run(const uint32_t *__restrict__ pre, int R,
 
 template <int SPT>
 __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const BatchDyn &dy, uint32_t li,
-                                           unsigned char *smem, WRed *s_r, int *s_dead, double *s_piv,
+                                           unsigned char *smem, WRed *s_r, int *s_dead,
                                            DevStats *stats_out, int r) {
   const int D = d.prop.D, K = d.prop.K, ldx = d.prop.ldx;
   switch (stg) {
@@ -134,7 +134,7 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
       break;
     case kBEmFinal:
       body_em_finalize(d.prop, d.w, d.mu, d.L, d.N, d.S, d.empart, d.counts, D, 1, (int)li, d.st,
-                       reinterpret_cast<double *>(smem), s_dead, s_piv);
+                       reinterpret_cast<double *>(smem), s_dead);
       break;
     case kBRenorm:
       body_em_renorm(K, d.w, d.st);
@@ -163,13 +163,12 @@ __global__ void __launch_bounds__(256, 1) batch_kernel(const BatchDesc *__restri
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ WRed s_r[8];
   __shared__ int s_dead;
-  __shared__ double s_piv;
   for (int stg = first; stg <= last; stg++) {
     const uint32_t *pre = starts + (size_t)stg * (R + 1);
     const uint32_t total = pre[R];
     for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
       const int r = find_run(pre, R, item);
-      batch_item<SPT>(stg, descs[r], dyn[r], item - pre[r], smem, s_r, &s_dead, &s_piv, stats_out, r);
+      batch_item<SPT>(stg, descs[r], dyn[r], item - pre[r], smem, s_r, &s_dead, stats_out, r);
       __syncthreads();
     }
     if (stg < last) grid.sync();

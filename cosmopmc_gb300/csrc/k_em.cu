@@ -168,11 +168,8 @@ __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *
                                    int band_limit, int whitened, const DevStats *st) {
   extern __shared__ double sh[];
   __shared__ int s_dead;
-  __shared__ double s_piv;
-  body_em_finalize(m, w, mu, L, N, S, part, counts, band_limit, whitened, blockIdx.x, st, sh, &s_dead, &s_piv);
+  body_em_finalize(m, w, mu, L, N, S, part, counts, band_limit, whitened, blockIdx.x, st, sh, &s_dead);
 }
-
-__global__ void em_renorm_kernel(int K, double *w, DevStats *st) { body_em_renorm(K, w, st); }
 
 int em_chunks(int K, size_t N) {
   // about 8 statistics blocks per SM (4 waves of 2 resident blocks); measured
@@ -233,9 +230,7 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
   }
   em_finalize_kernel<<<m.K, 256, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit, whitened, st);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  em_renorm_kernel<<<1, 32, 0, s>>>(m.K, m.w, st);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return devmix_prepare(m, s);
+  return devmix_prepare_after_em(m, st, s);
 }
 
 }  // namespace pmcg

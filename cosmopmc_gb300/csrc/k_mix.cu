@@ -5,6 +5,7 @@
 // (exec/cosmo_pmc.c:343) and for the MixMvdens target
 // (wrappers/src/param.c:1531-1537). The FP32 and preparation bodies are
 // shared with the batch kernel (pmcg_bodies.cuh).
+#include <cmath>
 #include "pmcg_bodies.cuh"
 
 namespace pmcg {
@@ -32,6 +33,12 @@ size_t devmix_bytes(int K, int D) {
 
 cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.K = K; m.D = D; m.df = df; m.ldx = round4(D);
+  if (df > 0) {
+    const double nu = (double)df;
+    m.cst = std::lgamma(0.5 * (nu + D)) - std::lgamma(0.5 * nu) - 0.5 * D * std::log(nu * PMCG_PI);
+  } else {
+    m.cst = -0.5 * D * PMCG_LN2PI;
+  }
   size_t off[14];
   const size_t o = devmix_layout(K, D, off);
   cudaError_t e = cudaMalloc(&m.arena, o);
@@ -70,6 +77,14 @@ __global__ void mix_prepare_consts_kernel(DevMixView m, const double *logdetL, d
   body_prepare_consts(m, logdetL, cw, lconst, lconst32);
 }
 
+// EM tail: renormalised weights, then the constants of the new weights.
+__global__ void mix_renorm_consts_kernel(DevMixView m, double *w, DevStats *st, const double *logdetL, double *cw,
+                                         double *lconst, float *lconst32) {
+  body_em_renorm(m.K, w, st);
+  __syncthreads();
+  body_prepare_consts(m, logdetL, cw, lconst, lconst32);
+}
+
 cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   DevMixView v = m.view();
   const size_t smem = prepare_smem(m.D);
@@ -78,10 +93,27 @@ cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
       (e = cudaFuncSetAttribute(mix_prepare_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
           cudaSuccess)
     return e;
-  mix_prepare_comp_kernel<<<m.K, 64, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
+  mix_prepare_comp_kernel<<<m.K, 256, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mix_prepare_consts_kernel<<<1, 256, 0, s>>>(v, m.logdetL, m.cw, m.lconst, m.lconst32);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !m.bimg) return e;
+  return launch_umma_bimage(v, m.bimg, s);
+}
+
+cudaError_t devmix_prepare_after_em(DevMix &m, DevStats *st, cudaStream_t s) {
+  DevMixView v = m.view();
+  const size_t smem = prepare_smem(m.D);
+  cudaError_t e;
+  if (smem > 48 * 1024 &&
+      (e = cudaFuncSetAttribute(mix_prepare_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess)
+    return e;
+  mix_prepare_comp_kernel<<<m.K, 256, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mix_renorm_consts_kernel<<<1, 256, 0, s>>>(v, m.w, st, m.logdetL, m.cw, m.lconst, m.lconst32);
   e = cudaGetLastError();
   if (e != cudaSuccess || !m.bimg) return e;
   return launch_umma_bimage(v, m.bimg, s);

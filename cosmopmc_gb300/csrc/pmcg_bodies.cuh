@@ -1186,7 +1186,8 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
 
 // ================================================================== (e) EM finalise
 __host__ __device__ inline size_t finalize_smem(int D, int whitened) {
-  return (size_t)(em_E(D) + (whitened ? 3 : 1) * D * D + D) * sizeof(double);
+  (void)whitened;
+  return (size_t)(em_E(D) + 3 * D * D + 2 * D) * sizeof(double);
 }
 
 // Component k: fixed-order sum of the chunk partials, new mean and covariance
@@ -1196,12 +1197,14 @@ __host__ __device__ inline size_t finalize_smem(int D, int whitened) {
 __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w, double *mu, double *L, size_t N,
                                                  int S, const double *__restrict__ part,
                                                  const int *__restrict__ counts, int band_limit, int whitened, int k,
-                                                 const DevStats *stats, double *sh, int *s_dead, double *s_piv) {
+                                                 const DevStats *stats, double *sh, int *s_dead) {
   const int D = m.D, E = em_E(D);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double *st = sh;             // E
   double *C = st + E;          // D*D
   double *Lo = C + D * D;      // D*D old factor (whitened only)
   double *T = Lo + D * D;      // D*D scratch (whitened only); then D: mean shift
+  double *rp = T + D * D + D;  // D reciprocal pivots
   if (stats->status != 0) return;  // the weight step failed: keep the proposal
   if (m.w[k] <= 0.0) {
     if (threadIdx.x == 0) w[k] = 0.0;
@@ -1228,12 +1231,12 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   for (int i = threadIdx.x; i < D; i += blockDim.x) dm[i] = st[2 + i] / St;
   __syncthreads();
   const double rS0 = 1.0 / S0;
-  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-    int i = e / D, j = e - i * D;
-    int a = i > j ? i : j, b = i > j ? j : i;
-    C[e] = (st[2 + D + tri_idx(a, b)] - St * dm[i] * dm[j]) * rS0;
-    if (whitened) Lo[e] = (j <= i) ? m.L[(size_t)k * D * D + e] : 0.0;
-  }
+  for (int i = warp; i < D; i += nw)
+    for (int j = lane; j < D; j += 32) {
+      const int a = i > j ? i : j, b = i > j ? j : i;
+      C[i * D + j] = (st[2 + D + tri_idx(a, b)] - St * dm[i] * dm[j]) * rS0;
+      if (whitened) Lo[i * D + j] = (j <= i) ? m.L[(size_t)k * D * D + i * D + j] : 0.0;
+    }
   __syncthreads();
   // Whitened frame without a band limit: Sigma' = Lo C Lo^T and L' = Lo chol(C)
   // is its Cholesky factor (a product of lower-triangular factors with positive
@@ -1274,27 +1277,32 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     }
     __syncthreads();
   }
-  // right-looking Cholesky of the lower triangle: pivot, scale the column by the
-  // reciprocal pivot, rank-1 update of the trailing triangle (short FP64 chains)
+  // Right-looking Cholesky of the lower triangle, one barrier per column: the
+  // columns stay unscaled (the update uses 1/p_j^2 = rp_j^2) and the thread
+  // that updates the next diagonal entry (thread 0: warp 0 takes the first row
+  // and lane 0 its first column) derives the next pivot; columns are scaled by
+  // rp_j at the end. Rows go to warps and columns to lanes.
+  auto pivot = [&](int j) {
+    double d = C[j * D + j];
+    if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
+    const double pv = sqrt(d);
+    C[j * D + j] = pv;
+    rp[j] = 1.0 / pv;
+  };
+  if (threadIdx.x == 0) pivot(0);
+  __syncthreads();
   for (int j = 0; j < D; j++) {
-    if (threadIdx.x == 0) {
-      double d = C[j * D + j];
-      if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
-      const double pv = sqrt(d);
-      C[j * D + j] = pv;
-      *s_piv = 1.0 / pv;
+    const double r2 = rp[j] * rp[j];
+    for (int i = j + 1 + warp; i < D; i += nw) {
+      const double cij = C[i * D + j] * r2;
+      for (int c = j + 1 + lane; c <= i; c += 32) C[i * D + c] = fma(-cij, C[c * D + j], C[i * D + c]);
     }
-    __syncthreads();
-    const double rp = *s_piv;
-    for (int i = j + 1 + threadIdx.x; i < D; i += blockDim.x) C[i * D + j] *= rp;
-    __syncthreads();
-    const int n1 = D - j - 1;
-    for (int e = threadIdx.x; e < n1 * n1; e += blockDim.x) {
-      const int i = j + 1 + e / n1, c = j + 1 + e % n1;
-      if (c <= i) C[i * D + c] = fma(-C[i * D + j], C[c * D + j], C[i * D + c]);
-    }
+    if (threadIdx.x == 0 && j + 1 < D) pivot(j + 1);
     __syncthreads();
   }
+  for (int i = warp; i < D; i += nw)
+    for (int j = lane; j < i; j += 32) C[i * D + j] *= rp[j];
+  __syncthreads();
   if (*s_dead) {
     if (threadIdx.x == 0) w[k] = 0.0;
     return;
@@ -1310,18 +1318,18 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     mu[(size_t)k * D + i] = m.mu[(size_t)k * D + i] + d;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-    int i = e / D, j = e - i * D;
-    double v = 0.0;
-    if (j <= i) {
-      if (via_lo) {
-        for (int q = j; q <= i; q++) v = fma(Lo[i * D + q], C[q * D + j], v);
-      } else {
-        v = C[e];
+  for (int i = warp; i < D; i += nw)
+    for (int j = lane; j < D; j += 32) {
+      double v = 0.0;
+      if (j <= i) {
+        if (via_lo) {
+          for (int q = j; q <= i; q++) v = fma(Lo[i * D + q], C[q * D + j], v);
+        } else {
+          v = C[i * D + j];
+        }
       }
+      L[(size_t)k * D * D + i * D + j] = v;
     }
-    L[(size_t)k * D * D + e] = v;
-  }
   if (threadIdx.x == 0) w[k] = S0;
 }
 
@@ -1374,56 +1382,55 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
                                                   float *W32, float *b32, float *L32, float *mu32, int k,
                                                   double *s) {
   const int D = m.D, T = D * (D + 1) / 2, ldx = m.ldx;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double *sL = s;            // D*D
   double *sW = s + D * D;    // D*D
-  const double *Lk = m.L + (size_t)k * D * D;
-  for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-    sL[e] = Lk[e];
-    sW[e] = 0.0;
-  }
-  for (int e = threadIdx.x; e < D * ldx; e += blockDim.x) {  // rows padded to ldx, zero above the diagonal
-    const int i = e / ldx, j = e - i * ldx;
-    L32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)Lk[i * D + j] : 0.0f;
-  }
-  for (int i = threadIdx.x; i < D; i += blockDim.x) mu32[(size_t)k * D + i] = (float)m.mu[(size_t)k * D + i];
   double *sR = sW + D * D;   // D: 1 / L_ii
   double *sG = sR + D;       // D: log L_ii
+  const double *Lk = m.L + (size_t)k * D * D;
+  // rows to warps, columns to lanes (rows padded to ldx, zero above the diagonal)
+  for (int i = warp; i < D; i += nw)
+    for (int j = lane; j < ldx; j += 32) {
+      const double v = (j < D) ? Lk[i * D + j] : 0.0;
+      if (j < D) {
+        sL[i * D + j] = v;
+        sW[i * D + j] = (i == j) ? 1.0 : 0.0;
+      }
+      L32[(size_t)k * D * ldx + (size_t)i * ldx + j] = (j <= i) ? (float)v : 0.0f;
+    }
   for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    mu32[(size_t)k * D + i] = (float)m.mu[(size_t)k * D + i];
     sR[i] = 1.0 / Lk[i * D + i];
     sG[i] = log(Lk[i * D + i]);
   }
   __syncthreads();
-  // L W = I by right-looking forward substitution: row q of W is final once
-  // scaled by 1/L_qq; then every later row subtracts L_iq W_q. Each sum runs in
-  // the same order as a column substitution would (terms q = j .. i-1).
-  for (int i = threadIdx.x; i < D; i += blockDim.x) sW[i * D + i] = 1.0;
-  __syncthreads();
+  // L W = I by right-looking forward substitution with one barrier per step:
+  // the rows U of W stay unscaled (W_q = U_q / L_qq); step q subtracts
+  // (L_iq / L_qq) U_q from every later row, in the order of q as a column
+  // substitution would; rows are scaled at the end.
   for (int q = 0; q < D; q++) {
-    for (int j = threadIdx.x; j <= q; j += blockDim.x) sW[q * D + j] *= sR[q];
-    __syncthreads();
-    const int nr = D - q - 1, nc = q + 1;
-    for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
-      const int i = q + 1 + e / nc, j = e % nc;
-      sW[i * D + j] = fma(-sL[i * D + q], sW[q * D + j], sW[i * D + j]);
+    const double rq = sR[q];
+    for (int i = q + 1 + warp; i < D; i += nw) {
+      const double f = sL[i * D + q] * rq;
+      for (int j = lane; j <= q; j += 32) sW[i * D + j] = fma(-f, sW[q * D + j], sW[i * D + j]);
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+  for (int i = warp; i < D; i += nw)
+    for (int j = lane; j <= i; j += 32) sW[i * D + j] *= sR[i];
+  __syncthreads();
+  for (int i = warp; i < D; i += nw) {
+    // b_i = sum_j W_ij mu_j (lanes over j, fixed-order warp tree)
     double t = 0.0;
-    for (int j = 0; j <= i; j++) t += sW[i * D + j] * m.mu[(size_t)k * D + j];
-    b[(size_t)k * D + i] = t;
-    b32[(size_t)k * D + i] = (float)t;
-  }
-  for (int e = threadIdx.x; e < D * ldx; e += blockDim.x) {
-    int i = e / ldx, j = e - i * ldx;
-    W32[(size_t)k * D * ldx + e] = (j <= i && j < D) ? (float)sW[i * D + j] : 0.0f;
-  }
-  for (int e = threadIdx.x; e < T; e += blockDim.x) {
-    int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);  // corrected below
-    while (tri_idx(i + 1, 0) <= e) i++;
-    while (tri_idx(i, 0) > e) i--;
-    int j = e - tri_idx(i, 0);
-    Wt[(size_t)k * T + e] = sW[i * D + j];
+    for (int j = lane; j <= i; j += 32) t = fma(sW[i * D + j], m.mu[(size_t)k * D + j], t);
+    t = warp_sum(t);
+    if (lane == 0) {
+      b[(size_t)k * D + i] = t;
+      b32[(size_t)k * D + i] = (float)t;
+    }
+    for (int j = lane; j < ldx; j += 32)
+      W32[(size_t)k * D * ldx + (size_t)i * ldx + j] = (j <= i && j < D) ? (float)sW[i * D + j] : 0.0f;
+    for (int j = lane; j <= i; j += 32) Wt[(size_t)k * T + tri_idx(i, j)] = sW[i * D + j];
   }
   if (threadIdx.x == 0) {
     double ld = 0.0;
@@ -1436,14 +1443,8 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
 // do) and the per-component log constants.
 __device__ __forceinline__ void body_prepare_consts(const DevMixView &m, const double *logdetL, double *cw,
                                                     double *lconst, float *lconst32) {
-  const int K = m.K, D = m.D;
-  double cst;
-  if (m.df > 0) {
-    double nu = (double)m.df;
-    cst = lgamma(0.5 * (nu + D)) - lgamma(0.5 * nu) - 0.5 * D * log(nu * PMCG_PI);
-  } else {
-    cst = -0.5 * D * PMCG_LN2PI;
-  }
+  const int K = m.K;
+  const double cst = m.cst;  // log normalising constant, from the host
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int k = 0; k < K; k++) { s += m.w[k]; cw[k] = s; }

@@ -107,6 +107,7 @@ struct DevMixView {
   const float *L32;      // [K*D*ldx] L, rows padded to ldx, zero above the diagonal (single-precision draws)
   const float *mu32;     // [K*D]
   const unsigned char *bimg;  // tensor-core operand image of L^-1 (D <= 32), or null
+  double cst;            // normalising constant of one component (depends on df and D only)
 };
 
 #define PMCG_CUDA_OK(expr) ((expr) == cudaSuccess)
