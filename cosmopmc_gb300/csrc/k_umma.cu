@@ -403,7 +403,11 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     const int quarter = warp & 3, ta = warp >> 2;
     const int srow = ta * 128 + quarter * 32 + lane;         // sample row within the tile
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-    const float hnd = 0.5f * ((float)m.df + (float)D), rnu = 1.0f / (float)m.df;
+    // l = lc - (nu+D)/2 ln(1 + Q/nu) = lc - hndl log2(1 + Q/nu); MUFU log2 and
+    // exp2 (relative error near 2^-22): a few 1e-6 in l, below the TF32-split
+    // products' error, and off the path that returns the accumulators
+    const float hndl = 0.5f * ((float)m.df + (float)D) * 0.69314718055994531f, rnu = 1.0f / (float)m.df;
+    const float kLog2e = 1.44269504088896341f;
     float4 xr[8];
     auto fetch = [&](size_t tile) {
       const size_t n0 = tile * kUmTile;
@@ -484,9 +488,9 @@ __global__ void __launch_bounds__(kUmThreads, 1)
           const float lc = s_lc[g * kUmGC + c];
           float l;
           if (lc == -INFINITY) l = -INFINITY;
-          else l = STUDENT ? lc - hnd * log1pf(qv * rnu) : lc - 0.5f * qv;
-          if (l > mx) { sm = sm * expf(mx - l) + 1.f; mx = l; }
-          else if (l > -INFINITY) sm += expf(l - mx);
+          else l = STUDENT ? lc - hndl * lg2_approx(fmaf(qv, rnu, 1.f)) : lc - 0.5f * qv;
+          if (l > mx) { sm = fmaf(sm, ex2_approx((mx - l) * kLog2e), 1.f); mx = l; }
+          else if (l > -INFINITY) sm += ex2_approx((l - mx) * kLog2e);
           if (n < N && lt) {
             lt[(size_t)k * N + n] = l;
             if (Qo) Qo[(size_t)k * N + n] = (lc == -INFINITY) ? 0.f : qv;
