@@ -139,13 +139,17 @@ def flush_l2(buf):
         buf.add_(1.0)
 
 
-def time_run(P, run, steps, warmup, l2buf, sync, prop):
+def time_run(P, run, steps, warmup, l2buf, sync, prop, stage_steps=3):
     """Every step is one full iteration from the same starting proposal (reset
-    outside the timed events), so each step does identical work."""
+    outside the timed events), so each step does identical work. The timed
+    steps run as in production (single-precision iterations replay one CUDA
+    graph) and are timed whole; stage_steps more iterations with every kernel
+    launched directly give the per-stage breakdown.
+    Returns (stats, ms per step, per-stage ms per step, launches, wall)."""
     for _ in range(warmup):
         run.set_proposal(prop)
         run.iterate(1.0)
-    run.set_timing(True)
+    run.set_timing(True, stages=False)
     launches = 0
     stats = None
     sync()
@@ -158,9 +162,16 @@ def time_run(P, run, steps, warmup, l2buf, sync, prop):
         launches += run.last_launches()
     sync()
     wall = time.perf_counter() - t0
-    ms, n = run.stage_ms()
+    tot, n = run.iteration_ms()
+    run.set_timing(True, stages=True)
+    for _ in range(stage_steps):
+        run.set_proposal(prop)
+        flush_l2(l2buf)
+        sync()
+        run.iterate(1.0)
+    ms, ns = run.stage_ms()
     run.set_timing(False)
-    return stats, ms, n, launches, wall
+    return stats, tot / n, ([v / ns for v in ms] if ns else None), launches, wall
 
 
 def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
@@ -184,10 +195,9 @@ def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
         rec = {"N": N}
         for prec, tag in ((P.MIXED, "mixed"), (P.FP64, "fp64")):
             run = P.Run(prop, post, N, precision=prec, seed=11, box=box)
-            st, ms, nt, _, _ = time_run(P, run, steps, warmup, l2buf, sync, prop)
-            step = sum(ms) / nt
+            st, step, ms, _, _ = time_run(P, run, steps, warmup, l2buf, sync, prop)
             rec[tag] = {"samples_per_s": N / (step / 1e3), "ms_per_step": step, "ln_evidence": st["ln_evidence"],
-                        "stage_ms": [v / nt for v in ms]}
+                        "stage_ms": ms}
             run.free()
         rec["speedup_mixed_vs_fp64"] = rec["mixed"]["samples_per_s"] / rec["fp64"]["samples_per_s"]
         out[name] = rec
@@ -408,10 +418,10 @@ def main():
     barrier()
     clk = ClockSampler(local)
     clk.start()
-    stats, stage_ms, nt, launches, wall = time_run(P, run, args.steps, args.warmup, l2buf, sync, prop)
+    stats, step_ms, stage_ms, launches, wall = time_run(P, run, args.steps, args.warmup, l2buf, sync, prop)
     clocks = clk.stop()
     barrier()
-    step_ms = sum(stage_ms) / nt
+    nt = 1  # stage_ms is per step
     t_local = torch.tensor([step_ms], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
@@ -422,8 +432,7 @@ def main():
     fp64 = None
     if not args.no_fp64:
         run64 = P.Run(prop, post, N, precision=P.FP64, seed=1000 + rank)
-        s64, ms64, n64, _, _ = time_run(P, run64, args.fp64_steps, 1, l2buf, sync, prop)
-        fp64_ms = sum(ms64) / n64
+        s64, fp64_ms, _, _, _ = time_run(P, run64, args.fp64_steps, 1, l2buf, sync, prop, stage_steps=0)
         fp64_value = N * world / (fp64_ms / 1000.0)
         run64.free()
         fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
@@ -517,7 +526,10 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "global_batch": N * world, "nsamples_per_gpu": N, "D": 32, "K": 64,
                    "nu": 3, "target_components": 16, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed between steps (256 MB write); per-iteration arrays also exceed L2"},
+                   "l2": "flushed between steps (256 MB write); per-iteration arrays also exceed L2",
+                   "timing": "CUDA events on the library stream around each iteration as run in production "
+                             "(one replayed CUDA graph per iteration); roofline.stage_ms from 3 more iterations "
+                             "with every kernel launched directly"},
         "fp64": fp64,
         "iteration_stats": {k: stats[k] for k in ("ln_evidence", "perplexity", "ess", "enc")},
         "e2e": e2e,

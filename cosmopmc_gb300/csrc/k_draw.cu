@@ -90,9 +90,11 @@ constexpr int kPickBlock = 256 * kPickPer;
 // Samples [n0, n1): component index, per-component counts (and, when ccounts
 // is given, the counts of this range alone).
 __global__ void __launch_bounds__(256) draw_pick_kernel(DevMixView m, size_t n0, size_t n1, uint32_t key0,
-                                                        uint32_t key1, uint32_t call, int *__restrict__ idx,
-                                                        int *__restrict__ counts, int *__restrict__ ccounts) {
+                                                        uint32_t key1, uint32_t call, const uint32_t *callp,
+                                                        int *__restrict__ idx, int *__restrict__ counts,
+                                                        int *__restrict__ ccounts) {
   extern __shared__ unsigned long long s_T[];
+  if (callp) call = *callp;  // from device memory (iterations replayed as one graph)
   int *s_cnt = reinterpret_cast<int *>(s_T + m.K);
   for (int k = threadIdx.x; k < m.K; k += blockDim.x) {
     s_T[k] = (unsigned long long)ceil(m.cw[k] * 9007199254740992.0);
@@ -164,11 +166,13 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t n0, size_t n1, 
 // any other warp reads its components from global memory.
 template <int MAXD>
 __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cnt, uint32_t key0, uint32_t key1,
-                                                         uint32_t call, const double *__restrict__ bmin,
+                                                         uint32_t call, const uint32_t *callp,
+                                                         const double *__restrict__ bmin,
                                                          const double *__restrict__ bmax,
                                                          const int *__restrict__ perm, const int *__restrict__ idx,
                                                          float *__restrict__ X32, short *__restrict__ flg) {
   __shared__ __align__(16) float sL[MAXD * MAXD + MAXD];
+  if (callp) call = *callp;
   const int D = m.D, ldx = m.ldx, df = m.df;
   const size_t p0 = (size_t)blockIdx.x * blockDim.x;  // < cnt: the grid covers cnt exactly
   const size_t p = p0 + threadIdx.x;
@@ -209,7 +213,8 @@ __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cn
 
 cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, size_t n1, uint64_t seed,
                                       uint32_t call, const double *bmin, const double *bmax, float *X32, int *idx,
-                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s) {
+                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s,
+                                      const uint32_t *callp) {
   if (m.D < 1 || m.D > kMaxD || m.K < 1 || m.K > kMaxK) return cudaErrorInvalidValue;
   if (N > (size_t)INT32_MAX || n0 > n1 || n1 > N) return cudaErrorInvalidValue;
   if (n1 == n0) return cudaSuccess;
@@ -220,14 +225,14 @@ cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, 
   cudaError_t e;
   if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * m.K * (whole ? 1 : 2), s)) != cudaSuccess) return e;
   const unsigned gp = (unsigned)((cnt + kPickBlock - 1) / kPickBlock);
-  draw_pick_kernel<<<gp, 256, (size_t)m.K * 12, s>>>(m, n0, n1, k0, k1, call, idx, counts, ccounts);
+  draw_pick_kernel<<<gp, 256, (size_t)m.K * 12, s>>>(m, n0, n1, k0, k1, call, callp, idx, counts, ccounts);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   draw_bucket_kernel<<<gp, 256, (size_t)m.K * 12, s>>>(n0, n1, m.K, idx, whole ? counts : ccounts, cursor,
                                                         perm + n0);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const unsigned g128 = (unsigned)((cnt + 127) / 128);
 #define PMCG_APPLY(MD) \
-  draw_apply_kernel<MD><<<g128, 128, 0, s>>>(m, cnt, k0, k1, call, bmin, bmax, perm + n0, idx, X32, flg)
+  draw_apply_kernel<MD><<<g128, 128, 0, s>>>(m, cnt, k0, k1, call, callp, bmin, bmax, perm + n0, idx, X32, flg)
   if (m.ldx <= 8) PMCG_APPLY(8);
   else if (m.ldx <= 16) PMCG_APPLY(16);
   else if (m.ldx <= 32) PMCG_APPLY(32);
@@ -238,8 +243,9 @@ cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, 
 
 cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
                                 const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
-                                int *cursor, cudaStream_t s) {
-  return launch_draw_grouped_range(m, N, 0, N, seed, call, bmin, bmax, X32, idx, flg, counts, perm, cursor, s);
+                                int *cursor, cudaStream_t s, const uint32_t *callp) {
+  return launch_draw_grouped_range(m, N, 0, N, seed, call, bmin, bmax, X32, idx, flg, counts, perm, cursor, s,
+                                   callp);
 }
 
 // ------------------------------------------------------------------ helpers

@@ -16,10 +16,12 @@ namespace pmcg {
 size_t weight_tiles(size_t N) { return N == 0 ? 1 : (N + kTileW - 1) / kTileW; }
 
 template <bool FAST>
-__global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, const double *__restrict__ logpost,
+__global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, const double *betap,
+                                                      const double *__restrict__ logpost,
                                                       const double *__restrict__ logq, short *__restrict__ flg,
                                                       double *__restrict__ logw, WRed *__restrict__ partials) {
   __shared__ WRed s_r[8];
+  if (betap) beta = *betap;  // from device memory (iterations replayed as one graph)
   body_weights_tile<FAST>(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
 }
 
@@ -31,10 +33,11 @@ __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *
 }
 
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
-                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast) {
+                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast,
+                           const double *betap) {
   const unsigned nb = (unsigned)weight_tiles(N);
-  if (fast) weights_kernel<true><<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
-  else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, partials);
+  if (fast) weights_kernel<true><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials);
+  else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (fast) weights_final_kernel<true><<<1, 256, 0, s>>>((int)nb, partials, N, st);

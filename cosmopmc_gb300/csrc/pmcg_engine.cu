@@ -105,12 +105,13 @@ static bool upload_box(Work &w, const double *bmin, const double *bmax, error **
          CK(cudaMemcpyAsync(w.bmax, bmax, sizeof(double) * w.D, cudaMemcpyHostToDevice, w.s), "box");
 }
 
-static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **err) {
+static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **err,
+                       const uint32_t *callp = nullptr) {
   if (!CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts")) return false;
   if (w.prec == 1) {
     w.launches += 3;
     return CK(launch_draw_grouped(w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
-                                  w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor, w.s),
+                                  w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor, w.s, callp),
               "draw kernels");
   }
   w.launches += 1;
@@ -166,10 +167,10 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
   return true;
 }
 
-static bool stage_weights(Work &w, double beta, bool with_logq, error **err) {
+static bool stage_weights(Work &w, double beta, bool with_logq, error **err, const double *betap = nullptr) {
   w.launches += 2;
   return CK(launch_weights(w.N, beta, w.logpost, with_logq ? w.logq : nullptr, w.flg, w.logw, w.wpart, w.dstats,
-                           w.s, w.prec == 1),
+                           w.s, w.prec == 1, betap),
             "weight kernels");
 }
 
@@ -181,10 +182,8 @@ static bool stage_em(Work &w, error **err) {
             "EM kernels");
 }
 
-static bool fetch_stats(Work &w, error **err) {
-  if (!CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "stats") ||
-      !CK(cudaStreamSynchronize(w.s), "iteration"))
-    return false;
+// Status of the statistics already copied to w.hstats.
+static bool check_stats(Work &w, error **err) {
   if (w.hstats->tc_err != 0) {
     set_error(err, PMCG_ETIMEOUT, __LINE__, "tensor-core log-density: a pipeline wait expired");
     return false;
@@ -195,6 +194,13 @@ static bool fetch_stats(Work &w, error **err) {
     return false;
   }
   return true;
+}
+
+static bool fetch_stats(Work &w, error **err) {
+  if (!CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "stats") ||
+      !CK(cudaStreamSynchronize(w.s), "iteration"))
+    return false;
+  return check_stats(w, err);
 }
 
 static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error **err) {
@@ -561,30 +567,88 @@ extern "C" pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_post
   return r;
 }
 
+static void drop_run_graph(pmcg_run *r) {
+  if (r->gexec) cudaGraphExecDestroy(r->gexec);
+  r->gexec = nullptr;
+}
+
+// Capture one single-precision iteration (parameter upload, the five stages,
+// statistics download) as a graph; false leaves the run on direct launches.
+static bool capture_run_graph(pmcg_run *r) {
+  Work &w = r->w;
+  if (!r->dpar && (cudaMalloc(&r->dpar, sizeof(pmcg_iter_params)) != cudaSuccess ||
+                   cudaMallocHost(&r->hpar, sizeof(pmcg_iter_params)) != cudaSuccess))
+    return false;
+  error *cerr = nullptr;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(w.s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return false;
+  w.launches = 0;
+  bool ok = cudaMemcpyAsync(r->dpar, r->hpar, sizeof(pmcg_iter_params), cudaMemcpyHostToDevice, w.s) == cudaSuccess;
+  ok = ok && stage_draw(w, r->box, r->seed, 0u, &cerr, &r->dpar->call) && stage_logq(w, &cerr) &&
+       stage_logpost(w, r->post, &cerr) && stage_weights(w, 1.0, true, &cerr, &r->dpar->beta) && stage_em(w, &cerr);
+  ok = ok && cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s) == cudaSuccess;
+  const bool ended = cudaStreamEndCapture(w.s, &g) == cudaSuccess;
+  ok = ok && ended && g && cudaGraphInstantiate(&r->gexec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (cerr) purgeError(&cerr);
+  if (!ok) {
+    r->gexec = nullptr;
+    cudaGetLastError();  // the failed capture is not an error of the run
+    return false;
+  }
+  r->graph_tc = g_use_tensor_cores;
+  r->graph_launches = w.launches;
+  return true;
+}
+
 extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err) {
   Work &w = r->w;
   w.launches = 0;
-  auto mark = [&](int i) { if (r->timing) cudaEventRecord(r->ev[i], w.s); };
-  mark(0);
-  bool ok = stage_draw(w, r->box, r->seed, r->calls, err);
-  mark(1);
-  ok = ok && stage_logq(w, err);
-  mark(2);
-  ok = ok && stage_logpost(w, r->post, err);
-  mark(3);
-  ok = ok && stage_weights(w, beta, true, err);
-  mark(4);
-  ok = ok && stage_em(w, err);
-  mark(5);
-  r->calls++;
-  r->last_launches = w.launches;
-  if (!ok) return;
-  if (!fetch_stats(w, err)) return;
+  bool ok = true;
+  const bool stages = r->timing == 1;
+  if (w.prec == PMCG_MIXED && !stages && !r->graph_off) {
+    if (r->gexec && r->graph_tc != g_use_tensor_cores) drop_run_graph(r);
+    if (!r->gexec && !capture_run_graph(r)) r->graph_off = true;
+  }
+  if (r->gexec && !stages) {
+    r->hpar->beta = beta;
+    r->hpar->call = r->calls;
+    if (r->timing) cudaEventRecord(r->ev[0], w.s);
+    ok = CK(cudaGraphLaunch(r->gexec, w.s), "iteration graph");
+    if (r->timing) cudaEventRecord(r->ev[PMCG_NSTAGE], w.s);
+    ok = ok && CK(cudaStreamSynchronize(w.s), "iteration");
+    w.launches = r->graph_launches;
+    r->calls++;
+    r->last_launches = w.launches;
+    if (!ok || !check_stats(w, err)) return;
+  } else {
+    auto mark = [&](int i) { if (r->timing) cudaEventRecord(r->ev[i], w.s); };
+    mark(0);
+    ok = stage_draw(w, r->box, r->seed, r->calls, err);
+    mark(1);
+    ok = ok && stage_logq(w, err);
+    mark(2);
+    ok = ok && stage_logpost(w, r->post, err);
+    mark(3);
+    ok = ok && stage_weights(w, beta, true, err);
+    mark(4);
+    ok = ok && stage_em(w, err);
+    mark(5);
+    r->calls++;
+    r->last_launches = w.launches;
+    if (!ok) return;
+    if (!fetch_stats(w, err)) return;
+  }
   if (r->timing) {
-    for (int i = 0; i < PMCG_NSTAGE; i++) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, r->ev[i], r->ev[i + 1]);
-      r->stage_ms[i] += ms;
+    float ms = 0.f;
+    if (stages) {
+      for (int i = 0; i < PMCG_NSTAGE; i++) {
+        cudaEventElapsedTime(&ms, r->ev[i], r->ev[i + 1]);
+        r->stage_ms[i] += ms;
+      }
+    } else {
+      cudaEventElapsedTime(&ms, r->ev[0], r->ev[PMCG_NSTAGE]);
+      r->iter_ms += ms;
     }
     r->timed++;
   }
@@ -657,6 +721,9 @@ extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {
 
 extern "C" void pmcg_run_free(pmcg_run **r) {
   if (!r || !*r) return;
+  drop_run_graph(*r);
+  if ((*r)->dpar) cudaFree((*r)->dpar);
+  if ((*r)->hpar) cudaFreeHost((*r)->hpar);
   for (int i = 0; i <= PMCG_NSTAGE; i++)
     if ((*r)->ev[i]) cudaEventDestroy((*r)->ev[i]);
   work_free((*r)->w);
@@ -665,14 +732,23 @@ extern "C" void pmcg_run_free(pmcg_run **r) {
 }
 
 extern "C" void pmcg_run_set_timing(pmcg_run *r, int on) {
-  r->timing = on != 0;
+  r->timing = (on == 1 || on == 2) ? on : 0;
   for (int i = 0; i < PMCG_NSTAGE; i++) r->stage_ms[i] = 0.0;
+  r->iter_ms = 0.0;
   r->timed = 0;
 }
 
 extern "C" int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage) {
-  for (int i = 0; i < nstage && i < PMCG_NSTAGE; i++) ms[i] = r->stage_ms[i];
-  return r->timed;
+  for (int i = 0; i < nstage && i < PMCG_NSTAGE; i++) ms[i] = r->timing == 1 ? r->stage_ms[i] : 0.0;
+  return r->timing == 1 ? r->timed : 0;
+}
+
+extern "C" int pmcg_run_iteration_ms(pmcg_run *r, double *ms) {
+  double t = r->iter_ms;
+  if (r->timing == 1)
+    for (int i = 0; i < PMCG_NSTAGE; i++) t += r->stage_ms[i];
+  if (ms) *ms = t;
+  return r->timing ? r->timed : 0;
 }
 
 extern "C" double pmcg_run_time_stage(pmcg_run *r, int stage, int reps, error **err) {

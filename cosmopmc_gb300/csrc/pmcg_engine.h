@@ -71,15 +71,30 @@ struct pmcg_posterior {
   std::vector<pmcg::Plugin> plugins;
 };
 
+// Per-iteration scalars read by the kernels of a captured iteration.
+struct pmcg_iter_params {
+  double beta;
+  uint32_t call;
+};
+
 struct pmcg_run {
   pmcg::Work w;
   const pmcg_posterior *post = nullptr;
   bool box = false;
   uint64_t seed = 0;
   uint32_t calls = 0;
-  bool timing = false;
+  int timing = 0;  // 1 per stage (direct launches), 2 whole iterations
   cudaEvent_t ev[PMCG_NSTAGE + 1] = {};
   double stage_ms[PMCG_NSTAGE] = {};
+  double iter_ms = 0.0;
   int timed = 0;
   int last_launches = 0;
+  // Single-precision runs replay one iteration as a CUDA graph: the kernels
+  // read beta and the call counter from dpar, which the graph's first node
+  // copies from the pinned hpar. Captured on first use; re-captured when the
+  // tensor-core switch changes; graph_off after a failed capture.
+  pmcg_iter_params *dpar = nullptr, *hpar = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_tc = -1, graph_launches = 0;
+  bool graph_off = false;
 };

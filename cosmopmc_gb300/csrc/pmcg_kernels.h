@@ -74,16 +74,18 @@ cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t s
 
 // (a) single-precision draws in component order (three launches; counts must
 // start at zero). perm: N ints, cursor: 2K ints of scratch. Same values as
-// launch_draw(precision 1) without pre-drawn variates.
+// launch_draw(precision 1) without pre-drawn variates. callp (optional): the
+// call counter read from device memory instead of call.
 cudaError_t launch_draw_grouped(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
                                 const double *bmax, float *X32, int *idx, short *flg, int *counts, int *perm,
-                                int *cursor, cudaStream_t s);
+                                int *cursor, cudaStream_t s, const uint32_t *callp = nullptr);
 // The samples [n0, n1) of an N-point draw alone (values depend only on the
 // sample index, so ranges drawn in any order give the whole draw); counts
 // accumulate over ranges.
 cudaError_t launch_draw_grouped_range(const DevMixView &m, size_t N, size_t n0, size_t n1, uint64_t seed,
                                       uint32_t call, const double *bmin, const double *bmax, float *X32, int *idx,
-                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s);
+                                      short *flg, int *counts, int *perm, int *cursor, cudaStream_t s,
+                                      const uint32_t *callp = nullptr);
 
 // (b) mixture log-pdf of N points. out[n] = LSE (accumulate=0) or out[n] += LSE + add (accumulate=1).
 // lt/Q optional, [K x N].
@@ -93,8 +95,10 @@ cudaError_t launch_mixlogpdf(int precision, const DevMixView &m, size_t N, const
 
 // (d) weights + reduction; writes logw and the scalars of DevStats. fast: the
 // per-sample factors e^{l-m} in single precision (single-precision runs).
+// betap (optional): beta read from device memory.
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
-                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast = 0);
+                           double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast = 0,
+                           const double *betap = nullptr);
 
 // (e) EM statistics, finalisation (Cholesky on the device) and renormalisation.
 size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);

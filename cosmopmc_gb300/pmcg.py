@@ -189,6 +189,7 @@ SIGNATURES = [
     ("pmcg_run_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
     ("pmcg_run_stage_ms", C.c_int, [C.c_void_p, _dp, C.c_int]),
+    ("pmcg_run_iteration_ms", C.c_int, [C.c_void_p, _dp]),
     ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
     ("pmcg_run_time_stage", C.c_double, [C.c_void_p, C.c_int, C.c_int, PErr]),
     ("pmcg_batch_create", C.c_void_p, [C.c_int, C.POINTER(C.c_void_p), PErr]),
@@ -551,13 +552,22 @@ class Run:
         call("pmcg_run_get_sample", self.p, ps.p)
         return ps
 
-    def set_timing(self, on=True):
-        load().pmcg_run_set_timing(self.p, 1 if on else 0)
+    def set_timing(self, on=True, stages=True):
+        """CUDA-event timing: per stage (every kernel launched directly) or, with
+        stages=False, whole iterations as they run in production (one replayed
+        CUDA graph per single-precision iteration)."""
+        load().pmcg_run_set_timing(self.p, (1 if stages else 2) if on else 0)
 
     def stage_ms(self):
         ms = (C.c_double * 5)()
         n = load().pmcg_run_stage_ms(self.p, ms, 5)
         return list(ms), n
+
+    def iteration_ms(self):
+        """(summed ms of the timed iterations, their number)."""
+        ms = C.c_double()
+        n = load().pmcg_run_iteration_ms(self.p, C.byref(ms))
+        return ms.value, n
 
     def last_launches(self):
         return load().pmcg_run_last_launches(self.p)

@@ -331,12 +331,16 @@ void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, error **err)
 /* Copy the last sample (X, log-weights, flg, indices) into psim. */
 void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err);
 void pmcg_run_free(pmcg_run **r);
-/* Stage timing with CUDA events on the run's stream: enable, then read
- * the summed milliseconds per stage (draw, logq, logpost, weights, em)
- * and the number of iterations they cover; reset clears the sums. */
+/* Timing with CUDA events on the run's stream. on = 1: per stage (draw,
+ * logq, logpost, weights, em; every kernel launched directly), read with
+ * pmcg_run_stage_ms; on = 2: whole iterations as they run in production
+ * (single-precision runs replay one captured CUDA graph per iteration), read
+ * with pmcg_run_iteration_ms; 0 off. Each call clears the sums; both readers
+ * return the number of iterations covered. */
 #define PMCG_NSTAGE 5
 void pmcg_run_set_timing(pmcg_run *r, int on);
 int pmcg_run_stage_ms(pmcg_run *r, double *ms, int nstage);
+int pmcg_run_iteration_ms(pmcg_run *r, double *ms);
 /* Re-evaluates stage 1 (proposal log-density) or 2 (log-posterior) of the
  * run's current sample reps times on the run's stream and returns the mean
  * milliseconds per evaluation (CUDA events); the results are unchanged. The
