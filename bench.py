@@ -174,6 +174,28 @@ def time_run(P, run, steps, warmup, l2buf, sync, prop, stage_steps=3):
     return stats, tot / n, ([v / ns for v in ms] if ns else None), launches, wall
 
 
+def same_draw_accuracy(P, prop, post, N, seed=2024):
+    """Both paths on the same draw: one iteration of a fresh mixed and a fresh
+    FP64 run with one seed (the samples agree to single precision), compared
+    by ln Z and by the weighted posterior mean and covariance in units of the
+    FP64 posterior standard deviations."""
+    out = {}
+    for prec, tag in ((P.MIXED, "mixed"), (P.FP64, "fp64")):
+        r = P.Run(prop, post, N, precision=prec, seed=seed)
+        st = r.iterate(1.0)
+        s = r.sample()
+        mean, cov = s.weighted_moments()
+        out[tag] = (st["ln_evidence"], mean, cov)
+        del s
+        r.free()
+    (z32, m32, c32), (z64, m64, c64) = out["mixed"], out["fp64"]
+    sig = np.sqrt(np.diag(c64))
+    return {"draw": f"first iteration of fresh runs, seed {seed}, both paths", "ln_evidence_mixed": z32,
+            "ln_evidence_fp64": z64, "abs_dlnZ": abs(z32 - z64),
+            "posterior_mean_max_sigma": float(np.max(np.abs(m32 - m64) / sig)),
+            "posterior_cov_max_sigma2": float(np.max(np.abs(c32 - c64) / np.outer(sig, sig)))}
+
+
 def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
     """The other likelihoods at their configuration sizes: SN Ia (D=6, K=10, 740
     supernovae, Fisher start; N = 10^4 as configured and N = 2^18) and the dense
@@ -437,7 +459,7 @@ def main():
         run64.free()
         fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
                 "speedup_mixed_vs_fp64": value / fp64_value,
-                "ln_evidence_fp64": s64["ln_evidence"], "ln_evidence_mixed": stats["ln_evidence"]}
+                "accuracy": same_draw_accuracy(P, prop, post, N)}
     if args.no_e2e:
         return finish(args, rank, world, value, step_ms_max, N, stats, fp64, None, launches, stage_ms, nt, clocks,
                       W)

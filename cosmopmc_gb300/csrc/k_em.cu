@@ -173,7 +173,9 @@ __global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *
 
 int em_chunks(int K, size_t N) {
   // about 8 statistics blocks per SM (4 waves of 2 resident blocks); measured
-  // against 2 and 16 per SM at the mixture workload
+  // against 2 and 16 per SM at the mixture workload. Chunks of at least 2048
+  // samples (measured against 256: more partials cost more than the shorter
+  // chunks save, for small samples and batches)
   int S = (8 * 152 + K - 1) / K;
   size_t maxS = (N + 2047) / 2048;
   if (maxS < 1) maxS = 1;
