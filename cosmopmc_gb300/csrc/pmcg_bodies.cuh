@@ -936,7 +936,12 @@ __device__ __forceinline__ void body_em_factor(size_t N, const double *__restric
 
 // Staging capacity of the compacted (sample, weight) list: one full tile plus
 // one scan step of up to 256 candidates.
-constexpr int kEmBuf = kTile32 + 256;
+// Rows per staging tile of the EM statistics: 64 for D > 16, more for small D
+// (each tile costs three barriers and a gather whose latency is exposed, so
+// small-D tiles carry more rows); the list buffer holds a tile plus one pass
+// of listing (at most 256 entries).
+__host__ __device__ inline int em_tile_rows(int Dp) { return Dp <= 8 ? 4 * kTile32 : (Dp <= 16 ? 2 * kTile32 : kTile32); }
+__host__ __device__ inline int em_list_buf(int Dp) { return em_tile_rows(Dp) + 256; }
 // A pair whose single-precision weight vt = exp(aw + lt) / itau underflows
 // (aw + lt below log FLT_MIN = -87.3) adds exactly nothing in FP32 and less
 // than 1e-38 relative in any precision: such pairs are skipped.
@@ -944,7 +949,8 @@ constexpr float kEmLogMin = -87.0f;
 
 __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t *tile_bytes, size_t *red_bytes) {
   const int Dp = ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, G = threads / NB;
-  *tile_bytes = (size_t)(Dp * Dp + Dp + kTile32 * Da + kTile32 * (Dp + 1) + 3 * kEmBuf + 40) * sizeof(float);
+  const int T = em_tile_rows(Dp);
+  *tile_bytes = (size_t)(Dp * Dp + Dp + T * Da + T * (Dp + 1) + 3 * em_list_buf(Dp) + 40) * sizeof(float);
   *red_bytes = (size_t)G * NB * 16 * sizeof(double);
 }
 
@@ -976,12 +982,14 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   const int G = blockDim.x / NB;
   float *sWT = reinterpret_cast<float *>(smem);   // [Dp][Dp]  (L^-1)^T
   float *sb = sWT + Dp * Dp;                      // [Dp]      L^-1 mu
-  float *sa = sb + Dp;                            // [kTile32][Da]
-  float *sx = sa + kTile32 * Da;                  // [kTile32][ldt]
-  float *lvt = sx + kTile32 * ldt;                // [kEmBuf] listed vt
-  float *ltau = lvt + kEmBuf;                     // [kEmBuf] listed 1/tau
-  int *lidx = reinterpret_cast<int *>(ltau + kEmBuf);  // [kEmBuf] listed sample offsets
-  int *wcnt = lidx + kEmBuf;                      // [32] per-warp counts
+  const int T = em_tile_rows(Dp), LB = em_list_buf(Dp);
+  const int flush_tiles = kFlushTiles * kTile32 / T;  // the same rows per FP32 partial for every T
+  float *sa = sb + Dp;                            // [T][Da]
+  float *sx = sa + T * Da;                        // [T][ldt]
+  float *lvt = sx + T * ldt;                      // [LB] listed vt
+  float *ltau = lvt + LB;                         // [LB] listed 1/tau
+  int *lidx = reinterpret_cast<int *>(ltau + LB);  // [LB] listed sample offsets
+  int *wcnt = lidx + LB;                          // [32] per-warp counts
   const size_t chunk = (N + S - 1) / S;
   const size_t n0 = (size_t)s * chunk, n1 = (n0 + chunk < N) ? n0 + chunk : N;
   const float nu = (float)m.df, rnd = 1.0f / ((float)m.df + (float)D);
@@ -1002,23 +1010,25 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   for (int e = 0; e < 16; e++) { acc[e] = 0.f; acc64[e] = 0.0; }
   int tiles = 0;
 
-  // Accumulate listed entries [0, nt) (nt <= kTile32).
+  // Accumulate listed entries [0, nt) (nt <= T).
   auto process = [&](int nt) {
-    if (tid < kTile32) {
-      float *row = sa + tid * Da;
+    for (int r = tid; r < T; r += blockDim.x) {
+      float *row = sa + r * Da;
       row[Dp] = 1.f;
-      row[Dp + 1] = (tid < nt) ? ltau[tid] : 1.f;
+      row[Dp + 1] = (r < nt) ? ltau[r] : 1.f;
       row[Dp + 2] = 0.f;
       row[Dp + 3] = 0.f;
     }
-    for (int e = tid; e < kTile32 * Dp; e += blockDim.x) {
+    for (int e = tid; e < T * Dp; e += blockDim.x) {
       const int r = e / Dp, i = e - r * Dp;
       sx[r * ldt + i] = (r < nt) ? X[(n0 + (size_t)lidx[r]) * Dp + i] : 0.f;
     }
     __syncthreads();
-    for (int u = warp; u < 2 * nib; u += nwarp) {
+    for (int u = warp; u < (T / 32) * nib; u += nwarp) {
+      // 32-row slices; alternate slices run the row blocks in reverse order so
+      // consecutive warps pair a long triangle row with a short one
       const int pair = u % nib, half = u / nib;
-      const int ib = half == 0 ? pair : nib - 1 - pair;
+      const int ib = (half & 1) == 0 ? pair : nib - 1 - pair;
       const int r = half * 32 + lane;
       float o0 = -sb[4 * ib], o1 = -sb[4 * ib + 1], o2 = -sb[4 * ib + 2], o3 = -sb[4 * ib + 3];
       const float *xr = sx + r * ldt;
@@ -1049,7 +1059,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
         acc[14] = fmaf(ai.w, aj.z, acc[14]); acc[15] = fmaf(ai.w, aj.w, acc[15]);
       }
     }
-    if (++tiles == kFlushTiles) {
+    if (++tiles == flush_tiles) {
       tiles = 0;
 #pragma unroll
       for (int e = 0; e < 16; e++) { acc64[e] += (double)acc[e]; acc[e] = 0.f; }
@@ -1058,14 +1068,14 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   };
 
   int fill = 0;  // listed entries (identical in every thread)
-  // Process full tiles and move the remainder (fill - kTile32 <= 256 entries) to the front.
+  // Process full tiles and move the remainder (fill - T <= 256 entries) to the front.
   auto drain = [&]() {
-    while (fill >= kTile32) {
-      process(kTile32);
-      const int rem = fill - kTile32;
+    while (fill >= T) {
+      process(T);
+      const int rem = fill - T;
       int ri = 0;
       float rv = 0.f, rt = 0.f;
-      if (tid < rem) { ri = lidx[kTile32 + tid]; rv = lvt[kTile32 + tid]; rt = ltau[kTile32 + tid]; }
+      if (tid < rem) { ri = lidx[T + tid]; rv = lvt[T + tid]; rt = ltau[T + tid]; }
       __syncthreads();
       if (tid < rem) { lidx[tid] = ri; lvt[tid] = rv; ltau[tid] = rt; }
       __syncthreads();
@@ -1102,7 +1112,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
       const int pos = off + incl - c;   // position of this word's first entry in this pass
       // emit in rounds that fit the list buffer, processing full tiles in between
       for (int done = 0; done < tot;) {
-        const int take = min(kEmBuf - fill, tot - done);
+        const int take = min(LB - fill, tot - done);
         uint32_t b = bits;
         int p = pos;
         while (b) {
