@@ -1181,11 +1181,16 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   }
   __syncthreads();
   double *out = part + ((size_t)k * S + s) * E;
-  if (grp == 0) {
-    for (int e = 0; e < 16; e++) {
-      double t = red[(size_t)blk * 16 + e];
-      for (int g = 1; g < G; g++) t += red[((size_t)g * NB + blk) * 16 + e];
-      const int r = 4 * bi + e / 4, c = 4 * bj + e % 4;
+  // one (block, entry) per thread: the sum over the G groups in a fixed order
+  for (int be = tid; be < NB * 16; be += blockDim.x) {
+    const int b = be >> 4, e = be & 15;
+    int rbi = 0;
+    while ((rbi + 1) * (rbi + 2) / 2 <= b) rbi++;
+    const int rbj = b - rbi * (rbi + 1) / 2;
+    {
+      double t = red[(size_t)b * 16 + e];
+      for (int g = 1; g < G; g++) t += red[((size_t)g * NB + b) * 16 + e];
+      const int r = 4 * rbi + e / 4, c = 4 * rbj + e % 4;
       if (r < D && c <= r) out[2 + D + tri_idx(r, c)] = t;
       else if (r == Dp && c < D) out[2 + c] = t;
       else if (r == Dp && c == Dp) out[1] = t;

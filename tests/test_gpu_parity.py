@@ -106,6 +106,29 @@ def test_dropin_ranged_draw_equals_single_pass(pmcg, oracle):
     run.free()
 
 
+def test_sn_large_sample_against_oracle(pmcg, oracle):
+    """Single precision over 40000 random points of the prior box (several waves
+    of one warp per point) against the FP64 oracle; a 3000-point subset alone
+    gives the same values."""
+    wl = W.sn_workload()
+    sn = wl["sn"]
+    post = pmcg.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(sn)
+    rng = np.random.default_rng(41)
+    N = 40000
+    P = rng.uniform(wl["bmin"], wl["bmax"], (N, 6))
+    ref, ok = oracle.sn_loglike(sn, P)
+    ref = ref + (-np.sum(np.log(wl["bmax"] - wl["bmin"])))
+    ll, flg = post.log_pdf_batch(P, precision=1)
+    ll_s, flg_s = post.log_pdf_batch(P[:3000], precision=1)
+    good = ok == 1
+    assert np.sum((flg == 1) != good) <= 2
+    np.testing.assert_array_equal(flg_s, flg[:3000])
+    np.testing.assert_array_equal(ll_s, ll[:3000])
+    # relative error grows with chi^2 (FP32 integrand nodes): 1e-4 over 40000 box points
+    b = good & (flg == 1)
+    assert np.max(np.abs(ll[b] - ref[b]) / np.maximum(1.0, np.abs(ref[b]))) < 1e-4
+
+
 # ----------------------------------------------------------------- (b) mixture log-pdf
 @pytest.mark.parametrize("tag", ["gauss", "t"])
 def test_mix_logpdf_golden(pmcg, tag):
