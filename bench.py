@@ -344,7 +344,11 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
         srv.free()
         lat = np.array([r["finish_s"] - r["submit_s"] for r, _, _ in res if r["status"] == 0])
         samples = sum(n * it for r, n, it in res if r["status"] == 0)
-        out.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "ok": int(len(lat)),
+        failed = {}
+        for r, _, _ in res:
+            if r["status"] != 0:
+                failed[str(r["status"])] = failed.get(str(r["status"]), 0) + 1
+        out.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "ok": int(len(lat)), "failed_status": failed,
                     "p50_ms": float(np.percentile(lat, 50) * 1e3) if len(lat) else None,
                     "p99_ms": float(np.percentile(lat, 99) * 1e3) if len(lat) else None,
                     "samples_per_s": samples / wall, "peak_resident": info["peak_resident"],
