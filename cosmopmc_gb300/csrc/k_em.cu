@@ -17,6 +17,7 @@
 // rule. The mixed, finalise and renormalise bodies are shared with the batch
 // kernel (pmcg_bodies.cuh).
 #include "pmcg_bodies.cuh"
+#include "umma_image.cuh"
 
 namespace pmcg {
 
@@ -163,12 +164,38 @@ __global__ void em_weight_factor_kernel(size_t N, const double *__restrict__ log
   body_em_factor(N, logw, logq, st, aw, blockIdx.x);
 }
 
-__global__ void em_finalize_kernel(DevMixView m, double *w, double *mu, double *L, size_t N, int S,
-                                   const double *__restrict__ part, const int *__restrict__ counts,
-                                   int band_limit, int whitened, const DevStats *st) {
+// The EM update after the statistics, one block per component: the new weight,
+// mean and factor (FP64), then for a live component its derived arrays (L^-1,
+// L^-1 mu, single-precision copies) and its rows of the tensor operand image.
+// The last block to finish (fence, then a counter; nothing waits) renormalises
+// the weights and writes the constants and the image's log-constants, which
+// depend on every weight. One launch instead of four dependent ones.
+__global__ void __launch_bounds__(256) em_update_kernel(DevMix m, size_t N, int S, const double *__restrict__ part,
+                                                        const int *__restrict__ counts, int band_limit,
+                                                        int whitened, DevStats *st) {
   extern __shared__ double sh[];
-  __shared__ int s_dead;
-  body_em_finalize(m, w, mu, L, N, S, part, counts, band_limit, whitened, blockIdx.x, st, sh, &s_dead);
+  __shared__ int s_dead, s_last;
+  const DevMixView v = m.view();
+  const int k = blockIdx.x;
+  body_em_finalize(v, m.w, m.mu, m.L, N, S, part, counts, band_limit, whitened, k, st, sh, &s_dead);
+  __syncthreads();
+  if (st->status == 0 && m.w[k] > 0.0) {
+    body_prepare_comp(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32, k, sh);
+    __syncthreads();
+    if (m.bimg) umma_image_component(v, m.bimg, k);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(m.em_done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  body_em_renorm(m.K, m.w, st);
+  __syncthreads();
+  body_prepare_consts(v, m.logdetL, m.cw, m.lconst, m.lconst32);
+  __syncthreads();
+  if (m.bimg) umma_image_lconst(v, m.bimg);
+  if (threadIdx.x == 0) *m.em_done = 0u;  // ready for the next update
 }
 
 int em_chunks(int K, size_t N) {
@@ -225,14 +252,14 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int whitened = precision != 0;
-  size_t fsmem = finalize_smem(D, whitened);
-  if (fsmem > 48 * 1024) {
-    e = cudaFuncSetAttribute(em_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
+  size_t usmem = finalize_smem(D, whitened);
+  if (prepare_smem(D) > usmem) usmem = prepare_smem(D);
+  if (usmem > 48 * 1024) {
+    e = cudaFuncSetAttribute(em_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usmem);
     if (e != cudaSuccess) return e;
   }
-  em_finalize_kernel<<<m.K, 256, fsmem, s>>>(v, m.w, m.mu, m.L, N, S, partials, counts, band_limit, whitened, st);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return devmix_prepare_after_em(m, st, s);
+  em_update_kernel<<<m.K, 256, usmem, s>>>(m, N, S, partials, counts, band_limit, whitened, st);
+  return cudaGetLastError();
 }
 
 }  // namespace pmcg

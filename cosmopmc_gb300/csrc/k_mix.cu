@@ -14,7 +14,7 @@ namespace pmcg {
 // Every array starts on a 256-byte boundary (the single-precision factors are
 // read as float4, the tensor-core image by bulk copies). The tensor-core image
 // of L^-1 (slot 13) exists for D <= 32 only.
-static size_t devmix_layout(int K, int D, size_t off[14]) {
+static size_t devmix_layout(int K, int D, size_t off[15]) {
   const size_t T = (size_t)D * (D + 1) / 2, Kz = (size_t)K, ldx = (size_t)round4(D);
   const size_t nd[8] = {Kz, Kz, Kz * D, Kz * D * D, Kz * T, Kz * D, Kz, Kz};
   const size_t nf[5] = {Kz * D * ldx, Kz * D, Kz, Kz * D * ldx, Kz * D};
@@ -22,12 +22,13 @@ static size_t devmix_layout(int K, int D, size_t off[14]) {
   for (int i = 0; i < 8; i++) { off[i] = o; o = (o + nd[i] * sizeof(double) + 255) & ~(size_t)255; }
   for (int i = 0; i < 5; i++) { off[8 + i] = o; o = (o + nf[i] * sizeof(float) + 255) & ~(size_t)255; }
   off[13] = o;
-  if (D <= 32) o += umma_bimage_bytes(K);
-  return o;
+  if (D <= 32) o = (o + umma_bimage_bytes(K) + 255) & ~(size_t)255;
+  off[14] = o;  // EM update counter
+  return o + 256;
 }
 
 size_t devmix_bytes(int K, int D) {
-  size_t off[14];
+  size_t off[15];
   return devmix_layout(K, D, off);
 }
 
@@ -39,7 +40,7 @@ cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   } else {
     m.cst = -0.5 * D * PMCG_LN2PI;
   }
-  size_t off[14];
+  size_t off[15];
   const size_t o = devmix_layout(K, D, off);
   cudaError_t e = cudaMalloc(&m.arena, o);
   if (e != cudaSuccess) { m.arena = nullptr; return e; }
@@ -58,6 +59,8 @@ cudaError_t devmix_alloc(DevMix &m, int K, int D, int df) {
   m.L32 = (float *)(a + off[11]);
   m.mu32 = (float *)(a + off[12]);
   m.bimg = (D <= 32) ? (unsigned char *)(a + off[13]) : nullptr;
+  m.em_done = (unsigned *)(a + off[14]);
+  if ((e = cudaMemset(m.em_done, 0, sizeof(unsigned))) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
@@ -77,14 +80,6 @@ __global__ void mix_prepare_consts_kernel(DevMixView m, const double *logdetL, d
   body_prepare_consts(m, logdetL, cw, lconst, lconst32);
 }
 
-// EM tail: renormalised weights, then the constants of the new weights.
-__global__ void mix_renorm_consts_kernel(DevMixView m, double *w, DevStats *st, const double *logdetL, double *cw,
-                                         double *lconst, float *lconst32) {
-  body_em_renorm(m.K, w, st);
-  __syncthreads();
-  body_prepare_consts(m, logdetL, cw, lconst, lconst32);
-}
-
 cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   DevMixView v = m.view();
   const size_t smem = prepare_smem(m.D);
@@ -97,23 +92,6 @@ cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mix_prepare_consts_kernel<<<1, 256, 0, s>>>(v, m.logdetL, m.cw, m.lconst, m.lconst32);
-  e = cudaGetLastError();
-  if (e != cudaSuccess || !m.bimg) return e;
-  return launch_umma_bimage(v, m.bimg, s);
-}
-
-cudaError_t devmix_prepare_after_em(DevMix &m, DevStats *st, cudaStream_t s) {
-  DevMixView v = m.view();
-  const size_t smem = prepare_smem(m.D);
-  cudaError_t e;
-  if (smem > 48 * 1024 &&
-      (e = cudaFuncSetAttribute(mix_prepare_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-          cudaSuccess)
-    return e;
-  mix_prepare_comp_kernel<<<m.K, 256, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  mix_renorm_consts_kernel<<<1, 256, 0, s>>>(v, m.w, st, m.logdetL, m.cw, m.lconst, m.lconst32);
   e = cudaGetLastError();
   if (e != cudaSuccess || !m.bimg) return e;
   return launch_umma_bimage(v, m.bimg, s);

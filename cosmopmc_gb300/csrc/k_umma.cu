@@ -30,15 +30,11 @@
 //    raises an abort flag that every other wait observes, sets the error
 //    flag, lets its copies and MMAs in flight land (bounded) and frees TMEM.
 #include "pmcg_bodies.cuh"
+#include "umma_image.cuh"
 
 namespace pmcg {
 
 constexpr int kUmTile = 256;                  // samples per CTA tile
-constexpr int kUmGC = 8;                      // components per group (256 operand rows)
-constexpr int kUmHalf = 128 * 128;            // bytes of one 128-row x 32-float operand (16 KB)
-constexpr int kUmOpBytes = 2 * kUmHalf;       // one 256-row operand (32 KB)
-constexpr int kUmCopyBytes = 2 * kUmOpBytes;  // streamed per group: hi + lo (64 KB)
-constexpr int kUmGroupStride = kUmCopyBytes + 1024;  // image stride per group: hi, lo, lc[8]
 constexpr int kUmStages = 2;                  // operand ring
 constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
 constexpr int kUmSmemOnes = kUmHalf;          // constant operand of the shift K-step
@@ -58,58 +54,16 @@ static size_t umma_smem_bytes(int K) {
   return (size_t)kUmSmemA + kUmSmemOnes + kUmSmemB + 1024 + (size_t)G * kUmGC * sizeof(float) + kUmBars * 8 + 16;
 }
 
-// Byte offset of element (row, col) (col < 32 floats) in a 128-byte-swizzled,
-// K-major operand: 8-row atoms of 1024 bytes, 16-byte chunk c of row r stored
-// at chunk c ^ (r mod 8).
-__host__ __device__ __forceinline__ uint32_t sw128_off(int row, int col) {
-  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((col >> 2) ^ (row & 7)) & 7) << 4) + (col & 3) * 4);
-}
-
-__device__ __forceinline__ float tf32_round(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-// ------------------------------------------------------------------ operand image
-// Group g, component c (k = 8g + c), row i = 8 rb + r, column j: operand row
-// n = 64 rb + 8 c + r holds W_k[i][:] split into TF32 hi and lo (zero for
-// padding rows / columns / components). The shift s_n = -(L^-1 mu)_k[i],
-// split into TF32 (hi, lo), sits in columns 24, 25 of rows that no K-step
-// reads there: rows n < 64 min(KS, 3) of the hi operand (upper triangle, or
-// unused when KS <= 3) and, for KS = 4, rows 192..255 in rows 0..63 of the lo
-// operand. After the operands: the eight log-constants (-inf for padding).
+// The whole image (every group and row, the log-constants): after an upload.
 __global__ void umma_bimage_kernel(DevMixView m, unsigned char *img) {
-  const int g = blockIdx.x, D = m.D, K = m.K, ldx = m.ldx;
-  const int KS = (D + 7) >> 3;
-  unsigned char *hi = img + (size_t)g * kUmGroupStride, *lo = hi + kUmOpBytes;
+  const int g = blockIdx.x;
   // block (g, y) writes operand rows 32 y .. 32 y + 31
-  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-    const int n = blockIdx.y * 32 + (e >> 5), j = e & 31;
-    const int rb = n >> 6, c = (n >> 3) & 7, r = n & 7, i = rb * 8 + r, k = g * kUmGC + c;
-    float w = 0.f;
-    if (k < K && i < D && j < D) w = m.W32[(size_t)k * D * ldx + (size_t)i * ldx + j];
-    float h = tf32_round(w);
-    float l = tf32_round(w - h);
-    // shift entries (the slots are zero in the factor)
-    if (j == 24 || j == 25) {
-      const int nh = n;                                   // hi slot -> operand row nh
-      const int nl = (KS == 4 && n < 64) ? n + 192 : -1;  // lo slot -> operand row nl
-      auto shift = [&](int row, float &hv) {
-        const int rrb = row >> 6, rc = (row >> 3) & 7, ri = rrb * 8 + (row & 7), rk = g * kUmGC + rc;
-        const float sv = (rk < K && ri < D) ? -m.b32[(size_t)rk * D + ri] : 0.f;
-        const float sh = tf32_round(sv);
-        hv = (j == 24) ? sh : tf32_round(sv - sh);
-      };
-      if (nh < 64 * (KS < 3 ? KS : 3)) shift(nh, h);
-      if (nl >= 0) shift(nl, l);
-    }
-    *reinterpret_cast<float *>(hi + sw128_off(n, j)) = h;
-    *reinterpret_cast<float *>(lo + sw128_off(n, j)) = l;
-  }
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x)
+    umma_image_entry(m, img, g, blockIdx.y * 32 + (e >> 5), e & 31);
   if (blockIdx.y == 0 && threadIdx.x < kUmGC) {
     const int k = g * kUmGC + threadIdx.x;
-    reinterpret_cast<float *>(hi + kUmCopyBytes)[threadIdx.x] = (k < K) ? m.lconst32[k] : -INFINITY;
+    reinterpret_cast<float *>(img + (size_t)g * kUmGroupStride + kUmCopyBytes)[threadIdx.x] =
+        (k < m.K) ? m.lconst32[k] : -INFINITY;
   }
 }
 

@@ -175,8 +175,8 @@ static bool stage_weights(Work &w, double beta, bool with_logq, error **err, con
 }
 
 static bool stage_em(Work &w, error **err) {
-  // FP64: stats, finalize, renorm, 2 prepare; mixed: + weight factor with listing bits; + operand image (D <= 32)
-  w.launches += (w.prec ? 6 : 5) + (w.prop.bimg ? 1 : 0);
+  // statistics and the fused update; mixed: + the weight factor with the listing bits
+  w.launches += w.prec ? 3 : 2;
   return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
                       w.empart, w.S, w.dstats, w.D, w.aw32, w.emmask, w.s),
             "EM kernels");

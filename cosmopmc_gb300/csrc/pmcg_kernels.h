@@ -34,8 +34,9 @@ struct DevMix {
   float *W32 = nullptr, *b32 = nullptr, *lconst32 = nullptr, *L32 = nullptr, *mu32 = nullptr;
   unsigned char *bimg = nullptr;  // tensor-core operand image (D <= 32)
   double cst = 0.0;  // log normalising constant of a component, set on the host at allocation
+  unsigned *em_done = nullptr;  // component blocks finished in the EM update (0 between launches)
   void *arena = nullptr;
-  DevMixView view() const {
+  __host__ __device__ DevMixView view() const {
     DevMixView v;
     v.K = K; v.D = D; v.df = df; v.ldx = ldx;
     v.w = w; v.cw = cw; v.mu = mu; v.L = L; v.Wt = Wt; v.b = b; v.lconst = lconst;
@@ -59,10 +60,6 @@ void devmix_free(DevMix &m);
 cudaError_t devmix_upload(DevMix &m, const double *w, const double *mu, const double *L, cudaStream_t s);
 // Recompute the derived arrays from w, mu, L already on the device.
 cudaError_t devmix_prepare(DevMix &m, cudaStream_t s);
-// After an EM update: the derived arrays of the new factors, then the weights
-// renormalised (unless the statistics report a failure) with the constants
-// and the tensor operand image of the new weights.
-cudaError_t devmix_prepare_after_em(DevMix &m, DevStats *st, cudaStream_t s);
 
 inline int round4(int d) { return (d + 3) & ~3; }
 
