@@ -15,14 +15,28 @@ namespace pmcg {
 
 size_t weight_tiles(size_t N) { return N == 0 ? 1 : (N + kTileW - 1) / kTileW; }
 
+// Tiles of kTileW samples; with done given, the last block to finish (fence,
+// then a counter; nothing waits) merges every tile's record into the
+// statistics, so the weight step is one launch.
 template <bool FAST>
 __global__ void __launch_bounds__(256) weights_kernel(size_t N, double beta, const double *betap,
                                                       const double *__restrict__ logpost,
                                                       const double *__restrict__ logq, short *__restrict__ flg,
-                                                      double *__restrict__ logw, WRed *__restrict__ partials) {
+                                                      double *__restrict__ logw, WRed *partials, DevStats *st,
+                                                      unsigned *done) {
   __shared__ WRed s_r[8];
+  __shared__ int s_last;
   if (betap) beta = *betap;  // from device memory (iterations replayed as one graph)
   body_weights_tile<FAST>(N, beta, logpost, logq, flg, logw, partials, blockIdx.x, s_r);
+  if (!done) return;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  body_weights_final<FAST>((int)gridDim.x, partials, N, st, s_r);
+  if (threadIdx.x == 0) *done = 0u;  // ready for the next weight step
 }
 
 template <bool FAST>
@@ -34,12 +48,12 @@ __global__ void __launch_bounds__(256) weights_final_kernel(int nb, const WRed *
 
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
                            double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast,
-                           const double *betap) {
+                           const double *betap, unsigned *done) {
   const unsigned nb = (unsigned)weight_tiles(N);
-  if (fast) weights_kernel<true><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials);
-  else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials);
+  if (fast) weights_kernel<true><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials, st, done);
+  else weights_kernel<false><<<nb, 256, 0, s>>>(N, beta, betap, logpost, logq, flg, logw, partials, st, done);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || done) return e;
   if (fast) weights_final_kernel<true><<<1, 256, 0, s>>>((int)nb, partials, N, st);
   else weights_final_kernel<false><<<1, 256, 0, s>>>((int)nb, partials, N, st);
   return cudaGetLastError();

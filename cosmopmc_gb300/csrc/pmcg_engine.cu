@@ -62,6 +62,7 @@ static void work_layout(Work &w, Carver &c, size_t empart_bytes) {
   w.perm = prec ? c.take<int>(N) : nullptr;
   w.cursor = prec ? c.take<int>(2 * (size_t)K) : nullptr;
   w.wpart = c.take<WRed>(weight_tiles(N));
+  w.wdone = c.take<unsigned>(1);
   w.empart = c.take<double>(empart_bytes / sizeof(double));
   w.dstats = c.take<DevStats>(1);
 }
@@ -94,7 +95,8 @@ bool work_alloc(Work &w, int K, int D, int df, int prec, size_t N, error **err) 
   if (!CK(cudaMallocHost(&w.hstats, sizeof(DevStats)), "pinned stats")) return false;
   if (!CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking), "stream")) return false;
   if (!CK(cudaMemsetAsync(w.dstats, 0, sizeof(DevStats), w.s), "stats") ||
-      !CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * K, w.s), "counts"))
+      !CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * K, w.s), "counts") ||
+      !CK(cudaMemsetAsync(w.wdone, 0, sizeof(unsigned), w.s), "weight counter"))
     return false;
   if (!CK(devmix_alloc(w.prop, K, D, df), "proposal buffers")) return false;
   return true;
@@ -168,10 +170,10 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
 }
 
 static bool stage_weights(Work &w, double beta, bool with_logq, error **err, const double *betap = nullptr) {
-  w.launches += 2;
+  w.launches += 1;
   return CK(launch_weights(w.N, beta, w.logpost, with_logq ? w.logq : nullptr, w.flg, w.logw, w.wpart, w.dstats,
-                           w.s, w.prec == 1, betap),
-            "weight kernels");
+                           w.s, w.prec == 1, betap, w.wdone),
+            "weight kernel");
 }
 
 static bool stage_em(Work &w, error **err) {

@@ -51,6 +51,7 @@ struct Work {
   uint32_t *emmask = nullptr;  // EM listing bits (mixed path)
   int *perm = nullptr, *cursor = nullptr;  // draws bucketed by component (mixed path)
   WRed *wpart = nullptr;
+  unsigned *wdone = nullptr;   // weight tiles finished (zero between weight steps)
   double *empart = nullptr;
   DevStats *dstats = nullptr, *hstats = nullptr;
   void *arena = nullptr;

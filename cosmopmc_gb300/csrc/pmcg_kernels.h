@@ -92,10 +92,12 @@ cudaError_t launch_mixlogpdf(int precision, const DevMixView &m, size_t N, const
 
 // (d) weights + reduction; writes logw and the scalars of DevStats. fast: the
 // per-sample factors e^{l-m} in single precision (single-precision runs).
-// betap (optional): beta read from device memory.
+// betap (optional): beta read from device memory. done (optional): a device
+// counter that is zero between calls; the last tile block then merges the
+// records (one launch), else a second kernel does.
 cudaError_t launch_weights(size_t N, double beta, const double *logpost, const double *logq, short *flg,
                            double *logw, WRed *partials, DevStats *st, cudaStream_t s, int fast = 0,
-                           const double *betap = nullptr);
+                           const double *betap = nullptr, unsigned *done = nullptr);
 
 // (e) EM statistics, finalisation (Cholesky on the device) and renormalisation.
 size_t em_partials_size(int precision, int K, int D, int *S_out, size_t N);
