@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -217,6 +218,9 @@ static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error *
 using namespace pmcg;
 
 // ===================================================================== posterior
+static std::atomic<uint64_t> g_post_stamp{0};
+static void restamp(pmcg_posterior *p) { p->stamp = ++g_post_stamp; }
+
 extern "C" pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, const double *max, error **err) {
   if (npar < 1 || npar > kMaxD) {
     set_error(err, PMCG_EDIM, __LINE__, "npar %d", npar);
@@ -238,11 +242,13 @@ extern "C" pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, con
       p->logpr -= std::log(max[j] - min[j]);
     }
   }
+  restamp(p);
   return p;
 }
 
 extern "C" void pmcg_posterior_free(pmcg_posterior **p) {
   if (!p || !*p) return;
+  forget_posterior(*p);
   for (Plugin &pl : (*p)->plugins) {
     devmix_free(pl.mix);
     if (pl.sn.arena) cudaFree(pl.sn.arena);
@@ -263,6 +269,7 @@ extern "C" void pmcg_posterior_add_mixmvdens(pmcg_posterior *p, const mix_mvdens
   if (!CK(devmix_alloc(pl.mix, target->ncomp, target->ndim, df), "target buffers")) return;
   if (!upload_mix(pl.mix, target, 0, err)) { devmix_free(pl.mix); return; }
   p->plugins.push_back(pl);
+  restamp(p);
 }
 
 extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *sd, error **err) {
@@ -384,6 +391,7 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
             up(s.fsn, fsn.data(), sizeof(float4) * fsn.size()) && up(s.fzl2, fzl2.data(), 4 * (size_t)n);
   if (!ok) { cudaFree(s.arena); return; }
   p->plugins.push_back(pl);
+  restamp(p);
 }
 
 extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const double *A, const double *C,
@@ -462,6 +470,7 @@ extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const 
          CK(cudaMemcpy(t.b32, b32.data(), 4 * b32.size(), cudaMemcpyHostToDevice), "template upload");
   if (!ok) { cudaFree(t.arena); return; }
   p->plugins.push_back(pl);
+  restamp(p);
 }
 
 // Batched log-posterior over N points (one Work scratch per call).
@@ -797,17 +806,28 @@ struct SimMirror {
   Work w;
   cudaStream_t cs = nullptr;             // device-to-host copies of the sample
   cudaEvent_t ev[kDrawChunks] = {};      // range drawn and converted
+  cudaEvent_t drawn = nullptr;           // the draw done and its flags saved (before the look-ahead)
+  short *flg0 = nullptr;                 // the draw's flags, copied to the host behind X
   bool x_valid = false;    // device X/flg/indices/counts match the host sample
   bool lt_valid = false;   // logq/lt/Q valid for (X, snapshot proposal)
   bool w_valid = false;    // logw and the device statistics valid
+  // Look-ahead: the posterior of the last weight step (and its stamp); after a
+  // draw its log-posterior is evaluated while X travels to the host, and
+  // lp_valid says w.logpost holds it (w.flg then carries its likelihood flags).
+  const pmcg_posterior *post = nullptr;
+  uint64_t post_stamp = 0;
+  bool lp_valid = false;
   std::vector<double> snap_w, snap_mu, snap_L;
   double *mom = nullptr;   // scratch of the weighted moments (allocated on first use)
 };
 
 static void mirror_delete(SimMirror *m) {
   if (m->cs) cudaStreamSynchronize(m->cs);
+  if (m->w.s) cudaStreamSynchronize(m->w.s);
   for (cudaEvent_t &e : m->ev)
     if (e) cudaEventDestroy(e);
+  if (m->drawn) cudaEventDestroy(m->drawn);
+  if (m->flg0) cudaFree(m->flg0);
   if (m->cs) cudaStreamDestroy(m->cs);
   work_free(m->w);
   if (m->mom) cudaFree(m->mom);
@@ -830,6 +850,8 @@ static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error *
     bool ok = work_alloc(m->w, K, D, df, prec, psim->nsamples, err) &&
               CK(cudaStreamCreateWithFlags(&m->cs, cudaStreamNonBlocking), "copy stream");
     for (cudaEvent_t &e : m->ev) ok = ok && CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    ok = ok && CK(cudaEventCreateWithFlags(&m->drawn, cudaEventDisableTiming), "event") &&
+         CK(cudaMalloc(&m->flg0, sizeof(short) * psim->nsamples + 16), "flag copy");
     if (!ok) {
       mirror_delete(m);
       m = nullptr;
@@ -864,6 +886,15 @@ void forget_simu(const pmc_simu *p) {
 
 void forget_mix(const mix_mvdens *) {}
 
+void forget_posterior(const pmcg_posterior *p) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto &kv : g_sims)
+    if (kv.second->post == p) {
+      kv.second->post = nullptr;
+      kv.second->lp_valid = false;
+    }
+}
+
 // Upload the proposal when it differs from the mirror's snapshot.
 static bool sync_proposal(SimMirror *m, const mix_mvdens *prop, error **err) {
   std::vector<double> w, mu, L;
@@ -890,6 +921,7 @@ static bool sync_sample(SimMirror *m, const pmc_simu *psim, error **err) {
   m->x_valid = true;
   m->lt_valid = false;
   m->w_valid = false;
+  m->lp_valid = false;
   return true;
 }
 
@@ -897,6 +929,7 @@ static bool sync_sample(SimMirror *m, const pmc_simu *psim, error **err) {
 static bool sync_weights(SimMirror *m, const pmc_simu *psim, error **err) {
   if (m->w_valid) return true;
   Work &w = m->w;
+  m->lp_valid = false;  // w.logpost is overwritten below
   bool ok = CK(cudaMemcpyAsync(w.logpost, psim->weights, 8 * w.N, cudaMemcpyHostToDevice, w.s), "weights upload");
   if (ok && !psim->isLog) ok = CK(launch_log_weights(w.N, w.logpost, w.flg, w.s), "log weights");
   ok = ok && stage_weights(w, 1.0, false, err) && fetch_stats(w, err);
@@ -916,7 +949,7 @@ extern "C" int pmcg_set_tensor_cores(int on) {
 
 extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {
   SimMirror *m = find_mirror(psim);
-  if (m) m->x_valid = m->lt_valid = m->w_valid = false;
+  if (m) m->x_valid = m->lt_valid = m->w_valid = m->lp_valid = false;
 }
 
 extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg_rng *rng, parabox *pb,
@@ -932,8 +965,7 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
   if (pb && !upload_box(w, pb->min, pb->max, err)) return 0;
   // The host-bound FP64 sample is the largest transfer of the drop-in step: in
   // the single-precision path the draw runs in kDrawChunks sample ranges, each
-  // converted and copied to the host (copy stream) while the next one draws;
-  // the flags follow the last range and are counted while X is in flight.
+  // converted and copied to the host (copy stream) while the next one draws.
   const int C = (w.prec && w.N >= (size_t)kDrawChunks * 4096) ? kDrawChunks : 1;
   const bool box = pb != nullptr;
   bool ok = true;
@@ -955,20 +987,41 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
   } else {
     ok = stage_draw(w, box, rng->seed, rng->calls, err);
     if (ok && w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
-    ok = ok && CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, w.s), "X");
+    ok = ok && CK(cudaEventRecord(m->ev[0], w.s), "event") && CK(cudaStreamWaitEvent(m->cs, m->ev[0], 0), "wait") &&
+         CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, m->cs), "X");
   }
-  ok = ok && CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, w.s), "indices") &&
-       CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
-       CK(cudaStreamSynchronize(w.s), "draw");
+  // The draw's flags are saved on the device (the look-ahead below may flag
+  // samples by likelihood); indices and flags follow X on the copy stream, so
+  // the look-ahead does not queue behind the host copies.
+  ok = ok && CK(cudaMemcpyAsync(m->flg0, w.flg, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags") &&
+       CK(cudaEventRecord(m->drawn, w.s), "event") && CK(cudaStreamWaitEvent(m->cs, m->drawn, 0), "wait") &&
+       CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, m->cs), "indices") &&
+       CK(cudaMemcpyAsync(psim->flg, m->flg0, 2 * w.N, cudaMemcpyDeviceToHost, m->cs), "flg");
+  // Look-ahead while X travels to the host: the weight step that follows a draw
+  // needs log q under this proposal and, most often, the log-posterior of the
+  // posterior it used last time; both are pure functions of X, queued after
+  // the draw's flags are saved and not waited for here. The weight step keeps
+  // what matches its arguments and recomputes the rest.
+  bool lt = false, lp = false;
+  if (ok) {
+    error *lerr = nullptr;
+    lt = stage_logq(w, &lerr);
+    if (lt && m->post && m->post->stamp == m->post_stamp) lp = stage_logpost(w, m->post, &lerr);
+    if (lerr) purgeError(&lerr);
+  }
+  const bool copied = CK(cudaStreamSynchronize(m->cs), "sample copy");  // even after a failure
+  ok = ok && copied;
   size_t nok = 0;
   if (ok)
     for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
-  const bool copied = CK(cudaStreamSynchronize(m->cs), "sample copy");  // even after a failure
-  ok = ok && copied;
   rng->calls++;
-  if (!ok) return 0;
+  if (!ok) {
+    cudaStreamSynchronize(w.s);
+    return 0;
+  }
   m->x_valid = true;
-  m->lt_valid = false;
+  m->lt_valid = lt;
+  m->lp_valid = lp;
   m->w_valid = false;
   psim->isLog = 1;
   return nok;
@@ -991,13 +1044,24 @@ extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim,
   if (!m) return 0;
   Work &w = m->w;
   if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err)) return 0;
-  bool ok = stage_logq(w, err) && stage_logpost(w, p, err) && stage_weights(w, beta, true, err);
+  bool ok = m->lt_valid || stage_logq(w, err);
+  const bool lp_hit = m->lp_valid && m->post == p && m->post_stamp == p->stamp;
+  if (ok && !lp_hit) {
+    // a look-ahead for another posterior flagged samples by its likelihood:
+    // the draw's flags come back first
+    if (m->lp_valid) ok = CK(cudaMemcpyAsync(w.flg, m->flg0, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags");
+    ok = ok && stage_logpost(w, p, err);
+  }
+  m->lp_valid = false;
+  ok = ok && stage_weights(w, beta, true, err);
   ok = ok && CK(cudaMemcpyAsync(psim->weights, w.logw, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
        CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg");
   if (!ok) return 0;
   if (!fetch_stats(w, err)) return 0;
   m->lt_valid = true;
   m->w_valid = true;
+  m->post = p;
+  m->post_stamp = p->stamp;
   psim->isLog = 1;
   psim->logSum = w.hstats->logSum;
   psim->maxW = w.hstats->maxW;
@@ -1056,7 +1120,7 @@ extern "C" size_t importance_sample(pmc_simu *psim, const pmcg_posterior *post, 
             CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
             CK(cudaStreamSynchronize(w.s), "importance sample");
   if (!ok) return 0;
-  m->lt_valid = m->w_valid = false;
+  m->lt_valid = m->w_valid = m->lp_valid = false;
   size_t count = 0;
   double mw = -INFINITY;
   for (size_t n = 0; n < psim->nsamples; n++) {

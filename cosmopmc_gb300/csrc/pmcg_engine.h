@@ -70,6 +70,7 @@ struct pmcg_posterior {
   double logpr = 0.0;
   std::vector<double> min, max;
   std::vector<pmcg::Plugin> plugins;
+  uint64_t stamp = 0;  // new at allocation and at every change (unique over the process)
 };
 
 // Per-iteration scalars read by the kernels of a captured iteration.

@@ -13,4 +13,7 @@ bool flatten_mix(const mix_mvdens *m, std::vector<double> &w, std::vector<double
 // Drop the device mirrors the library keeps for a host object.
 void forget_mix(const mix_mvdens *m);
 void forget_simu(const pmc_simu *p);
+// Forget a posterior that is about to be freed (the drop-in mirrors keep the
+// last one they weighed with).
+void forget_posterior(const pmcg_posterior *p);
 }  // namespace pmcg

@@ -268,6 +268,55 @@ def test_dropin_iteration_fp64_matches_oracle(pmcg, oracle, df):
     np.testing.assert_allclose(L2[live], new.L[live], rtol=1e-8, atol=1e-11)
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_dropin_lookahead_hit_and_miss(pmcg, prec):
+    """simulate_mix_mvdens evaluates log q, and the log-posterior of the posterior the
+    previous weight step used, while X travels to the host; the weight step keeps
+    what matches its arguments. Results equal those of a fresh sample object (no
+    look-ahead) holding the same draw, both when the posterior is the same (hit) and
+    when it changes (miss: the SN posterior's look-ahead flagged loitering
+    cosmologies, and the draw's own flags come back before the other posterior)."""
+    wl = W.sn_workload(K=10, init="fisher")
+    w, mu, cov, _ = wl["prop"]
+    # plus a component around a loitering cosmology (Omega_m ~ 0.05, Omega_de ~ 1.4, w0 ~ -2.8)
+    loiter = np.array([0.05, 1.4, -2.8, -19.1, 0.14, 3.1])
+    w2 = np.append(w * 0.5, 0.5)
+    mu2 = np.vstack([mu, loiter[None, :]])
+    cov2 = np.concatenate([cov, np.diag([0.02, 0.05, 0.1, 0.05, 0.02, 0.2])[None] ** 2 * 4.0])
+    m = make_mix(pmcg, w2, mu2, cov2, -1)
+    bmin, bmax = wl["bmin"], wl["bmax"]
+    post_a = pmcg.Posterior(6, bmin, bmax).add_snia(wl["sn"])
+    wt = np.array([1.0])
+    post_b = pmcg.Posterior(6, bmin, bmax).add_mix(make_mix(pmcg, wt, mu[:1], cov[:1] * 4.0, -1))
+    pmcg.set_dropin_precision(prec)
+    N = 20000
+    pb = pmcg.Parabox(bmin, bmax)
+
+    def fresh(call, post):
+        ps = pmcg.PmcSimu(N, 6)
+        rng = pmcg.Rng(5)
+        rng.p.contents.calls = call
+        pmcg.simulate_mix_mvdens(ps, m, rng, pb)
+        nok = pmcg.importance_weights(ps, m, post, 1.0)
+        return nok, ps.weights.copy(), ps.flg.copy(), ps.X.copy()
+
+    ps = pmcg.PmcSimu(N, 6)
+    rng = pmcg.Rng(5)
+    pmcg.simulate_mix_mvdens(ps, m, rng, pb)
+    pmcg.importance_weights(ps, m, post_a, 1.0)        # remembers post_a
+    for call, post in ((1, post_a), (2, post_b)):      # hit, then miss
+        pmcg.simulate_mix_mvdens(ps, m, rng, pb)
+        nok = pmcg.importance_weights(ps, m, post, 1.0)
+        r_nok, r_w, r_f, r_x = fresh(call, post)
+        np.testing.assert_array_equal(ps.X, r_x)
+        np.testing.assert_array_equal(ps.flg, r_f)
+        np.testing.assert_array_equal(ps.weights, r_w)
+        assert nok == r_nok
+    # the miss case really had a look-ahead to undo: the SN posterior flags some of these points
+    _, _, f_a, _ = fresh(2, post_a)
+    assert np.sum(f_a == 0) > np.sum(ps.flg == 0)
+
+
 @pytest.mark.parametrize("tag", ["gauss", "t"])
 def test_update_prop_rb_golden(pmcg, tag):
     """update_prop_rb on a host-built sample (normalised weights) vs the numpy EM."""
