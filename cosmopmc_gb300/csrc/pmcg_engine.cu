@@ -804,6 +804,7 @@ constexpr int kDrawChunks = 8;
 
 struct SimMirror {
   Work w;
+  void *pscratch = nullptr;  // post-processing scratch (allocated on first use)
   cudaStream_t cs = nullptr;             // device-to-host copies of the sample
   cudaEvent_t ev[kDrawChunks] = {};      // range drawn and converted
   cudaEvent_t drawn = nullptr;           // the draw done and its flags saved (before the look-ahead)
@@ -831,6 +832,7 @@ static void mirror_delete(SimMirror *m) {
   if (m->cs) cudaStreamDestroy(m->cs);
   work_free(m->w);
   if (m->mom) cudaFree(m->mom);
+  if (m->pscratch) cudaFree(m->pscratch);
   delete m;
 }
 
@@ -1157,6 +1159,103 @@ extern "C" void pmcg_weighted_moments(pmc_simu *psim, double *mean, double *cov,
             CK(cudaMemcpyAsync(mean, dmean, sizeof(double) * D, cudaMemcpyDeviceToHost, w.s), "mean") &&
             CK(cudaMemcpyAsync(cov, dcov, sizeof(double) * D * D, cudaMemcpyDeviceToHost, w.s), "covariance") &&
             CK(cudaStreamSynchronize(w.s), "moments");
+  (void)ok;
+}
+
+// Normalised weights of the sample on the device (wbar), with the post-processing
+// scratch; false on failure (err set).
+static bool post_setup(SimMirror *m, pmc_simu *psim, error **err) {
+  Work &w = m->w;
+  if (!sync_sample(m, psim, err) || !sync_weights(m, psim, err)) return false;
+  if (!m->pscratch &&
+      !CK(cudaMalloc(&m->pscratch, post_scratch_bytes(w.N) + sizeof(double) * (8 * (size_t)w.D + 64)),
+          "post-processing scratch"))
+    return false;
+  return CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise");
+}
+
+extern "C" void pmcg_weighted_summary(pmc_simu *psim, int use_median, double *center, double *sigma, error **err) {
+  if (!psim || !center || !sigma) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_weighted_summary: null argument");
+    return;
+  }
+  SimMirror *m = mirror_any(psim, err);
+  if (!m || !post_setup(m, psim, err)) return;
+  Work &w = m->w;
+  const int D = w.D;
+  if (!m->mom && !CK(cudaMalloc(&m->mom, sizeof(double) * (moments_scratch_doubles(D) + D + (size_t)D * D)),
+                     "moments scratch"))
+    return;
+  double *dmean = m->mom + moments_scratch_doubles(D), *dcov = dmean + D;
+  // outputs after the sort scratch: centre [D], limits [6D], status [D] (ints)
+  char *tail = reinterpret_cast<char *>(m->pscratch) + post_scratch_bytes(w.N);
+  double *dc = reinterpret_cast<double *>(tail), *ds = dc + D;
+  int *dst = reinterpret_cast<int *>(ds + 6 * D);
+  std::vector<int> st(D);
+  bool ok = CK(launch_moments(w.N, D, w.X64, w.wbar, w.flg, m->mom, dmean, dcov, w.s), "moments") &&
+            CK(launch_post_summary(w.N, D, w.X64, w.wbar, w.flg, dmean, use_median, m->pscratch, dc, ds, dst, w.s),
+               "summary") &&
+            CK(cudaMemcpyAsync(center, dc, sizeof(double) * D, cudaMemcpyDeviceToHost, w.s), "centre") &&
+            CK(cudaMemcpyAsync(sigma, ds, sizeof(double) * 6 * D, cudaMemcpyDeviceToHost, w.s), "limits") &&
+            CK(cudaMemcpyAsync(st.data(), dst, sizeof(int) * D, cudaMemcpyDeviceToHost, w.s), "status") &&
+            CK(cudaStreamSynchronize(w.s), "summary");
+  if (!ok) return;
+  for (int a = 0; a < D; a++)
+    if (st[a] != 0) {
+      set_error(err, PMCG_EARG, __LINE__,
+                st[a] == 1 ? "parameter %d: no counted sample" : "parameter %d: the weights do not reach 1/2", a);
+      return;
+    }
+}
+
+extern "C" void pmcg_weighted_hist1d(pmc_simu *psim, int nbin, const double *min, const double *max, double *hist,
+                                     error **err) {
+  if (!psim || !min || !max || !hist || nbin < 1) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_weighted_hist1d: invalid arguments");
+    return;
+  }
+  for (int a = 0; a < psim->ndim; a++)
+    if (!(max[a] > min[a])) {
+      set_error(err, PMCG_EARG, __LINE__, "histogram range of parameter %d is empty", a);
+      return;
+    }
+  SimMirror *m = mirror_any(psim, err);
+  if (!m || !post_setup(m, psim, err)) return;
+  Work &w = m->w;
+  double *dh = nullptr;
+  if (!CK(cudaMallocAsync(&dh, sizeof(double) * (size_t)nbin * w.D, w.s), "histogram")) return;
+  bool ok = CK(launch_post_hist1d(w.N, w.D, w.X64, w.wbar, w.flg, nbin, min, max, (double)w.N, m->pscratch, dh, w.s),
+               "histograms") &&
+            CK(cudaMemcpyAsync(hist, dh, sizeof(double) * (size_t)nbin * w.D, cudaMemcpyDeviceToHost, w.s),
+               "histograms");
+  cudaFreeAsync(dh, w.s);
+  ok = CK(cudaStreamSynchronize(w.s), "histograms") && ok;
+  (void)ok;
+}
+
+extern "C" void pmcg_weighted_hist2d(pmc_simu *psim, int nbin, int p, int q, const double *min, const double *max,
+                                     double *hist, error **err) {
+  if (!psim || !min || !max || !hist || nbin < 1 || p < 0 || q < 0 || p >= psim->ndim || q >= psim->ndim ||
+      (long long)nbin * nbin >= (1ll << 31)) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_weighted_hist2d: invalid arguments");
+    return;
+  }
+  if (!(max[p] > min[p]) || !(max[q] > min[q])) {
+    set_error(err, PMCG_EARG, __LINE__, "histogram range is empty");
+    return;
+  }
+  SimMirror *m = mirror_any(psim, err);
+  if (!m || !post_setup(m, psim, err)) return;
+  Work &w = m->w;
+  double *dh = nullptr;
+  const size_t nb2 = (size_t)nbin * nbin;
+  if (!CK(cudaMallocAsync(&dh, sizeof(double) * nb2, w.s), "histogram")) return;
+  bool ok = CK(launch_post_hist2d(w.N, w.D, w.X64, w.wbar, w.flg, nbin, p, q, min, max, (double)w.N, m->pscratch, dh,
+                                  w.s),
+               "histogram") &&
+            CK(cudaMemcpyAsync(hist, dh, sizeof(double) * nb2, cudaMemcpyDeviceToHost, w.s), "histogram");
+  cudaFreeAsync(dh, w.s);
+  ok = CK(cudaStreamSynchronize(w.s), "histogram") && ok;
   (void)ok;
 }
 

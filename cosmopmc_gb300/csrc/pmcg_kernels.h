@@ -116,6 +116,21 @@ size_t moments_scratch_doubles(int D);
 cudaError_t launch_moments(size_t N, int D, const double *X, const double *wbar, const short *flg, double *scratch,
                            double *mean_out, double *cov_out, cudaStream_t s);
 
+// Post-processing (k_post.cu): per parameter, sort (value, weight), FP64 scan,
+// then the centre and limits, or the 1-D bin masses; 2-D histograms by joint
+// bin index. scratch: post_scratch_bytes(N) bytes; status[a] 0 ok, 1 no
+// counted sample, 2 weights below 1/2 (median).
+size_t post_scratch_bytes(size_t N);
+cudaError_t launch_post_summary(size_t N, int D, const double *X, const double *wbar, const short *flg,
+                                const double *mean, int use_median, void *scratch, double *center, double *sigma,
+                                int *status, cudaStream_t s);
+cudaError_t launch_post_hist1d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin,
+                               const double *lo, const double *hi, double scale, void *scratch, double *hist,
+                               cudaStream_t s);
+cudaError_t launch_post_hist2d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin,
+                               int p, int q, const double *lo, const double *hi, double scale, void *scratch,
+                               double *hist, cudaStream_t s);
+
 // Convert the mixed-precision sample to FP64 row-major.
 cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
 // Normalised weights wbar = exp(logw - logSum) (0 where flg == 0).

@@ -147,6 +147,9 @@ SIGNATURES = [
                                                    C.POINTER(MixMvdensS), C.c_int, PErr]),
     ("importance_sample", C.c_size_t, [C.POINTER(PmcSimuS), C.c_void_p, C.c_int, PErr]),
     ("pmcg_weighted_moments", None, [C.POINTER(PmcSimuS), _dp, _dp, PErr]),
+    ("pmcg_weighted_summary", None, [C.POINTER(PmcSimuS), C.c_int, _dp, _dp, PErr]),
+    ("pmcg_weighted_hist1d", None, [C.POINTER(PmcSimuS), C.c_int, _dp, _dp, _dp, PErr]),
+    ("pmcg_weighted_hist2d", None, [C.POINTER(PmcSimuS), C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, PErr]),
     ("effective_number_of_components", C.c_double, [C.POINTER(MixMvdensS), PErr]),
     ("init_parabox", C.POINTER(ParaboxS), [C.c_int, PErr]),
     ("add_slab", None, [C.POINTER(ParaboxS), C.c_int, C.c_double, C.c_double, PErr]),
@@ -428,6 +431,29 @@ class PmcSimu:
         mean, cov = np.empty(D), np.empty((D, D))
         call("pmcg_weighted_moments", self.p, _dptr(mean), _dptr(cov))
         return mean, cov
+
+    def weighted_summary(self, median=False):
+        """(centre [D], limits [D, 6]): weighted mean (or median) of every parameter and
+        the one-sided 68.27/95.45/99.73 % limits right then left of it (-1: sample ended)."""
+        D = self.s.ndim
+        center, sigma = np.empty(D), np.empty((D, 6))
+        call("pmcg_weighted_summary", self.p, 1 if median else 0, _dptr(center), _dptr(sigma))
+        return center, sigma
+
+    def weighted_hist1d(self, nbin, lo, hi):
+        """[D, nbin] weighted histograms (normalised weights x nsamples) over [lo, hi]."""
+        D = self.s.ndim
+        lo, hi = _f64(lo), _f64(hi)
+        h = np.empty((D, nbin))
+        call("pmcg_weighted_hist1d", self.p, nbin, _dptr(lo), _dptr(hi), _dptr(h))
+        return h
+
+    def weighted_hist2d(self, nbin, p, q, lo, hi):
+        """[nbin, nbin] weighted histogram of parameters (p, q) over [lo, hi]."""
+        lo, hi = _f64(lo), _f64(hi)
+        h = np.empty((nbin, nbin))
+        call("pmcg_weighted_hist2d", self.p, nbin, p, q, _dptr(lo), _dptr(hi), _dptr(h))
+        return h
 
     def free(self):
         if self.p:

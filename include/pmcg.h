@@ -223,6 +223,27 @@ size_t importance_sample(pmc_simu *psim, const pmcg_posterior *post, int quiet, 
  * weights (normalised on the device; log or linear, as psim->isLog says), as
  * the reference's post-processing computes them (exec/exec_helper.c:63-349). */
 void pmcg_weighted_moments(pmc_simu *psim, double *mean, double *cov, error **err);
+/* Marginal summary of every parameter on the device, as mean_sigma_from_psim
+ * (exec/exec_helper.c:63-120) with median_from_psim and sigma_from_psim
+ * (:160-271): center[i] = weighted mean (use_median = 0) or median, and
+ * sigma[6i .. 6i+5] the one-sided 68.27 / 95.45 / 99.73 % limits to the right
+ * then to the left of it (-1 where the sample ends first), from the normalised
+ * weights of the samples with flg != 0. The reference copies the counted
+ * samples by sample index (tmp[i]) but sorts the first n entries; here the
+ * counted samples are compacted (its intent). A median whose first sample
+ * already carries more than half the weight is that sample's value. */
+void pmcg_weighted_summary(pmc_simu *psim, int use_median, double *center, double *sigma, error **err);
+/* Weighted histograms of the sample, as create_1d_hist / create_2d_hist
+ * (wrappers/src/param.c:1229-1357): the normalised weights times nsamples,
+ * nbin bins per parameter over [min[p], max[p]] (bin j: e_j <= x < e_{j+1},
+ * e_j = min + j (max - min) / nbin, the last bin closed at max; samples
+ * outside or with flg == 0 not counted; the reference's accumulation lives in
+ * pmclib, absent, so this binning is pinned here). hist1d: hist[p*nbin + b];
+ * hist2d for parameters (p, q): hist[bp*nbin + bq]. */
+void pmcg_weighted_hist1d(pmc_simu *psim, int nbin, const double *min, const double *max, double *hist,
+                          error **err);
+void pmcg_weighted_hist2d(pmc_simu *psim, int nbin, int p, int q, const double *min, const double *max,
+                          double *hist, error **err);
 
 /* Precision of the drop-in entry points above: PMCG_FP64 (default, the
  * plain FP64 path) or PMCG_MIXED. */

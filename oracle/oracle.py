@@ -94,6 +94,10 @@ def lib():
                                       C.c_double, C.POINTER(Stats), C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_iterate_mix.restype = C.c_int
         L.orc_num_threads.restype = C.c_int
+        L.orc_weighted_summary.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, _ip]
+        L.orc_hist1d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, C.c_double, _dp]
+        L.orc_hist2d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                 C.c_double, _dp]
         _lib = L
     return _lib
 
@@ -323,3 +327,33 @@ def iterate_mix(prop: Mix, target: Mix, logprior, N, seed, call, beta=1.0, bmin=
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def weighted_summary(X, wbar, flg, median=False):
+    """(centre [D], limits [D, 6], status [D]) of the reference's post-processing."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    center, sigma, st = np.zeros(D), np.zeros((D, 6)), np.zeros(D, dtype=np.int32)
+    lib().orc_weighted_summary(N, D, X, np.ascontiguousarray(wbar, dtype=np.float64),
+                               np.ascontiguousarray(flg, dtype=np.int16), 1 if median else 0, center, sigma, st)
+    return center, sigma, st
+
+
+def hist1d(X, wbar, flg, nbin, lo, hi, scale):
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    h = np.zeros((D, nbin))
+    lib().orc_hist1d(N, D, X, np.ascontiguousarray(wbar, dtype=np.float64), np.ascontiguousarray(flg, dtype=np.int16),
+                     nbin, np.ascontiguousarray(lo, dtype=np.float64), np.ascontiguousarray(hi, dtype=np.float64),
+                     scale, h)
+    return h
+
+
+def hist2d(X, wbar, flg, nbin, p, q, lo, hi, scale):
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    h = np.zeros((nbin, nbin))
+    lib().orc_hist2d(N, D, X, np.ascontiguousarray(wbar, dtype=np.float64), np.ascontiguousarray(flg, dtype=np.int16),
+                     nbin, p, q, np.ascontiguousarray(lo, dtype=np.float64), np.ascontiguousarray(hi, dtype=np.float64),
+                     scale, h)
+    return h

@@ -606,3 +606,100 @@ out:
   free(wbar); free(cw); free(dead);
   return rc;
 }
+
+/* ------------------------------------------------------------------ post-processing
+ * Marginal summaries and histograms of a weighted sample, following
+ * exec/exec_helper.c:63-271 (mean_sigma_from_psim, median_from_psim,
+ * sigma_from_psim) with the counted samples compacted (the reference copies
+ * them to tmp[i] by sample index but sorts the first n entries), the scan
+ * for imean capped at the last sample, and a median whose first sample carries
+ * more than half of the weight taken as that sample; and the weighted
+ * histograms of wrappers/src/param.c:1229-1357 with the binning pinned in
+ * include/pmcg.h (pmclib's accumulation is absent). Sequential sums in the
+ * reference's order. */
+typedef struct { double par, w; } orc_pw;
+static int orc_pw_cmp(const void *a, const void *b) {
+  const double x = ((const orc_pw *)a)->par, y = ((const orc_pw *)b)->par;
+  return (x < y) ? -1 : (x > y);
+}
+
+/* status[a]: 0 ok, 1 no counted sample, 2 the weights do not reach 1/2 */
+void orc_weighted_summary(size_t N, int D, const double *X, const double *wbar, const short *flg, int use_median,
+                          double *center, double *sigma, int *status) {
+  const double conf[3] = {0.682689492137085897 / 2.0, 0.954499736103641585 / 2.0, 0.997300203936739810 / 2.0};
+  orc_pw *t = (orc_pw *)malloc(sizeof(orc_pw) * (N ? N : 1));
+  for (int a = 0; a < D; a++) {
+    size_t n = 0;
+    double mean = 0.0;
+    for (size_t i = 0; i < N; i++) {
+      if (flg[i] == 0) continue;
+      mean += wbar[i] * X[i * D + a];
+      t[n].par = X[i * D + a];
+      t[n].w = wbar[i];
+      n++;
+    }
+    status[a] = 0;
+    if (n == 0) { status[a] = 1; continue; }
+    qsort(t, n, sizeof(orc_pw), orc_pw_cmp);
+    double c = mean;
+    if (use_median) {
+      double m = 0.0;
+      size_t i;
+      for (i = 0; i < n; i++) {
+        m += t[i].w;
+        if (m == 0.5) { c = t[i].par; break; }
+        if (m > 0.5) { c = (i == 0) ? t[0].par : 0.5 * (t[i].par + t[i - 1].par); break; }
+      }
+      if (i == n) { status[a] = 2; continue; }
+    }
+    size_t imean = 0;
+    while (t[imean].par < c && imean < n - 1) imean++;
+    for (int j = 0; j < 3; j++) {
+      double sum = 0.0;
+      size_t i = imean;
+      while (sum <= conf[j] && i < n) { sum += t[i].w; i++; }
+      sigma[6 * a + j] = (i == n) ? -1.0 : t[i].par - c;
+    }
+    for (int j = 0; j < 3; j++) {
+      double sum = 0.0;
+      long long i = (long long)imean - 1;
+      while (sum <= conf[j] && i >= 0) { sum += t[i].w; i--; }
+      sigma[6 * a + 3 + j] = (i == -1) ? -1.0 : c - t[i].par;
+    }
+    center[a] = c;
+  }
+  free(t);
+}
+
+static double orc_edge(double lo, double hi, int nbin, int j) {
+  return (j == nbin) ? hi : lo + (hi - lo) * (double)j / (double)nbin;
+}
+static int orc_bin(double x, double lo, double hi, int nbin) {
+  if (!(x >= lo && x <= hi)) return -1;
+  int j = (int)floor((x - lo) / (hi - lo) * (double)nbin);
+  j = j < 0 ? 0 : (j > nbin - 1 ? nbin - 1 : j);
+  if (x < orc_edge(lo, hi, nbin, j)) j--;
+  else if (j < nbin - 1 && x >= orc_edge(lo, hi, nbin, j + 1)) j++;
+  return j;
+}
+
+void orc_hist1d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin, const double *lo,
+                const double *hi, double scale, double *hist) {
+  memset(hist, 0, sizeof(double) * (size_t)D * nbin);
+  for (int a = 0; a < D; a++)
+    for (size_t i = 0; i < N; i++) {
+      if (!flg[i]) continue;
+      const int b = orc_bin(X[i * D + a], lo[a], hi[a], nbin);
+      if (b >= 0) hist[(size_t)a * nbin + b] += wbar[i] * scale;
+    }
+}
+
+void orc_hist2d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin, int p, int q,
+                const double *lo, const double *hi, double scale, double *hist) {
+  memset(hist, 0, sizeof(double) * (size_t)nbin * nbin);
+  for (size_t i = 0; i < N; i++) {
+    if (!flg[i]) continue;
+    const int bp = orc_bin(X[i * D + p], lo[p], hi[p], nbin), bq = orc_bin(X[i * D + q], lo[q], hi[q], nbin);
+    if (bp >= 0 && bq >= 0) hist[(size_t)bp * nbin + bq] += wbar[i] * scale;
+  }
+}

@@ -95,7 +95,19 @@ int orc_iterate_mix(int K, int D, int df, double *w, double *mu, double *L, doub
 
 int orc_num_threads(void);
 
+/* Post-processing: marginal centre (mean or median) and one-sided 68.27 /
+ * 95.45 / 99.73 % limits per parameter (sigma[6a .. 6a+5]: right, then left),
+ * and weighted histograms (exec/exec_helper.c:63-271,
+ * wrappers/src/param.c:1229-1357). */
+void orc_weighted_summary(size_t N, int D, const double *X, const double *wbar, const short *flg, int use_median,
+                          double *center, double *sigma, int *status);
+void orc_hist1d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin, const double *lo,
+                const double *hi, double scale, double *hist);
+void orc_hist2d(size_t N, int D, const double *X, const double *wbar, const short *flg, int nbin, int p, int q,
+                const double *lo, const double *hi, double scale, double *hist);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif
