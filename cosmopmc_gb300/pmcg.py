@@ -180,6 +180,9 @@ SIGNATURES = [
     ("pmcg_posterior_add_snia", None, [C.c_void_p, C.POINTER(SnData), PErr]),
     ("pmcg_posterior_add_template", None, [C.c_void_p, C.c_int, _dp, _dp, _dp, PErr]),
     ("pmcg_posterior_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
+    ("pmcg_fisher_matrix", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _dp, PErr]),
+    ("pmcg_fisher_proposal", None, [C.POINTER(MixMvdensS), _dp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
+                                    C.POINTER(RngS), PErr]),
     ("pmcg_posterior_log_pdf_batch", None, [C.c_void_p, C.c_size_t, _dp, _dp, C.POINTER(C.c_short), C.c_int,
                                             C.c_int, C.c_void_p, PErr]),
     ("pmcg_mix_log_pdf_batch", None, [C.POINTER(MixMvdensS), C.c_size_t, _dp, _dp, _dp, C.c_int, PErr]),
@@ -497,6 +500,15 @@ class Posterior:
         call("pmcg_posterior_add_mixmvdens", self.p, target.p)
         return self
 
+    def fisher(self, pos, bmin, bmax, diag_only=False, force_positive=False, with_positive=False):
+        """Fisher matrix -d^2 log P at pos (central differences, steps 0.001 (bmax - bmin)).
+        with_positive: also return whether F is positive definite."""
+        pos, bmin, bmax = _f64(pos), _f64(bmin), _f64(bmax)
+        F = np.empty((self.npar, self.npar))
+        pd = call("pmcg_fisher_matrix", self.p, _dptr(pos), _dptr(bmin), _dptr(bmax), int(diag_only),
+                  int(force_positive), _dptr(F))
+        return (F, bool(pd == 1)) if with_positive else F
+
     def add_snia(self, sn: dict):
         s = SnData()
         arrs = {k: _f64(sn[k]) for k in ("z", "mB", "x1", "c", "cov6")}
@@ -746,3 +758,14 @@ def set_tensor_cores(on):
 
 def device_count():
     return load().pmcg_device_count()
+
+
+FISHER_RSHIFT, FISHER_EIGEN = 0, 1
+
+
+def fisher_proposal(prop: MixMvdens, F, pos, bmin, bmax, kind=FISHER_EIGEN, fshift=0.1, fvar=1.0, rng=None):
+    """Fill prop (means, covariances fvar F^-1, equal weights) from a Fisher matrix."""
+    F, pos, bmin, bmax = _f64(F), _f64(pos), _f64(bmin), _f64(bmax)
+    call("pmcg_fisher_proposal", prop.p, _dptr(F), _dptr(pos), _dptr(bmin), _dptr(bmax), kind, fshift, fvar,
+         rng.p if rng is not None else None)
+    return prop

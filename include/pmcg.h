@@ -316,6 +316,34 @@ double pmcg_posterior_log_pdf_void(void *post, const double *x, error **err);
 void pmcg_posterior_log_pdf_batch(const pmcg_posterior *p, size_t N, const double *X, double *logpost,
                                   short *flg, int on_device, int precision, void *stream, error **err);
 
+/* Fisher matrix F[a*npar + b] = -d^2 log P / d theta_a d theta_b of a posterior
+ * at pos, by the reference's central differences (exec/go_fishing.c:37-86):
+ * steps h = fh (max - min) with fh = 0.001 (exec/mkmax.h:33), four points per
+ * element (the diagonal from f(+2h) - 2 f(0) + f(-2h)); every stencil point of
+ * the matrix is evaluated in one batched FP64 device call. Every point must lie
+ * in the prior box and pass the likelihood (else PMCG_EARG).
+ * diag_only: the diagonal alone, off-diagonal elements 0 (the 'Fisher_diag'
+ * initial type, exec/go_fishing.c:100,134). force_positive: afterwards |F_aa|
+ * on the diagonal and 0 off it (go_fishing's -f, force_positive, :248-260).
+ * Returns 1 when F is positive definite (a Cholesky decomposition succeeds, the
+ * test at :433-446), 0 when it is not (F is still written), -1 on error. */
+int pmcg_fisher_matrix(const pmcg_posterior *post, const double *pos, const double *min, const double *max,
+                       int diag_only, int force_positive, double *F, error **err);
+/* Initial proposal from a Fisher matrix F at pos, as
+ * read_initial_proposal_from_config (wrappers/src/param.c:511-625): equal
+ * weights, covariances fvar F^-1 (stored in comp->std with chol = 0: decompose
+ * with mix_mvdens_cholesky_decomp), means
+ *  PMCG_FISHER_RSHIFT: pos shifted per parameter by a uniform draw in
+ *    [-fshift (max-min), +fshift (max-min)], redrawn until inside [min, max]
+ *    (comp_shift_mean, :472-489; the draws come from rng, one call);
+ *  PMCG_FISHER_EIGEN: pos - r, pos + r with r = fshift (lambda_i / lambda_max) e_i
+ *    along the eigenvectors of F^-1, largest eigenvalue first (at most 2 npar
+ *    components). */
+#define PMCG_FISHER_RSHIFT 0
+#define PMCG_FISHER_EIGEN 1
+void pmcg_fisher_proposal(mix_mvdens *proposal, const double *F, const double *pos, const double *min,
+                          const double *max, int type, double fshift, double fvar, pmcg_rng *rng, error **err);
+
 /* Batched mixture log-density of N points (host pointers); lt (optional,
  * [ncomp x N]) receives log(alpha_k) + log f_k(x_n). */
 void pmcg_mix_log_pdf_batch(const mix_mvdens *m, size_t N, const double *X, double *logq, double *lt,

@@ -145,3 +145,72 @@ def test_weighted_histograms_match_oracle(pmcg, oracle):
     h2 = ps.weighted_hist2d(25, 0, 2, lo, hi)
     h2_ref = oracle.hist2d(X, wbar, flg, 25, 0, 2, lo, hi, float(N))
     np.testing.assert_allclose(h2, h2_ref, rtol=1e-9, atol=1e-9)
+
+
+def test_fisher_matrix_of_a_gaussian_posterior(pmcg):
+    """log P quadratic: the central differences give the precision matrix up to rounding;
+    all stencil points in one batched device evaluation."""
+    D = 5
+    rng = np.random.default_rng(9)
+    A = rng.normal(size=(D, D))
+    cov = A @ A.T + np.eye(D)
+    mu = rng.normal(size=D)
+    lo, hi = mu - 20.0, mu + 20.0
+    target = pmcg.MixMvdens.from_arrays([1.0], mu[None, :], cov=cov[None], df=-1).cholesky()
+    post = pmcg.Posterior(D, lo, hi).add_mix(target)
+    F = post.fisher(mu + 0.3, lo, hi)
+    np.testing.assert_allclose(F, np.linalg.inv(cov), rtol=1e-6, atol=1e-8)
+    np.testing.assert_array_equal(F, F.T)
+
+
+def sn_fisher_oracle(oracle, sn, pos, lo, hi):
+    """The reference's central differences (exec/go_fishing.c:37-86) on the
+    oracle's FP64 SN log-likelihood (the flat prior cancels in the stencil)."""
+    D = len(pos)
+    h = 1e-3 * (hi - lo)
+    sg = [(1, 1), (1, -1), (-1, 1), (-1, -1)]
+    pts = []
+    for a in range(D):
+        for b in range(a + 1):
+            for sa, sb in sg:
+                x = pos.copy()
+                x[a] += sa * h[a]
+                x[b] += sb * h[b]
+                pts.append(x)
+    f, ok = oracle.sn_loglike(sn, np.array(pts))
+    assert np.all(ok == 1)
+    F = np.zeros((D, D))
+    e = 0
+    for a in range(D):
+        for b in range(a + 1):
+            v = f[4 * e:4 * e + 4]
+            F[a, b] = F[b, a] = -(v[0] - v[1] - v[2] + v[3]) / (4 * h[a] * h[b])
+            e += 1
+    return F
+
+
+def test_fisher_start_for_the_sn_posterior(pmcg, oracle):
+    """SN posterior at the generating cosmology: the device Fisher matrix against the
+    oracle's; the positiveness verdict; the diagonal-only and force-positive forms;
+    an eigen-rule proposal from the latter inside the prior box."""
+    wl = W.sn_workload()
+    lo, hi = wl["bmin"], wl["bmax"]
+    post = pmcg.Posterior(6, lo, hi).add_snia(wl["sn"])
+    pos = W.SN_TRUTH.copy()
+    F, pd = post.fisher(pos, lo, hi, with_positive=True)
+    F_ref = sn_fisher_oracle(oracle, wl["sn"], pos, lo, hi)
+    scale = np.sqrt(np.outer(np.abs(np.diag(F_ref)), np.abs(np.diag(F_ref))))
+    assert np.max(np.abs(F - F_ref) / scale) < 1e-5
+    np.testing.assert_array_equal(F, F.T)
+    assert pd == bool(np.all(np.linalg.eigvalsh(F) > 0))
+    Fd, pdd = post.fisher(pos, lo, hi, diag_only=True, with_positive=True)
+    np.testing.assert_array_equal(np.diag(Fd), np.diag(F))
+    assert np.count_nonzero(Fd - np.diag(np.diag(Fd))) == 0
+    assert pdd == bool(np.all(np.diag(F) > 0))
+    Fp, pdp = post.fisher(pos, lo, hi, force_positive=True, with_positive=True)
+    np.testing.assert_array_equal(Fp, np.diag(np.abs(np.diag(F))))
+    assert pdp
+    prop = pmcg.fisher_proposal(pmcg.MixMvdens(10, 6), Fp, pos, lo, hi,
+                                kind=pmcg.FISHER_EIGEN, fshift=0.1, fvar=1.0)
+    _, mu, _ = prop.arrays()
+    assert np.all(mu >= lo) and np.all(mu <= hi)
