@@ -119,7 +119,74 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 200 ms"}
+
+
+class NvmlSampler:
+    """Reads the SM clock, its maximum and the clock-event reasons every 5 ms
+    through the driver's NVML library (ctypes; read-only queries), so a timed
+    region of a few tens of milliseconds still gets samples."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_slowdown"}
+
+    def __init__(self, index):
+        import ctypes as C
+        self.C = C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        cnt = C.c_uint(0)
+        lib.nvmlDeviceGetCount_v2(C.byref(cnt))
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v for v in vis.split(",") if v.strip()]
+        if cnt.value == 1:
+            idx = 0
+        elif ids and all(v.strip().isdigit() for v in ids) and index < len(ids):
+            idx = int(ids[index])
+        else:
+            idx = index
+        self.h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(idx, C.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.lib = lib
+        self.samples = []
+        self.stop_ev = threading.Event()
+
+    def _run(self):
+        C = self.C
+        clk, mx, rs = C.c_uint(0), C.c_uint(0), C.c_ulonglong(0)
+        while not self.stop_ev.is_set():
+            if (self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) == 0 and
+                    self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx)) == 0 and
+                    self.reasons_fn(self.h, C.byref(rs)) == 0):
+                self.samples.append((clk.value, mx.value, rs.value))
+            time.sleep(0.005)
+
+    def start(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        self.stop_ev.set()
+        self.t.join(timeout=2)
+        sm = [a for a, _, _ in self.samples]
+        reasons = set()
+        for _, _, r in self.samples:
+            for bit, nm in self.REASONS.items():
+                if r & bit:
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(b for _, b, _ in self.samples) if sm else None,
+                "reasons": sorted(reasons), "samples": len(sm), "source": "NVML, 5 ms"}
+
+
+def clock_sampler(index):
+    try:
+        return NvmlSampler(index)
+    except (OSError, AttributeError):
+        return ClockSampler(index)
 
 
 # ----------------------------------------------------------------- workload
@@ -442,7 +509,7 @@ def main():
     # ---------------- mixed-precision engine (the headline)
     run = P.Run(prop, post, N, precision=P.MIXED, seed=1000 + rank)
     barrier()
-    clk = ClockSampler(local)
+    clk = clock_sampler(local)
     clk.start()
     stats, step_ms, stage_ms, launches, wall = time_run(P, run, args.steps, args.warmup, l2buf, sync, prop)
     clocks = clk.stop()

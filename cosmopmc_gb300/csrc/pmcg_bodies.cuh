@@ -951,7 +951,7 @@ __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t 
   const int Dp = ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, G = threads / NB;
   const int T = em_tile_rows(Dp);
   *tile_bytes = (size_t)(Dp * Dp + Dp + T * Da + T * (Dp + 1) + 3 * em_list_buf(Dp) + 40) * sizeof(float);
-  *red_bytes = (size_t)G * NB * 16 * sizeof(double);
+  *red_bytes = (size_t)G * NB * 16 * sizeof(float2);
 }
 
 // Statistics of component k over sample chunk s, accumulated in the component's
@@ -966,7 +966,7 @@ __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t 
 // lengths balance), and accumulated: the augmented rows [a, 1, 1/tau, 0, 0]
 // with weight vt give in the lower triangle of sum vt a a^T: S2 (whitened), S1
 // (row Dp), St (Dp,Dp) and S0 (Dp+1,Dp). Each thread owns one 4x4 block for one
-// sample group; FP32 sums are flushed into FP64 every kFlushTiles tiles. The
+// sample group; FP32 sums are flushed into float-float pairs every kFlushTiles tiles. The
 // order of every sum depends only on the run's own data (deterministic).
 // mask (optional): bit j of word mask[k * W + w] set iff sample 32 w + j is
 // listed for component k (em_mask_kernel). With a mask the block walks 32-sample
@@ -1004,10 +1004,12 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   int bi = 0;
   while ((bi + 1) * (bi + 2) / 2 <= blk) bi++;
   const int bj = blk - bi * (bi + 1) / 2;
-  float acc[16];
-  double acc64[16];
+  // per-tile FP32 sums acc; every flush adds them exactly (TwoSum) into a
+  // float-float pair (chi, clo): FP32 instructions only, where an FP64 add costs
+  // a warp-wide pass of the narrow FP64 pipe
+  float acc[16], chi[16], clo[16];
 #pragma unroll
-  for (int e = 0; e < 16; e++) { acc[e] = 0.f; acc64[e] = 0.0; }
+  for (int e = 0; e < 16; e++) { acc[e] = 0.f; chi[e] = 0.f; clo[e] = 0.f; }
   int tiles = 0;
 
   // Accumulate listed entries [0, nt) (nt <= T).
@@ -1062,7 +1064,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
     if (++tiles == flush_tiles) {
       tiles = 0;
 #pragma unroll
-      for (int e = 0; e < 16; e++) { acc64[e] += (double)acc[e]; acc[e] = 0.f; }
+      for (int e = 0; e < 16; e++) { ff_add(chi[e], clo[e], acc[e], 0.f); acc[e] = 0.f; }
     }
     __syncthreads();
   };
@@ -1172,24 +1174,31 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   }
   if (fill > 0) process(fill);
 #pragma unroll
-  for (int e = 0; e < 16; e++) acc64[e] += (double)acc[e];
+  for (int e = 0; e < 16; e++) ff_add(chi[e], clo[e], acc[e], 0.f);
   __syncthreads();
-  double *red = reinterpret_cast<double *>(smem);
+  // entry-major [16][G][NB] pairs: for each entry a warp writes consecutive
+  // words (grp * NB + blk == tid)
+  float2 *red = reinterpret_cast<float2 *>(smem);
   if (active) {
 #pragma unroll
-    for (int e = 0; e < 16; e++) red[((size_t)grp * NB + blk) * 16 + e] = acc64[e];
+    for (int e = 0; e < 16; e++) red[((size_t)e * G + grp) * NB + blk] = make_float2(chi[e], clo[e]);
   }
   __syncthreads();
   double *out = part + ((size_t)k * S + s) * E;
-  // one (block, entry) per thread: the sum over the G groups in a fixed order
+  // one (block, entry) per thread: the float-float sum over the G groups in a
+  // fixed order, then one exact conversion (hi + lo spans at most 48 bits)
   for (int be = tid; be < NB * 16; be += blockDim.x) {
-    const int b = be >> 4, e = be & 15;
+    const int e = be / NB, b = be - e * NB;
     int rbi = 0;
     while ((rbi + 1) * (rbi + 2) / 2 <= b) rbi++;
     const int rbj = b - rbi * (rbi + 1) / 2;
     {
-      double t = red[(size_t)b * 16 + e];
-      for (int g = 1; g < G; g++) t += red[((size_t)g * NB + b) * 16 + e];
+      float2 v = red[(size_t)e * G * NB + b];
+      for (int g = 1; g < G; g++) {
+        const float2 u = red[((size_t)e * G + g) * NB + b];
+        ff_add(v.x, v.y, u.x, u.y);
+      }
+      const double t = (double)v.x + (double)v.y;
       const int r = 4 * rbi + e / 4, c = 4 * rbj + e % 4;
       if (r < D && c <= r) out[2 + D + tri_idx(r, c)] = t;
       else if (r == Dp && c < D) out[2 + c] = t;
@@ -1300,9 +1309,11 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   auto pivot = [&](int j) {
     double d = C[j * D + j];
     if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
-    const double pv = sqrt(d);
-    C[j * D + j] = pv;
-    rp[j] = 1.0 / pv;
+    // one reciprocal square root for both the pivot and its inverse: the FP64
+    // pipe is narrow and this chain runs on one thread between barriers
+    const double r = rsqrt(d);
+    C[j * D + j] = d * r;
+    rp[j] = r;
   };
   if (threadIdx.x == 0) pivot(0);
   __syncthreads();
