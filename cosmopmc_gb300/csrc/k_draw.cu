@@ -164,8 +164,10 @@ __global__ void __launch_bounds__(256) draw_bucket_kernel(size_t n0, size_t n1, 
 // shared memory (loads issued before the normals, so their latency overlaps
 // the generator) and warps whose samples all belong to it read them there;
 // any other warp reads its components from global memory.
+// D <= 32: eight resident blocks (64 registers, a few spilled; measured 4%
+// faster than six blocks at 74 registers); wider rows would spill heavily.
 template <int MAXD>
-__global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cnt, uint32_t key0, uint32_t key1,
+__global__ void __launch_bounds__(128, MAXD <= 32 ? 8 : 1) draw_apply_kernel(DevMixView m, size_t cnt, uint32_t key0, uint32_t key1,
                                                          uint32_t call, const uint32_t *callp,
                                                          const double *__restrict__ bmin,
                                                          const double *__restrict__ bmax,
@@ -193,21 +195,10 @@ __global__ void __launch_bounds__(128) draw_apply_kernel(DevMixView m, size_t cn
   const bool staged = __all_sync(0xffffffffu, k == kb);
   if (!live) return;
   const float sc = (df > 0) ? student_scale<float>(df, c2) : 1.f;
-  float x[MAXD];
-  const int in = staged ? draw_transform_rows<MAXD, true>(D, ldx, sL, sL + MAXD * MAXD, z, sc, bmin, bmax, x, 1)
-                        : draw_transform_f32<MAXD>(m, k, z, sc, bmin, bmax, x, 1);
   float *row = X32 + n * ldx;
-#pragma unroll
-  for (int j4 = 0; j4 < MAXD / 4; j4++) {
-    if (4 * j4 < ldx) {
-      float4 v;
-      v.x = (4 * j4 < D) ? x[4 * j4] : 0.f;
-      v.y = (4 * j4 + 1 < D) ? x[4 * j4 + 1] : 0.f;
-      v.z = (4 * j4 + 2 < D) ? x[4 * j4 + 2] : 0.f;
-      v.w = (4 * j4 + 3 < D) ? x[4 * j4 + 3] : 0.f;
-      *reinterpret_cast<float4 *>(row + 4 * j4) = v;
-    }
-  }
+  const int in = staged ? draw_transform_store<MAXD, true>(D, ldx, sL, sL + MAXD * MAXD, z, sc, bmin, bmax, row)
+                        : draw_transform_store<MAXD, false>(D, ldx, m.L32 + (size_t)k * D * ldx,
+                                                            m.mu32 + (size_t)k * D, z, sc, bmin, bmax, row);
   flg[n] = (short)in;
 }
 

@@ -151,6 +151,44 @@ __device__ __forceinline__ int draw_transform_rows(int D, int ldx, const float *
   }
   return in;
 }
+// The same rows as draw_transform_rows, stored to the sample's row (ldx
+// floats, zero padded) four at a time as each group of four is complete, so
+// no finished row stays in registers (the draw kernel's occupancy is set by
+// its registers).
+template <int MAXD, bool SHARED>
+__device__ __forceinline__ int draw_transform_store(int D, int ldx, const float *Lk, const float *mk,
+                                                    const float (&z)[MAXD], float sc, const double *__restrict__ bmin,
+                                                    const double *__restrict__ bmax, float *__restrict__ row) {
+  int in = 1;
+#pragma unroll
+  for (int i4 = 0; i4 < MAXD / 4; i4++) {
+    if (4 * i4 < ldx) {
+      float xv[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const int i = 4 * i4 + r;
+        xv[r] = 0.f;
+        if (i < D) {
+          float acc = 0.f;
+#pragma unroll
+          for (int j4 = 0; j4 <= i / 4; j4++) {
+            const float4 *q = reinterpret_cast<const float4 *>(Lk + (size_t)i * ldx + 4 * j4);
+            const float4 l4 = SHARED ? *q : __ldg(q);
+            acc = fmaf(l4.x, z[4 * j4], acc);
+            acc = fmaf(l4.y, z[4 * j4 + 1], acc);
+            acc = fmaf(l4.z, z[4 * j4 + 2], acc);
+            acc = fmaf(l4.w, z[4 * j4 + 3], acc);
+          }
+          const float xi = (SHARED ? mk[i] : __ldg(&mk[i])) + sc * acc;
+          xv[r] = xi;
+          if (bmin && ((double)xi < bmin[i] || (double)xi > bmax[i])) in = 0;
+        }
+      }
+      *reinterpret_cast<float4 *>(row + 4 * i4) = make_float4(xv[0], xv[1], xv[2], xv[3]);
+    }
+  }
+  return in;
+}
 template <int MAXD>
 __device__ __forceinline__ int draw_transform_f32(const DevMixView &m, int k, const float (&z)[MAXD], float sc,
                                                   const double *__restrict__ bmin, const double *__restrict__ bmax,
@@ -892,15 +930,65 @@ __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const d
   if (threadIdx.x == 0) part[tile] = a;
 }
 
-// Merge the nb tile records of one sample (strided per thread, then a fixed
-// tree) and derive logSum, evidence, perplexity and ESS.
+// Merge the nb tile records of one sample and derive logSum, evidence,
+// perplexity and ESS. The largest tile maximum M comes first (order keys,
+// integer compares); every record is then rescaled once to M (s e, t e, q e^2
+// with e = e^{m_b - M}) and s, t, q, n are plain sums, per thread strided,
+// then in a fixed tree: one exponential per record instead of two per merge,
+// and no exponential on the tree's dependent path. s_r: 8 records of shared
+// scratch (blockDim.x <= 256).
 template <bool FAST = false>
 __device__ __forceinline__ void body_weights_final(int nb, const WRed *__restrict__ part, size_t N, DevStats *st,
                                                    WRed *s_r) {
-  WRed a = wred_empty();
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) a = wred_merge<FAST>(a, part[b]);
-  a = block_wred<FAST>(a, s_r);
+  unsigned long long *skey = reinterpret_cast<unsigned long long *>(s_r);  // [8]
+  double *ssum = reinterpret_cast<double *>(s_r) + 8;                      // [8][4]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned long long km = 0ull;  // below the key of every value, -inf included
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const unsigned long long kb = dkey(part[b].m);
+    km = kb > km ? kb : km;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, km, o);
+    km = v > km ? v : km;
+  }
+  if (lane == 0) skey[warp] = km;
+  __syncthreads();
+  km = 0ull;
+  for (int w = 0; w < nw; w++) km = skey[w] > km ? skey[w] : km;
+  const double M = dkey_value(km);
+  double s = 0.0, t = 0.0, q = 0.0, n = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const WRed r = part[b];
+    n += r.n;
+    if (r.m == -INFINITY) continue;
+    const double e = FAST ? (double)expf((float)(r.m - M)) : exp(r.m - M);
+    s = fma(r.s, e, s);
+    t = fma(r.t, e, t);
+    q = fma(r.q * e, e, q);
+  }
+  s = warp_sum(s);
+  t = warp_sum(t);
+  q = warp_sum(q);
+  n = warp_sum(n);
+  if (lane == 0) {
+    ssum[4 * warp] = s;
+    ssum[4 * warp + 1] = t;
+    ssum[4 * warp + 2] = q;
+    ssum[4 * warp + 3] = n;
+  }
+  __syncthreads();
   if (threadIdx.x != 0) return;
+  WRed a;
+  a.m = M;
+  a.s = a.t = a.q = a.n = 0.0;
+  for (int w = 0; w < nw; w++) {
+    a.s += ssum[4 * w];
+    a.t += ssum[4 * w + 1];
+    a.q += ssum[4 * w + 2];
+    a.n += ssum[4 * w + 3];
+  }
   if (a.n == 0.0 || a.m == -INFINITY) {
     st->status = -9011;  // PMCG_ENOWEIGHT
     st->nok = 0.0;
