@@ -851,15 +851,30 @@ __device__ __forceinline__ void body_weights_tile(size_t N, double beta, const d
   if constexpr (FAST) {
     constexpr int PER = kTileW / 256;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double l[PER];
+    double l[PER], lq[PER];
+    short fl[PER];
     unsigned long long mk = 0ull;
+    // every load first (in bounds for n < N; values of unflagged samples are
+    // not used), so a thread waits for one round of loads, not one per sample
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const size_t n = base + threadIdx.x + (size_t)j * 256;
+      fl[j] = 0;
+      l[j] = 0.0;
+      lq[j] = 0.0;
+      if (n < N) {
+        fl[j] = flg[n];
+        l[j] = logpost[n];
+        if (logq) lq[j] = logq[n];
+      }
+    }
 #pragma unroll
     for (int j = 0; j < PER; j++) {
       const size_t n = base + threadIdx.x + (size_t)j * 256;
       double v = -INFINITY;
       if (n < N) {
-        if (flg[n]) {
-          v = beta * logpost[n] - (logq ? logq[n] : 0.0);
+        if (fl[j]) {
+          v = beta * l[j] - lq[j];
           if (!isfinite(v)) { v = -INFINITY; flg[n] = 0; }
         }
         logw[n] = v;
@@ -1200,7 +1215,10 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
         tot += cw;
       }
       const int pos = off + incl - c;   // position of this word's first entry in this pass
-      // emit in rounds that fit the list buffer, processing full tiles in between
+      // emit in rounds that fit the list buffer, processing full tiles in
+      // between: a word's entries are listed by index alone, then the new
+      // entries' weights are read one entry per thread (a dense word would
+      // otherwise wait for its up to 32 entries' loads one after another)
       for (int done = 0; done < tot;) {
         const int take = min(LB - fill, tot - done);
         uint32_t b = bits;
@@ -1208,17 +1226,17 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
         while (b) {
           const int j = __ffs(b) - 1;
           b &= b - 1u;
-          if (p >= done && p < done + take) {
-            const size_t n = wi * 32 + j;
-            const float e = aw[n] + lt[(size_t)k * N + n];
-            const float v = expf(e);
-            const float it = (m.df > 0) ? (nu + Qv[(size_t)k * N + n]) * rnd : 1.f;
-            const int q = fill + p - done;
-            lidx[q] = (int)(n - n0);
-            lvt[q] = v / it;
-            ltau[q] = it;
-          }
+          if (p >= done && p < done + take) lidx[fill + p - done] = (int)(wi * 32 + j - n0);
           p++;
+        }
+        __syncthreads();
+        for (int q = fill + tid; q < fill + take; q += blockDim.x) {
+          const size_t n = n0 + (size_t)lidx[q];
+          const float e = aw[n] + lt[(size_t)k * N + n];
+          const float v = expf(e);
+          const float it = (m.df > 0) ? (nu + Qv[(size_t)k * N + n]) * rnd : 1.f;
+          lvt[q] = v / it;
+          ltau[q] = it;
         }
         fill += take;
         done += take;
