@@ -15,20 +15,26 @@
 
 namespace pmcg {
 
-template <bool F32>
+template <bool F32, bool BATCH>
 __global__ void __launch_bounds__(128) sn_kernel(SnDev sn, size_t N, int D, const double *__restrict__ X64,
                                                  const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
                                                  short *__restrict__ flg) {
   const size_t n = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  body_sn<F32>(sn, N, D, X64, X32, ldx, logpost, flg, n, 0, 0.0);
+  body_sn<F32, BATCH>(sn, N, D, X64, X32, ldx, logpost, flg, n, 0, 0.0);
 }
+
+// Single precision below 2^16 samples (a few waves of warps): loads batched
+// ahead of use (measured at N = 10^4: 60.5 -> 51.6 us); above, the form with
+// fewer registers (measured at N = 2^18: 0.85 -> 0.76 ms per iteration).
+constexpr size_t kSnBatchBelow = (size_t)1 << 16;
 
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
                       int ldx, double *logpost, short *flg, cudaStream_t s) {
   if (N == 0) return cudaSuccess;
   unsigned grid = (unsigned)((N + 3) / 4);
-  if (precision == 0) sn_kernel<false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
-  else sn_kernel<true><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
+  if (precision == 0) sn_kernel<false, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
+  else if (N < kSnBatchBelow) sn_kernel<true, true><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
+  else sn_kernel<true, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
   return cudaGetLastError();
 }
 

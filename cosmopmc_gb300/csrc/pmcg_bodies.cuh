@@ -493,6 +493,11 @@ __device__ __forceinline__ float sk_series_f(float ok, float I, int &bad) {
 // planes indexed by supernova, so each warp load is 512 contiguous bytes.
 // The marginalised mode uses residuals without M, shift-invariant in
 // A - B^2/C.
+// BATCH: each block's loads are issued before their first use (more registers:
+// for small samples, where few warps per SM leave the load latency exposed);
+// otherwise each node is loaded as it is used (fewer registers, more resident
+// warps: for large samples). Both give the same values.
+template <bool BATCH = false>
 __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const float *__restrict__ X32, int ldx,
                                             double *__restrict__ logpost, short *__restrict__ flg, size_t n,
                                             int assign, double add) {
@@ -520,14 +525,31 @@ __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const flo
     float p = 0.f;
     float4 q0, q1, q2;
     if (i < nsn) {
-      for (int g = 0; g < G; g++) {
+      // BATCH: the supernova planes first, then the nodes four at a time
+      // (in-order accumulation as in the single-node loop)
+      float zl2 = 0.f;
+      if (BATCH) { q0 = p0[i]; q1 = p1[i]; q2 = p2[i]; zl2 = sn.fzl2[i]; }
+      int g = 0;
+      if (BATCH)
+      for (; g + 4 <= G; g += 4) {
+        float4 nd[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) nd[u] = node[(size_t)(g + u) * nsn + i];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const float e2 = fmaf(omf, nd[u].x, fmaf(okf, nd[u].y, odef * ex2_approx(exf * nd[u].z)));
+          bad |= !(e2 > 0.f);
+          p = fmaf(nd[u].w, rsqrt_approx(e2), p);
+        }
+      }
+      for (; g < G; g++) {
         const float4 nd = node[(size_t)g * nsn + i];
         const float e2 = fmaf(omf, nd.x, fmaf(okf, nd.y, odef * ex2_approx(exf * nd.z)));
         bad |= !(e2 > 0.f);
         p = fmaf(nd.w, rsqrt_approx(e2), p);
       }
-      q0 = p0[i]; q1 = p1[i]; q2 = p2[i];
-      const float e2z = fmaf(omf, q2.z, fmaf(okf, q2.w, odef * ex2_approx(exf * sn.fzl2[i])));
+      if (!BATCH) { q0 = p0[i]; q1 = p1[i]; q2 = p2[i]; zl2 = sn.fzl2[i]; }
+      const float e2z = fmaf(omf, q2.z, fmaf(okf, q2.w, odef * ex2_approx(exf * zl2)));
       bad |= !(e2z > 0.f);
     }
 #pragma unroll
@@ -575,12 +597,12 @@ __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const flo
 // One warp per sample n; the cumulative distance integral over redshift-sorted
 // supernovae is a warp prefix scan of per-interval Gauss-Legendre sums.
 // assign != 0: logpost[n] = add + logL; otherwise logpost[n] += logL.
-template <bool F32>
+template <bool F32, bool BATCH = false>
 __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const double *__restrict__ X64,
                                         const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
                                         short *__restrict__ flg, size_t n, int assign, double add) {
   if (F32) {
-    body_sn_f32(sn, N, X32, ldx, logpost, flg, n, assign, add);
+    body_sn_f32<BATCH>(sn, N, X32, ldx, logpost, flg, n, assign, add);
     return;
   }
   const int lane = threadIdx.x & 31;
