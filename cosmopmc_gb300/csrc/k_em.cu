@@ -141,11 +141,15 @@ __global__ void __launch_bounds__(256) em_factor_mask_kernel(size_t N, int K, co
     const size_t wd = n / 32, nl = n < N ? n : N - 1;  // padding lanes read a valid sample
     const float *lp = lt + nl;
     uint32_t *mp = mask + wd;
-#pragma unroll 1
-    for (int k0 = 0; k0 < K; k0 += 16) {  // 16 loads in flight per thread
-      float v[16];
+    // 16 components' loads in flight while the previous 16 are tested
+    float v[16], nv[16];
 #pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = (k0 + j < K) ? __ldg(lp + (size_t)j * N) : 0.f;
+    for (int j = 0; j < 16; j++) v[j] = (j < K) ? __ldg(lp + (size_t)j * N) : 0.f;
+    lp += (size_t)16 * N;
+#pragma unroll 1
+    for (int k0 = 0; k0 < K; k0 += 16) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) nv[j] = (k0 + 16 + j < K) ? __ldg(lp + (size_t)j * N) : 0.f;
       lp += (size_t)16 * N;
 #pragma unroll
       for (int j = 0; j < 16; j++) {
@@ -156,6 +160,8 @@ __global__ void __launch_bounds__(256) em_factor_mask_kernel(size_t N, int K, co
         }
       }
       mp += (size_t)16 * W;
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = nv[j];
     }
   }
 }
@@ -238,7 +244,7 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
     if (emmask) {
       const size_t W = (N + 31) / 32;
       size_t gx = (W * 32 + 255) / 256;
-      if (gx > 2432) gx = 2432;
+      if (gx > 4864) gx = 4864;  // 32 blocks per SM (measured against 16: 1 us less)
       em_factor_mask_kernel<<<(unsigned)gx, 256, 0, s>>>(N, m.K, logw, logq, st, aw32, lt32, emmask);
     } else {
       em_weight_factor_kernel<<<(unsigned)((N + kTileW - 1) / kTileW), 256, 0, s>>>(N, logw, logq, st, aw32);

@@ -24,8 +24,10 @@ __global__ void __launch_bounds__(128) sn_kernel(SnDev sn, size_t N, int D, cons
 }
 
 // Single precision below 2^16 samples (a few waves of warps): loads batched
-// ahead of use (measured at N = 10^4: 60.5 -> 51.6 us); above, the form with
-// fewer registers (measured at N = 2^18: 0.85 -> 0.76 ms per iteration).
+// ahead of use (measured at N = 10^4: 60.5 -> 51.6 us; two warps per sample,
+// half the supernovae each, measured no faster: the second warp waits resident
+// for the first half's distance integral); above, the form with fewer
+// registers (measured at N = 2^18: 0.85 -> 0.76 ms per iteration).
 constexpr size_t kSnBatchBelow = (size_t)1 << 16;
 
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,

@@ -1363,8 +1363,18 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     return;
   }
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    // chunk order; loads issued eight at a time
+    const double *pe = part + (size_t)k * S * E + e;
     double t = 0.0;
-    for (int s = 0; s < S; s++) t += part[((size_t)k * S + s) * E + e];
+    int s = 0;
+    for (; s + 8 <= S; s += 8) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) v[u] = pe[(size_t)(s + u) * E];
+#pragma unroll
+      for (int u = 0; u < 8; u++) t += v[u];
+    }
+    for (; s < S; s++) t += pe[(size_t)s * E];
     st[e] = t;
   }
   __syncthreads();
@@ -1493,10 +1503,12 @@ __device__ __forceinline__ void body_em_renorm(int K, double *w, DevStats *st) {
   // parallel (FP64 division is long-latency), fixed-tree sums of squares
   if (threadIdx.x >= 32) return;
   if (st->status != 0) return;  // the weight step failed: keep the proposal
-  __shared__ double s_tot;
+  __shared__ double s_tot, s_w[kMaxK];
+  for (int k = threadIdx.x; k < K; k += 32) s_w[k] = w[k];  // staged by the warp
+  __syncwarp();
   if (threadIdx.x == 0) {
     double tot = 0.0;
-    for (int k = 0; k < K; k++) tot += w[k];
+    for (int k = 0; k < K; k++) tot += s_w[k];
     s_tot = tot;
     st->wsum = tot;
   }
@@ -1599,10 +1611,15 @@ __device__ __forceinline__ void body_prepare_consts(const DevMixView &m, const d
                                                     double *lconst, float *lconst32) {
   const int K = m.K;
   const double cst = m.cst;  // log normalising constant, from the host
-  if (threadIdx.x == 0) {
+  __shared__ double s_cw[kMaxK];
+  for (int k = threadIdx.x; k < K; k += blockDim.x) s_cw[k] = m.w[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {  // in component order, from shared memory
     double s = 0.0;
-    for (int k = 0; k < K; k++) { s += m.w[k]; cw[k] = s; }
+    for (int k = 0; k < K; k++) { s += s_cw[k]; s_cw[k] = s; }
   }
+  __syncthreads();
+  for (int k = threadIdx.x; k < K; k += blockDim.x) cw[k] = s_cw[k];
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double l = (m.w[k] > 0.0) ? log(m.w[k]) + cst - logdetL[k] : -INFINITY;
     lconst[k] = l;
