@@ -124,7 +124,7 @@ class ClockSampler:
 
 class NvmlSampler:
     """Reads the SM clock, its maximum and the clock-event reasons every 5 ms
-    through the driver's NVML library (ctypes; read-only queries), so a timed
+    through NVIDIA's NVML library (ctypes; read-only queries), so a timed
     region of a few tens of milliseconds still gets samples."""
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
                0x40: "hw_thermal_slowdown", 0x80: "hw_slowdown"}

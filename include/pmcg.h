@@ -154,7 +154,7 @@ pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, cons
 void pmc_simu_realloc(pmc_simu *psim, size_t nsamples, error **err);                /* cosmo_pmc.c:313 */
 void pmc_simu_free(pmc_simu **psim);                                                /* cosmo_pmc.c:738 */
 
-/* Random stream replacing the gsl_rng the driver passes to the draw.
+/* Random stream replacing the gsl_rng that cosmo_pmc passes to the draw.
  * Philox4x32-10 (Salmon et al. 2011), keyed by a 64-bit seed; each draw
  * call consumes one counter block per sample and advances `calls`. */
 typedef struct {

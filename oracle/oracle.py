@@ -1,7 +1,8 @@
 """ctypes bindings of the FP64 C oracle (oracle/pmc_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
-baseline leg of bench.py, as the checker. The product library never imports
+baseline leg of bench.py, as the reference the CUDA path is compared with. The
+product library never imports
 it. Parity with pmclib/nicaea is unpinned (both are external, absent
 libraries); the oracle is pinned to scipy and analytic answers by
 tests/golden.

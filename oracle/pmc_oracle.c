@@ -1,7 +1,7 @@
 /*
  * pmc_oracle.c — FP64 CPU restatement of one CosmoPMC PMC iteration.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for libpmcg's CUDA path, and the
+ * TEST INFRASTRUCTURE ONLY: the results libpmcg's CUDA path is compared with, and the
  * timed CPU baseline. Nothing in the library links or calls it.
  *
  * Parity with pmclib/nicaea is unpinned (both external and absent); the

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. The library never links, loads or calls this
  * code; only the tests, the smoke check and the benchmark's CPU-baseline leg
- * use it, as the checker.
+ * use it, to compare the CUDA path's results with.
  *
  * Parity with pmclib/nicaea is unpinned: both are external libraries that
  * the reference clones at install time (install_CosmoPMC.sh:241-266) and
