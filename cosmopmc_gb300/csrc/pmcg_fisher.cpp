@@ -254,3 +254,183 @@ extern "C" void pmcg_fisher_proposal(mix_mvdens *proposal, const double *F, cons
       proposal->comp[k]->mean[j] = pos[j] + sign * fshift * lam[d] / lmax * V[(size_t)j * D + d];
   }
 }
+
+// ------------------------------------------------------------------ maximum posterior
+namespace {
+
+constexpr double kLogBig = 1e30;  // objective outside the box or where log P fails
+constexpr double kRtolTiny = 1e-10;
+
+// One Nelder-Mead search (reflection 1, expansion 2, contraction 1/2, shrink
+// 1/2) on f = -log P. `want` holds the points it needs evaluated next.
+struct Simplex {
+  int D = 0, lo = 0, hi = 0, nhi = 0, phase = 0, evals = 0;
+  bool done = false;
+  std::vector<double> x, f, c, xr, xt, want;
+  double fr = 0.0;
+  enum { kInit, kReflect, kExpand, kContract, kShrink };
+
+  double *v(int i) { return &x[(size_t)i * D]; }
+
+  void order() {
+    lo = 0;
+    hi = 0;
+    for (int i = 1; i <= D; i++) {
+      if (f[i] < f[lo]) lo = i;
+      if (f[i] > f[hi]) hi = i;
+    }
+    nhi = (hi == 0) ? 1 : 0;
+    for (int i = 0; i <= D; i++)
+      if (i != hi && f[i] > f[nhi]) nhi = i;
+  }
+  // the point c + a (c - x_hi) (a = 1 reflects, 2 expands, -1/2 contracts)
+  void along(double a, std::vector<double> &out) {
+    out.resize(D);
+    for (int j = 0; j < D; j++) out[j] = c[j] + a * (c[j] - v(hi)[j]);
+  }
+  void replace_hi(const std::vector<double> &p, double fp) {
+    std::copy(p.begin(), p.end(), v(hi));
+    f[hi] = fp;
+  }
+  // the next iteration: convergence test, centroid, reflected point
+  void next(double ftol) {
+    order();
+    const double rtol = 2.0 * std::fabs(f[hi] - f[lo]) / (std::fabs(f[hi]) + std::fabs(f[lo]) + kRtolTiny);
+    if (rtol < ftol) {
+      done = true;
+      want.clear();
+      return;
+    }
+    c.assign(D, 0.0);
+    for (int i = 0; i <= D; i++)
+      if (i != hi)
+        for (int j = 0; j < D; j++) c[j] += v(i)[j];
+    for (int j = 0; j < D; j++) c[j] /= D;
+    along(1.0, xr);
+    want = xr;
+    phase = kReflect;
+  }
+  // results of the points in `want`, in order
+  void take(const double *fv, double ftol) {
+    switch (phase) {
+      case kInit:
+        std::copy(fv, fv + D + 1, f.begin());
+        next(ftol);
+        break;
+      case kReflect:
+        fr = fv[0];
+        if (fr < f[lo]) {
+          along(2.0, xt);
+          want = xt;
+          phase = kExpand;
+        } else if (fr < f[nhi]) {
+          replace_hi(xr, fr);
+          next(ftol);
+        } else {
+          if (fr < f[hi]) replace_hi(xr, fr);
+          along(-0.5, xt);
+          want = xt;
+          phase = kContract;
+        }
+        break;
+      case kExpand:
+        if (fv[0] < fr) replace_hi(xt, fv[0]);
+        else replace_hi(xr, fr);
+        next(ftol);
+        break;
+      case kContract:
+        if (fv[0] < f[hi]) {
+          replace_hi(xt, fv[0]);
+          next(ftol);
+        } else {  // shrink every vertex halfway to the best one
+          want.clear();
+          for (int i = 0; i <= D; i++) {
+            if (i == lo) continue;
+            for (int j = 0; j < D; j++) {
+              v(i)[j] = v(lo)[j] + 0.5 * (v(i)[j] - v(lo)[j]);
+              want.push_back(v(i)[j]);
+            }
+          }
+          phase = kShrink;
+        }
+        break;
+      case kShrink: {
+        int q = 0;
+        for (int i = 0; i <= D; i++)
+          if (i != lo) f[i] = fv[q++];
+        next(ftol);
+        break;
+      }
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" int pmcg_max_posterior(const pmcg_posterior *post, int nstart, const double *starts, const double *min,
+                                  const double *max, double ftol, int max_evals, double *best, double *logp,
+                                  error **err) {
+  if (!post || nstart < 1 || !starts || !min || !max || !best || !logp || !(ftol > 0.0)) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_max_posterior: invalid argument");
+    return -1;
+  }
+  const int D = post->npar;
+  if (max_evals < D + 1) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_max_posterior: max_evals below the %d start points", D + 1);
+    return -1;
+  }
+  std::vector<Simplex> S(nstart);
+  for (int s = 0; s < nstart; s++) {
+    Simplex &m = S[s];
+    m.D = D;
+    m.x.resize((size_t)(D + 1) * D);
+    m.f.assign(D + 1, kLogBig);
+    for (int i = 0; i <= D; i++) {
+      std::memcpy(m.v(i), starts + (size_t)s * D, sizeof(double) * D);
+      if (i > 0) m.v(i)[i - 1] += (max[i - 1] - min[i - 1]) / 5.0;
+    }
+    m.want = m.x;
+    m.phase = Simplex::kInit;
+  }
+  std::vector<double> X, lp, fv;
+  std::vector<short> flg;
+  std::vector<size_t> off(nstart + 1);
+  for (;;) {
+    X.clear();
+    for (int s = 0; s < nstart; s++) {
+      off[s] = X.size() / D;
+      if (!S[s].done) {
+        if (S[s].evals + (int)(S[s].want.size() / D) > max_evals) {
+          set_error(err, PMCG_ESTEPS, __LINE__, "search %d: more than %d evaluations without converging", s,
+                    max_evals);
+          return -1;
+        }
+        X.insert(X.end(), S[s].want.begin(), S[s].want.end());
+        S[s].evals += (int)(S[s].want.size() / D);
+      }
+    }
+    off[nstart] = X.size() / D;
+    const size_t P = off[nstart];
+    if (P == 0) break;
+    lp.resize(P);
+    flg.resize(P);
+    pmcg_posterior_log_pdf_batch(post, P, X.data(), lp.data(), flg.data(), 0, PMCG_FP64, nullptr, err);
+    if (err && *err) return -1;
+    fv.resize(P);
+    for (size_t q = 0; q < P; q++) {
+      bool in = flg[q] != 0 && std::isfinite(lp[q]);
+      for (int j = 0; j < D && in; j++) in = X[q * D + j] >= min[j] && X[q * D + j] <= max[j];
+      fv[q] = in ? -lp[q] : kLogBig;
+    }
+    for (int s = 0; s < nstart; s++)
+      if (!S[s].done) S[s].take(&fv[off[s]], ftol);
+  }
+  int ib = 0;
+  for (int s = 0; s < nstart; s++) {
+    Simplex &m = S[s];
+    std::memcpy(best + (size_t)s * D, m.v(m.lo), sizeof(double) * D);
+    logp[s] = (m.f[m.lo] >= kLogBig) ? -INFINITY : -m.f[m.lo];
+    if (logp[s] > logp[ib]) ib = s;
+  }
+  return ib;
+}

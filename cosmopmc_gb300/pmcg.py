@@ -23,7 +23,7 @@ SN_CHI2_FULL, SN_CHI2_MARG = 0, 1
 ERRORS = {
     -9001: "PMCG_ECUDA", -9002: "PMCG_EDIM", -9003: "PMCG_ECHOL", -9004: "PMCG_ENOSAMPLE",
     -9005: "PMCG_ENEGWEIGHT", -9006: "PMCG_EUNSUPPORTED", -9007: "PMCG_EALLOC", -9008: "PMCG_EARG",
-    -9009: "PMCG_ETIMEOUT", -9010: "PMCG_EIO", -9011: "PMCG_ENOWEIGHT",
+    -9009: "PMCG_ETIMEOUT", -9010: "PMCG_EIO", -9011: "PMCG_ENOWEIGHT", -9012: "PMCG_ESTEPS",
 }
 
 
@@ -181,6 +181,7 @@ SIGNATURES = [
     ("pmcg_posterior_add_template", None, [C.c_void_p, C.c_int, _dp, _dp, _dp, PErr]),
     ("pmcg_posterior_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
     ("pmcg_fisher_matrix", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _dp, PErr]),
+    ("pmcg_max_posterior", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double, C.c_int, _dp, _dp, PErr]),
     ("pmcg_fisher_proposal", None, [C.POINTER(MixMvdensS), _dp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
                                     C.POINTER(RngS), PErr]),
     ("pmcg_posterior_log_pdf_batch", None, [C.c_void_p, C.c_size_t, _dp, _dp, C.POINTER(C.c_short), C.c_int,
@@ -508,6 +509,19 @@ class Posterior:
         pd = call("pmcg_fisher_matrix", self.p, _dptr(pos), _dptr(bmin), _dptr(bmax), int(diag_only),
                   int(force_positive), _dptr(F))
         return (F, bool(pd == 1)) if with_positive else F
+
+    def max_posterior(self, starts, bmin, bmax, ftol=1e-8, max_evals=5000):
+        """Nelder-Mead searches for the maximum of log P from each row of starts
+        (advanced together, trial points evaluated in batches on the device).
+        Returns (best point, its log P, every search's best points, their log P)."""
+        starts = np.ascontiguousarray(np.atleast_2d(starts), dtype=np.float64)
+        bmin, bmax = _f64(bmin), _f64(bmax)
+        ns = starts.shape[0]
+        best = np.empty((ns, self.npar))
+        lp = np.empty(ns)
+        i = call("pmcg_max_posterior", self.p, ns, _dptr(starts), _dptr(bmin), _dptr(bmax), float(ftol),
+                 int(max_evals), _dptr(best), _dptr(lp))
+        return best[i].copy(), float(lp[i]), best, lp
 
     def add_snia(self, sn: dict):
         s = SnData()

@@ -55,6 +55,7 @@ typedef struct _err {
 #define PMCG_ETIMEOUT     (-9 + pmcg_base)  /* bounded wait ran out (serving loop)                */
 #define PMCG_EIO          (-10 + pmcg_base) /* file read/write error                              */
 #define PMCG_ENOWEIGHT    (-11 + pmcg_base) /* every sample has zero weight                       */
+#define PMCG_ESTEPS       (-12 + pmcg_base) /* evaluation limit reached (pmclib math_tooManySteps) */
 
 error *addError(int code, const char *text, error *next, int line);
 int isError(const error *err);
@@ -329,6 +330,20 @@ void pmcg_posterior_log_pdf_batch(const pmcg_posterior *p, size_t N, const doubl
  * test at :433-446), 0 when it is not (F is still written), -1 on error. */
 int pmcg_fisher_matrix(const pmcg_posterior *post, const double *pos, const double *min, const double *max,
                        int diag_only, int force_positive, double *F, error **err);
+/* Maximum of the posterior by Nelder-Mead simplex searches (Nelder & Mead
+ * 1965), the 'amoeba' method of exec/max_post.c:182-224 / exec/mkmax.c:409-520:
+ * the objective is -log P, with MC_LOGBIG (1e30 here) outside [min, max] or
+ * where the likelihood fails (post_cg, exec/mkmax.c:9-40); the start simplex
+ * of a search is its start point and, for each parameter j, the start point
+ * moved by (max_j - min_j) / 5 along j; a search stops when
+ * 2 |f_hi - f_lo| / (|f_hi| + |f_lo| + 1e-10) < ftol, and more than max_evals
+ * evaluations is PMCG_ESTEPS (the reference's NMAX = 5000). The nstart
+ * searches (starts: [nstart x npar]) advance together: each round evaluates
+ * every active search's trial points in one batched FP64 device call.
+ * best: [nstart x npar], each search's best vertex; logp: [nstart] its log P.
+ * Returns the index of the search with the highest log P (-1 on error). */
+int pmcg_max_posterior(const pmcg_posterior *post, int nstart, const double *starts, const double *min,
+                       const double *max, double ftol, int max_evals, double *best, double *logp, error **err);
 /* Initial proposal from a Fisher matrix F at pos, as
  * read_initial_proposal_from_config (wrappers/src/param.c:511-625): equal
  * weights, covariances fvar F^-1 (stored in comp->std with chol = 0: decompose

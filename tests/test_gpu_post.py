@@ -214,3 +214,55 @@ def test_fisher_start_for_the_sn_posterior(pmcg, oracle):
                                 kind=pmcg.FISHER_EIGEN, fshift=0.1, fvar=1.0)
     _, mu, _ = prop.arrays()
     assert np.all(mu >= lo) and np.all(mu <= hi)
+
+
+def test_max_posterior_of_a_gaussian(pmcg):
+    """Nelder-Mead from three starts, advanced together (exec/max_post.c:182-224):
+    every search ends at the mean, at the analytic maximum of log P."""
+    D = 4
+    rng = np.random.default_rng(12)
+    A = rng.normal(size=(D, D))
+    cov = A @ A.T + np.eye(D)
+    mu = rng.normal(size=D)
+    lo, hi = mu - 10.0, mu + 10.0
+    target = pmcg.MixMvdens.from_arrays([1.0], mu[None, :], cov=cov[None], df=-1).cholesky()
+    post = pmcg.Posterior(D, lo, hi).add_mix(target)
+    starts = mu + rng.uniform(-3.0, 3.0, (3, D))
+    x, lp, xs, lps = post.max_posterior(starts, lo, hi, ftol=1e-13)
+    expected = -0.5 * D * np.log(2 * np.pi) - 0.5 * np.linalg.slogdet(cov)[1] - np.sum(np.log(hi - lo))
+    sig = np.sqrt(np.diag(cov))
+    assert lp == pytest.approx(expected, abs=1e-9)
+    np.testing.assert_allclose(lps, expected, atol=1e-9)
+    assert np.max(np.abs(xs - mu) / sig) < 1e-3
+
+
+def test_max_posterior_evaluation_limit(pmcg):
+    D = 3
+    target = pmcg.MixMvdens.from_arrays([1.0], np.zeros((1, D)), cov=np.eye(D)[None], df=-1).cholesky()
+    lo, hi = -np.ones(D) * 5, np.ones(D) * 5
+    post = pmcg.Posterior(D, lo, hi).add_mix(target)
+    with pytest.raises(pmcg.PmcgError) as e:
+        post.max_posterior(np.full((1, D), 2.0), lo, hi, ftol=1e-14, max_evals=D + 3)
+    assert e.value.code == -9012
+
+
+def test_max_posterior_then_fisher_for_the_sn_posterior(pmcg, oracle):
+    """The go_fishing start: maximum posterior from the generating cosmology and
+    two nearby points, its log-likelihood against the oracle, and the diagonal
+    Fisher matrix there (go_fishing's Fisher_diag remedy) positive definite:
+    every parameter's own curvature is downward at the maximum. The full matrix
+    can stay indefinite: SN data alone leave a nearly flat curved valley in
+    (Omega_m, Omega_de, w0) whose curvature the central differences resolve to
+    either sign."""
+    wl = W.sn_workload()
+    lo, hi = wl["bmin"], wl["bmax"]
+    post = pmcg.Posterior(6, lo, hi).add_snia(wl["sn"])
+    starts = np.stack([W.SN_TRUTH, W.SN_TRUTH + 0.02 * (hi - lo), W.SN_TRUTH - 0.02 * (hi - lo)])
+    x, lp, _, _ = post.max_posterior(starts, lo, hi, ftol=1e-10)
+    logpr = -np.sum(np.log(hi - lo))
+    ll, ok = oracle.sn_loglike(wl["sn"], np.stack([x, W.SN_TRUTH]))
+    assert ok.all()
+    assert lp == pytest.approx(ll[0] + logpr, rel=1e-11, abs=1e-8)
+    assert ll[0] >= ll[1]
+    Fd, pdd = post.fisher(x, lo, hi, diag_only=True, with_positive=True)
+    assert pdd and np.all(np.diag(Fd) > 0)
