@@ -18,6 +18,7 @@
 #include <thrust/scan.h>
 #include <thrust/sort.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "pmcg_bodies.cuh"
@@ -245,6 +246,46 @@ cudaError_t launch_post_hist2d(size_t N, int D, const double *X, const double *w
   const int nb2 = nbin * nbin;
   post_hist2d_kernel<<<(nb2 + 255) / 256 < 1024 ? (nb2 + 255) / 256 : 1024, 256, 0, s>>>((long long)N, key, C, nb2,
                                                                                         scale, hist);
+  return cudaGetLastError();
+}
+
+}  // namespace pmcg
+
+namespace pmcg {
+
+// Weight clipping: keys ~order_key(log w) for counted samples (largest weight
+// first), all ones for the others; a stable sort keeps equal weights in
+// sample order, so ties go to the lower index.
+__global__ void clip_keys_kernel(size_t N, const double *__restrict__ logw, const short *__restrict__ flg,
+                                 unsigned long long *__restrict__ key, unsigned long long *__restrict__ idx) {
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (size_t)gridDim.x * blockDim.x) {
+    key[n] = flg[n] ? ~dkey(logw[n]) : ~0ull;
+    idx[n] = n;
+  }
+}
+
+__global__ void clip_apply_kernel(int k, const unsigned long long *__restrict__ key,
+                                  const unsigned long long *__restrict__ idx, short *__restrict__ flg, int *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k && key[i] != ~0ull) {
+    flg[idx[i]] = 0;
+    atomicAdd(count, 1);
+  }
+}
+
+cudaError_t launch_clip_largest(size_t N, const double *logw, short *flg, int k, void *scratch, int *count,
+                                cudaStream_t s) {
+  if (N == 0 || k <= 0) return cudaMemsetAsync(count, 0, sizeof(int), s);
+  if ((size_t)k > N) k = (int)N;
+  unsigned long long *key = reinterpret_cast<unsigned long long *>(scratch);
+  unsigned long long *idx = key + N;  // the first weight array of the post-processing scratch
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)std::min<size_t>((N + 255) / 256, 4096);
+  clip_keys_kernel<<<grid, 256, 0, s>>>(N, logw, flg, key, idx);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  thrust::stable_sort_by_key(thrust::cuda::par.on(s), key, key + N, idx);
+  clip_apply_kernel<<<(unsigned)((k + 255) / 256), 256, 0, s>>>(k, key, idx, flg, count);
   return cudaGetLastError();
 }
 

@@ -1089,6 +1089,45 @@ extern "C" double normalize_importance_weight(pmc_simu *psim, error **err) {
   return psim->logSum;
 }
 
+// clip_weights (exec/cosmo_pmc.c:395-399; the manual: the nclipw points with
+// the largest weights are not considered in subsequent calculations of moments,
+// perplexity, evidence, Manual/manual.tex:636-642, 2105-2106). pmclib's routine
+// is absent, so the semantics are pinned here: the nclipw largest weights among
+// counted samples (ties to the lower index) get flg = 0, chosen on the device
+// by a stable sort; a normalised sample (isLog = 0) is renormalised over the
+// samples kept (logSum, maxW updated), a log-weight sample keeps its weights.
+extern "C" void clip_weights(pmc_simu *psim, int nclipw, FILE *out, error **err) {
+  if (!psim || nclipw < 0) {
+    set_error(err, PMCG_EARG, __LINE__, "clip_weights: invalid arguments");
+    return;
+  }
+  if (nclipw == 0 || psim->nsamples == 0) return;
+  SimMirror *m = mirror_any(psim, err);
+  if (!m) return;
+  Work &w = m->w;
+  if (!m->x_valid && !CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload"))
+    return;
+  if (!sync_weights(m, psim, err)) return;
+  if (!m->pscratch &&
+      !CK(cudaMalloc(&m->pscratch, post_scratch_bytes(w.N) + sizeof(double) * (8 * (size_t)w.D + 64)),
+          "post-processing scratch"))
+    return;
+  int *dcount = reinterpret_cast<int *>(reinterpret_cast<char *>(m->pscratch) + post_scratch_bytes(w.N));
+  int nclip = 0;
+  bool ok = CK(launch_clip_largest(w.N, w.logw, w.flg, nclipw, m->pscratch, dcount, w.s), "clip") &&
+            CK(cudaMemcpyAsync(&nclip, dcount, sizeof(int), cudaMemcpyDeviceToHost, w.s), "clip count") &&
+            stage_weights(w, 1.0, false, err) && fetch_stats(w, err) &&
+            CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flags");
+  if (ok && !psim->isLog)
+    ok = CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise") &&
+         CK(cudaMemcpyAsync(psim->weights, w.wbar, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights");
+  ok = ok && CK(cudaStreamSynchronize(w.s), "clip");
+  if (!ok) return;
+  if (!psim->isLog) psim->logSum = w.hstats->logSum;
+  psim->maxW = w.hstats->maxW;
+  if (out) fprintf(out, "clip_weights: %d of the largest weights discarded\n", nclip);
+}
+
 // Replaces every sample's weight by its log-posterior, as exec/importance_sample.c:26-91
 // does point by point: flg = 1, or 0 outside the posterior's prior box or on a
 // likelihood error; isLog = 1; maxW. Returns the number of counted samples.

@@ -131,6 +131,12 @@ cudaError_t launch_post_hist2d(size_t N, int D, const double *X, const double *w
                                int p, int q, const double *lo, const double *hi, double scale, void *scratch,
                                double *hist, cudaStream_t s);
 
+// Weight clipping (k_post.cu): flg = 0 for the k largest log-weights among
+// counted samples (ties to the lower index); count: how many were clipped.
+// scratch: post_scratch_bytes(N) bytes.
+cudaError_t launch_clip_largest(size_t N, const double *logw, short *flg, int k, void *scratch, int *count,
+                                cudaStream_t s);
+
 // Convert the mixed-precision sample to FP64 row-major.
 cudaError_t launch_x32_to_x64(size_t N, int D, int ldx, const float *X32, double *X64, cudaStream_t s);
 // Normalised weights wbar = exp(logw - logSum) (0 where flg == 0).

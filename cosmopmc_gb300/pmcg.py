@@ -181,6 +181,7 @@ SIGNATURES = [
     ("pmcg_posterior_add_template", None, [C.c_void_p, C.c_int, _dp, _dp, _dp, PErr]),
     ("pmcg_posterior_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
     ("pmcg_fisher_matrix", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _dp, PErr]),
+    ("clip_weights", None, [C.POINTER(PmcSimuS), C.c_int, C.c_void_p, PErr]),
     ("pmcg_max_posterior", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double, C.c_int, _dp, _dp, PErr]),
     ("pmcg_fisher_proposal", None, [C.POINTER(MixMvdensS), _dp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
                                     C.POINTER(RngS), PErr]),
@@ -733,6 +734,12 @@ def importance_weights(psim: PmcSimu, prop: MixMvdens, post: Posterior, beta=1.0
 
 def normalize_importance_weight(psim: PmcSimu):
     return call("normalize_importance_weight", psim.p)
+
+
+def clip_weights(psim: PmcSimu, nclipw: int):
+    """Flag out the nclipw largest weights (ties to the lower index); a
+    normalised sample is renormalised over the samples kept."""
+    call("clip_weights", psim.p, int(nclipw), None)
 
 
 def update_prop_rb(prop: MixMvdens, psim: PmcSimu):

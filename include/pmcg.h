@@ -188,6 +188,11 @@ size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim, mix_mvdens
 /* logSum = log sum exp(logw) over flg==1; weights become normalised
  * (isLog=0). Returns logSum (exec/cosmo_pmc.c:378). */
 double normalize_importance_weight(pmc_simu *psim, error **err);
+/* The nclipw largest weights among counted samples (ties to the lower index)
+ * get flg = 0; a normalised sample is renormalised over the samples kept.
+ * Replaces pmclib clip_weights (exec/cosmo_pmc.c:395-399); out (optional)
+ * receives one line. */
+void clip_weights(pmc_simu *psim, int nclipw, FILE *out, error **err);
 
 /* Rao-Blackwellised EM update of the proposal from the last weighted
  * sample; dead components (fewer than 20 draws or weight < 1/N, or a

@@ -358,3 +358,16 @@ def hist2d(X, wbar, flg, nbin, p, q, lo, hi, scale):
                      nbin, p, q, np.ascontiguousarray(lo, dtype=np.float64), np.ascontiguousarray(hi, dtype=np.float64),
                      scale, h)
     return h
+
+
+def clip_weights(logw, flg, k):
+    """Flags after clipping the k largest log-weights among counted samples,
+    ties to the lower index (the semantics pinned for the absent pmclib
+    clip_weights; exec/cosmo_pmc.c:395-399, Manual/manual.tex:636-642)."""
+    logw = np.asarray(logw, dtype=np.float64)
+    out = np.asarray(flg, dtype=np.int16).copy()
+    cand = np.flatnonzero(out != 0)
+    order = cand[np.argsort(-logw[cand], kind="stable")]
+    out[order[:k]] = 0
+    return out
+

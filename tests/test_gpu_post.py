@@ -266,3 +266,36 @@ def test_max_posterior_then_fisher_for_the_sn_posterior(pmcg, oracle):
     assert ll[0] >= ll[1]
     Fd, pdd = post.fisher(x, lo, hi, diag_only=True, with_positive=True)
     assert pdd and np.all(np.diag(Fd) > 0)
+
+
+@pytest.mark.parametrize("normalised", [False, True])
+def test_clip_weights_matches_oracle(pmcg, oracle, normalised):
+    """The nclipw largest weights leave the sample (flags bit-exact against the
+    oracle, ties to the lower index); a normalised sample is renormalised."""
+    rng = np.random.default_rng(40 + normalised)
+    N, D, k = 30001, 3, 25
+    logw = np.round(rng.normal(0, 2, N) * 2) / 2   # many equal weights: ties at the k-th place
+    logw[[10, 20, 30]] = logw.max() + 1.0
+    flg = (rng.uniform(size=N) > 0.1).astype(np.int16)
+    flg[20] = 0                              # the largest but not counted
+    ps = pmcg.PmcSimu(N, D)
+    ps.X[:] = rng.normal(size=(N, D))
+    ps.weights[:] = logw
+    ps.flg[:] = flg
+    ps.s.isLog = 1
+    ps.host_modified()
+    if normalised:
+        pmcg.normalize_importance_weight(ps)
+    pmcg.clip_weights(ps, k)
+    ref = oracle.clip_weights(logw, flg, k)
+    kth = np.sort(logw[flg == 1])[::-1][k - 1]
+    assert np.sum(logw[flg == 1] == kth) > 1          # the boundary is a tie
+    np.testing.assert_array_equal(ps.flg, ref)
+    assert np.sum(flg) - np.sum(ps.flg) == k
+    if normalised:
+        keep = ref == 1
+        m = logw[keep].max()
+        wb = np.exp(logw[keep] - m)
+        wb /= wb.sum()
+        np.testing.assert_allclose(ps.weights[keep], wb, rtol=1e-12)
+        assert ps.s.logSum == pytest.approx(m + np.log(np.sum(np.exp(logw[keep] - m))), rel=1e-12)
