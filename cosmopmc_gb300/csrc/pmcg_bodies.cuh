@@ -1339,7 +1339,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
 // ================================================================== (e) EM finalise
 __host__ __device__ inline size_t finalize_smem(int D, int whitened) {
   (void)whitened;
-  return (size_t)(em_E(D) + 3 * D * D + 2 * D) * sizeof(double);
+  return (size_t)(em_E(D) + 3 * D * D + 3 * D) * sizeof(double);  // C padded to D x (D + 1)
 }
 
 // Component k: fixed-order sum of the chunk partials, new mean and covariance
@@ -1353,8 +1353,9 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   const int D = m.D, E = em_E(D);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double *st = sh;             // E
-  double *C = st + E;          // D*D
-  double *Lo = C + D * D;      // D*D old factor (whitened only)
+  const int ldc = D + 1;       // row stride of C: a column read by 32 lanes spans all banks
+  double *C = st + E;          // D*ldc
+  double *Lo = C + D * ldc;    // D*D old factor (whitened only)
   double *T = Lo + D * D;      // D*D scratch (whitened only); then D: mean shift
   double *rp = T + D * D + D;  // D reciprocal pivots
   if (stats->status != 0) return;  // the weight step failed: keep the proposal
@@ -1389,14 +1390,14 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   }
   const double S0 = st[0], St = st[1];
   // the weighted mean shift d = S1 / St (D divisions in parallel) and 1 / S0
-  double *dm = whitened ? T + D * D : C + D * D;
+  double *dm = whitened ? T + D * D : C + D * ldc;
   for (int i = threadIdx.x; i < D; i += blockDim.x) dm[i] = st[2 + i] / St;
   __syncthreads();
   const double rS0 = 1.0 / S0;
   for (int i = warp; i < D; i += nw)
     for (int j = lane; j < D; j += 32) {
       const int a = i > j ? i : j, b = i > j ? j : i;
-      C[i * D + j] = (st[2 + D + tri_idx(a, b)] - St * dm[i] * dm[j]) * rS0;
+      C[i * ldc + j] = (st[2 + D + tri_idx(a, b)] - St * dm[i] * dm[j]) * rS0;
       if (whitened) Lo[i * D + j] = (j <= i) ? m.L[(size_t)k * D * D + i * D + j] : 0.0;
     }
   __syncthreads();
@@ -1410,7 +1411,7 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // T = Lo C
       int i = e / D, j = e - i * D;
       double t = 0.0;
-      for (int q = 0; q <= i; q++) t += Lo[i * D + q] * C[q * D + j];
+      for (int q = 0; q <= i; q++) t += Lo[i * D + q] * C[q * ldc + j];
       T[e] = t;
     }
     __syncthreads();
@@ -1418,24 +1419,24 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
       int i = e / D, j = e - i * D;
       double t = 0.0;
       for (int q = 0; q <= j; q++) t += T[i * D + q] * Lo[j * D + q];
-      C[e] = t;
+      C[i * ldc + j] = t;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {  // symmetrise exactly
       int i = e / D, j = e - i * D;
-      if (j < i) T[e] = 0.5 * (C[i * D + j] + C[j * D + i]);
+      if (j < i) T[e] = 0.5 * (C[i * ldc + j] + C[j * ldc + i]);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
       int i = e / D, j = e - i * D;
-      if (j < i) { C[i * D + j] = T[e]; C[j * D + i] = T[e]; }
+      if (j < i) { C[i * ldc + j] = T[e]; C[j * ldc + i] = T[e]; }
     }
     __syncthreads();
   }
   if (banded) {
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
       int i = e / D, j = e - i * D;
-      if ((i > j ? i - j : j - i) >= band_limit) C[e] = 0.0;
+      if ((i > j ? i - j : j - i) >= band_limit) C[i * ldc + j] = 0.0;
     }
     __syncthreads();
   }
@@ -1445,12 +1446,12 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   // and lane 0 its first column) derives the next pivot; columns are scaled by
   // rp_j at the end. Rows go to warps and columns to lanes.
   auto pivot = [&](int j) {
-    double d = C[j * D + j];
+    double d = C[j * ldc + j];
     if (!(d > 0.0) || !isfinite(d)) { *s_dead = 1; d = 1.0; }
     // one reciprocal square root for both the pivot and its inverse: the FP64
     // pipe is narrow and this chain runs on one thread between barriers
     const double r = rsqrt(d);
-    C[j * D + j] = d * r;
+    C[j * ldc + j] = d * r;
     rp[j] = r;
   };
   if (threadIdx.x == 0) pivot(0);
@@ -1458,14 +1459,14 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
   for (int j = 0; j < D; j++) {
     const double r2 = rp[j] * rp[j];
     for (int i = j + 1 + warp; i < D; i += nw) {
-      const double cij = C[i * D + j] * r2;
-      for (int c = j + 1 + lane; c <= i; c += 32) C[i * D + c] = fma(-cij, C[c * D + j], C[i * D + c]);
+      const double cij = C[i * ldc + j] * r2;
+      for (int c = j + 1 + lane; c <= i; c += 32) C[i * ldc + c] = fma(-cij, C[c * ldc + j], C[i * ldc + c]);
     }
     if (threadIdx.x == 0 && j + 1 < D) pivot(j + 1);
     __syncthreads();
   }
   for (int i = warp; i < D; i += nw)
-    for (int j = lane; j < i; j += 32) C[i * D + j] *= rp[j];
+    for (int j = lane; j < i; j += 32) C[i * ldc + j] *= rp[j];
   __syncthreads();
   if (*s_dead) {
     if (threadIdx.x == 0) w[k] = 0.0;
@@ -1487,9 +1488,9 @@ __device__ __forceinline__ void body_em_finalize(const DevMixView &m, double *w,
       double v = 0.0;
       if (j <= i) {
         if (via_lo) {
-          for (int q = j; q <= i; q++) v = fma(Lo[i * D + q], C[q * D + j], v);
+          for (int q = j; q <= i; q++) v = fma(Lo[i * D + q], C[q * ldc + j], v);
         } else {
-          v = C[i * D + j];
+          v = C[i * ldc + j];
         }
       }
       L[(size_t)k * D * D + i * D + j] = v;
