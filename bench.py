@@ -63,6 +63,22 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(ms_local, world, device):
+    """The largest per-rank time over all ranks, on every rank (replicas: each
+    rank times its own independent run; the whole job takes the slowest)."""
+    import torch
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, ms_max, world):
+    """Units of all ranks per second of the slowest rank."""
+    return units_per_rank * world / (ms_max / 1000.0)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -515,18 +531,16 @@ def main():
     clocks = clk.stop()
     barrier()
     nt = 1  # stage_ms is per step
-    t_local = torch.tensor([step_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
-    step_ms_max = float(t_local.item())
-    value = N * world / (step_ms_max / 1000.0)
+    step_ms_max = max_over_ranks(step_ms, world, "cuda")
+    value = whole_job_rate(N, step_ms_max, world)
 
     # ---------------- plain FP64 path on the same workload
     fp64 = None
     if not args.no_fp64:
         run64 = P.Run(prop, post, N, precision=P.FP64, seed=1000 + rank)
         s64, fp64_ms, _, _, _ = time_run(P, run64, args.fp64_steps, 1, l2buf, sync, prop, stage_steps=0)
-        fp64_value = N * world / (fp64_ms / 1000.0)
+        fp64_ms = max_over_ranks(fp64_ms, world, "cuda")
+        fp64_value = whole_job_rate(N, fp64_ms, world)
         run64.free()
         fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
                 "speedup_mixed_vs_fp64": value / fp64_value,
@@ -563,14 +577,12 @@ def main():
         dropin_step()
         e2e_tot += time.perf_counter() - t0
     e2e_ms = 1000.0 * e2e_tot / args.steps
-    e2e_t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = N * world / (float(e2e_t.item()) / 1000.0)
+    e2e_ms_max = max_over_ranks(e2e_ms, world, "cuda")
+    e2e_value = whole_job_rate(N, e2e_ms_max, world)
     K, D = 64, 32
     h2d = K * (1 + D + D * D) * 8 + 2 * K * (1 + D + D * D) * 8   # proposal uploads (draw + update)
     d2h = N * D * 8 + N * 4 + N * 2 + N * 8 + N * 2 + N * 8 + K * (1 + D + D * D) * 8
-    e2e = {"value": e2e_value, "unit": UNIT, "ms_per_step": float(e2e_t.item()), "h2d_bytes_per_step": h2d,
+    e2e = {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms_max, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h,
            "path": "simulate_mix_mvdens + generic_get_importance_weight + normalize + update_prop_rb + "
                    "perplexity_and_ess + evidence, pinned pmc_simu host arrays"}
