@@ -1,7 +1,9 @@
-// pmcg_fisher.cpp — Fisher matrix of a posterior by central differences (all
-// stencil points in one batched FP64 device evaluation) and the initial PMC
-// proposals built from it (exec/go_fishing.c:37-86,
-// wrappers/src/param.c:472-625).
+// pmcg_fisher.cpp — the start of a PMC run: the maximum of the posterior by
+// Nelder-Mead searches advanced together (exec/max_post.c:182-224), the Fisher
+// matrix there by central differences (exec/go_fishing.c:37-86), and the
+// initial PMC proposals built from it (wrappers/src/param.c:472-625). Every
+// posterior evaluation is a batched FP64 device call: all stencil points of the
+// matrix at once, all searches' trial points of a round at once.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
