@@ -39,7 +39,7 @@ WORKLOAD = "mixture microbench: D=32, K=64 Student-t nu=3 (cond 1e6), 16-comp Ga
 # DRAM traffic of one launch of the tensor-core proposal log-density at the
 # mixture workload (N = 2^20): dram__bytes_read.sum + dram__bytes_write.sum of
 # one ncu capture at N = 262144 (34.20 + 74.93 MB), scaled by 4 (traffic grows
-# with N); profiles/umma_logq_mixture.md.
+# with N).
 UMMA_TRAFFIC_BYTES = 4 * (34.20e6 + 74.93e6)
 
 
@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-likelihoods", action="store_true", help="skip the SN and template measurements")
     ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
                     help="single-precision log-densities on tcgen05 (1) or CUDA cores (0); default: library setting")
+    ap.add_argument("--profile-case", default=None, choices=["mixture", "sn", "template"],
+                    help="run one workload for --iterations iterations with every kernel launched directly and "
+                         "print its per-stage times (the command that profiler captures start from); no JSON line")
+    ap.add_argument("--iterations", type=int, default=2, help="iterations of --profile-case")
     return ap.parse_args()
 
 
@@ -496,10 +500,51 @@ def run_reference(args):
     return 0
 
 
+def profile_case(args):
+    """One workload of the benchmark, mixed precision, every kernel launched
+    directly with per-stage CUDA events: "mixture" (D=32, K=64 Student-t nu=3,
+    condition 1e6, 16-component target), "sn" (740 supernovae, D=6, K=10 Fisher
+    start), "template" (D=12, M=2048, P=91, K=16)."""
+    from cosmopmc_gb300 import pmcg as P
+    from cosmopmc_gb300 import workloads as W
+    P.load()
+    if args.tensor_cores is not None:
+        P.set_tensor_cores(args.tensor_cores)
+    N = args.nsamples
+    box = None
+    if args.profile_case == "mixture":
+        prop, target, post = build_workload(P, W, N)
+    elif args.profile_case == "sn":
+        wl = W.sn_workload(K=10, init="fisher")
+        w, mu, cov, df = wl["prop"]
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+        post = P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"])
+        box = P.Parabox(wl["bmin"], wl["bmax"])
+    else:
+        tw = W.template_workload(D=12, M=2048, K=16)
+        w, mu, cov, df = tw["prop"]
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+        post = P.Posterior(12, tw["bmin"], tw["bmax"]).add_template(tw["A"], tw["C"], tw["dobs"])
+        box = P.Parabox(tw["bmin"], tw["bmax"])
+    run = P.Run(prop, post, N, precision=P.MIXED, seed=11, box=box)
+    run.set_timing(True, stages=True)
+    st = None
+    for _ in range(args.iterations):
+        st = run.iterate(1.0)
+    ms, n = run.stage_ms()
+    run.free()
+    names = ["draw", "logq", "logpost", "weights", "em"]
+    print(f"{args.profile_case} N={N}: ln Z = {st['ln_evidence']:.6f}; ms per iteration "
+          + ", ".join(f"{k} {v / n:.4f}" for k, v in zip(names, ms)), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return profile_case(args)
     rank, world, local = dist_env()
     import torch
     torch.cuda.set_device(local)

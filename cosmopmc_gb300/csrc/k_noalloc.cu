@@ -14,10 +14,13 @@
 // so a call accepts at most kNoAllocMaxSamples samples and rejects more with
 // PMCG_EDIM. The first call on a device looks up the array's device address
 // (cudaGetSymbolAddress, with that device current); make that first call before
-// any stream capture. All calls share the array and every call overwrites the
-// records it reads, so nothing carries over from the previous call — but calls
-// whose kernels overlap on the GPU (other streams, other host threads) race on
-// the array and must be serialised by the caller.
+// any stream capture. Every call is synchronous: it launches two kernels on the
+// caller's stream, copies the final record into a host variable and waits for
+// the stream, because the scalars are returned on the host. All calls share the
+// array and every call overwrites the records it reads, so nothing carries over
+// from the previous call — but calls whose kernels overlap on the GPU (other
+// streams, other host threads) race on the array and must be serialised by the
+// caller.
 #include <mutex>
 
 #include "../../include/pmcg.h"
@@ -141,6 +144,14 @@ extern "C" void pmcg_importance_weights_noalloc(size_t N, double beta, const dou
   }
   WRed *part = noalloc_scratch(dev, err);
   if (!part) return;
+  // An error left on this thread by earlier, unrelated work is reported as
+  // such (and cleared) instead of being taken for a failure of these launches.
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(err, PMCG_ECUDA, __LINE__, "CUDA error pending from earlier work on this thread: %s",
+              cudaGetErrorString(e));
+    return;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   const int nb = (int)((N + kNoAllocSamplesPerBlock - 1) / kNoAllocSamplesPerBlock);
   noalloc_weights_kernel<<<nb, 256, 0, s>>>(N, beta, logpost, logq, flg, logw, part);

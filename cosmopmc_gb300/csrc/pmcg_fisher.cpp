@@ -131,6 +131,30 @@ bool positive_definite(int n, const double *A) {
 
 using pmcg::set_error;
 
+// Log-posterior of P points (FP64, one batched device call) into lp/flg. The
+// evaluation reports into a chain of its own, so a failure is seen whether or
+// not the caller passed an error pointer and an error already in the caller's
+// chain does not stop the work; a failure is moved to the front of the
+// caller's chain (or dropped when there is none) and false returned.
+static bool eval_points(const pmcg_posterior *post, size_t P, const double *X, double *lp, short *flg,
+                        error **err) {
+  error *ev = nullptr;
+  pmcg_posterior_log_pdf_batch(post, P, X, lp, flg, 0, PMCG_FP64, nullptr, &ev);
+  if (!isError(ev)) {
+    purgeError(&ev);
+    return true;
+  }
+  if (err) {
+    error *tail = ev;
+    while (tail->next) tail = tail->next;
+    tail->next = *err;
+    *err = ev;
+  } else {
+    purgeError(&ev);
+  }
+  return false;
+}
+
 extern "C" int pmcg_fisher_matrix(const pmcg_posterior *post, const double *pos, const double *min,
                                   const double *max, int diag_only, int force_positive, double *F, error **err) {
   if (!post || !pos || !min || !max || !F) {
@@ -166,8 +190,7 @@ extern "C" int pmcg_fisher_matrix(const pmcg_posterior *post, const double *pos,
     }
   std::vector<double> lp(P);
   std::vector<short> flg(P);
-  pmcg_posterior_log_pdf_batch(post, P, X.data(), lp.data(), flg.data(), 0, PMCG_FP64, nullptr, err);
-  if (err && *err) return -1;
+  if (!eval_points(post, P, X.data(), lp.data(), flg.data(), err)) return -1;
   for (int i = 0; i < D * D; i++) F[i] = 0.0;
   for (size_t e = 0; e < nel; e++) {
     const int a = ea[e], b = eb[e];
@@ -416,8 +439,7 @@ extern "C" int pmcg_max_posterior(const pmcg_posterior *post, int nstart, const 
     if (P == 0) break;
     lp.resize(P);
     flg.resize(P);
-    pmcg_posterior_log_pdf_batch(post, P, X.data(), lp.data(), flg.data(), 0, PMCG_FP64, nullptr, err);
-    if (err && *err) return -1;
+    if (!eval_points(post, P, X.data(), lp.data(), flg.data(), err)) return -1;
     fv.resize(P);
     for (size_t q = 0; q < P; q++) {
       bool in = flg[q] != 0 && std::isfinite(lp[q]);

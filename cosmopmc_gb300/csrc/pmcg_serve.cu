@@ -102,6 +102,9 @@ static void retire(pmcg_server *s, Job *j, int status) {
         status = getErrorValue(e);
       }
       mix_mvdens_free(&out);
+    } else {
+      // no host proposal to copy the result into: the job is not a success
+      status = isError(e) ? getErrorValue(e) : PMCG_EALLOC;
     }
     purgeError(&e);
   }

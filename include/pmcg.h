@@ -496,7 +496,9 @@ void pmcg_server_free(pmcg_server **s);
  * *stats (host). The partial sums use a fixed device array inside the library
  * (one per GPU, held until exit), which limits N to 8,388,608 (larger N:
  * PMCG_EDIM). The first call on a device looks the array up; make it before
- * any stream capture. Calls that overlap on the GPU share that array and race. */
+ * any stream capture. Each call is synchronous: it waits for `stream` before
+ * it returns the scalars. Calls that overlap on the GPU share that array and
+ * race. */
 typedef struct {
   double logSum, maxW, ln_evidence, perplexity, ess;
   size_t nok;

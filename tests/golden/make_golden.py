@@ -8,7 +8,10 @@ known-answer vectors (Salmon et al. 2011), and the two tempering demo targets
 of the reference (Demo/tempering/*/config_pmc, read as text when the reference
 tree is present; their analytic evidence is 1, Demo/tempering/README.md:14-21).
 
-Run:  python tests/golden/make_golden.py   (needs numpy + scipy; writes golden.npz)
+Run:  python tests/golden/make_golden.py --reference <CosmoPMC source tree>
+      (needs numpy + scipy; writes golden.npz; without --reference, or with
+      the PMCG_REFERENCE environment variable unset, the demo targets are left
+      out)
 """
 from __future__ import annotations
 
@@ -24,7 +27,6 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from cosmopmc_gb300 import workloads as W  # noqa: E402
 
-REF_DEMO = "/root/reference/Demo/tempering"
 C_KMS = 299792.458
 
 
@@ -114,10 +116,14 @@ def em_ref(w, mu, cov, df, X, wbar, flg, idx, N):
     return nw, nmu, ncov, dead, logq, lt, Qs
 
 
-def demo_targets():
+def demo_targets(reference):
+    """Targets of the reference's two tempering demos, read as text from
+    <reference>/Demo/tempering/*/config_pmc; None without a reference tree."""
+    if not reference:
+        return None
     out = {}
     for name in ("1_mvnorm_2D_temp_none", "2_mixmvnorm_2D_temp_none"):
-        path = os.path.join(REF_DEMO, name, "config_pmc")
+        path = os.path.join(reference, "Demo", "tempering", name, "config_pmc")
         if not os.path.exists(path):
             return None
         vals = {}
@@ -136,7 +142,12 @@ def demo_targets():
     return out
 
 
-def main():
+def main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser(description="Write tests/golden/golden.npz and golden.json.")
+    ap.add_argument("--reference", default=os.environ.get("PMCG_REFERENCE"),
+                    help="CosmoPMC source tree (for the Demo/tempering targets)")
+    args = ap.parse_args(argv)
     rng = np.random.default_rng(20261203)
     g = {}
     meta = {}
@@ -235,7 +246,7 @@ def main():
                 b = np.exp(it / (6 - 2.0) * (-np.log(0.05)) + np.log(0.05))
             bet.append([kind, it, b])
     g["tempering"] = np.array(bet)
-    demos = demo_targets()
+    demos = demo_targets(args.reference)
     if demos is not None:
         m1 = demos["1_mvnorm_2D_temp_none"]
         m2 = demos["2_mixmvnorm_2D_temp_none"]

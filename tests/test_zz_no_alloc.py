@@ -85,3 +85,61 @@ def test_noalloc_rejects_more_samples_than_its_scratch_holds(pmcg):
     with pytest.raises(pmcg.PmcgError) as e:
         err.check()
     assert e.value.code == -9002
+
+
+def _call(pmcg, lib, N, beta, lp_d, lq_d, flg_d, logw_d):
+    st = pmcg.WeightStats()
+    err = pmcg._Err()
+    lib.pmcg_importance_weights_noalloc(N, beta, lp_d.data_ptr(), lq_d.data_ptr(), flg_d.data_ptr(),
+                                        logw_d.data_ptr(), C.byref(st), None, err.ref)
+    return st, err
+
+
+def test_noalloc_at_its_sample_limit_matches_a_float64_reduction(pmcg):
+    """N = 8,388,608 exactly (4096 partial records, the merge's strided loop at its
+    longest), some samples flagged out, against numpy in float64."""
+    torch = pytest.importorskip("torch")
+    lib = pmcg.load()
+    N, beta = 8388608, 0.7
+    rng = np.random.default_rng(8)
+    lp = rng.normal(-3.0, 2.0, N)
+    lq = rng.normal(0.0, 1.5, N)
+    flg = (rng.uniform(size=N) > 0.05).astype(np.int16)
+    dev = torch.device("cuda", 0)
+    lp_d = torch.tensor(lp, device=dev)
+    lq_d = torch.tensor(lq, device=dev)
+    for call in range(2):
+        flg_d = torch.tensor(flg, device=dev)
+        logw_d = torch.zeros(N, dtype=torch.float64, device=dev)
+        st, err = _call(pmcg, lib, N, beta, lp_d, lq_d, flg_d, logw_d)
+        err.check()
+        ok = flg == 1
+        l = beta * lp[ok] - lq[ok]
+        m = l.max()
+        s = np.exp(l - m).sum()
+        logsum = m + np.log(s)
+        wb = np.exp(l - logsum)
+        assert abs(st.logSum - logsum) < 1e-9
+        assert st.maxW == m
+        assert abs(st.ln_evidence - (logsum - np.log(N))) < 1e-9
+        perp = np.exp(-np.sum(wb * np.log(wb))) / N
+        assert abs(st.perplexity / perp - 1.0) < 1e-9
+        assert abs(st.ess / (1.0 / np.sum(wb * wb)) - 1.0) < 1e-9
+        assert st.nok == int(ok.sum())
+        logw = logw_d.cpu().numpy()
+        np.testing.assert_allclose(logw[ok], l, rtol=1e-12, atol=1e-12)  # FMA contraction on the device
+        assert np.all(np.isneginf(logw[~ok]))
+
+
+def test_noalloc_reports_no_weight_when_every_sample_is_flagged_out(pmcg):
+    torch = pytest.importorskip("torch")
+    lib = pmcg.load()
+    N = 5000
+    t = torch.zeros(N, dtype=torch.float64, device="cuda")
+    flg_d = torch.zeros(N, dtype=torch.int16, device="cuda")
+    logw_d = torch.zeros(N, dtype=torch.float64, device="cuda")
+    st, err = _call(pmcg, lib, N, 1.0, t, t, flg_d, logw_d)
+    with pytest.raises(pmcg.PmcgError) as e:
+        err.check()
+    assert e.value.code == -9011
+    assert np.all(np.isneginf(logw_d.cpu().numpy()))
