@@ -313,41 +313,67 @@ def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
     return out
 
 
+TEMPER_LEVELS, TEMPER_TMIN = 10, 0.01
+
+
+def tempering_level(rng):
+    """A tempering level of the log schedule (exec/cosmo_pmc.c:464-495): the beta
+    of a random iteration of a 10-level schedule starting at t_min = 0.01."""
+    from cosmopmc_gb300 import pmcg as P
+    return P.get_tempering_beta(P.TEMPERING_LOG, int(rng.integers(0, TEMPER_LEVELS)), TEMPER_TMIN, TEMPER_LEVELS)
+
+
 def ragged_specs(R, seed=256):
-    """Batched workload: R runs, half SN-type (D=6, 740 supernovae, Fisher-matrix start),
-    half Gaussian-mixture targets with D ~ U{2..20}, K ~ U{1..20}, N ~ logU(1e3, 1e5)."""
+    """Batched workload: R runs, half SN-type (740 supernovae, the six SN parameters
+    plus flat-prior nuisance parameters, D ~ U{6..20}, Fisher-matrix start), half
+    Gaussian-mixture targets with D ~ U{2..20}; K ~ U{1..20}, N ~ logU(1e3, 1e5);
+    each run at a tempering level of the log schedule."""
     rng = np.random.default_rng(seed)
     specs = []
     for r in range(R):
         N = int(round(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))))
         K = int(rng.integers(1, 21))
+        beta = tempering_level(rng)
         if r % 2 == 0:
-            specs.append(("sn", 6, max(K, 2), N, 740 + r))
+            specs.append(("sn", int(rng.integers(6, 21)), max(K, 2), N, 740 + r, beta))
         else:
-            specs.append(("mix", int(rng.integers(2, 21)), K, N, 1000 + r))
+            specs.append(("mix", int(rng.integers(2, 21)), K, N, 1000 + r, beta))
     return specs
 
 
+NUIS_HALF = 1.0   # nuisance parameters: flat prior on [-1, 1]
+
+
 def build_spec(P, W, spec, cache):
-    kind, D, K, N, seed = spec
+    kind, D, K, N, seed = spec[:5]
     if kind == "sn":
-        if "sn_post" not in cache:
+        if "sn_data" not in cache:
             wl = W.sn_workload()
-            cache["sn_post"] = (P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"]),
-                                P.Parabox(wl["bmin"], wl["bmax"]))
+            cache["sn_data"] = wl["sn"]
             cache["sn_fisher"] = W.sn_fisher(wl["sn"], W.SN_TRUTH)
-        post, box = cache["sn_post"]
+        if ("sn_post", D) not in cache:
+            bmin = np.concatenate([W.SN_BOX_MIN, -NUIS_HALF * np.ones(D - 6)])
+            bmax = np.concatenate([W.SN_BOX_MAX, NUIS_HALF * np.ones(D - 6)])
+            F = np.zeros((D, D))
+            F[:6, :6] = cache["sn_fisher"]
+            F[6:, 6:] = np.eye(D - 6) / (0.5 * NUIS_HALF) ** 2   # nuisance: proposal sd 0.5 x sqrt(2)
+            theta0 = np.concatenate([W.SN_TRUTH, np.zeros(D - 6)])
+            cache[("sn_post", D)] = (P.Posterior(D, bmin, bmax).add_snia(cache["sn_data"]), P.Parabox(bmin, bmax),
+                                     F, theta0, bmin, bmax)
+        post, box, F, theta0, bmin, bmax = cache[("sn_post", D)]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.fisher_proposal(rng, K, W.SN_TRUTH, cache["sn_fisher"], W.SN_BOX_MIN, W.SN_BOX_MAX)
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, F, bmin, bmax)
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     if kind == "tpl":
         if "tpl_post" not in cache:
             wl = W.template_workload(D=12, M=2048, K=16)
             cache["tpl_post"] = (P.Posterior(12, wl["bmin"], wl["bmax"]).add_template(wl["A"], wl["C"], wl["dobs"]),
                                  P.Parabox(wl["bmin"], wl["bmax"]))
+            cache["tpl_fisher"] = (W.template_fisher(wl), wl["theta0"])
         post, box = cache["tpl_post"]
+        F, theta0 = cache["tpl_fisher"]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.random_pos_proposal(rng, 16, -np.ones(12), np.ones(12))
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, F, -np.ones(12), np.ones(12))
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=-1, seed=seed, prop_hi=2.0)
     w, mu, cov, df = wl["prop"]
@@ -359,58 +385,85 @@ def build_spec(P, W, spec, cache):
     return prop, post, None
 
 
+def _iterate_each(P, runs, betas, reps):
+    """Seconds per pass of one iteration of every run, one run at a time."""
+    import torch
+    for r, b in zip(runs, betas):  # warm-up
+        try:
+            r.iterate(b)
+        except P.PmcgError:
+            pass
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for r, b in zip(runs, betas):
+            try:
+                r.iterate(b)
+            except P.PmcgError:
+                pass
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps
+
+
 def batch_bench(P, W, R=256, iters=5):
-    """256 ragged runs: one persistent launch per iteration vs the same runs one at a time."""
+    """256 ragged runs: one persistent launch per iteration vs the same runs one at
+    a time (mixed precision) and vs the plain FP64 path one at a time."""
     specs = ragged_specs(R)
     cache = {}
     built = [build_spec(P, W, s, cache) for s in specs]
+    betas = np.array([s[5] for s in specs])
     runs_b = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
-    runs_s = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
     total = sum(s[3] for s in specs)
     batch = P.Batch(runs_b)
     t0 = time.perf_counter()
     batch.autotune()
     tune_s = time.perf_counter() - t0
-    batch.iterate()  # warm-up
+    batch.iterate(betas)  # warm-up
     ms = []
     failed = 0
     for _ in range(iters):
-        st = batch.iterate()
+        st = batch.iterate(betas)
         ms.append(batch.last_ms())
         failed += sum(1 for x in st if x["status"] != 0)
-    for r in runs_s:  # warm-up of the one-at-a-time path
-        try:
-            r.iterate()
-        except P.PmcgError:
-            pass
-    import torch
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(2):
-        for r in runs_s:
-            try:
-                r.iterate()
-            except P.PmcgError:
-                pass
-    seq_s = (time.perf_counter() - t0) / 2
     med = float(np.median(ms))
     cfg = batch.config()
     batch.free()
-    return {"workload": f"{R} runs, half SN (D=6), half GMM (D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5)",
-            "samples_per_iter": total, "value": total / (med / 1e3), "unit": UNIT, "ms_per_iter": med,
+    del runs_b
+    runs_s = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    seq_s = _iterate_each(P, runs_s, betas, 2)
+    for r in runs_s:
+        r.free()
+    runs_64 = [P.Run(pp, po, s[3], precision=P.FP64, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    fp64_s = _iterate_each(P, runs_64, betas, 1)
+    for r in runs_64:
+        r.free()
+    value = total / (med / 1e3)
+    return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + flat nuisance), half GMM "
+                        f"(D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5), beta from the log tempering schedule "
+                        f"(t_min {TEMPER_TMIN}, {TEMPER_LEVELS} levels)",
+            "samples_per_iter": total, "value": value, "unit": UNIT, "ms_per_iter": med,
             "one_run_at_a_time_samples_per_s": total / seq_s, "speedup_vs_one_at_a_time": (seq_s * 1e3) / med,
+            "fp64_one_run_at_a_time_samples_per_s": total / fp64_s,
+            "speedup_mixed_vs_fp64": value / (total / fp64_s),
             "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed,
-            "timing": "CUDA events around each graph launch (library stream), median of iterations"}
+            "timing": "CUDA events around each graph launch (library stream), median of iterations; the one-at-a-time "
+                      "legs by host clock around a synchronised pass over all runs"}
 
 
-def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4):
-    """Poisson arrivals of jobs (90% from the ragged mix, 10% template-sized), 5-10 iterations each."""
+def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4, fp64_jobs=96):
+    """Poisson arrivals of jobs (90% from the ragged mix, 10% template-sized), 5-10
+    iterations each on the log tempering schedule; and the plain FP64 path on jobs
+    drawn from the same mix, run one after another."""
     rng = np.random.default_rng(seed)
     pool_specs = ragged_specs(64, seed=99)
     cache = {}
     pool = [(s, build_spec(P, W, s, cache)) for s in pool_specs]
-    tpl_spec = ("tpl", 12, 16, 262144, 91)
+    tpl_spec = ("tpl", 12, 16, 262144, 91, 1.0)
     tpl = (tpl_spec, build_spec(P, W, tpl_spec, cache))
+
+    def pick(r):
+        return tpl if r.uniform() < 0.1 else pool[int(r.integers(0, len(pool)))]
+
     out = []
     for rate in rates:
         srv = P.Server()
@@ -422,9 +475,10 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
             dt = arrivals[i] - (time.perf_counter() - t_start)
             if dt > 0:
                 time.sleep(dt)
-            spec, (pp, po, bx) = tpl if rng.uniform() < 0.1 else pool[int(rng.integers(0, len(pool)))]
+            spec, (pp, po, bx) = pick(rng)
             niter = int(rng.integers(5, 11))
-            ids.append((srv.submit(pp, po, spec[3], niter, int(rng.integers(1, 1 << 30)), box=bx), spec[3], niter))
+            ids.append((srv.submit(pp, po, spec[3], niter, int(rng.integers(1, 1 << 30)), box=bx,
+                                   tempering=P.TEMPERING_LOG, t_min=TEMPER_TMIN), spec[3], niter))
         res = [(srv.wait(j, timeout=600), n, it) for j, n, it in ids]
         wall = time.perf_counter() - t_start
         info = srv.info()
@@ -440,9 +494,36 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
                     "p99_ms": float(np.percentile(lat, 99) * 1e3) if len(lat) else None,
                     "samples_per_s": samples / wall, "peak_resident": info["peak_resident"],
                     "epochs": info["epochs"]})
+    # plain FP64 path: jobs of the same mix, each run to completion before the next
+    import torch
+    r64 = np.random.default_rng(seed + 1)
+    jobs = []
+    for _ in range(fp64_jobs):
+        spec, (pp, po, bx) = pick(r64)
+        jobs.append((spec, pp, po, bx, int(r64.integers(5, 11)), int(r64.integers(1, 1 << 30))))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    samples64, failed64 = 0, 0
+    for spec, pp, po, bx, niter, sd in jobs:
+        run = P.Run(pp, po, spec[3], precision=P.FP64, seed=sd, box=bx)
+        try:
+            for it in range(niter):
+                run.iterate(P.get_tempering_beta(P.TEMPERING_LOG, it, TEMPER_TMIN, niter))
+            samples64 += spec[3] * niter
+        except P.PmcgError:
+            failed64 += 1
+        run.free()
+    torch.cuda.synchronize()
+    fp64_rate = samples64 / (time.perf_counter() - t0)
+    peak = max(r["samples_per_s"] for r in out)
     return {"workload": "Poisson arrivals; 90% jobs from the ragged mix, 10% template-sized (D=12, N=2^18, "
-                        "M=2048); 5-10 iterations per job; mixed precision",
-            "latency": "job submit to result (server clock)", "rates": out}
+                        "M=2048, Fisher start); 5-10 iterations per job on the log tempering schedule "
+                        f"(t_min {TEMPER_TMIN}); mixed precision",
+            "latency": "job submit to result (server clock)", "rates": out,
+            "fp64": {"samples_per_s": fp64_rate, "jobs": fp64_jobs, "failed": failed64,
+                     "how": "plain FP64 runs of jobs drawn from the same mix (job creation included), one job "
+                            "at a time, host clock"},
+            "speedup_mixed_vs_fp64": peak / fp64_rate}
 
 
 def cpu_baseline(O, W, nsample, seed=5):
@@ -463,6 +544,13 @@ def cpu_baseline(O, W, nsample, seed=5):
     return nsample * reps / el, O.num_threads(), reps
 
 
+def workload_config(N, world):
+    """The config of both arms (identical keys and values)."""
+    return {"workload": WORKLOAD, "global_batch": N * world, "nsamples_per_gpu": N, "D": 32, "K": 64, "nu": 3,
+            "target_components": 16, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "flushed between steps (256 MB write); per-iteration arrays also exceed L2"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -476,7 +564,7 @@ def run_reference(args):
     wt, mut, covt, _ = wl["target"]
     prop = O.Mix(w, mu, cov, df=df)
     target = O.Mix(wt, mut, covt, df=-1)
-    n = args.cpu_sample
+    n = args.nsamples   # the whole workload per step, as the GPU arm
     for i in range(args.warmup):
         O.iterate_mix(prop.copy(), target, 0.0, n, 5, i, check=False)
     times = []
@@ -491,9 +579,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded, shapes of the mixture microbench)",
-        "config": {"workload": WORKLOAD, "global_batch": n, "sample_per_step": n, "parallelism": "host threads"},
+        "config": workload_config(n, world),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-                         "sample": f"{n} samples of the N=2^20 workload per step (oracle/pmc_oracle.c, OpenMP)"},
+                         "sample": f"the whole workload ({n} samples) per step; oracle/pmc_oracle.c, OpenMP over "
+                                   f"all host threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -648,22 +737,25 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
     except OSError:
         pass
     sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    # algorithmic flops of the proposal log-density: per (sample, component) the
-    # triangular product L^-1 (x - mu) (D (D+1) / 2 multiply-adds) and |y|^2 (D)
-    flops = N * K * (D * (D + 1) + 2 * D)
+    # algorithmic flops of the proposal log-density per launch: the batched
+    # Mahalanobis contraction X [N x D] times K factors [D x D], 2 N K D^2
+    flops = 2.0 * N * K * D * D
     t_ms = per_stage["logq"]
     achieved = flops / (t_ms / 1000.0) / 1e12
     if tc:
         bf16 = peaks.get("bf16_tflops")
-        peak = bf16 / 2.0 if bf16 else 1900.0 / 2.0
+        peak = bf16 if bf16 else 1900.0
         roof = {"bound": "tensor", "kernel": "umma_logq_kernel (tcgen05 kind::tf32, three-term split)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                # DRAM bytes per launch at this workload from the ncu capture in profiles/ (lt and Q writes dominate)
+                # DRAM bytes per launch at this workload from an ncu capture (lt and Q writes dominate)
                 "traffic": UMMA_TRAFFIC_BYTES, "stage_ms": per_stage,
-                "peak_note": ("dense TF32 = half the measured cuBLAS bf16 burst rate of MEASURED_PEAKS.json"
-                              if bf16 else "dense TF32 = half the fallback bf16 1.9 PFLOP/s"),
-                "flops_note": "algorithmic FP32 flops D(D+1)+2D per (sample, component); the tensor cores "
-                              "execute 3x that (TF32 split) on the lower triangle"}
+                "peak_note": ("measured cuBLAS bf16 dense burst rate (MEASURED_PEAKS.json bf16_tflops)"
+                              if bf16 else "fallback bf16 1.9 PFLOP/s"),
+                "flops_note": "2 N K D^2 per launch (the full D x D product per sample and component); the "
+                              "kernel multiplies only the lower triangle, three times (TF32 split), in "
+                              "kind::tf32, whose dense rate is half the bf16 one: against that rate "
+                              f"frac = {2 * achieved / peak:.3f}",
+                "tf32_frac": 2 * achieved / peak}
     else:
         fp32_peak = 152 * 128 * 2 * (sm_mhz * 1e6) / 1e12
         roof = {"bound": "fp32", "kernel": "mixlogpdf_f32_kernel", "achieved": achieved, "peak": fp32_peak,
@@ -674,12 +766,10 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "global_batch": N * world, "nsamples_per_gpu": N, "D": 32, "K": 64,
-                   "nu": 3, "target_components": 16, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed between steps (256 MB write); per-iteration arrays also exceed L2",
-                   "timing": "CUDA events on the library stream around each iteration as run in production "
-                             "(one replayed CUDA graph per iteration); roofline.stage_ms from 3 more iterations "
-                             "with every kernel launched directly"},
+        "config": workload_config(N, world),
+        "timing": "CUDA events on the library stream around each iteration as run in production (one replayed CUDA "
+                  "graph per iteration); roofline.stage_ms from 3 more iterations with every kernel launched "
+                  "directly",
         "fp64": fp64,
         "iteration_stats": {k: stats[k] for k in ("ln_evidence", "perplexity", "ess", "enc")},
         "e2e": e2e,

@@ -341,13 +341,15 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
   b->hdesc.resize(nruns);
   for (int r = 0; r < nruns; r++) {
     pmcg_run *run = runs[r];
-    const Work &w = run->w;
-    if (!run || w.prec != PMCG_MIXED || w.D > 32 || !run->post || run->post->plugins.size() != 1) {
+    if (!run || run->w.prec != PMCG_MIXED || run->w.D > 32 || !run->post || run->post->plugins.size() != 1 ||
+        run->post->has_prior) {
       set_error(err, PMCG_EUNSUPPORTED, __LINE__,
-                "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood", r);
+                "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood (no subset prior)",
+                r);
       delete b;
       return nullptr;
     }
+    const Work &w = run->w;
     const Plugin &pl = run->post->plugins[0];
     BatchDesc &d = b->hdesc[r];
     memset(&d, 0, sizeof(d));

@@ -167,6 +167,11 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
         return false;
     }
   }
+  if (p->has_prior) {
+    w.launches += 1;
+    if (!CK(launch_prior(w.prec, p->prior, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.s), "prior kernel"))
+      return false;
+  }
   return true;
 }
 
@@ -242,6 +247,7 @@ extern "C" pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, con
       p->logpr -= std::log(max[j] - min[j]);
     }
   }
+  p->logpr_box = p->logpr;
   restamp(p);
   return p;
 }
@@ -254,6 +260,7 @@ extern "C" void pmcg_posterior_free(pmcg_posterior **p) {
     if (pl.sn.arena) cudaFree(pl.sn.arena);
     if (pl.tpl.arena) cudaFree(pl.tpl.arena);
   }
+  if ((*p)->prior.arena) cudaFree((*p)->prior.arena);
   delete *p;
   *p = nullptr;
 }
@@ -269,6 +276,133 @@ extern "C" void pmcg_posterior_add_mixmvdens(pmcg_posterior *p, const mix_mvdens
   if (!CK(devmix_alloc(pl.mix, target->ncomp, target->ndim, df), "target buffers")) return;
   if (!upload_mix(pl.mix, target, 0, err)) { devmix_free(pl.mix); return; }
   p->plugins.push_back(pl);
+  restamp(p);
+}
+
+// prior_log_pdf_special (wrappers/src/param.c:1055-1101): a constant per point,
+// log of the box volume of the affected parameters minus log of the special
+// prior's volume; applied once per point with the flat prior (:994-999).
+extern "C" void pmcg_posterior_set_special(pmcg_posterior *p, int special, int ind_w0, int ind_w1, double a_acc,
+                                           error **err) {
+  if (!p) {
+    set_error(err, PMCG_EARG, __LINE__, "null posterior");
+    return;
+  }
+  double c = 0.0;
+  const bool box = !p->min.empty();
+  switch (special) {
+    case PMCG_SPECIAL_NONE:
+      break;
+    case PMCG_SPECIAL_UNITY:
+      // minus the default flat prior
+      if (box)
+        for (int i = 0; i < p->npar; i++) c += std::log(p->max[i] - p->min[i]);
+      break;
+    case PMCG_SPECIAL_DE_CONSERVATIVE: {
+      if (ind_w0 < -1 || ind_w0 >= p->npar || ind_w1 < -1 || ind_w1 >= p->npar || (ind_w1 >= 0 && ind_w0 < 0) ||
+          (ind_w1 >= 0 && !(a_acc < 1.0))) {
+        set_error(err, PMCG_EARG, __LINE__, "de_conservative: parameter indices (%d, %d) or a_acc %g invalid",
+                  ind_w0, ind_w1, a_acc);
+        return;
+      }
+      if (ind_w0 < 0) break;  // no w0_de among the parameters: nothing added
+      if (!box) {
+        set_error(err, PMCG_EARG, __LINE__, "de_conservative needs the prior box of w0_de");
+        return;
+      }
+      const double lo = p->min[ind_w0], hi = p->max[ind_w0];
+      if (lo > -1.0 || hi < -1.0 / 3.0) {
+        set_error(err, PMCG_EARG, __LINE__,
+                  "Range of w0_de [%g;%g] should not be smaller than de_conservative prior [-1;-1/3]", lo, hi);
+        return;
+      }
+      if (ind_w1 < 0) {
+        c = std::log(hi - lo) - std::log(2.0 / 3.0);
+      } else {
+        const double t = 0.5 * (2.0 / 3.0) * (2.0 / 3.0);
+        c = std::log(hi - lo) + std::log(p->max[ind_w1] - p->min[ind_w1]) - std::log(t / (1.0 - a_acc)) -
+            std::log(t);
+      }
+      break;
+    }
+    default:
+      set_error(err, PMCG_EARG, __LINE__, "Unknown special prior type %d", special);
+      return;
+  }
+  p->special = special;
+  p->logpr_special = c;
+  p->logpr = p->logpr_box + c;
+  restamp(p);
+}
+
+// The config prior with indprior (wrappers/src/param.c:1009-1026): the prior's
+// coordinates are the flagged parameters in increasing order.
+extern "C" void pmcg_posterior_add_mvdens_prior(pmcg_posterior *p, const mvdens *prior, const int *indprior,
+                                                error **err) {
+  if (!p || !prior || prior->ndim < 1) {
+    set_error(err, PMCG_EARG, __LINE__, "invalid prior");
+    return;
+  }
+  const int d = prior->ndim;
+  std::vector<int> idx;
+  for (int j = 0; j < p->npar; j++)
+    if (!indprior || indprior[j] == 1) idx.push_back(j);
+  if ((int)idx.size() != d) {
+    set_error(err, PMCG_EDIM, __LINE__, "prior has %d dimensions, %d parameters are flagged", d, (int)idx.size());
+    return;
+  }
+  // Cholesky factor (copy), its inverse (packed rows) and the constant
+  std::vector<double> L((size_t)d * d, 0.0);
+  double logdetL = 0.0;
+  if (prior->chol) {
+    for (int i = 0; i < d; i++)
+      for (int j = 0; j <= i; j++) L[(size_t)i * d + j] = prior->std[(size_t)i * d + j];
+    for (int i = 0; i < d; i++) logdetL += std::log(L[(size_t)i * d + i]);
+  } else if (host_cholesky(d, prior->std, L.data(), &logdetL) != 0) {
+    set_error(err, PMCG_ECHOL, __LINE__, "prior covariance is not positive definite");
+    return;
+  }
+  // L^-1 by forward substitution of the identity columns; stored as packed rows
+  std::vector<double> Wt((size_t)d * (d + 1) / 2), Winv((size_t)d * d, 0.0);
+  for (int c = 0; c < d; c++) {
+    for (int i = c; i < d; i++) {
+      double t = (i == c) ? 1.0 : 0.0;
+      for (int k = c; k < i; k++) t -= L[(size_t)i * d + k] * Winv[(size_t)k * d + c];
+      Winv[(size_t)i * d + c] = t / L[(size_t)i * d + i];
+    }
+  }
+  for (int i = 0, o = 0; i < d; i++)
+    for (int j = 0; j <= i; j++) Wt[o++] = Winv[(size_t)i * d + j];
+  PriorDev pd;
+  pd.d = d;
+  pd.df = prior->df > 0 ? prior->df : -1;
+  for (int i = 0; i < d; i++) pd.idx[i] = idx[i];
+  if (pd.df > 0) {
+    const double nu = pd.df;
+    pd.lconst = std::lgamma(0.5 * (nu + d)) - std::lgamma(0.5 * nu) - 0.5 * d * std::log(nu * PMCG_PI) - logdetL;
+  } else {
+    pd.lconst = -0.5 * d * PMCG_LN2PI - logdetL;
+  }
+  const size_t nw = Wt.size();
+  Carver cv;
+  for (int pass = 0; pass < 2; pass++) {
+    cv.off = 0;
+    pd.mu = cv.take<double>(d); pd.Wt = cv.take<double>(nw);
+    pd.mu32 = cv.take<float>(d); pd.Wt32 = cv.take<float>(nw);
+    if (pass == 0) {
+      if (!CK(cudaMalloc(&pd.arena, cv.off + 256), "prior buffers")) return;
+      cv.base = (char *)pd.arena;
+    }
+  }
+  std::vector<float> mu32(prior->mean, prior->mean + d), Wt32(Wt.begin(), Wt.end());
+  const bool ok = CK(cudaMemcpy(pd.mu, prior->mean, 8 * (size_t)d, cudaMemcpyHostToDevice), "prior upload") &&
+                  CK(cudaMemcpy(pd.Wt, Wt.data(), 8 * nw, cudaMemcpyHostToDevice), "prior upload") &&
+                  CK(cudaMemcpy(pd.mu32, mu32.data(), 4 * (size_t)d, cudaMemcpyHostToDevice), "prior upload") &&
+                  CK(cudaMemcpy(pd.Wt32, Wt32.data(), 4 * nw, cudaMemcpyHostToDevice), "prior upload");
+  if (!ok) { cudaFree(pd.arena); return; }
+  if (p->prior.arena) cudaFree(p->prior.arena);
+  p->prior = pd;
+  p->has_prior = true;
   restamp(p);
 }
 

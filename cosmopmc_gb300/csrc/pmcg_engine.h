@@ -67,9 +67,14 @@ size_t work_bytes(int K, int D, int df, int prec, size_t N);
 
 struct pmcg_posterior {
   int npar = 0;
-  double logpr = 0.0;
+  double logpr = 0.0;          // constant per point: logpr_box + logpr_special
+  double logpr_box = 0.0;      // flat box prior, -sum log(max - min)
+  double logpr_special = 0.0;  // special prior (volume correction)
+  int special = 0;
   std::vector<double> min, max;
   std::vector<pmcg::Plugin> plugins;
+  bool has_prior = false;      // Gaussian / Student-t prior on a parameter subset
+  pmcg::PriorDev prior;
   uint64_t stamp = 0;  // new at allocation and at every change (unique over the process)
 };
 

@@ -190,6 +190,21 @@ constexpr int kGramMaxP = 96;
 cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X64, const float *X32, int ldx,
                        double *logpost, const short *flg, cudaStream_t s);
 
+// (c) Gaussian / Student-t prior on a subset of the parameters (the config
+// prior with indprior of posterior_log_pdf_common, wrappers/src/param.c:1009-1026):
+// logpost[n] += lconst - 1/2 Q (Gaussian) or lconst - (nu+d)/2 ln(1 + Q/nu),
+// Q = |L^-1 (x_sub - mu)|^2, x_sub = the parameters idx[0..d).
+struct PriorDev {
+  int d = 0, df = -1;
+  int idx[kMaxD] = {};
+  double lconst = 0.0;   // log normalising constant, -log det L included
+  double *mu = nullptr, *Wt = nullptr;       // [d], L^-1 packed by rows [d(d+1)/2]
+  float *mu32 = nullptr, *Wt32 = nullptr;
+  void *arena = nullptr;
+};
+cudaError_t launch_prior(int precision, const PriorDev &p, size_t N, int D, const double *X64, const float *X32,
+                         int ldx, double *logpost, cudaStream_t s);
+
 // Helpers.
 cudaError_t launch_fill_f64(double *p, size_t n, double v, cudaStream_t s);
 cudaError_t launch_x64_to_x32(size_t N, int D, int ldx, const double *X64, float *X32, cudaStream_t s);

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_HERE, "libpmcg.so")
 
 FP64 = 0
 MIXED = 1
+SPECIAL_NONE, SPECIAL_UNITY, SPECIAL_DE_CONSERVATIVE = 0, 1, 2
 TEMPERING_NONE, TEMPERING_LINEAR, TEMPERING_LOG = 0, 1, 2
 SN_CHI2_FULL, SN_CHI2_MARG = 0, 1
 
@@ -179,6 +180,8 @@ SIGNATURES = [
     ("pmcg_posterior_add_mixmvdens", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_posterior_add_snia", None, [C.c_void_p, C.POINTER(SnData), PErr]),
     ("pmcg_posterior_add_template", None, [C.c_void_p, C.c_int, _dp, _dp, _dp, PErr]),
+    ("pmcg_posterior_set_special", None, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, PErr]),
+    ("pmcg_posterior_add_mvdens_prior", None, [C.c_void_p, C.POINTER(Mvdens), C.POINTER(C.c_int), PErr]),
     ("pmcg_posterior_log_pdf_void", C.c_double, [C.c_void_p, _dp, PErr]),
     ("pmcg_fisher_matrix", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _dp, PErr]),
     ("clip_weights", None, [C.POINTER(PmcSimuS), C.c_int, C.c_void_p, PErr]),
@@ -539,6 +542,26 @@ class Posterior:
         s.def_Omegam, s.def_w0, s.def_M = float(sn["def_om"]), float(sn["def_w0"]), float(sn["def_M"])
         s.def_alpha, s.def_beta = float(sn["def_alpha"]), float(sn["def_beta"])
         call("pmcg_posterior_add_snia", self.p, C.byref(s))
+        return self
+
+    def set_special(self, special, ind_w0=-1, ind_w1=-1, a_acc=0.0):
+        """Special prior (SPECIAL_NONE / SPECIAL_UNITY / SPECIAL_DE_CONSERVATIVE)."""
+        call("pmcg_posterior_set_special", self.p, int(special), int(ind_w0), int(ind_w1), float(a_acc))
+        return self
+
+    def add_prior(self, mean, cov, df=-1, indprior=None):
+        """Gaussian (df <= 0) or Student-t prior on the parameters flagged by indprior."""
+        mean, cov = _f64(mean), _f64(cov)
+        d = len(mean)
+        m = Mvdens()
+        m.ndim, m.df, m.band_limit, m.chol, m.det = d, int(df), d, 0, 0.0
+        m.mean = _dptr(mean)
+        m.std = _dptr(cov)
+        ind = None
+        if indprior is not None:
+            ind = np.ascontiguousarray(indprior, dtype=np.int32)
+        call("pmcg_posterior_add_mvdens_prior", self.p, C.byref(m),
+             None if ind is None else ind.ctypes.data_as(C.POINTER(C.c_int)))
         return self
 
     def add_template(self, A, Cm, dobs):

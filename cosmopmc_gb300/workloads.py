@@ -217,3 +217,22 @@ def template_workload(D=12, M=2048, K=16, rho=0.9, seed=91):
     bmin, bmax = -np.ones(D), np.ones(D)
     w, mu, covs, df = random_pos_proposal(np.random.default_rng(seed + 1), K, bmin, bmax)
     return dict(A=A, C=Cm, dobs=dobs, bmin=bmin, bmax=bmax, prop=(w, mu, covs, df), theta0=theta0)
+
+
+def template_fisher(tw, theta=None):
+    """Fisher matrix J^T C^-1 J of the template likelihood at theta (default the
+    truth theta0), J = A dphi/dtheta (exact for the quadratic monomials)."""
+    theta = np.asarray(tw["theta0"] if theta is None else theta, float)
+    D = len(theta)
+    P = tpl_nphi(D)
+    dphi = np.zeros((P, D))
+    for i in range(D):
+        dphi[1 + i, i] = 1.0
+    p = 1 + D
+    for i in range(D):
+        for j in range(i, D):
+            dphi[p, i] += theta[j]
+            dphi[p, j] += theta[i]
+            p += 1
+    J = tw["A"] @ dphi
+    return J.T @ np.linalg.solve(tw["C"], J)

@@ -309,6 +309,36 @@ void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *sn, error **
 void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const double *A, const double *C,
                                  const double *dobs, error **err);
 
+/* Special prior, as prior_log_pdf_special (wrappers/src/param.c:1055-1101),
+ * added once per point with the flat box prior (:994-999). It is a constant:
+ * the log of the box volume of the affected parameters minus the log of the
+ * special prior's volume.
+ *  PMCG_SPECIAL_NONE: 0.
+ *  PMCG_SPECIAL_UNITY: + sum log(max - min) (cancels the flat prior).
+ *  PMCG_SPECIAL_DE_CONSERVATIVE: ind_w0 (< 0: no w0_de parameter, nothing
+ *    added) alone: log(max_w0 - min_w0) - log(2/3); with ind_w1 >= 0:
+ *    log(max_w0 - min_w0) + log(max_w1 - min_w1) - log(1/2 (2/3)^2 / (1 - a_acc))
+ *    - log(1/2 (2/3)^2). a_acc is the scale factor constant that nicaea (the
+ *    reference's cosmology library, absent here) supplies; the caller passes it.
+ *    A w0_de range narrower than [-1, -1/3] is PMCG_EARG (the reference's
+ *    mk_special_prior). The per-point dark-energy range test that the
+ *    reference's likelihood plugins apply under this prior lives in nicaea and
+ *    is not provided.
+ * Calling again replaces the previous choice. */
+#define PMCG_SPECIAL_NONE 0
+#define PMCG_SPECIAL_UNITY 1
+#define PMCG_SPECIAL_DE_CONSERVATIVE 2
+void pmcg_posterior_set_special(pmcg_posterior *p, int special, int ind_w0, int ind_w1, double a_acc, error **err);
+
+/* Gaussian or Student-t prior on a subset of the parameters (the config prior
+ * with indprior, wrappers/src/param.c:1009-1026): mvdens_log_pdf(prior, x_sub)
+ * is added to every point's log-posterior, x_sub = the parameters j with
+ * indprior[j] == 1 in increasing order (indprior NULL: every parameter);
+ * prior->ndim must equal their number. The prior is copied (covariance, or its
+ * Cholesky factor when prior->chol == 1). A second call replaces the first.
+ * Batched runs and served jobs do not take posteriors with such a prior. */
+void pmcg_posterior_add_mvdens_prior(pmcg_posterior *p, const mvdens *prior, const int *indprior, error **err);
+
 /* Single-point log-posterior (the per-point callback shape); evaluates one
  * point on the GPU. Passing this function to the weight step selects the
  * batched device evaluation. */

@@ -95,6 +95,9 @@ def lib():
                                       C.c_double, C.POINTER(Stats), C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_iterate_mix.restype = C.c_int
         L.orc_num_threads.restype = C.c_int
+        L.orc_prior_special.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double,
+                                        C.POINTER(C.c_double)]
+        L.orc_prior_special.restype = C.c_int
         L.orc_weighted_summary.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, _ip]
         L.orc_hist1d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, C.c_double, _dp]
         L.orc_hist2d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, C.c_int, C.c_int, _dp, _dp,
@@ -328,6 +331,62 @@ def iterate_mix(prop: Mix, target: Mix, logprior, N, seed, call, beta=1.0, bmin=
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def prior_special(special, bmin, bmax, ind_w0=-1, ind_w1=-1, a_acc=0.0):
+    """The special prior's constant (wrappers/src/param.c:1055-1101)."""
+    bmin = np.ascontiguousarray(bmin, dtype=np.float64)
+    bmax = np.ascontiguousarray(bmax, dtype=np.float64)
+    out = C.c_double()
+    rc = lib().orc_prior_special(int(special), len(bmin), bmin, bmax, int(ind_w0), int(ind_w1), float(a_acc),
+                                 C.byref(out))
+    if rc:
+        raise ValueError("w0 range narrower than the de_conservative prior")
+    return out.value
+
+
+def mvdens_prior_logpdf(mean, cov, df, X, indprior=None):
+    """mvdens_log_pdf of the parameters flagged by indprior (all when None), as the
+    config prior of posterior_log_pdf_common (wrappers/src/param.c:1009-1026): a
+    one-component mixture of weight 1 through the oracle's mixture log-pdf."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    cols = np.arange(X.shape[1]) if indprior is None else np.flatnonzero(np.asarray(indprior) == 1)
+    m = Mix([1.0], np.atleast_2d(mean), cov=np.asarray(cov)[None], df=df)
+    return mix_logpdf(m, np.ascontiguousarray(X[:, cols]))
+
+
+def iterate_posterior(prop: Mix, logpost_fn, N, seed, call, beta=1.0, bmin=None, bmax=None):
+    """One whole FP64 iteration in the order of run_pmc_iteration_MPI
+    (exec/cosmo_pmc.c:313-399) with any log-posterior, composed from the
+    oracle's primitives (the same steps as orc_iterate_mix): the draw of
+    (seed, call), log q with its per-component terms, logpost_fn(X, flg) ->
+    (log posterior, ok) where ok = 0 marks a failed likelihood, the log-weights
+    (non-finite ones flagged out), the normalisation, perplexity/ESS and the
+    Rao-Blackwellised update. Returns (updated Mix or None when every component
+    died, stats); stats["status"] is 0, or -1 when no sample had a weight and -2
+    when the update buried every component."""
+    u, z, chi2 = randoms(seed, call, N, prop.D, prop.df)
+    X, idx, flg, _ = draw(prop, u, z, chi2, bmin, bmax)
+    logq, lt, Q = mix_logpdf(prop, X, want_terms=True)
+    lp, ok = logpost_fn(X, flg)
+    flg = (flg.astype(bool) & (np.asarray(ok) != 0)).astype(np.int16)
+    logw = logweights(beta, lp, logq, flg)
+    flg[~np.isfinite(logw)] = 0
+    st = {"nok": int(flg.sum()), "status": 0}
+    try:
+        wbar, ls, mw = normalize(logw, flg)
+    except ValueError:
+        st["status"] = -1
+        return None, st
+    perp, ess = perplexity(wbar, flg)
+    st.update(logSum=ls, maxW=mw, ln_evidence=ls - np.log(N), perplexity=perp, ess=ess)
+    try:
+        new, dead = update_rb(prop, X, wbar, flg, lt, logq, Q if prop.df > 0 else None, idx)
+    except ValueError:
+        st["status"] = -2
+        return None, st
+    st.update(enc=enc(new.w), ndead=int(dead.sum()))
+    return new, st
 
 
 def weighted_summary(X, wbar, flg, median=False):

@@ -703,3 +703,28 @@ void orc_hist2d(size_t N, int D, const double *X, const double *wbar, const shor
     if (bp >= 0 && bq >= 0) hist[(size_t)bp * nbin + bq] += wbar[i] * scale;
   }
 }
+
+/* ---------------------------------------------------------------- special prior
+ * prior_log_pdf_special, wrappers/src/param.c:1055-1101: unity returns
+ * sum log(max - min) (minus the default flat prior); de_conservative returns
+ * the box volume of w0 (and w1) minus the special prior's volume, and fails
+ * when the w0 range is narrower than [-1, -1/3] (:1082-1084). */
+int orc_prior_special(int special, int npar, const double *min, const double *max, int ind_w0, int ind_w1,
+                      double a_acc, double *out) {
+  *out = 0.0;
+  if (special == 1) {
+    double s = 0.0;
+    for (int i = 0; i < npar; i++) s += log(max[i] - min[i]);
+    *out = s;
+    return 0;
+  }
+  if (special != 2 || ind_w0 < 0) return 0;
+  if (min[ind_w0] > -1.0 || max[ind_w0] < -1.0 / 3.0) return -1;
+  if (ind_w1 < 0) {
+    *out = log(max[ind_w0] - min[ind_w0]) - log(2.0 / 3.0);
+  } else {
+    *out = log(max[ind_w0] - min[ind_w0]) + log(max[ind_w1] - min[ind_w1]) -
+           log(0.5 * 2.0 / 3.0 * 2.0 / 3.0 / (1.0 - a_acc)) - log(0.5 * 2.0 / 3.0 * 2.0 / 3.0);
+  }
+  return 0;
+}

@@ -95,6 +95,13 @@ int orc_iterate_mix(int K, int D, int df, double *w, double *mu, double *L, doub
 
 int orc_num_threads(void);
 
+/* Special prior (prior_log_pdf_special, wrappers/src/param.c:1055-1101): the
+ * constant added once per point to the flat prior. special 0 none, 1 unity,
+ * 2 de_conservative (ind_w0/ind_w1 < 0: absent). Returns 0, or -1 when the w0
+ * range is narrower than [-1, -1/3] (the reference's mk_special_prior). */
+int orc_prior_special(int special, int npar, const double *min, const double *max, int ind_w0, int ind_w1,
+                      double a_acc, double *out);
+
 /* Post-processing: marginal centre (mean or median) and one-sided 68.27 /
  * 95.45 / 99.73 % limits per parameter (sigma[6a .. 6a+5]: right, then left),
  * and weighted histograms (exec/exec_helper.c:63-271,
