@@ -325,7 +325,8 @@ def tempering_level(rng):
 
 def ragged_specs(R, seed=256):
     """Batched workload: R runs, half SN-type (740 supernovae, the six SN parameters
-    plus flat-prior nuisance parameters, D ~ U{6..20}, Fisher-matrix start), half
+    plus Gaussian nuisance parameters in a flat box, D ~ U{6..20}, Fisher-matrix
+    start), half
     Gaussian-mixture targets with D ~ U{2..20}; K ~ U{1..20}, N ~ logU(1e3, 1e5);
     each run at a tempering level of the log schedule."""
     rng = np.random.default_rng(seed)
@@ -341,7 +342,7 @@ def ragged_specs(R, seed=256):
     return specs
 
 
-NUIS_HALF = 1.0   # nuisance parameters: flat prior on [-1, 1]
+NUIS_HALF, NUIS_SD = 1.0, 0.25   # nuisance parameters: box [-1, 1], Gaussian term N(0, 0.25^2)
 
 
 def build_spec(P, W, spec, cache):
@@ -356,10 +357,13 @@ def build_spec(P, W, spec, cache):
             bmax = np.concatenate([W.SN_BOX_MAX, NUIS_HALF * np.ones(D - 6)])
             F = np.zeros((D, D))
             F[:6, :6] = cache["sn_fisher"]
-            F[6:, 6:] = np.eye(D - 6) / (0.5 * NUIS_HALF) ** 2   # nuisance: proposal sd 0.5 x sqrt(2)
+            F[6:, 6:] = np.eye(D - 6) / NUIS_SD ** 2
             theta0 = np.concatenate([W.SN_TRUTH, np.zeros(D - 6)])
-            cache[("sn_post", D)] = (P.Posterior(D, bmin, bmax).add_snia(cache["sn_data"]), P.Parabox(bmin, bmax),
-                                     F, theta0, bmin, bmax)
+            post = P.Posterior(D, bmin, bmax).add_snia(cache["sn_data"])
+            if D > 6:   # Gaussian nuisance parameters: a Gaussian term on the subset 6..D-1
+                post.add_prior(np.zeros(D - 6), NUIS_SD ** 2 * np.eye(D - 6), df=-1,
+                               indprior=np.r_[np.zeros(6, int), np.ones(D - 6, int)])
+            cache[("sn_post", D)] = (post, P.Parabox(bmin, bmax), F, theta0, bmin, bmax)
         post, box, F, theta0, bmin, bmax = cache[("sn_post", D)]
         rng = np.random.default_rng(seed)
         w, mu, cov, df = W.fisher_proposal(rng, K, theta0, F, bmin, bmax)
@@ -438,7 +442,7 @@ def batch_bench(P, W, R=256, iters=5):
     for r in runs_64:
         r.free()
     value = total / (med / 1e3)
-    return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + flat nuisance), half GMM "
+    return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + Gaussian nuisance in a flat box), half GMM "
                         f"(D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5), beta from the log tempering schedule "
                         f"(t_min {TEMPER_TMIN}, {TEMPER_LEVELS} levels)",
             "samples_per_iter": total, "value": value, "unit": UNIT, "ms_per_iter": med,

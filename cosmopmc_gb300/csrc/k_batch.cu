@@ -32,7 +32,7 @@ namespace cg = cooperative_groups;
 namespace pmcg {
 
 enum BatchStage {
-  kBDraw = 0, kBLogq, kBLogpost, kBWeights, kBWFinal, kBFactor, kBEmStats, kBEmFinal, kBRenorm, kBPrepComp,
+  kBDraw = 0, kBLogq, kBLogpost, kBPrior, kBWeights, kBWFinal, kBFactor, kBEmStats, kBEmFinal, kBRenorm, kBPrepComp,
   kBPrepConsts, kBStages
 };
 
@@ -43,6 +43,8 @@ struct BatchDesc {
   SnDev sn;
   TplDev tpl;
   double logpr;
+  int has_prior;
+  PriorDev prior;
   size_t N;
   int S, CHp, CHt, maxd;
   uint32_t key0, key1;
@@ -120,6 +122,9 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
       }
       break;
     }
+    case kBPrior:
+      body_prior_any<float>(d.prior, d.N, D, nullptr, d.X32, ldx, d.logpost, (size_t)li * blockDim.x + threadIdx.x);
+      break;
     case kBWeights:
       body_weights_tile<true>(d.N, dy.beta, d.logpost, d.logq, d.flg, d.logw, d.wpart, li, s_r);
       break;
@@ -166,6 +171,7 @@ __global__ void __launch_bounds__(256, 1) batch_kernel(const BatchDesc *__restri
   for (int stg = first; stg <= last; stg++) {
     const uint32_t *pre = starts + (size_t)stg * (R + 1);
     const uint32_t total = pre[R];
+    if (total == 0) continue;  // a stage without work (the same for every block) needs no barrier
     for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
       const int r = find_run(pre, R, item);
       batch_item<SPT>(stg, descs[r], dyn[r], item - pre[r], smem, s_r, &s_dead, stats_out, r);
@@ -186,6 +192,7 @@ static size_t items_of(int stg, const BatchDesc &d, int spt, int threads) {
       if (d.ptype == kPluginMix) return (N + (size_t)threads * spt - 1) / ((size_t)threads * spt);
       if (d.ptype == kPluginSn) return (N + (threads / 32) - 1) / (threads / 32);
       return (N + threads - 1) / threads;
+    case kBPrior: return d.has_prior ? (N + threads - 1) / threads : 0;
     case kBWeights:
     case kBFactor: return (N + kTileW - 1) / kTileW;
     case kBEmStats: return (size_t)K * d.S;
@@ -341,11 +348,9 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
   b->hdesc.resize(nruns);
   for (int r = 0; r < nruns; r++) {
     pmcg_run *run = runs[r];
-    if (!run || run->w.prec != PMCG_MIXED || run->w.D > 32 || !run->post || run->post->plugins.size() != 1 ||
-        run->post->has_prior) {
+    if (!run || run->w.prec != PMCG_MIXED || run->w.D > 32 || !run->post || run->post->plugins.size() != 1) {
       set_error(err, PMCG_EUNSUPPORTED, __LINE__,
-                "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood (no subset prior)",
-                r);
+                "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood", r);
       delete b;
       return nullptr;
     }
@@ -359,6 +364,8 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
     if (pl.type == kPluginSn) d.sn = pl.sn;
     if (pl.type == kPluginTpl) d.tpl = pl.tpl;
     d.logpr = run->post->logpr;
+    d.has_prior = run->post->has_prior ? 1 : 0;
+    d.prior = run->post->prior;
     d.N = w.N;
     d.S = w.S;
     d.CHp = mix_chunk(w.D, w.ldx, w.K);

@@ -76,50 +76,11 @@ cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X
   return cudaGetLastError();
 }
 
-// One thread per sample. The centred coordinates x_sub - mu are formed first
-// (so the single-precision form differences O(1) numbers, not O(|mu|) ones),
-// then y = L^-1 (x_sub - mu) row by row from the packed factor (broadcast
-// loads: every thread reads the same entry) and Q = |y|^2.
-template <typename Real, int MAXD>
+template <typename Real>
 __global__ void __launch_bounds__(128) prior_kernel(PriorDev p, size_t N, int D, const double *__restrict__ X64,
                                                     const float *__restrict__ X32, int ldx,
                                                     double *__restrict__ logpost) {
-  const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  const int d = p.d;
-  const Real *mu = (sizeof(Real) == 8) ? (const Real *)p.mu : (const Real *)p.mu32;
-  const Real *W = (sizeof(Real) == 8) ? (const Real *)p.Wt : (const Real *)p.Wt32;
-  Real c[MAXD];
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < d) {
-      const int j = p.idx[i];
-      const Real x = (sizeof(Real) == 8) ? (Real)X64[n * D + j] : (Real)X32[n * ldx + j];
-      c[i] = x - __ldg(mu + i);
-    }
-  }
-  Real q = 0;
-  int off = 0;
-#pragma unroll
-  for (int i = 0; i < MAXD; i++) {
-    if (i < d) {
-      Real y = 0;
-#pragma unroll
-      for (int j = 0; j <= i; j++) y = fma(__ldg(W + off + j), c[j], y);
-      q = fma(y, y, q);
-      off += i + 1;
-    }
-  }
-  // the variable term in the working precision, the constant added in FP64
-  Real v;
-  if (p.df > 0) {
-    const Real t = q / (Real)p.df;
-    if constexpr (sizeof(Real) == 4) v = -0.5f * ((float)p.df + (float)d) * log1pf(t);
-    else v = -0.5 * ((double)p.df + d) * log1p(t);
-  } else {
-    v = (Real)-0.5 * q;
-  }
-  logpost[n] += p.lconst + (double)v;
+  body_prior_any<Real>(p, N, D, X64, X32, ldx, logpost, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 cudaError_t launch_prior(int precision, const PriorDev &p, size_t N, int D, const double *X64, const float *X32,
@@ -127,13 +88,8 @@ cudaError_t launch_prior(int precision, const PriorDev &p, size_t N, int D, cons
   if (N == 0) return cudaSuccess;
   if (p.d < 1 || p.d > kMaxD) return cudaErrorInvalidValue;
   const unsigned grid = (unsigned)((N + 127) / 128);
-  if (precision == 0) {
-    if (p.d <= 8) prior_kernel<double, 8><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
-    else prior_kernel<double, kMaxD><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
-  } else {
-    if (p.d <= 8) prior_kernel<float, 8><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
-    else prior_kernel<float, kMaxD><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
-  }
+  if (precision == 0) prior_kernel<double><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
+  else prior_kernel<float><<<grid, 128, 0, s>>>(p, N, D, X64, X32, ldx, logpost);
   return cudaGetLastError();
 }
 

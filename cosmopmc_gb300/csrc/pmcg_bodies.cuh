@@ -672,6 +672,63 @@ __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const 
   }
 }
 
+// ================================================================== (c) subset prior
+// Gaussian / Student-t prior on a parameter subset, added to logpost[n] (one
+// thread per sample). The centred coordinates x_sub - mu are formed first (so
+// the single-precision form differences O(1) numbers, not O(|mu|) ones), then
+// y = L^-1 (x_sub - mu) row by row from the packed factor (broadcast loads:
+// every thread reads the same entry) and Q = |y|^2; the variable term in the
+// working precision, the constant added in FP64.
+template <typename Real, int MAXD>
+__device__ __forceinline__ void body_prior(const PriorDev &p, size_t N, int D, const double *__restrict__ X64,
+                                           const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
+                                           size_t n) {
+  if (n >= N) return;
+  const int d = p.d;
+  const Real *mu = (sizeof(Real) == 8) ? (const Real *)p.mu : (const Real *)p.mu32;
+  const Real *W = (sizeof(Real) == 8) ? (const Real *)p.Wt : (const Real *)p.Wt32;
+  Real c[MAXD];
+#pragma unroll
+  for (int i = 0; i < MAXD; i++) {
+    if (i < d) {
+      const int j = p.idx[i];
+      const Real x = (sizeof(Real) == 8) ? (Real)X64[n * D + j] : (Real)X32[n * ldx + j];
+      c[i] = x - __ldg(mu + i);
+    }
+  }
+  Real q = 0;
+  int off = 0;
+#pragma unroll
+  for (int i = 0; i < MAXD; i++) {
+    if (i < d) {
+      Real y = 0;
+#pragma unroll
+      for (int j = 0; j <= i; j++) y = fma(__ldg(W + off + j), c[j], y);
+      q = fma(y, y, q);
+      off += i + 1;
+    }
+  }
+  Real v;
+  if (p.df > 0) {
+    const Real t = q / (Real)p.df;
+    if constexpr (sizeof(Real) == 4) v = -0.5f * ((float)p.df + (float)d) * log1pf(t);
+    else v = -0.5 * ((double)p.df + d) * log1p(t);
+  } else {
+    v = (Real)-0.5 * q;
+  }
+  logpost[n] += p.lconst + (double)v;
+}
+
+// The prior body with its register footprint chosen by the prior's dimension
+// (the same choice in the standalone kernel and the batch kernel).
+template <typename Real>
+__device__ __forceinline__ void body_prior_any(const PriorDev &p, size_t N, int D, const double *X64,
+                                               const float *X32, int ldx, double *logpost, size_t n) {
+  if (p.d <= 8) body_prior<Real, 8>(p, N, D, X64, X32, ldx, logpost, n);
+  else if (p.d <= 20) body_prior<Real, 20>(p, N, D, X64, X32, ldx, logpost, n);
+  else body_prior<Real, kMaxD>(p, N, D, X64, X32, ldx, logpost, n);
+}
+
 // ================================================================== (c) template
 constexpr int kMT = 32;
 template <typename Real>

@@ -163,8 +163,14 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
       if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "SN kernel"))
         return false;
     } else if (pl.type == kPluginTpl) {
-      if (!CK(launch_tpl(w.prec, pl.tpl, w.N, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "template kernel"))
+      if (w.prec == 1 && g_use_tensor_cores && pl.tpl.uimg) {
+        if (!CK(launch_tpl_umma(pl.tpl.uimg, pl.tpl.Dpar, w.N, w.X32, w.ldx, w.logpost, w.flg, &w.dstats->tc_err,
+                                w.s),
+                "tensor-core template kernel"))
+          return false;
+      } else if (!CK(launch_tpl(w.prec, pl.tpl, w.N, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "template kernel")) {
         return false;
+      }
     }
   }
   if (p->has_prior) {
@@ -583,12 +589,37 @@ extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const 
     }
     t.c0 = c0;
   }
+  // Tensor-core form (D <= 12): chi2 = |U phi|^2, U^T U = At'^T At', At' = At
+  // with column 0 replaced by At_0 - dt (phi_0 = 1); U in FP32 [96 x 96].
+  const bool tc = D <= kTplUmmaMaxD;
+  std::vector<float> U32;
+  if (tc) {
+    std::vector<double> Gp((size_t)P * P, 0.0), Lg((size_t)P * P);
+    std::vector<double> a(P);
+    for (int i = 0; i < M; i++) {
+      for (int q = 0; q < P; q++) a[q] = At[(size_t)i * P + q];
+      a[0] -= dt[i];
+      for (int p1 = 0; p1 < P; p1++)
+        for (int p2 = 0; p2 <= p1; p2++) Gp[(size_t)p1 * P + p2] += a[p1] * a[p2];
+    }
+    for (int p1 = 0; p1 < P; p1++)
+      for (int p2 = 0; p2 < p1; p2++) Gp[(size_t)p2 * P + p1] = Gp[(size_t)p1 * P + p2];
+    if (host_cholesky(P, Gp.data(), Lg.data(), nullptr) != 0) {
+      set_error(err, PMCG_ECHOL, __LINE__, "template Gram matrix is not positive definite (fewer data than monomials?)");
+      return;
+    }
+    U32.assign(96 * 96, 0.f);
+    for (int i = 0; i < P; i++)
+      for (int j = i; j < P; j++) U32[(size_t)i * 96 + j] = (float)Lg[(size_t)j * P + i];   // U = L^T
+  }
   Carver cv;
+  float *dU32 = nullptr;
   for (int pass = 0; pass < 2; pass++) {
     cv.off = 0;
     t.At = cv.take<double>((size_t)M * P); t.dt = cv.take<double>(M);
     t.At32 = cv.take<float>((size_t)M * P); t.dt32 = cv.take<float>(M);
     if (gram) { t.G32 = cv.take<float>((size_t)Pp * Pp); t.b32 = cv.take<float>(Pp); }
+    if (tc) { t.uimg = cv.take<unsigned char>(tpl_uimage_bytes()); dU32 = cv.take<float>(96 * 96); }
     if (pass == 0) {
       if (!CK(cudaMalloc(&t.arena, cv.off + 256), "template buffers")) return;
       cv.base = (char *)t.arena;
@@ -602,6 +633,10 @@ extern "C" void pmcg_posterior_add_template(pmcg_posterior *p, int ndata, const 
   if (ok && gram)
     ok = CK(cudaMemcpy(t.G32, G32.data(), 4 * G32.size(), cudaMemcpyHostToDevice), "template upload") &&
          CK(cudaMemcpy(t.b32, b32.data(), 4 * b32.size(), cudaMemcpyHostToDevice), "template upload");
+  if (ok && tc)
+    ok = CK(cudaMemcpy(dU32, U32.data(), 4 * U32.size(), cudaMemcpyHostToDevice), "template upload") &&
+         CK(launch_tpl_uimage(dU32, t.uimg, 0), "template operand image") &&
+         CK(cudaDeviceSynchronize(), "template operand image");
   if (!ok) { cudaFree(t.arena); return; }
   p->plugins.push_back(pl);
   restamp(p);

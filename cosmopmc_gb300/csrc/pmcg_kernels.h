@@ -184,9 +184,19 @@ struct TplDev {
   // c0 = dt.dt (computed in FP64 at set-up)
   float *G32 = nullptr, *b32 = nullptr;
   double c0 = 0.0;
+  unsigned char *uimg = nullptr;  // tensor-core operand image of U (D <= kTplUmmaMaxD), else null
   void *arena = nullptr;
 };
 constexpr int kGramMaxP = 96;
+// Single precision on the tensor cores (k_tpl_umma.cu), D <= 12 (P <= 96):
+// chi2 = |U phi|^2 with U the upper Cholesky factor of At'^T At' (At' = At with
+// column 0 replaced by At_0 - dt). uimg: tpl_uimage_bytes() bytes, written from
+// U32 ([96 x 96] row-major FP32, zero beyond P) by launch_tpl_uimage.
+constexpr int kTplUmmaMaxD = 12;
+size_t tpl_uimage_bytes();
+cudaError_t launch_tpl_uimage(const float *U32, unsigned char *img, cudaStream_t s);
+cudaError_t launch_tpl_umma(const unsigned char *uimg, int Dp, size_t N, const float *X, int ldx, double *logpost,
+                            const short *flg, int *errflag, cudaStream_t s);
 cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X64, const float *X32, int ldx,
                        double *logpost, const short *flg, cudaStream_t s);
 

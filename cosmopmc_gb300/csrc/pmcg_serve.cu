@@ -245,9 +245,8 @@ extern "C" int64_t pmcg_server_submit(pmcg_server *s, const mix_mvdens *proposal
     set_error(err, PMCG_EARG, __LINE__, "pmcg_server_submit: invalid job");
     return 0;
   }
-  if (proposal->ndim > 32 || post->plugins.size() != 1 || post->has_prior) {
-    set_error(err, PMCG_EUNSUPPORTED, __LINE__,
-              "served jobs need D <= 32 and exactly one likelihood (no subset prior)");
+  if (proposal->ndim > 32 || post->plugins.size() != 1) {
+    set_error(err, PMCG_EUNSUPPORTED, __LINE__, "served jobs need D <= 32 and exactly one likelihood");
     return 0;
   }
   Job *j = new Job();

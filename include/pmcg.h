@@ -335,8 +335,7 @@ void pmcg_posterior_set_special(pmcg_posterior *p, int special, int ind_w0, int 
  * is added to every point's log-posterior, x_sub = the parameters j with
  * indprior[j] == 1 in increasing order (indprior NULL: every parameter);
  * prior->ndim must equal their number. The prior is copied (covariance, or its
- * Cholesky factor when prior->chol == 1). A second call replaces the first.
- * Batched runs and served jobs do not take posteriors with such a prior. */
+ * Cholesky factor when prior->chol == 1). A second call replaces the first. */
 void pmcg_posterior_add_mvdens_prior(pmcg_posterior *p, const mvdens *prior, const int *indprior, error **err);
 
 /* Single-point log-posterior (the per-point callback shape); evaluates one

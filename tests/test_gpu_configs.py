@@ -88,11 +88,23 @@ def _run_against_oracle(pmcg, oracle, prop, post, box, lpf, N, seed, iters, bmin
         _stats_close(st, so, it)
         p64 = r64.proposal()
         _proposals_close(p64, new, it)
-        s32 = r32.iterate(1.0)
-        if it == 0:
-            np.testing.assert_array_equal(r32.sample().indices, r64.sample().indices)
-        assert s32["ndead"] == st["ndead"], (it, s32, st)
-        assert abs(s32["ln_evidence"] - st["ln_evidence"]) <= lnz_tol(st["ln_evidence"]), (it, s32, st)
+        try:
+            s32 = r32.iterate(1.0)
+        except pmcg.PmcgError as e:
+            # with a handful of effective samples the single-precision EM may find the
+            # update of the last live component singular where FP64 does not
+            assert e.code == -9005 and st["ess"] < 5.0, (it, e, st)
+            s32 = None
+        p32, p64s = r32.sample(), r64.sample()
+        np.testing.assert_array_equal(p32.indices, p64s.indices)   # same proposal: same components
+        # ln Z of the same draw, from the sample's log-weights (the weight step ran in either case)
+        ok32 = p32.flg == 1
+        lw = p32.weights[ok32]
+        lnz32 = np.max(lw) + np.log(np.sum(np.exp(lw - np.max(lw)))) - np.log(N)
+        assert abs(lnz32 - st["ln_evidence"]) <= lnz_tol(st["ln_evidence"]), (it, lnz32, st)
+        if s32 is not None:
+            assert abs(s32["ln_evidence"] - lnz32) < 1e-9
+            assert s32["ndead"] == st["ndead"] or st["ess"] < 5.0, (it, s32, st)
         out.append(st)
         # continue both paths from the device FP64 proposal
         w, mu, L = p64.arrays()

@@ -148,3 +148,76 @@ def test_run_meets_precision_targets(pmcg, tensor_cores):
         sd = np.sqrt(np.diagonal(np.einsum("kij,klj->kil", L64, L64), axis1=1, axis2=2))
         assert np.max(np.abs(mu64[live] - mu32[live]) / sd[live]) < 0.05
         assert np.max(np.abs(w64 - w32)) < 1e-3
+
+
+# ----------------------------------------------------------------- template likelihood
+def _tpl_both(pmcg, post, T):
+    prev = pmcg.set_tensor_cores(True)
+    try:
+        tc = post.log_pdf_batch(T, precision=pmcg.MIXED)
+        pmcg.set_tensor_cores(False)
+        cc = post.log_pdf_batch(T, precision=pmcg.MIXED)
+    finally:
+        pmcg.set_tensor_cores(prev)
+    return tc, cc
+
+
+@pytest.mark.parametrize("N", [1, 77, 128, 129, 30001])
+def test_template_tensor_cores_vs_oracle(pmcg, oracle, N):
+    """c2 shape (D=12, P=91, M=2048): chi2 = |U phi|^2 on the tensor cores against
+    the FP64 oracle: |d log L| < 5e-3 over the prior box (chi2 up to ~1e4;
+    3e-6 relative) and < 2e-3 at the truth; ragged tiles (N not a multiple of
+    128, fewer samples than one tile)."""
+    wl = W.template_workload(D=12, M=2048)
+    post = pmcg.Posterior(12).add_template(wl["A"], wl["C"], wl["dobs"])
+    At, dt = oracle.tpl_prepare(wl["A"], wl["C"], wl["dobs"])
+    T = np.random.default_rng(N).uniform(-1, 1, (N, 12))
+    T[0] = wl["theta0"]
+    ref = oracle.tpl_loglike(At, dt, T)
+    (tc, ftc), (cc, fcc) = _tpl_both(pmcg, post, T)
+    assert ftc.all() and fcc.all()
+    err = np.abs(tc - ref)
+    assert np.max(err) < 5e-3 and np.max(err / np.abs(ref)) < 3e-6, (np.max(err), np.max(err / np.abs(ref)))
+    assert err[0] < 2e-3
+    # the CUDA-core Gram form (its own tolerance, 1e-2) agrees too
+    assert np.max(np.abs(cc - ref)) < 1e-2
+    # every sample is computed alone: a prefix gives the same values bit for bit
+    if N > 64:
+        (tc_s, _), _ = _tpl_both(pmcg, post, T[:64])
+        np.testing.assert_array_equal(tc_s, tc[:64])
+
+
+@pytest.mark.parametrize("D", [1, 3, 7])
+def test_template_tensor_cores_small_dimensions(pmcg, oracle, D):
+    """P = 3, 10, 36 monomials (one to five K-steps; zero padding up to 96)."""
+    wl = W.template_workload(D=D, M=257, seed=7 + D)
+    post = pmcg.Posterior(D).add_template(wl["A"], wl["C"], wl["dobs"])
+    At, dt = oracle.tpl_prepare(wl["A"], wl["C"], wl["dobs"])
+    T = np.random.default_rng(D).uniform(-1, 1, (1000, D))
+    ref = oracle.tpl_loglike(At, dt, T)
+    (tc, _), _ = _tpl_both(pmcg, post, T)
+    np.testing.assert_allclose(tc, ref, rtol=3e-6, atol=1e-3)
+
+
+def test_template_tensor_cores_iteration_and_flags(pmcg):
+    """A whole c2-shape iteration with the tensor-core template: the same ln Z as the
+    CUDA-core run within 1e-3, and samples outside the box (flg = 0) skipped."""
+    wl = W.template_workload(D=12, M=2048, K=16)
+    F = W.template_fisher(wl)
+    w, mu, cov, df = W.fisher_proposal(np.random.default_rng(3), 16, wl["theta0"], F, wl["bmin"], wl["bmax"])
+    prop = make_mix(pmcg, w, mu, cov, df)
+    post = pmcg.Posterior(12, wl["bmin"], wl["bmax"]).add_template(wl["A"], wl["C"], wl["dobs"])
+    box = pmcg.Parabox(wl["bmin"], wl["bmax"])
+    out = {}
+    for on in (1, 0):
+        prev = pmcg.set_tensor_cores(bool(on))
+        try:
+            run = pmcg.Run(prop, post, 100003, precision=pmcg.MIXED, seed=5, box=box)
+            out[on] = [run.iterate(1.0) for _ in range(2)]
+            s = run.sample()
+            assert np.all(np.isneginf(s.weights[s.flg == 0]))
+            run.free()
+        finally:
+            pmcg.set_tensor_cores(prev)
+    for a, b in zip(out[1], out[0]):
+        assert abs(a["ln_evidence"] - b["ln_evidence"]) < 1e-3, (a, b)
