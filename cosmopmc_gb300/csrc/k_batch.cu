@@ -144,10 +144,18 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
     case kBRenorm:
       body_em_renorm(K, d.w, d.st);
       break;
-    case kBPrepComp:
+    case kBPrepComp: {
+      __shared__ unsigned long long s_rmax;
+      if (threadIdx.x == 0) s_rmax = 0ull;
+      __syncthreads();
       body_prepare_comp(d.prop, d.logdetL, d.Wt, d.b, d.W32, d.b32, d.L32, d.mu32, (int)li,
-                        reinterpret_cast<double *>(smem));
+                        reinterpret_cast<double *>(smem), &s_rmax);
+      __syncthreads();
+      if (threadIdx.x == 0 && d.st->status == 0 && d.w[li] > 0.0 &&
+          __longlong_as_double((long long)s_rmax) > kF32RangeMax)
+        atomicCAS(&d.st->f32_range, 0, (int)li + 1);
       break;
+    }
     case kBPrepConsts:
       body_prepare_consts(d.prop, d.logdetL, d.cw, d.lconst, d.lconst32);
       for (int k = threadIdx.x; k < K; k += blockDim.x) d.counts[k] = 0;  // the next draw counts afresh
@@ -451,7 +459,8 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
       const DevStats &h = b->h_stats[r];
       pmcg_iter_stats &o = stats[r];
       o.ln_evidence = h.ln_evidence; o.perplexity = h.perplexity; o.ess = h.ess; o.enc = h.enc;
-      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead; o.status = h.status;
+      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead;
+      o.status = h.status != 0 ? h.status : (h.f32_range != 0 ? PMCG_EPRECISION : 0);
     }
   }
 }

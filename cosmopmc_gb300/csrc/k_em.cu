@@ -184,13 +184,20 @@ __global__ void __launch_bounds__(256) em_update_kernel(DevMix m, size_t N, int 
                                                         int whitened, DevStats *st) {
   extern __shared__ double sh[];
   __shared__ int s_dead, s_last;
+  __shared__ unsigned long long s_rmax;
   const DevMixView v = m.view();
   const int k = blockIdx.x;
   body_em_finalize(v, m.w, m.mu, m.L, N, S, part, counts, band_limit, whitened, k, st, sh, &s_dead);
+  if (threadIdx.x == 0) s_rmax = 0ull;
   __syncthreads();
   if (st->status == 0 && m.w[k] > 0.0) {
-    body_prepare_comp(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32, k, sh);
+    body_prepare_comp(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32, k, sh, &s_rmax);
     __syncthreads();
+    // single precision (the whitened update): a component narrower than single
+    // precision resolves makes the next iteration's samples and densities
+    // meaningless; the FP64 update itself is valid and kept
+    if (whitened && threadIdx.x == 0 && __longlong_as_double((long long)s_rmax) > kF32RangeMax)
+      atomicCAS(&st->f32_range, 0, k + 1);
     if (m.bimg) umma_image_component(v, m.bimg, k);
   }
   __threadfence();

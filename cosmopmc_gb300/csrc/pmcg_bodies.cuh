@@ -1074,6 +1074,7 @@ __device__ __forceinline__ void body_weights_final(int nb, const WRed *__restric
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
+  st->f32_range = 0;  // set again by this iteration's update if needed
   WRed a;
   a.m = M;
   a.s = a.t = a.q = a.n = 0.0;
@@ -1602,9 +1603,13 @@ __host__ __device__ inline size_t prepare_smem(int D) { return (2 * (size_t)D * 
 
 // Component k: W = L^-1 by column substitution, b = W mu, log|L|, and the
 // single-precision copies used by the mixed kernels.
+// Component k's derived arrays: L^-1 (packed and single precision), L^-1 mu,
+// the single-precision factor and mean, log det L. rmax (optional, shared):
+// receives max_i sum_j |(L^-1)_ij mu_j| as the bits of a non-negative double
+// (atomicMax), for the single-precision range check; zero it before the call.
 __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *logdetL, double *Wt, double *b,
                                                   float *W32, float *b32, float *L32, float *mu32, int k,
-                                                  double *s) {
+                                                  double *s, unsigned long long *rmax = nullptr) {
   const int D = m.D, T = D * (D + 1) / 2, ldx = m.ldx;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double *sL = s;            // D*D
@@ -1645,12 +1650,18 @@ __device__ __forceinline__ void body_prepare_comp(const DevMixView &m, double *l
   __syncthreads();
   for (int i = warp; i < D; i += nw) {
     // b_i = sum_j W_ij mu_j (lanes over j, fixed-order warp tree)
-    double t = 0.0;
-    for (int j = lane; j <= i; j += 32) t = fma(sW[i * D + j], m.mu[(size_t)k * D + j], t);
+    double t = 0.0, ta = 0.0;
+    for (int j = lane; j <= i; j += 32) {
+      const double wj = sW[i * D + j], mj = m.mu[(size_t)k * D + j];
+      t = fma(wj, mj, t);
+      ta = fma(fabs(wj), fabs(mj), ta);
+    }
     t = warp_sum(t);
+    if (rmax) ta = warp_sum(ta);
     if (lane == 0) {
       b[(size_t)k * D + i] = t;
       b32[(size_t)k * D + i] = (float)t;
+      if (rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(isfinite(ta) ? ta : 1e300));
     }
     for (int j = lane; j < ldx; j += 32)
       W32[(size_t)k * D * ldx + (size_t)i * ldx + j] = (j <= i && j < D) ? (float)sW[i * D + j] : 0.0f;

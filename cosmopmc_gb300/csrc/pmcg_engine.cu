@@ -207,6 +207,13 @@ static bool check_stats(Work &w, error **err) {
               w.hstats->status == PMCG_ENOWEIGHT ? "every sample has zero weight" : "all component weights are zero");
     return false;
   }
+  if (w.hstats->f32_range != 0) {
+    set_error(err, PMCG_EPRECISION, __LINE__,
+              "component %d of the updated proposal is narrower than single precision resolves around its mean; "
+              "the FP64 update is kept: continue with a PMCG_FP64 run",
+              w.hstats->f32_range - 1);
+    return false;
+  }
   return true;
 }
 
@@ -217,9 +224,41 @@ static bool fetch_stats(Work &w, error **err) {
   return check_stats(w, err);
 }
 
-static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error **err) {
+// Single-precision runs: every live component must be wider than single
+// precision resolves around its mean (max_i sum_j |(L^-1)_ij mu_j| at most
+// kF32RangeMax, the device check of the EM update); else PMCG_EPRECISION.
+static bool f32_range_ok(const std::vector<double> &w, const std::vector<double> &mu, const std::vector<double> &L,
+                         int K, int D, error **err) {
+  std::vector<double> Wr((size_t)D * D);
+  for (int k = 0; k < K; k++) {
+    if (!(w[k] > 0.0)) continue;
+    const double *Lk = &L[(size_t)k * D * D], *mk = &mu[(size_t)k * D];
+    double rmax = 0.0;
+    for (int i = 0; i < D; i++) {   // row i of L^-1 by forward substitution
+      double ra = 0.0;
+      for (int j = i; j >= 0; j--) {
+        double t = (i == j) ? 1.0 : 0.0;
+        for (int q = j + 1; q <= i; q++) t -= Lk[(size_t)q * D + j] * Wr[(size_t)i * D + q];
+        Wr[(size_t)i * D + j] = t / Lk[(size_t)j * D + j];
+      }
+      for (int j = 0; j <= i; j++) ra += std::fabs(Wr[(size_t)i * D + j]) * std::fabs(mk[j]);
+      if (!(ra <= rmax)) rmax = ra;
+    }
+    if (!(rmax <= kF32RangeMax)) {
+      set_error(err, PMCG_EPRECISION, __LINE__,
+                "proposal component %d is narrower than single precision resolves around its mean "
+                "(max_i sum_j |(L^-1)_ij mu_j| = %g); use a PMCG_FP64 run",
+                k, rmax);
+      return false;
+    }
+  }
+  return true;
+}
+
+static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error **err, bool f32 = false) {
   std::vector<double> w, mu, L;
   if (!flatten_mix(mix, w, mu, L, err)) return false;
+  if (f32 && !f32_range_ok(w, mu, L, mix->ncomp, mix->ndim, err)) return false;
   return CK(devmix_upload(m, w.data(), mu.data(), L.data(), s), "mixture upload") &&
          CK(cudaStreamSynchronize(s), "mixture upload");
 }
@@ -732,7 +771,7 @@ extern "C" pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_post
   pmcg_run *r = new pmcg_run();
   if (!work_alloc(r->w, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, precision ? 1 : 0, nsamples,
                   err) ||
-      !upload_mix(r->w.prop, proposal, r->w.s, err)) {
+      !upload_mix(r->w.prop, proposal, r->w.s, err, precision != 0)) {
     work_free(r->w);
     delete r;
     return nullptr;
@@ -877,7 +916,7 @@ extern "C" void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, e
     set_error(err, PMCG_EDIM, __LINE__, "proposal shape differs from the run's");
     return;
   }
-  upload_mix(w.prop, proposal, w.s, err);
+  upload_mix(w.prop, proposal, w.s, err, w.prec != 0);
 }
 
 extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {

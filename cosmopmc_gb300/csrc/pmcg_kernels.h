@@ -9,6 +9,12 @@ namespace pmcg {
 
 constexpr int kMaxD = 64;    // largest parameter dimension
 constexpr int kMaxK = 256;   // largest component count
+// Largest row sum max_i sum_j |(L^-1)_ij mu_j| of a component that single
+// precision still resolves: the coordinates of a single-precision sample carry
+// a relative rounding of 2^-24, which moves y = L^-1 (x - mu) by about 2^-24
+// times this sum; above 2^18 that is more than 0.016 (the proposal is narrower
+// than single precision resolves around its mean).
+constexpr double kF32RangeMax = 262144.0;
 // Tiles of the weight reduction (one partial record per 2048 samples).
 size_t weight_tiles(size_t N);
 // Sample chunks per component of the EM statistics.
@@ -24,6 +30,8 @@ struct DevStats {
   int ndead;        // components with weight 0 after the update
   int status;       // 0 ok, else a PMCG_E* code
   int tc_err;       // set by the tensor-core log-density when one of its waits expired
+  int f32_range;    // single-precision runs: 1 + a component whose updated proposal is
+                    // narrower than single precision resolves (0: none)
 };
 
 // Device-resident mixture; one allocation, carved into the arrays below.

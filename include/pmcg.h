@@ -56,6 +56,7 @@ typedef struct _err {
 #define PMCG_EIO          (-10 + pmcg_base) /* file read/write error                              */
 #define PMCG_ENOWEIGHT    (-11 + pmcg_base) /* every sample has zero weight                       */
 #define PMCG_ESTEPS       (-12 + pmcg_base) /* evaluation limit reached (pmclib math_tooManySteps) */
+#define PMCG_EPRECISION   (-13 + pmcg_base) /* proposal narrower than single precision resolves (use PMCG_FP64) */
 
 error *addError(int code, const char *text, error *next, int line);
 int isError(const error *err);

@@ -39,6 +39,20 @@ def make_run(P, kind, D, K, N, seed):
         prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
         post = P.Posterior(D, wl["bmin"], wl["bmax"]).add_template(wl["A"], wl["C"], wl["dobs"])
         return prop, post, P.Parabox(wl["bmin"], wl["bmax"])
+    if kind == "snprior":  # SN parameters + Gaussian nuisance parameters (a subset prior)
+        wl = W.sn_workload(K=K, seed=seed, init="fisher")
+        w, mu, cov, df = wl["prop"]
+        nx = D - 6
+        mu = np.concatenate([mu, np.zeros((K, nx))], axis=1)
+        cov2 = np.zeros((K, D, D))
+        cov2[:, :6, :6] = cov
+        cov2[:, 6:, 6:] = 0.1 * np.eye(nx)
+        prop = P.MixMvdens.from_arrays(w, mu, cov=cov2, df=df).cholesky()
+        bmin = np.r_[wl["bmin"], -np.ones(nx)]
+        bmax = np.r_[wl["bmax"], np.ones(nx)]
+        post = P.Posterior(D, bmin, bmax).add_snia(wl["sn"])
+        post.add_prior(np.zeros(nx), 0.0625 * np.eye(nx), indprior=np.r_[np.zeros(6, int), np.ones(nx, int)])
+        return prop, post, P.Parabox(bmin, bmax)
     if kind == "dead":  # every draw falls outside the box
         prop = P.MixMvdens.from_arrays([1.0], [[10.0, 10.0]], cov=[np.eye(2) * 0.01], df=-1).cholesky()
         target = P.MixMvdens.from_arrays([1.0], [[0.0, 0.0]], cov=[np.eye(2)], df=-1).cholesky()
@@ -48,7 +62,7 @@ def make_run(P, kind, D, K, N, seed):
 
 
 SPECS = [("mix", 2, 1, 1000, 1), ("mix", 5, 3, 3001, 2), ("mix", 13, 7, 20000, 3), ("mix", 20, 12, 9000, 5),
-         ("sn", 6, 5, 4000, 740), ("tpl", 3, 4, 2500, 91), ("dead", 2, 1, 777, 9)]
+         ("sn", 6, 5, 4000, 740), ("snprior", 9, 4, 3000, 741), ("tpl", 3, 4, 2500, 91), ("dead", 2, 1, 777, 9)]
 
 
 def test_batch_is_bit_identical_to_runs_alone(pmcg):
