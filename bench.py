@@ -286,7 +286,8 @@ def same_draw_accuracy(P, prop, post, N, seed=2024):
 def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
     """The other likelihoods at their configuration sizes: SN Ia (D=6, K=10, 740
     supernovae, Fisher start; N = 10^4 as configured and N = 2^18) and the dense
-    template (D=12, K=16, M=2048, N = 2^18); mixed precision vs FP64, same seeds."""
+    template (D=12, K=16, M=2048, N = 2^18, Fisher start); mixed precision vs
+    FP64, same seeds."""
     out = {}
     wl = W.sn_workload(K=10, init="fisher")
     w, mu, cov, df = wl["prop"]
@@ -294,7 +295,8 @@ def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
     sn_post = P.Posterior(6, wl["bmin"], wl["bmax"]).add_snia(wl["sn"])
     sn_box = P.Parabox(wl["bmin"], wl["bmax"])
     tw = W.template_workload(D=12, M=2048, K=16)
-    w, mu, cov, df = tw["prop"]
+    w, mu, cov, df = W.fisher_proposal(np.random.default_rng(92), 16, tw["theta0"], W.template_fisher(tw),
+                                       tw["bmin"], tw["bmax"])
     tpl_prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
     tpl_post = P.Posterior(12, tw["bmin"], tw["bmax"]).add_template(tw["A"], tw["C"], tw["dobs"])
     tpl_box = P.Parabox(tw["bmin"], tw["bmax"])
@@ -597,7 +599,7 @@ def profile_case(args):
     """One workload of the benchmark, mixed precision, every kernel launched
     directly with per-stage CUDA events: "mixture" (D=32, K=64 Student-t nu=3,
     condition 1e6, 16-component target), "sn" (740 supernovae, D=6, K=10 Fisher
-    start), "template" (D=12, M=2048, P=91, K=16)."""
+    start), "template" (D=12, M=2048, P=91, K=16, Fisher start)."""
     from cosmopmc_gb300 import pmcg as P
     from cosmopmc_gb300 import workloads as W
     P.load()
@@ -615,7 +617,8 @@ def profile_case(args):
         box = P.Parabox(wl["bmin"], wl["bmax"])
     else:
         tw = W.template_workload(D=12, M=2048, K=16)
-        w, mu, cov, df = tw["prop"]
+        w, mu, cov, df = W.fisher_proposal(np.random.default_rng(92), 16, tw["theta0"], W.template_fisher(tw),
+                                           tw["bmin"], tw["bmax"])
         prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
         post = P.Posterior(12, tw["bmin"], tw["bmax"]).add_template(tw["A"], tw["C"], tw["dobs"])
         box = P.Parabox(tw["bmin"], tw["bmax"])

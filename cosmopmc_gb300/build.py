@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libpmcg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
-SOURCES = ["k_draw.cu", "k_mix.cu", "k_weights.cu", "k_em.cu", "k_like.cu", "k_noalloc.cu", "k_umma.cu", "k_tpl_umma.cu", "k_post.cu", "k_batch.cu", "pmcg_serve.cu", "pmcg_engine.cu", "pmcg_fisher.cpp",
+SOURCES = ["k_draw.cu", "k_mix.cu", "k_weights.cu", "k_em.cu", "k_like.cu", "k_noalloc.cu", "k_umma.cu", "k_tpl_umma.cu", "k_post.cu", "k_batch.cu", "pmcg_serve.cu", "pmcg_engine.cu", "pmcg_fisher.cpp", "pmcg_config.cpp",
            "pmcg_host.cpp"]
 
 

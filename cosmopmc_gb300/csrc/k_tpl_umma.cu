@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(kTuThreads, 1)
     bool ok = true;
     tu_fetch<D>(X, ldx, N, (size_t)blockIdx.x * kTuTile + tid, th);
     size_t n_prev = 0;
+    short f_prev = 0;
+    double lp_prev = 0.0;
     for (int i = 0; i <= my_tiles && ok; i++) {
       float chi2 = 0.f;
       if (i > 0) {
@@ -206,9 +208,13 @@ __global__ void __launch_bounds__(kTuThreads, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive_warp(afull);
       }
-      if (i > 0 && n_prev < N && flg[n_prev]) logpost[n_prev] += -0.5 * (double)chi2;
+      if (i > 0 && f_prev) logpost[n_prev] = lp_prev - 0.5 * (double)chi2;
       if (i < my_tiles) {
+        // this tile's flag and log-posterior, and the next tile's parameters: loads
+        // in flight while the MMAs run
         n_prev = (blockIdx.x + (size_t)i * gridDim.x) * kTuTile + tid;
+        f_prev = (n_prev < N) ? flg[n_prev] : (short)0;
+        lp_prev = (n_prev < N) ? logpost[n_prev] : 0.0;
         if (i + 1 < my_tiles) tu_fetch<D>(X, ldx, N, (blockIdx.x + (size_t)(i + 1) * gridDim.x) * kTuTile + tid, th);
       }
     }

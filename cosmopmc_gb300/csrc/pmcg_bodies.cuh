@@ -510,8 +510,11 @@ __device__ __forceinline__ void body_sn_f32(const SnDev &sn, size_t N, const flo
   if (sn.ip_ode >= 0) { odef = par(sn.ip_ode, 0.f); okf = (1.f - omf) - odef; }
   else { odef = 1.f - omf; okf = 0.f; }
   const float exf = 3.f * (1.f + par(sn.ip_w0, sn.fdef_w0));
-  const float dMf = par(sn.ip_M, sn.fdef_M) - sn.mref;
-  const float al = par(sn.ip_alpha, sn.fdef_alpha), be = par(sn.ip_beta, sn.fdef_beta);
+  // a parameter may hold -M or -beta (the reference's storage)
+  const float Mf = (sn.ip_M >= 0 && sn.neg_M) ? -par(sn.ip_M, 0.f) : par(sn.ip_M, sn.fdef_M);
+  const float dMf = Mf - sn.mref;
+  const float al = par(sn.ip_alpha, sn.fdef_alpha);
+  const float be = (sn.ip_beta >= 0 && sn.neg_beta) ? -par(sn.ip_beta, 0.f) : par(sn.ip_beta, sn.fdef_beta);
   const float a2 = al * al, b2 = be * be, ab = al * be;
   const int G = sn.G, nsn = sn.nsn;
   const float4 *__restrict__ node = sn.fnode;
@@ -617,9 +620,10 @@ __device__ __forceinline__ void body_sn(const SnDev &sn, size_t N, int D, const 
   if (sn.ip_ode >= 0) { ode = par(sn.ip_ode, 0.0); ok = 1.0 - om - ode; }
   else { ode = 1.0 - om; ok = 0.0; }
   const double w0 = par(sn.ip_w0, sn.def_w0);
-  const double M = par(sn.ip_M, sn.def_M);
+  // a parameter may hold -M or -beta (the reference's storage)
+  const double M = (sn.ip_M >= 0 && sn.neg_M) ? -par(sn.ip_M, 0.0) : par(sn.ip_M, sn.def_M);
   const double al = par(sn.ip_alpha, sn.def_alpha);
-  const double be = par(sn.ip_beta, sn.def_beta);
+  const double be = (sn.ip_beta >= 0 && sn.neg_beta) ? -par(sn.ip_beta, 0.0) : par(sn.ip_beta, sn.def_beta);
   const double ex = 3.0 * (1.0 + w0);
   const int G = sn.G, nsn = sn.nsn;
   int bad = 0;

@@ -268,6 +268,25 @@ static bool upload_mix(DevMix &m, const mix_mvdens *mix, cudaStream_t s, error *
 using namespace pmcg;
 
 // ===================================================================== posterior
+// Device posteriors standing in for the caller's posterior callbacks, keyed by
+// the callback's extra pointer.
+static std::mutex g_reg_mu;
+static std::unordered_map<const void *, const pmcg_posterior *> g_registered;
+
+namespace pmcg {
+const pmcg_posterior *registered_posterior(const void *extra) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_registered.find(extra);
+  return it == g_registered.end() ? nullptr : it->second;
+}
+}  // namespace pmcg
+
+extern "C" void pmcg_register_posterior(const void *extra, const pmcg_posterior *post) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  if (post) g_registered[extra] = post;
+  else g_registered.erase(extra);
+}
+
 static std::atomic<uint64_t> g_post_stamp{0};
 static void restamp(pmcg_posterior *p) { p->stamp = ++g_post_stamp; }
 
@@ -300,6 +319,13 @@ extern "C" pmcg_posterior *pmcg_posterior_alloc(int npar, const double *min, con
 extern "C" void pmcg_posterior_free(pmcg_posterior **p) {
   if (!p || !*p) return;
   forget_posterior(*p);
+  {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    for (auto it = g_registered.begin(); it != g_registered.end();) {
+      if (it->second == *p) it = g_registered.erase(it);
+      else ++it;
+    }
+  }
   for (Plugin &pl : (*p)->plugins) {
     devmix_free(pl.mix);
     if (pl.sn.arena) cudaFree(pl.sn.arena);
@@ -517,6 +543,7 @@ extern "C" void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *s
   s.nsn = n; s.G = G; s.chi2mode = sd->chi2mode; s.add_logdet = sd->add_logdet;
   s.ip_om = sd->ip_Omegam; s.ip_ode = sd->ip_Omegade; s.ip_w0 = sd->ip_w0; s.ip_M = sd->ip_M;
   s.ip_alpha = sd->ip_alpha; s.ip_beta = sd->ip_beta;
+  s.neg_M = sd->neg_M ? 1 : 0; s.neg_beta = sd->neg_beta ? 1 : 0;
   s.def_om = sd->def_Omegam; s.def_w0 = sd->def_w0; s.def_M = sd->def_M; s.def_alpha = sd->def_alpha;
   s.def_beta = sd->def_beta;
   s.dh = ckms / (100.0 * sd->h);
@@ -1162,12 +1189,15 @@ extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {
   if (m) m->x_valid = m->lt_valid = m->w_valid = m->lp_valid = false;
 }
 
-extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg_rng *rng, parabox *pb,
+extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, void *rng, parabox *pb,
                                       error **err) {
   if (!psim || !proposal || !rng || proposal->ndim != psim->ndim || (pb && pb->ndim != psim->ndim)) {
     set_error(err, PMCG_EARG, __LINE__, "simulate_mix_mvdens: invalid arguments");
     return 0;
   }
+  uint64_t rseed = 0;
+  uint32_t *rcalls = nullptr;
+  if (!rng_stream(rng, &rseed, &rcalls, err)) return 0;
   SimMirror *m = mirror_for(psim, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, err);
   if (!m) return 0;
   Work &w = m->w;
@@ -1184,7 +1214,7 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
     ok = CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts");
     for (int c = 0; ok && c < C; c++) {
       const size_t n0 = w.N * c / C, n1 = w.N * (c + 1) / C;
-      ok = CK(launch_draw_grouped_range(w.prop.view(), w.N, n0, n1, rng->seed, rng->calls, box ? w.bmin : nullptr,
+      ok = CK(launch_draw_grouped_range(w.prop.view(), w.N, n0, n1, rseed, *rcalls, box ? w.bmin : nullptr,
                                         box ? w.bmax : nullptr, w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor,
                                         w.s),
               "draw kernels") &&
@@ -1195,7 +1225,7 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
               "X");
     }
   } else {
-    ok = stage_draw(w, box, rng->seed, rng->calls, err);
+    ok = stage_draw(w, box, rseed, *rcalls, err);
     if (ok && w.prec) ok = CK(launch_x32_to_x64(w.N, w.D, w.ldx, w.X32, w.X64, w.s), "convert");
     ok = ok && CK(cudaEventRecord(m->ev[0], w.s), "event") && CK(cudaStreamWaitEvent(m->cs, m->ev[0], 0), "wait") &&
          CK(cudaMemcpyAsync(psim->X, w.X64, 8 * w.N * w.D, cudaMemcpyDeviceToHost, m->cs), "X");
@@ -1224,7 +1254,7 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg
   size_t nok = 0;
   if (ok)
     for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
-  rng->calls++;
+  (*rcalls)++;
   if (!ok) {
     cudaStreamSynchronize(w.s);
     return 0;
@@ -1243,13 +1273,18 @@ extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim,
                                                                  int quiet, error **err) {
   (void)ded;
   (void)quiet;
-  if (q != mix_mvdens_log_pdf_void || post != pmcg_posterior_log_pdf_void || !extra) {
+  // the caller's own posterior callback with a registered extra pointer (the
+  // reference passes posterior_log_pdf_common_void and &config->base), or the
+  // library's callback with the device posterior itself
+  const pmcg_posterior *p = extra ? registered_posterior(extra) : nullptr;
+  if (!p && post == pmcg_posterior_log_pdf_void) p = (const pmcg_posterior *)extra;
+  if (q != mix_mvdens_log_pdf_void || !p) {
     set_error(err, PMCG_EUNSUPPORTED, __LINE__,
-              "the device weight step needs q = mix_mvdens_log_pdf_void and post = pmcg_posterior_log_pdf_void "
-              "with extra = pmcg_posterior*");
+              "the device weight step needs q = mix_mvdens_log_pdf_void and either post = "
+              "pmcg_posterior_log_pdf_void with extra = pmcg_posterior*, or an extra pointer registered with "
+              "pmcg_register_posterior");
     return 0;
   }
-  const pmcg_posterior *p = (const pmcg_posterior *)extra;
   SimMirror *m = mirror_for(psim, proposal->ncomp, proposal->ndim, proposal->comp[0]->df, err);
   if (!m) return 0;
   Work &w = m->w;

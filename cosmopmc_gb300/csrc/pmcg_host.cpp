@@ -9,6 +9,10 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -383,9 +387,11 @@ extern "C" void pmc_simu_realloc(pmc_simu *p, size_t nsamples, error **err) {
 // .., n_ded = ..", column titles, parameter names) and one row per counted
 // sample: the unnormalised log-weight, minus the component index, the
 // parameters and the deduced parameters, each "%16.9g".
-extern "C" void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const char *const *par_names,
-                                       double norm, error **err) {
-  (void)norm;
+// The sample file of exec/exec_helper.c:351-427 (header, then one row per
+// counted sample: unnormalised log-weight, -component, parameters, deduced
+// parameters, %16.9g); name_of(i) gives parameter i's name for the header.
+template <typename NameOf>
+static void write_pmc_simu(const char *name, const pmc_simu *psim, NameOf name_of, error **err) {
   FILE *f = fopen(name, "w");
   if (!f) {
     set_error(err, PMCG_EIO, __LINE__, "cannot open %s for writing", name);
@@ -397,10 +403,7 @@ extern "C" void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, c
   for (int i = 0; i < D; i++) fprintf(f, "        param[%d]", i);
   for (int i = 0; i < Dd; i++) fprintf(f, "    param_ded[%d]", i);
   fprintf(f, "\n#                               ");
-  for (int i = 0; i < D; i++) {
-    if (par_names && par_names[i]) fprintf(f, "%16s", par_names[i]);
-    else fprintf(f, "%16s", "p");
-  }
+  for (int i = 0; i < D; i++) fprintf(f, "%16s", name_of(i));
   fprintf(f, "\n");
   const double lognorm = psim->logSum;
   for (size_t n = 0; n < psim->nsamples; n++) {
@@ -414,6 +417,32 @@ extern "C" void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, c
     fprintf(f, "\n");
   }
   if (fclose(f) != 0) set_error(err, PMCG_EIO, __LINE__, "write error on %s", name);
+}
+
+// The par_t name table (the reference's spar_t strings), set by the caller.
+static std::mutex g_names_mu;
+static std::vector<std::string> g_par_names;
+
+extern "C" void pmcg_set_par_names(int n, const char *const *names) {
+  std::lock_guard<std::mutex> lk(g_names_mu);
+  g_par_names.clear();
+  for (int i = 0; i < n && names; i++) g_par_names.emplace_back(names[i] ? names[i] : "p");
+}
+
+extern "C" void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const void *par, double norm,
+                                       error **err) {
+  (void)norm;
+  std::lock_guard<std::mutex> lk(g_names_mu);
+  const int *codes = (const int *)par;
+  write_pmc_simu(name, psim, [&](int i) -> const char * {
+    if (!codes || codes[i] < 0 || codes[i] >= (int)g_par_names.size()) return "p";
+    return g_par_names[codes[i]].c_str();
+  }, err);
+}
+
+extern "C" void pmcg_out_pmc_simu_names(const char *name, const pmc_simu *psim, const char *const *names,
+                                        error **err) {
+  write_pmc_simu(name, psim, [&](int i) -> const char * { return (names && names[i]) ? names[i] : "p"; }, err);
 }
 
 // Reads a sample file written as above (at most nsamples rows; comment lines
@@ -498,17 +527,75 @@ extern "C" void pmc_simu_free(pmc_simu **p) {
   *p = nullptr;
 }
 
+// ------------------------------------------------------------------ random streams
+// The library's own generators, and the streams of foreign generators (the
+// caller's gsl_rng*): key from the seed hook at first sight, call count kept
+// here. One lock for both tables.
+namespace {
+struct ForeignStream {
+  uint64_t seed;
+  uint32_t calls;
+};
+std::mutex g_rng_mu;
+std::unordered_set<const void *> g_own_rngs;
+std::unordered_map<const void *, ForeignStream> g_foreign;
+pmcg_rng_seed_fn *g_seed_hook = nullptr;
+}  // namespace
+
 extern "C" pmcg_rng *pmcg_rng_alloc(uint64_t seed) {
   pmcg_rng *r = (pmcg_rng *)calloc(1, sizeof(pmcg_rng));
-  if (r) r->seed = seed;
+  if (r) {
+    r->seed = seed;
+    std::lock_guard<std::mutex> lk(g_rng_mu);
+    g_own_rngs.insert(r);
+  }
   return r;
 }
 
 extern "C" void pmcg_rng_free(pmcg_rng **r) {
-  if (!r) return;
+  if (!r || !*r) return;
+  {
+    std::lock_guard<std::mutex> lk(g_rng_mu);
+    g_own_rngs.erase(*r);
+  }
   free(*r);
   *r = nullptr;
 }
+
+extern "C" void pmcg_set_rng_seed_hook(pmcg_rng_seed_fn *fn) {
+  std::lock_guard<std::mutex> lk(g_rng_mu);
+  g_seed_hook = fn;
+}
+
+extern "C" void pmcg_rng_forget(void *rng) {
+  std::lock_guard<std::mutex> lk(g_rng_mu);
+  g_foreign.erase(rng);
+}
+
+namespace pmcg {
+bool rng_stream(void *rng, uint64_t *seed, uint32_t **calls, error **err) {
+  std::lock_guard<std::mutex> lk(g_rng_mu);
+  if (g_own_rngs.count(rng)) {
+    pmcg_rng *r = (pmcg_rng *)rng;
+    *seed = r->seed;
+    *calls = &r->calls;
+    return true;
+  }
+  auto it = g_foreign.find(rng);
+  if (it == g_foreign.end()) {
+    if (!g_seed_hook) {
+      set_error(err, PMCG_EARG, __LINE__,
+                "simulate_mix_mvdens: the generator is not a pmcg_rng and no seed hook is set "
+                "(pmcg_set_rng_seed_hook)");
+      return false;
+    }
+    it = g_foreign.emplace(rng, ForeignStream{g_seed_hook(rng), 0u}).first;
+  }
+  *seed = it->second.seed;
+  *calls = &it->second.calls;
+  return true;
+}
+}  // namespace pmcg
 
 // get_tempering_beta, exec/cosmo_pmc.c:464-495.
 extern "C" double get_tempering_beta(int tempering, int iter, double t_min, int nmax, error **err) {

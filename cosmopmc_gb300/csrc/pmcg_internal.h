@@ -16,4 +16,10 @@ void forget_simu(const pmc_simu *p);
 // Forget a posterior that is about to be freed (the drop-in mirrors keep the
 // last one they weighed with).
 void forget_posterior(const pmcg_posterior *p);
+// The stream of a draw's generator argument: a pmcg_rng of this library, or a
+// foreign generator keyed by the seed hook the first time it is seen. On
+// success *seed and *calls (the call counter to use and advance) are set.
+bool rng_stream(void *rng, uint64_t *seed, uint32_t **calls, error **err);
+// The device posterior registered for a callback's extra pointer (or null).
+const pmcg_posterior *registered_posterior(const void *extra);
 }  // namespace pmcg

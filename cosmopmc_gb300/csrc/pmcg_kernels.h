@@ -155,6 +155,7 @@ cudaError_t launch_normalise(size_t N, const double *logw, const short *flg, con
 struct SnDev {
   int nsn = 0, G = 0, chi2mode = 0, add_logdet = 0;
   int ip_om = -1, ip_ode = -1, ip_w0 = -1, ip_M = -1, ip_alpha = -1, ip_beta = -1;
+  int neg_M = 0, neg_beta = 0;  // 1: the parameter holds -M (-beta)
   double def_om = 0.3, def_w0 = -1.0, def_M = -19.3, def_alpha = 0.0, def_beta = 0.0;
   double dh = 0.0, sig_int2 = 0.0;
   // sorted by redshift: z, 1/z-dependent peculiar-velocity variance, m_B, x1, c, cov6;

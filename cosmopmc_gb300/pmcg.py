@@ -75,7 +75,7 @@ class SnData(C.Structure):
                 ("ip_Omegam", C.c_int), ("ip_Omegade", C.c_int), ("ip_w0", C.c_int), ("ip_M", C.c_int),
                 ("ip_alpha", C.c_int), ("ip_beta", C.c_int),
                 ("def_Omegam", C.c_double), ("def_w0", C.c_double), ("def_M", C.c_double),
-                ("def_alpha", C.c_double), ("def_beta", C.c_double)]
+                ("def_alpha", C.c_double), ("def_beta", C.c_double), ("neg_M", C.c_int), ("neg_beta", C.c_int)]
 
 
 class IterStats(C.Structure):
@@ -143,7 +143,15 @@ SIGNATURES = [
     ("mix_mvdens_dump", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
     ("mix_mvdens_dwnp", C.POINTER(MixMvdensS), [C.c_void_p, PErr]),
     ("mix_mvdens_print", None, [C.c_void_p, C.POINTER(MixMvdensS)]),
-    ("out_pmc_simu_cosmo_pmc", None, [C.c_char_p, C.POINTER(PmcSimuS), C.POINTER(C.c_char_p), C.c_double, PErr]),
+    ("out_pmc_simu_cosmo_pmc", None, [C.c_char_p, C.POINTER(PmcSimuS), C.c_void_p, C.c_double, PErr]),
+    ("pmcg_set_par_names", None, [C.c_int, C.POINTER(C.c_char_p)]),
+    ("pmcg_out_pmc_simu_names", None, [C.c_char_p, C.POINTER(PmcSimuS), C.POINTER(C.c_char_p), PErr]),
+    ("pmcg_set_rng_seed_hook", None, [C.c_void_p]),
+    ("pmcg_rng_forget", None, [C.c_void_p]),
+    ("pmcg_register_posterior", None, [C.c_void_p, C.c_void_p]),
+    ("pmcg_posterior_from_config", C.c_void_p, [C.c_int, C.POINTER(C.c_int), _dp, _dp, C.c_int, C.POINTER(C.c_int),
+                                                C.POINTER(C.c_void_p), C.POINTER(Mvdens), C.POINTER(C.c_int),
+                                                C.c_double, PErr]),
     ("pmc_simu_from_file", C.POINTER(PmcSimuS), [C.c_void_p, C.c_size_t, C.c_int, C.c_int,
                                                    C.POINTER(MixMvdensS), C.c_int, PErr]),
     ("importance_sample", C.c_size_t, [C.POINTER(PmcSimuS), C.c_void_p, C.c_int, PErr]),
@@ -162,7 +170,7 @@ SIGNATURES = [
     ("pmc_simu_free", None, [C.POINTER(C.POINTER(PmcSimuS))]),
     ("pmcg_rng_alloc", C.POINTER(RngS), [C.c_uint64]),
     ("pmcg_rng_free", None, [C.POINTER(C.POINTER(RngS))]),
-    ("simulate_mix_mvdens", C.c_size_t, [C.POINTER(PmcSimuS), C.POINTER(MixMvdensS), C.POINTER(RngS),
+    ("simulate_mix_mvdens", C.c_size_t, [C.POINTER(PmcSimuS), C.POINTER(MixMvdensS), C.c_void_p,
                                          C.POINTER(ParaboxS), PErr]),
     ("generic_get_importance_weight_and_deduced_verb", C.c_size_t,
      [C.POINTER(PmcSimuS), C.POINTER(MixMvdensS), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
@@ -414,7 +422,7 @@ class PmcSimu:
         names = None
         if par_names is not None:
             names = (C.c_char_p * len(par_names))(*[n.encode() for n in par_names])
-        call("out_pmc_simu_cosmo_pmc", str(path).encode(), self.p, names, 0.0)
+        call("pmcg_out_pmc_simu_names", str(path).encode(), self.p, names)
 
     @classmethod
     def read(cls, path, nsamples, ndim, n_ded=0):
@@ -541,6 +549,7 @@ class Posterior:
         s.ip_M, s.ip_alpha, s.ip_beta = int(sn["ip_M"]), int(sn["ip_alpha"]), int(sn["ip_beta"])
         s.def_Omegam, s.def_w0, s.def_M = float(sn["def_om"]), float(sn["def_w0"]), float(sn["def_M"])
         s.def_alpha, s.def_beta = float(sn["def_alpha"]), float(sn["def_beta"])
+        s.neg_M, s.neg_beta = int(sn.get("neg_M", 0)), int(sn.get("neg_beta", 0))
         call("pmcg_posterior_add_snia", self.p, C.byref(s))
         return self
 

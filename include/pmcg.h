@@ -143,10 +143,20 @@ pmc_simu *pmc_simu_init_mpi(size_t nsamples, int ndim, int n_ded, error **err); 
 pmc_simu *pmc_simu_init_plus_ded(size_t nsamples, int ndim, int n_ded, error **err);/* cosmo_pmc.c:429 */
 /* Sample files (exec/exec_helper.c:351-427): writes the counted samples as
  * "unnormalised log-weight, -component, parameters, deduced parameters"
- * (%16.9g) under the CosmoPMC header; par_names may be NULL. norm is unused
- * (kept for the reference's signature). */
-void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const char *const *par_names, double norm,
-                            error **err);                                           /* cosmo_pmc.c:431 */
+ * (%16.9g) under the CosmoPMC header. par: the caller's par_t array (the
+ * reference's parameter codes, tools/include/par.h:11-33, an enum read as
+ * int; may be NULL); the header's name row prints names[par[i]] of the table
+ * given to pmcg_set_par_names (the reference's spar_t strings), "p" without
+ * one. norm is unused (kept for the reference's signature,
+ * exec/exec_helper.h:61). */
+void out_pmc_simu_cosmo_pmc(const char *name, const pmc_simu *psim, const void *par, double norm,
+                            error **err);                                           /* cosmo_pmc.c:391 */
+/* The name table for the par_t codes 0..n-1 (the reference builds it from its
+ * spar_t macro); copied. No counterpart in the reference (its names are a
+ * macro of the caller's build). */
+void pmcg_set_par_names(int n, const char *const *names);
+/* The same file with the parameter names given directly (names may be NULL). */
+void pmcg_out_pmc_simu_names(const char *name, const pmc_simu *psim, const char *const *names, error **err);
 /* Reads such a file (at most nsamples rows; exec/importance_sample.c:198,
  * exec/cosmo_pmc.c:416): weights normalised (isLog = 0, logSum, maxW of the
  * file's log-weights), flg = 1, indices from the second column. proposal
@@ -156,9 +166,14 @@ pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, cons
 void pmc_simu_realloc(pmc_simu *psim, size_t nsamples, error **err);                /* cosmo_pmc.c:313 */
 void pmc_simu_free(pmc_simu **psim);                                                /* cosmo_pmc.c:738 */
 
-/* Random stream replacing the gsl_rng that cosmo_pmc passes to the draw.
- * Philox4x32-10 (Salmon et al. 2011), keyed by a 64-bit seed; each draw
- * call consumes one counter block per sample and advances `calls`. */
+/* Random streams. The draw samples from a counter-based generator on the
+ * device, Philox4x32-10 (Salmon et al. 2011), keyed by a 64-bit seed; each
+ * draw call consumes one counter block per sample and advances a call count.
+ * The generator argument of the draw is the caller's own: a pmcg_rng of this
+ * library, or any other generator pointer (the gsl_rng* that cosmo_pmc passes,
+ * exec/cosmo_pmc.c:320), whose stream key the library takes once, the first
+ * time it sees the pointer, from the seed hook (e.g. two gsl_rng_get calls);
+ * the library then counts that generator's draw calls itself. */
 typedef struct {
   uint64_t seed;
   uint32_t calls;
@@ -166,22 +181,32 @@ typedef struct {
 
 pmcg_rng *pmcg_rng_alloc(uint64_t seed);
 void pmcg_rng_free(pmcg_rng **r);
+/* The seed hook for foreign generators (NULL: none; a draw with a foreign
+ * generator is then PMCG_EARG). No counterpart in the reference. */
+typedef uint64_t pmcg_rng_seed_fn(void *rng);
+void pmcg_set_rng_seed_hook(pmcg_rng_seed_fn *fn);
+/* Forget a foreign generator's stream (before the caller frees it). */
+void pmcg_rng_forget(void *rng);
 
 /* Draw psim->nsamples points from the proposal into psim->X/indices/flg.
  * Points outside `pb` get flg=0 (weight 0, no redraw). Returns the number
- * inside the box. Replaces pmclib simulate_mix_mvdens (exec/cosmo_pmc.c:320). */
-size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, pmcg_rng *rng, parabox *pb, error **err);
+ * inside the box. rng: a pmcg_rng*, or the caller's generator (see above).
+ * Replaces pmclib simulate_mix_mvdens (exec/cosmo_pmc.c:320). */
+size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, void *rng, parabox *pb, error **err);
 
 /* Log-density callback type (wrappers/src/param.c:948). */
 typedef double logpdf_fn(void *extra, const double *x, error **err);
 typedef void retrieve_ded_fn(const void *extra, double *x_ded);
 
 /* Importance log-weights: logw = beta*logpost(x) - log q(x); errors give
- * flg=0. q must be mix_mvdens_log_pdf_void and post must be
- * pmcg_posterior_log_pdf_void (extra = pmcg_posterior*): both are
- * evaluated on the GPU for the whole sample. Other host callbacks are
- * rejected with PMCG_EUNSUPPORTED (there is no CPU evaluation path).
- * Returns the number of samples with flg==1.
+ * flg=0. q must be mix_mvdens_log_pdf_void; the posterior is either
+ * post = pmcg_posterior_log_pdf_void with extra = pmcg_posterior*, or the
+ * caller's own callback (posterior_log_pdf_common_void with &config->base,
+ * exec/cosmo_pmc.c:343-345) for an extra pointer registered with
+ * pmcg_register_posterior: the registered device posterior is evaluated in
+ * its place. Both densities are evaluated on the GPU for the whole sample;
+ * any other combination is rejected with PMCG_EUNSUPPORTED (there is no CPU
+ * evaluation path). Returns the number of samples with flg==1.
  * Replaces pmclib (exec/cosmo_pmc.c:343-345). */
 size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim, mix_mvdens *proposal,
     logpdf_fn *q, logpdf_fn *post, retrieve_ded_fn *ded, void *extra, double beta, int quiet, error **err);
@@ -300,6 +325,9 @@ typedef struct {
   int ip_Omegam, ip_Omegade, ip_w0, ip_M, ip_alpha, ip_beta;
   /* defaults for absent parameters */
   double def_Omegam, def_w0, def_M, def_alpha, def_beta;
+  /* 1: the parameter at ip_M (ip_beta) holds -M (-beta), the reference's
+   * storage (par_files/cosmo_SN.par:9); 0: +M (+beta) */
+  int neg_M, neg_beta;
 } pmcg_sn_data;
 void pmcg_posterior_add_snia(pmcg_posterior *p, const pmcg_sn_data *sn, error **err);
 
@@ -338,6 +366,64 @@ void pmcg_posterior_set_special(pmcg_posterior *p, int special, int ind_w0, int 
  * prior->ndim must equal their number. The prior is copied (covariance, or its
  * Cholesky factor when prior->chol == 1). A second call replaces the first. */
 void pmcg_posterior_add_mvdens_prior(pmcg_posterior *p, const mvdens *prior, const int *indprior, error **err);
+
+/* The device posterior that stands in for the caller's posterior callback
+ * with this extra pointer (the reference passes &config->base) in the weight
+ * step; post NULL removes the entry. The posterior must outlive the entry. */
+void pmcg_register_posterior(const void *extra, const pmcg_posterior *post);
+
+/* ------------------------------------------------------------------ *
+ * The reference's configuration: data types of its data section      *
+ * (wrappers/include/types.h:5-21) and the par_t codes                *
+ * (tools/include/par.h:11-33) the device plugins read.               *
+ * ------------------------------------------------------------------ */
+#define PMCG_DATA_MVDENS     0
+#define PMCG_DATA_MIXMVDENS  1
+#define PMCG_DATA_SNIA       3
+#define PMCG_P_OMEGAM   0   /* p_Omegam */
+#define PMCG_P_OMEGADE  2   /* p_Omegade: given -> non-flat, Omega_K = 1 - Omega_m - Omega_de */
+#define PMCG_P_H100     3   /* p_h100: absorbed in M for SNe (Manual/manual.tex:1321-1322) */
+#define PMCG_P_W0DE    14   /* p_w0de */
+#define PMCG_P_M       37   /* p_M: the parameter holds -M (par_files/cosmo_SN.par:9) */
+#define PMCG_P_ALPHA   38   /* p_alpha */
+#define PMCG_P_BETA    39   /* p_beta: the parameter holds -beta */
+
+/* An SN Ia data set as the reference reads it (read_from_config_SNIa and
+ * init_SNIa, wrappers/src/sn.c:20-130; the SN_SALT light-curve columns): peak
+ * magnitude m, stretch s, colour c and the covariance of (m, s, c); the SN
+ * parameter file's Theta2 = (-M, alpha, -beta) defaults; the cosmology file's
+ * Omega_m and w0_de defaults. The distance modulus is m - M + alpha (s - 1)
+ * - beta c (Manual/manual.tex:1290-1295). */
+typedef struct {
+  int nsn;
+  const double *z, *m, *s, *c;
+  const double *cov6;        /* [nsn*6]: mm, ss, cc, ms, mc, sc */
+  double Theta2[3];          /* -M, alpha, -beta */
+  double sig_int, v_pec, h;
+  double Omega_m, w0_de;
+  int chi2mode;              /* PMCG_SN_CHI2_FULL (chi2_simple) or PMCG_SN_CHI2_MARG */
+  int add_logdetCov;
+  int quad_nodes;            /* Gauss-Legendre nodes per redshift interval (1..16; 0: 4) */
+  int special;               /* PMCG_SPECIAL_* (sspecial of the data section) */
+} pmcg_snia_config;
+
+/* The device posterior of a reference configuration (config_base,
+ * posterior_log_pdf_common, wrappers/src/param.c:958-1041): npar parameters
+ * with par_t codes par[] and the flat box [min, max]; ndata data sets of types
+ * data[] with states data_state[]: PMCG_DATA_SNIA -> const pmcg_snia_config*,
+ * PMCG_DATA_MIXMVDENS -> const mix_mvdens*, PMCG_DATA_MVDENS -> const mvdens*
+ * (likeli_MixMvdens / likeli_Mvdens, :1485-1537). The special prior is the
+ * first data set's (:998, a_acc as for pmcg_posterior_set_special); prior
+ * (NULL: none) is the config prior over the parameters flagged by indprior
+ * (:1009-1026). SN parameters follow likeli_SNIa (wrappers/src/sn.c:167-224)
+ * and the flatness rules of set_base_parameters (wrappers/src/param.c:
+ * 1544-1656): Omega_de absent -> flat. SN parameters the device plugin does not
+ * model (Omega_K, the physical densities, w1_de, the polynomial dark energy,
+ * log beta, beta_z, stretch/colour offsets, Theta1, beta_d), other data types
+ * and an SN data set other than the first are PMCG_EUNSUPPORTED. */
+pmcg_posterior *pmcg_posterior_from_config(int npar, const int *par, const double *min, const double *max,
+                                           int ndata, const int *data, const void *const *data_state,
+                                           const mvdens *prior, const int *indprior, double a_acc, error **err);
 
 /* Single-point log-posterior (the per-point callback shape); evaluates one
  * point on the GPU. Passing this function to the weight step selects the

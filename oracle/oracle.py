@@ -42,6 +42,7 @@ class SN(C.Structure):
         ("ip_alpha", C.c_int), ("ip_beta", C.c_int),
         ("def_om", C.c_double), ("def_w0", C.c_double), ("def_M", C.c_double),
         ("def_alpha", C.c_double), ("def_beta", C.c_double),
+        ("neg_M", C.c_int), ("neg_beta", C.c_int),
     ]
 
 
@@ -216,6 +217,7 @@ def make_sn(data: dict, keep):
         setattr(s, k, float(data[k]))
     for k in ("chi2mode", "add_logdet", "quad_nodes", "ip_om", "ip_ode", "ip_w0", "ip_M", "ip_alpha", "ip_beta"):
         setattr(s, k, int(data[k]))
+    s.neg_M, s.neg_beta = int(data.get("neg_M", 0)), int(data.get("neg_beta", 0))
     return s
 
 
@@ -355,7 +357,7 @@ def mvdens_prior_logpdf(mean, cov, df, X, indprior=None):
     return mix_logpdf(m, np.ascontiguousarray(X[:, cols]))
 
 
-def iterate_posterior(prop: Mix, logpost_fn, N, seed, call, beta=1.0, bmin=None, bmax=None):
+def iterate_posterior(prop: Mix, logpost_fn, N, seed, call, beta=1.0, bmin=None, bmax=None, want_sample=False):
     """One whole FP64 iteration in the order of run_pmc_iteration_MPI
     (exec/cosmo_pmc.c:313-399) with any log-posterior, composed from the
     oracle's primitives (the same steps as orc_iterate_mix): the draw of
@@ -364,7 +366,8 @@ def iterate_posterior(prop: Mix, logpost_fn, N, seed, call, beta=1.0, bmin=None,
     (non-finite ones flagged out), the normalisation, perplexity/ESS and the
     Rao-Blackwellised update. Returns (updated Mix or None when every component
     died, stats); stats["status"] is 0, or -1 when no sample had a weight and -2
-    when the update buried every component."""
+    when the update buried every component. want_sample: also return the sample
+    (X, unnormalised log-weights, flags, component indices)."""
     u, z, chi2 = randoms(seed, call, N, prop.D, prop.df)
     X, idx, flg, _ = draw(prop, u, z, chi2, bmin, bmax)
     logq, lt, Q = mix_logpdf(prop, X, want_terms=True)
@@ -386,7 +389,7 @@ def iterate_posterior(prop: Mix, logpost_fn, N, seed, call, beta=1.0, bmin=None,
         st["status"] = -2
         return None, st
     st.update(enc=enc(new.w), ndead=int(dead.sum()))
-    return new, st
+    return (new, st, (X, logw, flg, idx)) if want_sample else (new, st)
 
 
 def weighted_summary(X, wbar, flg, median=False):

@@ -304,9 +304,9 @@ static double sn_loglike_sorted(const orc_sn *sn, const int *ix, const double *x
   if (sn->ip_ode >= 0) { ode = p[sn->ip_ode]; ok = 1.0 - om - ode; }
   else { ode = 1.0 - om; ok = 0.0; }
   double w0 = sn->ip_w0 >= 0 ? p[sn->ip_w0] : sn->def_w0;
-  double M = sn->ip_M >= 0 ? p[sn->ip_M] : sn->def_M;
+  double M = sn->ip_M >= 0 ? (sn->neg_M ? -p[sn->ip_M] : p[sn->ip_M]) : sn->def_M;
   double al = sn->ip_alpha >= 0 ? p[sn->ip_alpha] : sn->def_alpha;
-  double be = sn->ip_beta >= 0 ? p[sn->ip_beta] : sn->def_beta;
+  double be = sn->ip_beta >= 0 ? (sn->neg_beta ? -p[sn->ip_beta] : p[sn->ip_beta]) : sn->def_beta;
   double dh = ORC_C_KMS / (100.0 * sn->h);
   int G = sn->quad_nodes, bad = 0;
   double I = 0.0, zprev = 0.0;

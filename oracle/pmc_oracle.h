@@ -51,6 +51,7 @@ typedef struct {
   int chi2mode, add_logdet, quad_nodes;
   int ip_om, ip_ode, ip_w0, ip_M, ip_alpha, ip_beta;
   double def_om, def_w0, def_M, def_alpha, def_beta;
+  int neg_M, neg_beta;   /* 1: the parameter holds -M (-beta), par_files/cosmo_SN.par:9 */
 } orc_sn;
 void orc_gauss_legendre(int G, double *x, double *w);
 double orc_sn_loglike_one(const orc_sn *sn, const double *p, int *status);

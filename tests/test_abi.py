@@ -184,3 +184,21 @@ def test_sample_file_roundtrip(pmcg, tmp_path):
     with pytest.raises(pmcg.PmcgError):
         pmcg.call("pmc_simu_from_file", f, 100, D, 0, None, 2)  # weight clipping is not provided
     libc.fclose(f)
+
+
+def test_c_caller_compiles_against_the_header(pmcg, tmp_path):
+    """tests/c/dropin_sequence.c, a C caller of the pmclib-named entry points,
+    compiles with gcc against include/pmcg.h and links to libpmcg.so (it runs
+    under -m gpu)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    lib_dir = os.path.join(ROOT, "cosmopmc_gb300")
+    out = tmp_path / "dropin_sequence"
+    r = subprocess.run([gcc, "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "c", "dropin_sequence.c"), "-L", lib_dir, "-lpmcg",
+                        f"-Wl,-rpath,{lib_dir}", "-lm", "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert out.exists()

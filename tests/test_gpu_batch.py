@@ -76,7 +76,7 @@ def test_batch_is_bit_identical_to_runs_alone(pmcg):
     batch = P.Batch(batch_runs)
     cfg = batch.config()
     assert cfg["grid"] > 0
-    betas = [1.0, 0.5, 1.0, 0.8, 1.0, 1.0, 1.0]
+    betas = [1.0, 0.5, 1.0, 0.8, 1.0, 0.7, 1.0, 1.0]
     for it in range(3):
         bst = batch.iterate(betas)
         for r, (spec, run) in enumerate(zip(SPECS, alone_runs)):

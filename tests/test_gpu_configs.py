@@ -93,9 +93,11 @@ def _run_against_oracle(pmcg, oracle, prop, post, box, lpf, N, seed, iters, bmin
             try:
                 s32 = r32.iterate(1.0)
             except pmcg.PmcgError as e:
-                # the (FP64) update left a component narrower than single precision
-                # resolves around its mean: the mixed run reports it and stops here
-                assert e.code == -9013, (it, e)
+                # the mixed run stops where the update is degenerate: a component left
+                # narrower than single precision resolves around its mean (the FP64
+                # update is kept), or, from an effective sample of a few points, an
+                # update that single-precision statistics cannot factor (all buried)
+                assert e.code == -9013 or (e.code == -9005 and st["ess"] < 5.0), (it, e, st)
                 mixed_until = it + 1
             p32, p64s = r32.sample(), r64.sample()
             np.testing.assert_array_equal(p32.indices, p64s.indices)   # same proposal: same components
