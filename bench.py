@@ -597,7 +597,8 @@ def run_reference(args):
 
 def profile_case(args):
     """One workload of the benchmark, mixed precision, every kernel launched
-    directly with per-stage CUDA events: "mixture" (D=32, K=64 Student-t nu=3,
+    directly with per-stage CUDA events, after one untimed iteration from the same
+    proposal: "mixture" (D=32, K=64 Student-t nu=3,
     condition 1e6, 16-component target), "sn" (740 supernovae, D=6, K=10 Fisher
     start), "template" (D=12, M=2048, P=91, K=16, Fisher start)."""
     from cosmopmc_gb300 import pmcg as P
@@ -623,6 +624,8 @@ def profile_case(args):
         post = P.Posterior(12, tw["bmin"], tw["bmax"]).add_template(tw["A"], tw["C"], tw["dobs"])
         box = P.Parabox(tw["bmin"], tw["bmax"])
     run = P.Run(prop, post, N, precision=P.MIXED, seed=11, box=box)
+    run.iterate(1.0)               # untimed: loads every kernel (lazy module loading)
+    run.set_proposal(prop)
     run.set_timing(True, stages=True)
     st = None
     for _ in range(args.iterations):

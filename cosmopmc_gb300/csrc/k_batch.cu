@@ -2,10 +2,10 @@
 //
 // A batch holds runs of uneven dimension, component count, sample count and
 // likelihood (mixture, SN Ia or template target), all mixed precision. One
-// iteration of every run is one cooperative kernel: eleven stages (draw, log q,
-// log posterior, weight tiles, weight merge, EM weight factor, EM statistics,
-// EM finalise, renormalise, mixture preparation, constants), separated by grid
-// barriers. In each stage the blocks walk a flat list of work items
+// iteration of every run is one cooperative kernel: twelve stages (draw, log q,
+// log posterior, subset prior, weight tiles, weight merge, EM weight factor, EM
+// statistics, EM finalise, mixture preparation, renormalise, constants),
+// separated by grid barriers (a stage without work items is skipped). In each stage the blocks walk a flat list of work items
 // (per-run tiles, components or runs); a block finds its run by a binary
 // search over the stage's prefix table. The per-item work is the same body the
 // single-run kernels execute, with the same tiling, so each run's results are
@@ -32,7 +32,7 @@ namespace cg = cooperative_groups;
 namespace pmcg {
 
 enum BatchStage {
-  kBDraw = 0, kBLogq, kBLogpost, kBPrior, kBWeights, kBWFinal, kBFactor, kBEmStats, kBEmFinal, kBRenorm, kBPrepComp,
+  kBDraw = 0, kBLogq, kBLogpost, kBPrior, kBWeights, kBWFinal, kBFactor, kBEmStats, kBEmFinal, kBPrepComp, kBRenorm,
   kBPrepConsts, kBStages
 };
 
@@ -151,9 +151,13 @@ __device__ __forceinline__ void batch_item(int stg, const BatchDesc &d, const Ba
       body_prepare_comp(d.prop, d.logdetL, d.Wt, d.b, d.W32, d.b32, d.L32, d.mu32, (int)li,
                         reinterpret_cast<double *>(smem), &s_rmax);
       __syncthreads();
+      // a component narrower than single precision resolves is buried before the
+      // renormalisation stage, as in the single-run update
       if (threadIdx.x == 0 && d.st->status == 0 && d.w[li] > 0.0 &&
-          __longlong_as_double((long long)s_rmax) > kF32RangeMax)
-        atomicCAS(&d.st->f32_range, 0, (int)li + 1);
+          __longlong_as_double((long long)s_rmax) > kF32RangeMax) {
+        d.w[li] = 0.0;
+        atomicAdd(&d.st->f32_range, 1);
+      }
       break;
     }
     case kBPrepConsts:
@@ -459,8 +463,7 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
       const DevStats &h = b->h_stats[r];
       pmcg_iter_stats &o = stats[r];
       o.ln_evidence = h.ln_evidence; o.perplexity = h.perplexity; o.ess = h.ess; o.enc = h.enc;
-      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead;
-      o.status = h.status != 0 ? h.status : (h.f32_range != 0 ? PMCG_EPRECISION : 0);
+      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead; o.status = h.status;
     }
   }
 }

@@ -194,11 +194,17 @@ __global__ void __launch_bounds__(256) em_update_kernel(DevMix m, size_t N, int 
     body_prepare_comp(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32, k, sh, &s_rmax);
     __syncthreads();
     // single precision (the whitened update): a component narrower than single
-    // precision resolves makes the next iteration's samples and densities
-    // meaningless; the FP64 update itself is valid and kept
-    if (whitened && threadIdx.x == 0 && __longlong_as_double((long long)s_rmax) > kF32RangeMax)
-      atomicCAS(&st->f32_range, 0, k + 1);
-    if (m.bimg) umma_image_component(v, m.bimg, k);
+    // precision resolves around its mean is numerically singular there, and is
+    // buried like a component whose update is not positive definite (before the
+    // renormalisation, which the last block does)
+    if (whitened && __longlong_as_double((long long)s_rmax) > kF32RangeMax) {
+      if (threadIdx.x == 0) {
+        m.w[k] = 0.0;
+        atomicAdd(&st->f32_range, 1);
+      }
+    } else if (m.bimg) {
+      umma_image_component(v, m.bimg, k);
+    }
   }
   __threadfence();
   __syncthreads();

@@ -18,14 +18,17 @@
 //    the never-read upper-triangle blocks of the operand image and added by
 //    one more K-step against a constant operand of ones, so the accumulators
 //    hold y = L^-1 (x - mu) and the epilogue only forms |y|^2.
-//  * CTA = 9 warps, persistent (one per SM); tiles of 256 samples = two
-//    M=128 accumulators of 256 TMEM columns each. Warp 8 is the producer: one
-//    thread streams the operand image of each group (cp.async.bulk into a
-//    2-stage ring, mbarrier complete_tx) and issues the MMAs, accumulator 0
-//    then 1. Warps 0-7 stage the samples (TF32 hi/lo, 128-byte swizzle), read
-//    the accumulators (tcgen05.ld 32x32b; 4 warps per accumulator, one sample
-//    and all eight components per thread) and evaluate the densities: while
-//    one accumulator is read, the MMAs of the other run.
+//  * CTA = 10 warps, persistent (one per SM); tiles of 256 samples = two
+//    M=128 accumulators of 256 TMEM columns each, one per sample half. The
+//    halves are independent pipelines that share the operand-image stream:
+//    warp 8 + t issues accumulator t's MMAs (one thread), warp 8 also streams
+//    the operand image of each group (cp.async.bulk into a 2-stage ring,
+//    mbarrier complete_tx; a stage is refilled once both accumulators' MMAs
+//    reading it are complete). Warps 4t .. 4t+3 stage half t's samples (TF32
+//    hi/lo, 128-byte swizzle), read accumulator t (tcgen05.ld 32x32b; one
+//    sample and all eight components per thread) and evaluate the densities:
+//    while one accumulator is read, the MMAs of the other run, and neither
+//    accumulator's hand-off waits for the other's.
 //  * Every mbarrier wait is bounded (about one second): on expiry the CTA
 //    raises an abort flag that every other wait observes, sets the error
 //    flag, lets its copies and MMAs in flight land (bounded) and frees TMEM.
@@ -41,10 +44,10 @@ constexpr int kUmSmemA = 4 * kUmHalf;         // two accumulators x (hi, lo)
 constexpr int kUmSmemOnes = kUmHalf;          // constant operand of the shift K-step
 constexpr int kUmSmemB = kUmStages * kUmCopyBytes;
 constexpr int kUmEpi = 256;                   // 8 epilogue warps
-constexpr int kUmThreads = kUmEpi + 32;       // + 1 producer warp
+constexpr int kUmThreads = kUmEpi + 64;       // + 2 producer warps (one per accumulator)
 
-// Barriers: bfull[2], bempty[2], mfull[2], tfree[2], afull
-constexpr int kUmBars = 2 * kUmStages + 5;
+// Barriers: bfull[2], bempty[2], mfull[2], tfree[2], afull[2]
+constexpr int kUmBars = 2 * kUmStages + 6;
 
 size_t umma_bimage_bytes(int K) { return (size_t)((K + kUmGC - 1) / kUmGC) * kUmGroupStride; }
 
@@ -121,17 +124,18 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   // barrier addresses: bfull(s) = bfull0 + 8 s, mfull(t) = mfull0 + 8 t, ...
   const uint32_t bfull0 = smem_u32(&bars[0]), bempty0 = smem_u32(&bars[kUmStages]);
   const uint32_t mfull0 = smem_u32(&bars[2 * kUmStages]), tfree0 = smem_u32(&bars[2 * kUmStages + 2]);
-  const uint32_t afull = smem_u32(&bars[2 * kUmStages + 4]);
+  const uint32_t afull0 = smem_u32(&bars[2 * kUmStages + 4]);
   const uint32_t sA_u = smem_u32(sA), sOnes_u = smem_u32(sOnes), sB_u = smem_u32(sB);
 
   if (tid == 0) {
     s_abort = 0;
+    // a stage is empty when both accumulators' MMAs reading it are complete
 #pragma unroll
-    for (int s = 0; s < kUmStages; s++) { mbar_init(bfull0 + 8 * s, 1); mbar_init(bempty0 + 8 * s, 1); }
+    for (int s = 0; s < kUmStages; s++) { mbar_init(bfull0 + 8 * s, 1); mbar_init(bempty0 + 8 * s, 2); }
     mbar_init(mfull0, 1); mbar_init(mfull0 + 8, 1);
-    // epilogue barriers count warps (one arrival per warp)
+    // epilogue barriers count the four warps of one sample half (one arrival per warp)
     mbar_init(tfree0, kUmEpi / 64); mbar_init(tfree0 + 8, kUmEpi / 64);
-    mbar_init(afull, kUmEpi / 32);
+    mbar_init(afull0, kUmEpi / 64); mbar_init(afull0 + 8, kUmEpi / 64);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // constant operand of the shift K-step and the log-constants of every group
@@ -154,9 +158,13 @@ __global__ void __launch_bounds__(kUmThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_hold;
 
-  if (warp == kUmEpi / 32) {
-    // ================================================================ producer
+  if (warp >= kUmEpi / 32) {
+    // ================================================================ producers
+    // warp 8 + t issues accumulator t's MMAs (sample half t of every tile), so
+    // the two accumulators' hand-offs do not wait on one another; warp 8 also
+    // streams the operand images
     if (lane == 0) {
+      const int t = warp - kUmEpi / 32;
       int issued_loads = 0, last_commit = -1;
       auto load = [&](int q) {
         const int st = q % kUmStages, g = q % G;
@@ -164,30 +172,26 @@ __global__ void __launch_bounds__(kUmThreads, 1)
                   bfull0 + 8 * st);
         issued_loads++;
       };
-      for (int q = 0; q < kUmStages && q < items; q++) load(q);
+      if (t == 0)
+        for (int q = 0; q < kUmStages && q < items; q++) load(q);
       bool ok = true;
       const uint64_t ones_desc = sw128_desc(sOnes_u + 96);          // columns 24..31 of the ones operand
-      const uint64_t a_desc = sw128_desc(sA_u), b_desc = sw128_desc(sB_u);
-      for (int q = 0; q < items && ok; q++) {
+      const uint64_t a_desc = desc_add(sw128_desc(sA_u), (uint32_t)(2 * t) * kUmHalf), b_desc = sw128_desc(sB_u);
+      const uint32_t dacc = tmem + (uint32_t)t * 256;
+      for (int q = 0; q < items; q++) {
         const int g = q % G, st = q % kUmStages;
-        if (g == 0 && !mbar_wait(afull, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
+        if (g == 0 && !mbar_wait(afull0 + 8 * t, (uint32_t)((q / G) & 1), abort)) { ok = false; break; }
         if (!mbar_wait(bfull0 + 8 * st, (uint32_t)((q / kUmStages) & 1), abort)) { ok = false; break; }
-        const uint64_t bd = desc_add(b_desc, (uint32_t)st * kUmCopyBytes);
-#pragma unroll 1
-        for (int t = 0; t < 2; t++) {
-          // accumulator t was read for item q-1
-          if (q >= 1 && !mbar_wait(tfree0 + 8 * t, (uint32_t)((q - 1) & 1), abort)) { ok = false; break; }
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          issue_group<KS>(tmem + (uint32_t)t * 256, desc_add(a_desc, (uint32_t)(2 * t) * kUmHalf), bd, ones_desc);
-          umma_commit(mfull0 + 8 * t);
-        }
-        if (!ok) break;
+        // accumulator t was read for item q-1
+        if (q >= 1 && !mbar_wait(tfree0 + 8 * t, (uint32_t)((q - 1) & 1), abort)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        issue_group<KS>(dacc, a_desc, desc_add(b_desc, (uint32_t)st * kUmCopyBytes), ones_desc);
+        umma_commit(mfull0 + 8 * t);
         umma_commit(bempty0 + 8 * st);
         last_commit = q;
-        // Load group q+1 into the stage of item q-1, whose MMAs are complete: the
-        // epilogue released its accumulators (tfree, waited above) only after
-        // they had landed.
-        if (q >= 1 && q + 1 < items) {
+        // Load group q+1 into the stage of item q-1 once both accumulators'
+        // MMAs reading it are complete.
+        if (t == 0 && q >= 1 && q + 1 < items) {
           if (!mbar_wait(bempty0 + 8 * ((q - 1) % kUmStages), (uint32_t)(((q - 1) / kUmStages) & 1), abort)) {
             ok = false;
             break;
@@ -196,11 +200,10 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         }
       }
       if (!ok) atomicExch(errflag, 1);
-      // Let the MMAs and copies still in flight land before shared memory and
-      // TMEM are released (both complete at once on the normal path; after an
-      // abort of either role the waits are bounded).
-      if (last_commit >= 0)
-        mbar_drain(bempty0 + 8 * (last_commit % kUmStages), (uint32_t)((last_commit / kUmStages) & 1));
+      // Let this warp's MMAs and copies still in flight land before shared
+      // memory and TMEM are released (they are complete on the normal path;
+      // after an abort of any role the waits are bounded).
+      if (last_commit >= 0) mbar_drain(mfull0 + 8 * t, (uint32_t)(last_commit & 1));
       for (int q = last_commit + 1; q < issued_loads; q++)
         mbar_drain(bfull0 + 8 * (q % kUmStages), (uint32_t)((q / kUmStages) & 1));
     }
@@ -215,12 +218,14 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     // products' error, and off the path that returns the accumulators
     const float hndl = 0.5f * ((float)m.df + (float)D) * 0.69314718055994531f, rnu = 1.0f / (float)m.df;
     const float kLog2e = 1.44269504088896341f;
+    // the four warps of half ta stage its 128 sample rows (8 float4 per thread)
+    const int ht = tid & 127;
     float4 xr[8];
     auto fetch = [&](size_t tile) {
-      const size_t n0 = tile * kUmTile;
+      const size_t n0 = tile * kUmTile + (size_t)ta * 128;
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        const int s = (tid >> 3) + 32 * j, c = tid & 7;
+        const int s = (ht >> 3) + 16 * j, c = ht & 7;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (n0 + s < N && c * 4 < D) {
           v = __ldg(reinterpret_cast<const float4 *>(X + (n0 + s) * ldx + c * 4));
@@ -234,8 +239,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
     auto stage = [&]() {
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        const int s = (tid >> 3) + 32 * j, c = tid & 7;
-        const int t = s >> 7, r = s & 127;
+        const int r = (ht >> 3) + 16 * j, c = ht & 7, t = ta;
         const uint32_t off = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
         const float4 v = xr[j];
         float4 h, l;
@@ -246,7 +250,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         *reinterpret_cast<float4 *>(sA + (2 * t + 1) * kUmHalf + off) = l;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive_warp(afull);
+      mbar_arrive_warp(afull0 + 8 * ta);
     };
 
     bool ok = true;
@@ -283,8 +287,8 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive_warp(tfree0 + 8 * ta);                  // accumulator free for the next group
         if (g == G - 1 && i + 1 < my_tiles) {
-          // every MMA reading A (accumulator 1's are issued last) is done: stage the next tile
-          if (ta == 0 && !mbar_wait_warp(mfull0 + 8, (uint32_t)(q & 1), abort)) { ok = false; break; }
+          // every MMA reading this half's operand rows is done (its last group's
+          // accumulator has just been read): stage the next tile's half
           stage();
         }
 #pragma unroll

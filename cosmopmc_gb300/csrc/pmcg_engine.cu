@@ -207,13 +207,6 @@ static bool check_stats(Work &w, error **err) {
               w.hstats->status == PMCG_ENOWEIGHT ? "every sample has zero weight" : "all component weights are zero");
     return false;
   }
-  if (w.hstats->f32_range != 0) {
-    set_error(err, PMCG_EPRECISION, __LINE__,
-              "component %d of the updated proposal is narrower than single precision resolves around its mean; "
-              "the FP64 update is kept: continue with a PMCG_FP64 run",
-              w.hstats->f32_range - 1);
-    return false;
-  }
   return true;
 }
 

@@ -30,8 +30,8 @@ struct DevStats {
   int ndead;        // components with weight 0 after the update
   int status;       // 0 ok, else a PMCG_E* code
   int tc_err;       // set by the tensor-core log-density when one of its waits expired
-  int f32_range;    // single-precision runs: 1 + a component whose updated proposal is
-                    // narrower than single precision resolves (0: none)
+  int f32_range;    // single-precision runs: components of this update buried because
+                    // they are narrower than single precision resolves (counted in ndead)
 };
 
 // Device-resident mixture; one allocation, carved into the arrays below.

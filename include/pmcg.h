@@ -56,7 +56,8 @@ typedef struct _err {
 #define PMCG_EIO          (-10 + pmcg_base) /* file read/write error                              */
 #define PMCG_ENOWEIGHT    (-11 + pmcg_base) /* every sample has zero weight                       */
 #define PMCG_ESTEPS       (-12 + pmcg_base) /* evaluation limit reached (pmclib math_tooManySteps) */
-#define PMCG_EPRECISION   (-13 + pmcg_base) /* proposal narrower than single precision resolves (use PMCG_FP64) */
+#define PMCG_EPRECISION   (-13 + pmcg_base) /* proposal given to a PMCG_MIXED run narrower than single
+                                                precision resolves around its mean (use PMCG_FP64) */
 
 error *addError(int code, const char *text, error *next, int line);
 int isError(const error *err);
@@ -503,7 +504,11 @@ typedef struct {
 } pmcg_iter_stats;
 
 /* A run keeps its proposal, sample and scratch on the GPU. nsamples is
- * fixed at creation. pb may be NULL (no box). */
+ * fixed at creation. pb may be NULL (no box). A PMCG_MIXED run refuses a
+ * proposal (here and in pmcg_run_set_proposal) with a component narrower than
+ * single precision resolves around its mean, max_i sum_j |(L^-1)_ij mu_j| >
+ * 2^18 (PMCG_EPRECISION); its EM update buries such a component, as the dead
+ * rule buries an update that is not positive definite. */
 pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_posterior *post, const parabox *pb,
                           size_t nsamples, int precision, uint64_t seed, error **err);
 /* One PMC iteration (draw, log q, log posterior, weights, evidence,

@@ -50,10 +50,12 @@ def _mix(pmcg, w, mu, cov, df):
 
 
 def _stats_close(st, so, it):
+    """ln Z to 1e-8; perplexity, ESS and ENC to 1e-6 relative (weights carried by a
+    few samples amplify the ~1e-11 relative differences of the likelihoods' sums)."""
     for key in ("ln_evidence", "logSum", "maxW"):
         assert abs(st[key] - so[key]) <= 1e-8 * max(1.0, abs(so[key])), (it, key, st[key], so[key])
     for key in ("perplexity", "ess", "enc"):
-        assert abs(st[key] / so[key] - 1.0) <= 1e-7, (it, key, st[key], so[key])
+        assert abs(st[key] / so[key] - 1.0) <= 1e-6, (it, key, st[key], so[key])
     assert st["nok"] == so["nok"] and st["ndead"] == so["ndead"], (it, st, so)
 
 
@@ -93,11 +95,11 @@ def _run_against_oracle(pmcg, oracle, prop, post, box, lpf, N, seed, iters, bmin
             try:
                 s32 = r32.iterate(1.0)
             except pmcg.PmcgError as e:
-                # the mixed run stops where the update is degenerate: a component left
-                # narrower than single precision resolves around its mean (the FP64
-                # update is kept), or, from an effective sample of a few points, an
-                # update that single-precision statistics cannot factor (all buried)
-                assert e.code == -9013 or (e.code == -9005 and st["ess"] < 5.0), (it, e, st)
+                # the mixed run stops where the update is degenerate: fitted to an
+                # effective sample of a few points, its last live component is
+                # narrower than single precision resolves (or cannot be factored) and
+                # is buried, leaving none
+                assert e.code == -9005 and st["ess"] < 5.0, (it, e, st)
                 mixed_until = it + 1
             p32, p64s = r32.sample(), r64.sample()
             np.testing.assert_array_equal(p32.indices, p64s.indices)   # same proposal: same components
@@ -142,7 +144,8 @@ def test_c0_sn_random_start_ten_iterations(pmcg, oracle):
     # the behaviour of this start: 9 of 10 components buried by the first update, ENC 1
     # after; the survivor, fitted to an effective sample of one point, has standard
     # deviations down to 1e-9 around parameters of order 1-20, which single precision
-    # cannot represent: the mixed run stops after the first iteration with PMCG_EPRECISION
+    # cannot represent: the mixed run buries it (all components dead after the first
+    # iteration), and a mixed run refuses that proposal at upload (PMCG_EPRECISION)
     assert out[0]["ndead"] == 9 and abs(out[-1]["enc"] - 1.0) < 1e-12
     assert mixed_until == 1
 

@@ -11,8 +11,9 @@ pmcg_posterior_from_config, and the sample file written with its par_t codes.
 
 Every iteration is compared with the FP64 oracle (same draw: the generator's
 stream key is the caller's seed, the call count the iteration), continuing
-from the C program's updated proposal: counts exactly, scalars to 1e-8
-relative, proposals to 1e-7 of the component's standard deviations, and the
+from the C program's updated proposal: counts exactly, ln Z to 1e-8 relative,
+perplexity/ESS/ENC to 1e-6, proposals to 1e-7 of the component's standard
+deviations, and the
 sample file row by row (unnormalised log-weight, -component, parameters)."""
 import os
 import shutil
@@ -52,8 +53,8 @@ def _inputs(K=5, N=20000, niter=3, seed=5150, beta=1.0):
     sd = np.array([0.05, 0.2, 0.04, 0.02, 0.15])
     mu = TRUTH[None, :] + 0.5 * sd[None, :] * rng.standard_normal((K, 5))
     cov = np.repeat(np.diag((2 * sd) ** 2)[None], K, axis=0)
-    lines = [f"5 {niter} {N} {seed} {beta!r}", " ".join(map(str, PAR)),
-             " ".join(repr(v) for v in BMIN), " ".join(repr(v) for v in BMAX), str(len(sn["z"]))]
+    lines = [f"5 {niter} {N} {seed} {float(beta)!r}", " ".join(map(str, PAR)),
+             " ".join(repr(float(v)) for v in BMIN), " ".join(repr(float(v)) for v in BMAX), str(len(sn["z"]))]
     for i in range(len(sn["z"])):
         lines.append(" ".join(repr(float(v)) for v in
                               [sn["z"][i], sn["mB"][i], s[i], sn["c"][i], *sn["cov6"][i]]))
@@ -106,7 +107,7 @@ def test_c_caller_runs_the_driver_sequence_like_the_oracle(binary, oracle, tmp_p
         for key in ("ln_evidence", "logSum"):
             assert abs(got[key] - so[key]) <= 1e-8 * max(1.0, abs(so[key])), (it, key, got[key], so[key])
         for key in ("perplexity", "ess", "enc"):
-            assert abs(got[key] / so[key] - 1.0) <= 1e-7, (it, key, got[key], so[key])
+            assert abs(got[key] / so[key] - 1.0) <= 1e-6, (it, key, got[key], so[key])
         # the updated proposal (lower Cholesky factors)
         w = np.array([c[1] for c in comps[it]])
         np.testing.assert_allclose(w, new.w, rtol=1e-8, atol=1e-13)
