@@ -347,7 +347,9 @@ def ragged_specs(R, seed=256):
 NUIS_HALF, NUIS_SD = 1.0, 0.25   # nuisance parameters: box [-1, 1], Gaussian term N(0, 0.25^2)
 
 
-def build_spec(P, W, spec, cache):
+def build_spec(P, W, spec, cache, beta0=1.0):
+    """Proposal, posterior and box of one run. Fisher starts use the Fisher matrix
+    of the tempered target, beta0 F (beta0: the tempering level the run starts at)."""
     kind, D, K, N, seed = spec[:5]
     if kind == "sn":
         if "sn_data" not in cache:
@@ -368,7 +370,7 @@ def build_spec(P, W, spec, cache):
             cache[("sn_post", D)] = (post, P.Parabox(bmin, bmax), F, theta0, bmin, bmax)
         post, box, F, theta0, bmin, bmax = cache[("sn_post", D)]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, F, bmin, bmax)
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, bmin, bmax)
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     if kind == "tpl":
         if "tpl_post" not in cache:
@@ -379,7 +381,7 @@ def build_spec(P, W, spec, cache):
         post, box = cache["tpl_post"]
         F, theta0 = cache["tpl_fisher"]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, F, -np.ones(12), np.ones(12))
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, -np.ones(12), np.ones(12))
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=-1, seed=seed, prop_hi=2.0)
     w, mu, cov, df = wl["prop"]
@@ -416,9 +418,19 @@ def batch_bench(P, W, R=256, iters=5):
     a time (mixed precision) and vs the plain FP64 path one at a time."""
     specs = ragged_specs(R)
     cache = {}
-    built = [build_spec(P, W, s, cache) for s in specs]
+    built = [build_spec(P, W, s, cache, beta0=s[5]) for s in specs]
     betas = np.array([s[5] for s in specs])
-    runs_b = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+
+    def make_runs(prec):
+        runs = []
+        for s, (pp, po, bx) in zip(specs, built):
+            r = P.Run(pp, po, s[3], precision=prec, seed=s[4], box=bx)
+            if bx is not None:
+                r.set_dead_comp(P.DEAD_REVIVE, 0.1)   # revival needs the prior box
+            runs.append(r)
+        return runs
+
+    runs_b = make_runs(P.MIXED)
     total = sum(s[3] for s in specs)
     batch = P.Batch(runs_b)
     t0 = time.perf_counter()
@@ -435,16 +447,17 @@ def batch_bench(P, W, R=256, iters=5):
     cfg = batch.config()
     batch.free()
     del runs_b
-    runs_s = [P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    runs_s = make_runs(P.MIXED)
     seq_s = _iterate_each(P, runs_s, betas, 2)
     for r in runs_s:
         r.free()
-    runs_64 = [P.Run(pp, po, s[3], precision=P.FP64, seed=s[4], box=bx) for s, (pp, po, bx) in zip(specs, built)]
+    runs_64 = make_runs(P.FP64)
     fp64_s = _iterate_each(P, runs_64, betas, 1)
     for r in runs_64:
         r.free()
     value = total / (med / 1e3)
-    return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + Gaussian nuisance in a flat box), half GMM "
+    return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + Gaussian nuisance in a flat box, "
+                        f"start from the tempered Fisher matrix, dead components revived), half GMM "
                         f"(D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5), beta from the log tempering schedule "
                         f"(t_min {TEMPER_TMIN}, {TEMPER_LEVELS} levels)",
             "samples_per_iter": total, "value": value, "unit": UNIT, "ms_per_iter": med,
@@ -463,16 +476,17 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
     rng = np.random.default_rng(seed)
     pool_specs = ragged_specs(64, seed=99)
     cache = {}
-    pool = [(s, build_spec(P, W, s, cache)) for s in pool_specs]
+    # jobs run the log schedule from t_min: Fisher starts use t_min F
+    pool = [(s, build_spec(P, W, s, cache, beta0=TEMPER_TMIN)) for s in pool_specs]
     tpl_spec = ("tpl", 12, 16, 262144, 91, 1.0)
-    tpl = (tpl_spec, build_spec(P, W, tpl_spec, cache))
+    tpl = (tpl_spec, build_spec(P, W, tpl_spec, cache, beta0=TEMPER_TMIN))
 
     def pick(r):
         return tpl if r.uniform() < 0.1 else pool[int(r.integers(0, len(pool)))]
 
     out = []
     for rate in rates:
-        srv = P.Server()
+        srv = P.Server(dead_comp=P.DEAD_REVIVE, fshift=0.1)
         n_jobs = max(8, int(rate * window_s))
         arrivals = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
         ids = []
@@ -512,6 +526,8 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
     samples64, failed64 = 0, 0
     for spec, pp, po, bx, niter, sd in jobs:
         run = P.Run(pp, po, spec[3], precision=P.FP64, seed=sd, box=bx)
+        if bx is not None:
+            run.set_dead_comp(P.DEAD_REVIVE, 0.1)
         try:
             for it in range(niter):
                 run.iterate(P.get_tempering_beta(P.TEMPERING_LOG, it, TEMPER_TMIN, niter))
@@ -523,8 +539,9 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
     fp64_rate = samples64 / (time.perf_counter() - t0)
     peak = max(r["samples_per_s"] for r in out)
     return {"workload": "Poisson arrivals; 90% jobs from the ragged mix, 10% template-sized (D=12, N=2^18, "
-                        "M=2048, Fisher start); 5-10 iterations per job on the log tempering schedule "
-                        f"(t_min {TEMPER_TMIN}); mixed precision",
+                        "M=2048); Fisher starts from the t_min-tempered Fisher matrix; 5-10 iterations per job on "
+                        f"the log tempering schedule (t_min {TEMPER_TMIN}); dead components revived (jobs with a "
+                        "prior box); mixed precision",
             "latency": "job submit to result (server clock)", "rates": out,
             "fp64": {"samples_per_s": fp64_rate, "jobs": fp64_jobs, "failed": failed64,
                      "how": "plain FP64 runs of jobs drawn from the same mix (job creation included), one job "

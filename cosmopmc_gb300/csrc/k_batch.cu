@@ -459,11 +459,18 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
     *run->w.hstats = b->h_stats[r];
     run->calls++;
     run->last_launches = 1;
+    int status = b->h_stats[r].status;
+    if (status == 0) {
+      // runs in revive mode revive their dead components, as when iterated alone
+      error *le = nullptr;
+      if (!run_revive_dead(run, &le)) status = isError(le) ? getErrorValue(le) : PMCG_ECUDA;
+      purgeError(&le);
+    }
     if (stats) {
       const DevStats &h = b->h_stats[r];
       pmcg_iter_stats &o = stats[r];
       o.ln_evidence = h.ln_evidence; o.perplexity = h.perplexity; o.ess = h.ess; o.enc = h.enc;
-      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead; o.status = h.status;
+      o.logSum = h.logSum; o.maxW = h.maxW; o.nok = (size_t)h.nok; o.ndead = h.ndead; o.status = status;
     }
   }
 }

@@ -11,11 +11,20 @@
 // multiply/xor round function with a Weyl-sequence key schedule.
 struct P4 { uint32_t x, y, z, w; };
 
-__device__ __forceinline__ P4 philox4x32_10(P4 c, uint32_t k0, uint32_t k1) {
+// High word of a 32 x 32-bit product (the device's mul.hi; the same value on the host).
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ P4 philox4x32_10(P4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; r++) {
-    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = mulhi32(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = mulhi32(0xCD9E8D57u, c.z);
     P4 n;
     n.x = hi1 ^ c.y ^ k0;
     n.y = lo1;
@@ -29,7 +38,7 @@ __device__ __forceinline__ P4 philox4x32_10(P4 c, uint32_t k0, uint32_t k1) {
 }
 
 // 53-bit dyadic uniform in [0,1) from two words (same mapping as the oracle).
-__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+__host__ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 // 24-bit uniform in [0,1) for the single-precision sampler.

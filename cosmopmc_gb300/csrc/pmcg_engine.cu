@@ -800,6 +800,8 @@ extern "C" pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_post
   r->seed = seed;
   if (pb) {
     r->box = true;
+    r->hmin.assign(pb->min, pb->min + pb->ndim);
+    r->hmax.assign(pb->max, pb->max + pb->ndim);
     if (!upload_box(r->w, pb->min, pb->max, err)) { work_free(r->w); delete r; return nullptr; }
   }
   for (int i = 0; i <= PMCG_NSTAGE; i++) cudaEventCreate(&r->ev[i]);
@@ -891,6 +893,7 @@ extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stat
     }
     r->timed++;
   }
+  if (!run_revive_dead(r, err)) return;
   if (stats) {
     const DevStats &h = *w.hstats;
     stats->ln_evidence = h.ln_evidence;
@@ -938,6 +941,86 @@ extern "C" void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, e
   }
   upload_mix(w.prop, proposal, w.s, err, w.prec != 0);
 }
+
+extern "C" void pmcg_run_set_dead_comp(pmcg_run *r, int mode, double fshift, error **err) {
+  if (!r || (mode != PMCG_DEAD_BURY && mode != PMCG_DEAD_REVIVE) || !(fshift > 0.0)) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_set_dead_comp: invalid mode %d or fshift %g", mode, fshift);
+    return;
+  }
+  if (mode == PMCG_DEAD_REVIVE && r->hmin.empty()) {
+    set_error(err, PMCG_EARG, __LINE__, "reviving components needs the run's prior box");
+    return;
+  }
+  r->dead_mode = mode;
+  r->fshift = fshift;
+  r->nrevive = 1;
+}
+
+namespace pmcg {
+// update_and_deal_with_dead's revive branch (exec/cosmo_pmc.c:252-275) with
+// revive_comp (:205-236) and comp_shift_mean (wrappers/src/param.c:471-489).
+bool run_revive_dead(pmcg_run *r, error **err) {
+  if (r->dead_mode != PMCG_DEAD_REVIVE) return true;
+  r->nrevive *= 2;  // every update in revive mode (:259)
+  Work &w = r->w;
+  if (w.hstats->ndead == 0) return true;
+  const int K = w.K, D = w.D;
+  std::vector<double> wt(K), mu((size_t)K * D), L((size_t)K * D * D);
+  bool ok = CK(cudaMemcpyAsync(wt.data(), w.prop.w, 8 * K, cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(mu.data(), w.prop.mu, 8 * mu.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaMemcpyAsync(L.data(), w.prop.L, 8 * L.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
+            CK(cudaStreamSynchronize(w.s), "proposal");
+  if (!ok) return false;
+  const uint32_t call = r->calls - 1;   // the call of the iteration that made this update
+  const double fs = r->fshift / (double)r->nrevive;
+  bool changed = false;
+  for (int i = 0; i < K; i++) {
+    if (!(wt[i] < 1e-12)) continue;
+    int imax = -1;
+    double wmax = 0.0;
+    for (int j = 0; j < K; j++)
+      if (wt[j] > wmax) { wmax = wt[j]; imax = j; }
+    if (imax < 0) {
+      set_error(err, PMCG_ENEGWEIGHT, __LINE__, "Components weights are all zero");
+      return false;
+    }
+    // copy of the largest component, mean shifted inside the box
+    std::memcpy(&L[(size_t)i * D * D], &L[(size_t)imax * D * D], sizeof(double) * D * D);
+    uint32_t k = 0;
+    for (int d = 0; d < D; d++) {
+      const double box = r->hmax[d] - r->hmin[d];
+      double m;
+      do {
+        if (++k > 50) {
+          set_error(err, PMCG_ESTEPS, __LINE__,
+                    "Could not place proposal component in box. Make sure that fshift is not too large");
+          return false;
+        }
+        P4 c;
+        c.x = 0xFFFFFFF0u; c.y = (uint32_t)i; c.z = k - 1; c.w = call;
+        const P4 o = philox4x32_10(c, (uint32_t)r->seed, (uint32_t)(r->seed >> 32));
+        const double u = u53(o.x, o.y);
+        m = mu[(size_t)imax * D + d] + (-fs * box + 2.0 * fs * box * u);
+      } while (m < r->hmin[d] || m > r->hmax[d]);
+      mu[(size_t)i * D + d] = m;
+    }
+    wt[imax] /= 2.0;
+    wt[i] = wt[imax];
+    changed = true;
+  }
+  if (!changed) return true;
+  double sum = 0.0;
+  for (int i = 0; i < K; i++) sum += wt[i];
+  if (!(sum > 0.0) || !std::isfinite(sum)) {
+    set_error(err, PMCG_ENEGWEIGHT, __LINE__, "Sum of weight is %g", sum);
+    return false;
+  }
+  for (int i = 0; i < K; i++) wt[i] /= sum;
+  if (w.prec != 0 && !f32_range_ok(wt, mu, L, K, D, err)) return false;
+  return CK(devmix_upload(w.prop, wt.data(), mu.data(), L.data(), w.s), "proposal upload") &&
+         CK(cudaStreamSynchronize(w.s), "proposal upload");
+}
+}  // namespace pmcg
 
 extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {
   Work &w = r->w;

@@ -104,4 +104,16 @@ struct pmcg_run {
   cudaGraphExec_t gexec = nullptr;
   int graph_tc = -1, graph_launches = 0;
   bool graph_off = false;
+  // Dead components (sdead_comp, exec/cosmo_pmc.c:239-284): buried (default) or
+  // revived after each update; the box on the host for the revival's shifts.
+  int dead_mode = PMCG_DEAD_BURY;
+  double fshift = 0.1;
+  int nrevive = 1;
+  std::vector<double> hmin, hmax;
 };
+
+namespace pmcg {
+// The revival step of a run in PMCG_DEAD_REVIVE mode after a successful update
+// (the run's statistics are in w.hstats); no-op in bury mode.
+bool run_revive_dead(pmcg_run *r, error **err);
+}  // namespace pmcg

@@ -141,7 +141,10 @@ static void server_loop(pmcg_server *s) {
     for (Job *j : admitted) {
       error *e = nullptr;
       j->run = pmcg_run_create(j->prop, j->post, j->pb, j->N, PMCG_MIXED, j->seed, &e);
-      if (!j->run) {
+      // revival needs the job's prior box; jobs without one keep burying
+      if (j->run && j->pb && s->opts.dead_comp == PMCG_DEAD_REVIVE)
+        pmcg_run_set_dead_comp(j->run, PMCG_DEAD_REVIVE, s->opts.fshift, &e);
+      if (!j->run || isError(e)) {
         int code = getErrorValue(e);
         purgeError(&e);
         retire(s, j, code ? code : PMCG_EALLOC);
@@ -227,6 +230,8 @@ extern "C" pmcg_server *pmcg_server_create(const pmcg_server_opts *opts, error *
   if (opts) s->opts = *opts;
   cudaGetDevice(&s->device);
   if (s->opts.max_jobs <= 0) s->opts.max_jobs = 512;
+  if (!(s->opts.fshift > 0.0)) s->opts.fshift = 0.1;
+  if (s->opts.dead_comp != PMCG_DEAD_REVIVE) s->opts.dead_comp = PMCG_DEAD_BURY;
   if (s->opts.hbm_budget_bytes == 0) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);

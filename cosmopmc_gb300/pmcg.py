@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libpmcg.so")
 FP64 = 0
 MIXED = 1
 SPECIAL_NONE, SPECIAL_UNITY, SPECIAL_DE_CONSERVATIVE = 0, 1, 2
+DEAD_BURY, DEAD_REVIVE = 0, 1
 TEMPERING_NONE, TEMPERING_LINEAR, TEMPERING_LOG = 0, 1, 2
 SN_CHI2_FULL, SN_CHI2_MARG = 0, 1
 
@@ -96,7 +97,8 @@ class WeightStats(C.Structure):
 
 
 class ServerOpts(C.Structure):
-    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_jobs", C.c_int), ("autotune", C.c_int)]
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_jobs", C.c_int), ("autotune", C.c_int),
+                ("dead_comp", C.c_int), ("fshift", C.c_double)]
 
 
 class JobResult(C.Structure):
@@ -204,6 +206,7 @@ SIGNATURES = [
     ("pmcg_run_iterate", None, [C.c_void_p, C.c_double, C.POINTER(IterStats), PErr]),
     ("pmcg_run_get_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_run_get_sample", None, [C.c_void_p, C.POINTER(PmcSimuS), PErr]),
+    ("pmcg_run_set_dead_comp", None, [C.c_void_p, C.c_int, C.c_double, PErr]),
     ("pmcg_run_set_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_run_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
@@ -629,6 +632,10 @@ class Run:
         call("pmcg_run_get_proposal", self.p, m.p)
         return m
 
+    def set_dead_comp(self, mode, fshift=0.1):
+        """DEAD_BURY (default) or DEAD_REVIVE (revive_comp, needs the run's box)."""
+        call("pmcg_run_set_dead_comp", self.p, int(mode), float(fshift))
+
     def set_proposal(self, m: MixMvdens):
         call("pmcg_run_set_proposal", self.p, m.p)
 
@@ -714,8 +721,8 @@ class Batch:
 class Server:
     """Continuous-batching PMC server (pmcg_server_*)."""
 
-    def __init__(self, hbm_budget_bytes=0, max_jobs=0, autotune=False):
-        o = ServerOpts(hbm_budget_bytes, max_jobs, 1 if autotune else 0)
+    def __init__(self, hbm_budget_bytes=0, max_jobs=0, autotune=False, dead_comp=DEAD_BURY, fshift=0.1):
+        o = ServerOpts(hbm_budget_bytes, max_jobs, 1 if autotune else 0, dead_comp, fshift)
         self.p = C.c_void_p(call("pmcg_server_create", C.byref(o)))
         self._keep = {}
 

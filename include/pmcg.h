@@ -520,6 +520,21 @@ void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err);
 void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, error **err);
 /* Copy the last sample (X, log-weights, flg, indices) into psim. */
 void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err);
+/* Dead components after each update (sdead_comp, exec/cosmo_pmc.c:239-284):
+ * PMCG_DEAD_BURY (default) keeps them buried; PMCG_DEAD_REVIVE revives each
+ * component whose weight is below 1e-12 as revive_comp does (:205-236): the
+ * counter Nrevive doubles at every update (from 1), and each dead component in
+ * index order becomes a copy of the component of largest weight (mean and
+ * covariance) whose mean is shifted, coordinate by coordinate, by a uniform
+ * draw in [-f (max-min), f (max-min)], f = fshift / Nrevive, redrawn while it
+ * leaves the box (more than 50 draws for one component: PMCG_ESTEPS); the two
+ * share the larger one's weight equally. fshift: 0.1 for the reference's
+ * non-Fisher starts (FSHIFT_DEFAULT), its fshift for the Fisher ones. The draws
+ * come from the run's random stream (Philox counter {0xFFFFFFF0, component,
+ * draw, call}), so a revival is reproducible. Needs the run's prior box. */
+#define PMCG_DEAD_BURY   0
+#define PMCG_DEAD_REVIVE 1
+void pmcg_run_set_dead_comp(pmcg_run *r, int mode, double fshift, error **err);
 void pmcg_run_free(pmcg_run **r);
 /* Timing with CUDA events on the run's stream. on = 1: per stage (draw,
  * logq, logpost, weights, em; every kernel launched directly), read with
@@ -577,6 +592,8 @@ typedef struct {
   size_t hbm_budget_bytes;  /* 0: 80% of the free device memory at creation */
   int max_jobs;             /* resident jobs at most (0: 512) */
   int autotune;             /* tune each new batch shape (cached per shape) */
+  int dead_comp;            /* PMCG_DEAD_BURY (0) or PMCG_DEAD_REVIVE for every job with a prior box */
+  double fshift;            /* revival shift (0: 0.1) */
 } pmcg_server_opts;
 typedef struct {
   int status;               /* 0 done, > 0 queued/running, < 0 PMCG_E* error */

@@ -99,6 +99,9 @@ def lib():
         L.orc_prior_special.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double,
                                         C.POINTER(C.c_double)]
         L.orc_prior_special.restype = C.c_int
+        L.orc_revive.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_uint64,
+                                 C.c_uint32]
+        L.orc_revive.restype = C.c_int
         L.orc_weighted_summary.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, _ip]
         L.orc_hist1d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, _dp, _dp, C.c_double, _dp]
         L.orc_hist2d.argtypes = [C.c_size_t, C.c_int, _dp, _dp, _sp, C.c_int, C.c_int, C.c_int, _dp, _dp,
@@ -433,3 +436,14 @@ def clip_weights(logw, flg, k):
     out[order[:k]] = 0
     return out
 
+
+
+def revive(mix: Mix, bmin, bmax, fshift, nrevive, seed, call):
+    """The revive step (exec/cosmo_pmc.c:205-275) on a copy of mix; returns the new Mix."""
+    m = mix.copy()
+    rc = lib().orc_revive(m.K, m.D, m.w, m.mu, m.L, np.ascontiguousarray(bmin, dtype=np.float64),
+                          np.ascontiguousarray(bmax, dtype=np.float64), float(fshift), int(nrevive), int(seed),
+                          int(call))
+    if rc:
+        raise ValueError(f"revive failed ({rc})")
+    return Mix(m.w, m.mu, df=m.df, L=m.L)

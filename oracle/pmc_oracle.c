@@ -728,3 +728,44 @@ int orc_prior_special(int special, int npar, const double *min, const double *ma
   }
   return 0;
 }
+
+/* ---------------------------------------------------------------- revival
+ * The revive branch of update_and_deal_with_dead (exec/cosmo_pmc.c:252-275):
+ * each component of weight below 1e-12, in index order, becomes a copy of the
+ * component of largest weight (revive_comp, :205-236) whose mean is shifted by
+ * comp_shift_mean (wrappers/src/param.c:471-489): per coordinate a uniform
+ * shift in [-f box, f box], f = fshift / nrevive, redrawn while outside the
+ * box, at most 50 draws in all; the two then share the larger weight. */
+int orc_revive(int K, int D, double *w, double *mu, double *L, const double *bmin, const double *bmax,
+               double fshift, int nrevive, uint64_t seed, uint32_t call) {
+  const double fs = fshift / (double)nrevive;
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (int i = 0; i < K; i++) {
+    if (!(w[i] < 1e-12)) continue;
+    int imax = -1;
+    double wmax = 0.0;
+    for (int j = 0; j < K; j++)
+      if (w[j] > wmax) { wmax = w[j]; imax = j; }
+    if (imax < 0) return -1;
+    memcpy(L + (size_t)i * D * D, L + (size_t)imax * D * D, sizeof(double) * D * D);
+    uint32_t k = 0;
+    for (int d = 0; d < D; d++) {
+      const double box = bmax[d] - bmin[d];
+      double m;
+      do {
+        if (++k > 50) return -2;
+        uint32_t ctr[4] = {0xFFFFFFF0u, (uint32_t)i, k - 1, call}, o[4];
+        orc_philox(ctr, key, o);
+        m = mu[(size_t)imax * D + d] + (-fs * box + 2.0 * fs * box * u53(o[0], o[1]));
+      } while (m < bmin[d] || m > bmax[d]);
+      mu[(size_t)i * D + d] = m;
+    }
+    w[imax] /= 2.0;
+    w[i] = w[imax];
+  }
+  double sum = 0.0;
+  for (int i = 0; i < K; i++) sum += w[i];
+  if (!(sum > 0.0) || !isfinite(sum)) return -3;
+  for (int i = 0; i < K; i++) w[i] /= sum;
+  return 0;
+}

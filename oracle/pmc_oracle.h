@@ -103,6 +103,16 @@ int orc_num_threads(void);
 int orc_prior_special(int special, int npar, const double *min, const double *max, int ind_w0, int ind_w1,
                       double a_acc, double *out);
 
+/* Revival of dead components (sdead_comp revive: update_and_deal_with_dead,
+ * exec/cosmo_pmc.c:252-275; revive_comp :205-236; comp_shift_mean,
+ * wrappers/src/param.c:471-489), the draws from the library's stream (Philox
+ * counter {0xFFFFFFF0, component, draw, call} keyed by seed; the reference's
+ * gsl_rng is absent). nrevive: the counter after its doubling for this update.
+ * w/mu/L updated in place. Returns 0, -1 all weights zero, -2 more than 50
+ * draws for one component, -3 invalid weight sum. */
+int orc_revive(int K, int D, double *w, double *mu, double *L, const double *bmin, const double *bmax,
+               double fshift, int nrevive, uint64_t seed, uint32_t call);
+
 /* Post-processing: marginal centre (mean or median) and one-sided 68.27 /
  * 95.45 / 99.73 % limits per parameter (sigma[6a .. 6a+5]: right, then left),
  * and weighted histograms (exec/exec_helper.c:63-271,
