@@ -349,7 +349,8 @@ NUIS_HALF, NUIS_SD = 1.0, 0.25   # nuisance parameters: box [-1, 1], Gaussian te
 
 def build_spec(P, W, spec, cache, beta0=1.0):
     """Proposal, posterior and box of one run. Fisher starts use the Fisher matrix
-    of the tempered target, beta0 F (beta0: the tempering level the run starts at)."""
+    of the tempered target, beta0 F (beta0: the tempering level the run starts at),
+    with every standard deviation capped at a quarter of the box width."""
     kind, D, K, N, seed = spec[:5]
     if kind == "sn":
         if "sn_data" not in cache:
@@ -370,7 +371,7 @@ def build_spec(P, W, spec, cache, beta0=1.0):
             cache[("sn_post", D)] = (post, P.Parabox(bmin, bmax), F, theta0, bmin, bmax)
         post, box, F, theta0, bmin, bmax = cache[("sn_post", D)]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, bmin, bmax)
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, bmin, bmax, box_frac=0.25)
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     if kind == "tpl":
         if "tpl_post" not in cache:
@@ -381,7 +382,7 @@ def build_spec(P, W, spec, cache, beta0=1.0):
         post, box = cache["tpl_post"]
         F, theta0 = cache["tpl_fisher"]
         rng = np.random.default_rng(seed)
-        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, -np.ones(12), np.ones(12))
+        w, mu, cov, df = W.fisher_proposal(rng, K, theta0, beta0 * F, -np.ones(12), np.ones(12), box_frac=0.25)
         return P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky(), post, box
     wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=-1, seed=seed, prop_hi=2.0)
     w, mu, cov, df = wl["prop"]

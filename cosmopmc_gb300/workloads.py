@@ -136,14 +136,21 @@ def sn_fisher(sn, theta, rel_step=1e-4):
     return J.T @ (J / sig2[:, None])
 
 
-def fisher_proposal(rng, K, theta0, F, bmin, bmax, fshift=1.0, frescale=2.0, df=-1):
+def fisher_proposal(rng, K, theta0, F, bmin, bmax, fshift=1.0, frescale=2.0, df=-1, box_frac=None):
     """Initial proposal from a Fisher matrix (the reference's Fisher start): every
     component has covariance frescale * F^-1 and a mean shifted from theta0 by
-    fshift * F^-1/2 xi, xi ~ N(0, I), clipped into the box; equal weights."""
+    fshift * F^-1/2 xi, xi ~ N(0, I), clipped into the box; equal weights.
+    box_frac: cap every standard deviation of F^-1 at box_frac (max - min),
+    keeping the correlations (a Fisher matrix of a strongly tempered target
+    is wider than the prior box)."""
     Cf = np.linalg.inv(F)
     Cf = 0.5 * (Cf + Cf.T)
-    L = np.linalg.cholesky(Cf)
     bmin, bmax = np.asarray(bmin, float), np.asarray(bmax, float)
+    if box_frac is not None:
+        sd = np.sqrt(np.diag(Cf))
+        f = np.minimum(1.0, box_frac * (bmax - bmin) / sd)
+        Cf = Cf * np.outer(f, f)
+    L = np.linalg.cholesky(Cf)
     mu = theta0[None, :] + fshift * (rng.standard_normal((K, len(theta0))) @ L.T)
     mu = np.clip(mu, bmin + 1e-3 * (bmax - bmin), bmax - 1e-3 * (bmax - bmin))
     covs = np.repeat((frescale * Cf)[None], K, axis=0)

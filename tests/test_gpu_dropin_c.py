@@ -126,11 +126,15 @@ def test_c_caller_runs_the_driver_sequence_like_the_oracle(binary, oracle, tmp_p
         rows = np.loadtxt(path, comments="#", ndmin=2)
         ok = flg == 1
         assert rows.shape == (int(ok.sum()), 2 + D)
-        # the file holds log(normalised weight) + logSum: -inf where the normalised
-        # weight underflows, as the reference writes it (exec/exec_helper.c:408-420)
+        # the file holds log(normalised weight) + logSum, as the reference writes it
+        # (exec/exec_helper.c:408-420): -inf where the normalised weight underflows,
+        # fewer bits where it is subnormal (below 2.2e-308, log < -708.4)
+        rel = logw[ok] - so["logSum"]
         fin = np.isfinite(rows[:, 0])
-        assert np.all(logw[ok][~fin] - so["logSum"] < -700.0)
-        np.testing.assert_allclose(rows[fin, 0], logw[ok][fin], rtol=1e-8, atol=1e-8)
+        assert np.all(rel[~fin] < -700.0)
+        normal = rel > -708.0
+        np.testing.assert_allclose(rows[normal, 0], logw[ok][normal], rtol=1e-8, atol=1e-8)
+        np.testing.assert_allclose(rows[fin & ~normal, 0], logw[ok][fin & ~normal], rtol=0, atol=1.0)
         np.testing.assert_array_equal(rows[:, 1], -idx[ok].astype(float))
         np.testing.assert_allclose(rows[:, 2:], X[ok], rtol=1e-8, atol=1e-12)
         # continue from the C program's proposal

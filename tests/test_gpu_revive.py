@@ -88,7 +88,6 @@ def test_batch_and_server_revive_like_runs_alone(pmcg):
         for it in range(3):
             sa = alone.iterate(1.0)
             sb = batch.iterate([1.0])[0]
-            sb.pop("status")
             assert sa == sb, (it, sa, sb)
             wa, ma, La = alone.proposal().arrays()
             wb, mb, Lb = inb.proposal().arrays()
