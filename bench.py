@@ -348,9 +348,10 @@ NUIS_HALF, NUIS_SD = 1.0, 0.25   # nuisance parameters: box [-1, 1], Gaussian te
 
 
 def build_spec(P, W, spec, cache, beta0=1.0):
-    """Proposal, posterior and box of one run. Fisher starts use the Fisher matrix
-    of the tempered target, beta0 F (beta0: the tempering level the run starts at),
-    with every standard deviation capped at a quarter of the box width."""
+    """Proposal, posterior and box of one run, started for the tempered target p^beta0
+    (beta0: the tempering level the run starts at). Fisher starts use the Fisher
+    matrix beta0 F, with every standard deviation capped at a quarter of the box
+    width; Gaussian-mixture starts have their covariances divided by beta0."""
     kind, D, K, N, seed = spec[:5]
     if kind == "sn":
         if "sn_data" not in cache:
@@ -387,7 +388,10 @@ def build_spec(P, W, spec, cache, beta0=1.0):
     wl = W.mixture_workload(D=D, K=K, Kt=max(1, K // 3), nu=-1, seed=seed, prop_hi=2.0)
     w, mu, cov, df = wl["prop"]
     wt, mut, covt, _ = wl["target"]
-    prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    # the tempered target p^beta0 of a Gaussian component has covariance cov / beta0:
+    # the start is widened to match (a start fitted to beta = 1 under a flat target
+    # leaves the weights to the proposal's tails)
+    prop = P.MixMvdens.from_arrays(w, mu, cov=cov / beta0, df=df).cholesky()
     target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
     post = P.Posterior(D).add_mix(target)
     cache.setdefault("keep", []).append(target)
@@ -439,11 +443,14 @@ def batch_bench(P, W, R=256, iters=5):
     tune_s = time.perf_counter() - t0
     batch.iterate(betas)  # warm-up
     ms = []
-    failed = 0
+    failed = {}
     for _ in range(iters):
         st = batch.iterate(betas)
         ms.append(batch.last_ms())
-        failed += sum(1 for x in st if x["status"] != 0)
+        for s, x in zip(specs, st):
+            if x["status"] != 0:
+                key = f"{s[0]}:{x['status']}"
+                failed[key] = failed.get(key, 0) + 1
     med = float(np.median(ms))
     cfg = batch.config()
     batch.free()
@@ -466,6 +473,7 @@ def batch_bench(P, W, R=256, iters=5):
             "fp64_one_run_at_a_time_samples_per_s": total / fp64_s,
             "speedup_mixed_vs_fp64": value / (total / fp64_s),
             "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed,
+            "failed_note": "kind:status of run iterations that failed (-9005: every component dead)",
             "timing": "CUDA events around each graph launch (library stream), median of iterations; the one-at-a-time "
                       "legs by host clock around a synchronised pass over all runs"}
 
@@ -499,17 +507,18 @@ def serve_bench(P, W, rates=(10, 30, 100, 300, 1000, 2000), window_s=2.5, seed=4
             spec, (pp, po, bx) = pick(rng)
             niter = int(rng.integers(5, 11))
             ids.append((srv.submit(pp, po, spec[3], niter, int(rng.integers(1, 1 << 30)), box=bx,
-                                   tempering=P.TEMPERING_LOG, t_min=TEMPER_TMIN), spec[3], niter))
-        res = [(srv.wait(j, timeout=600), n, it) for j, n, it in ids]
+                                   tempering=P.TEMPERING_LOG, t_min=TEMPER_TMIN), spec[3], niter, spec[0]))
+        res = [(srv.wait(j, timeout=600), n, it, kind) for j, n, it, kind in ids]
         wall = time.perf_counter() - t_start
         info = srv.info()
         srv.free()
-        lat = np.array([r["finish_s"] - r["submit_s"] for r, _, _ in res if r["status"] == 0])
-        samples = sum(n * it for r, n, it in res if r["status"] == 0)
+        lat = np.array([r["finish_s"] - r["submit_s"] for r, _, _, _ in res if r["status"] == 0])
+        samples = sum(n * it for r, n, it, _ in res if r["status"] == 0)
         failed = {}
-        for r, _, _ in res:
+        for r, _, _, kind in res:
             if r["status"] != 0:
-                failed[str(r["status"])] = failed.get(str(r["status"]), 0) + 1
+                key = f"{kind}:{r['status']}"
+                failed[key] = failed.get(key, 0) + 1
         out.append({"rate_jobs_per_s": rate, "jobs": n_jobs, "ok": int(len(lat)), "failed_status": failed,
                     "p50_ms": float(np.percentile(lat, 50) * 1e3) if len(lat) else None,
                     "p99_ms": float(np.percentile(lat, 99) * 1e3) if len(lat) else None,

@@ -141,9 +141,10 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float *v) {
       : "r"(taddr));
 }
 
-// acc += (a, b)^2 elementwise on a packed pair (one f32x2 FMA).
+// acc += (a, b)^2 elementwise on a packed pair (one f32x2 FMA); volatile keeps
+// it in program order with the TMEM loads and waits around it.
 __device__ __forceinline__ void sq2_acc(unsigned long long &acc, float a, float b) {
-  asm("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1, %2};\n\tfma.rn.f32x2 %0, t, t, %0;\n\t}"
+  asm volatile("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1, %2};\n\tfma.rn.f32x2 %0, t, t, %0;\n\t}"
       : "+l"(acc)
       : "f"(a), "f"(b));
 }
