@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--no-likelihoods", action="store_true", help="skip the SN and template measurements")
     ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
                     help="single-precision log-densities on tcgen05 (1) or CUDA cores (0); default: library setting")
-    ap.add_argument("--profile-case", default=None, choices=["mixture", "sn", "template"],
+    ap.add_argument("--profile-case", default=None, choices=["mixture", "sn", "template", "ragged"],
                     help="run one workload for --iterations iterations with every kernel launched directly and "
                          "print its per-stage times (the command that profiler captures start from); no JSON line")
     ap.add_argument("--iterations", type=int, default=2, help="iterations of --profile-case")
@@ -283,11 +283,25 @@ def same_draw_accuracy(P, prop, post, N, seed=2024):
             "posterior_cov_max_sigma2": float(np.max(np.abs(c32 - c64) / np.outer(sig, sig)))}
 
 
-def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
+def oracle_iteration_rate(O, prop, lpf, bmin, bmax, n, min_s=3.0, max_reps=4):
+    """samples/s of whole FP64 oracle iterations (draw, log q, log posterior,
+    weights, EM) on the host cores, from the same proposal each time."""
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.iterate_posterior(prop, lpf, n, 11, reps, 1.0, bmin, bmax)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > min_s or reps >= max_reps:
+            return n * reps / el, reps
+
+
+def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3, O=None):
     """The other likelihoods at their configuration sizes: SN Ia (D=6, K=10, 740
     supernovae, Fisher start; N = 10^4 as configured and N = 2^18) and the dense
     template (D=12, K=16, M=2048, N = 2^18, Fisher start); mixed precision vs
-    FP64, same seeds."""
+    FP64, same seeds. With the oracle module O: the FP64 oracle's iterations on
+    the host cores beside them (SN at N = 10^4, the template on a 2^14 sample)."""
     out = {}
     wl = W.sn_workload(K=10, init="fisher")
     w, mu, cov, df = wl["prop"]
@@ -312,6 +326,28 @@ def likelihood_bench(P, W, l2buf, sync, steps=5, warmup=3):
             run.free()
         rec["speedup_mixed_vs_fp64"] = rec["mixed"]["samples_per_s"] / rec["fp64"]["samples_per_s"]
         out[name] = rec
+    if O is not None:
+        ow, omu, oL = sn_prop.arrays()
+        lpr = -np.sum(np.log(wl["bmax"] - wl["bmin"]))
+
+        def sn_lpf(X, flg):
+            l, ok = O.sn_loglike(wl["sn"], X, flg)
+            return l + lpr, ok
+
+        v, reps = oracle_iteration_rate(O, O.Mix(ow, omu, df=sn_prop.df, L=oL), sn_lpf, wl["bmin"], wl["bmax"], 10000)
+        out["sn_N1e4"]["cpu_oracle"] = {"samples_per_s": v, "cores": O.num_threads(),
+                                        "sample": f"{reps} x 10^4 samples (whole iterations)"}
+        At, dt = O.tpl_prepare(tw["A"], tw["C"], tw["dobs"])
+        tpr = -np.sum(np.log(tw["bmax"] - tw["bmin"]))
+
+        def tpl_lpf(X, flg):
+            return O.tpl_loglike(At, dt, X, flg) + tpr, np.ones(len(X), np.int16)
+
+        ow, omu, oL = tpl_prop.arrays()
+        v, reps = oracle_iteration_rate(O, O.Mix(ow, omu, df=tpl_prop.df, L=oL), tpl_lpf, tw["bmin"], tw["bmax"],
+                                        1 << 14)
+        out["template_N2e18"]["cpu_oracle"] = {"samples_per_s": v, "cores": O.num_threads(),
+                                               "sample": f"{reps} x 2^14 samples (whole iterations)"}
     return out
 
 
@@ -398,8 +434,9 @@ def build_spec(P, W, spec, cache, beta0=1.0):
     return prop, post, None
 
 
-def _iterate_each(P, runs, betas, reps):
-    """Seconds per pass of one iteration of every run, one run at a time."""
+def _iterate_each(P, runs, betas, reps, sizes):
+    """(seconds per pass of one iteration of every run, one run at a time;
+    samples per pass of the iterations that succeeded)."""
     import torch
     for r, b in zip(runs, betas):  # warm-up
         try:
@@ -407,15 +444,17 @@ def _iterate_each(P, runs, betas, reps):
         except P.PmcgError:
             pass
     torch.cuda.synchronize()
+    ok = 0
     t0 = time.perf_counter()
     for _ in range(reps):
-        for r, b in zip(runs, betas):
+        for r, b, n in zip(runs, betas, sizes):
             try:
                 r.iterate(b)
+                ok += n
             except P.PmcgError:
                 pass
     torch.cuda.synchronize()
-    return (time.perf_counter() - t0) / reps
+    return (time.perf_counter() - t0) / reps, ok / reps
 
 
 def batch_bench(P, W, R=256, iters=5):
@@ -441,39 +480,47 @@ def batch_bench(P, W, R=256, iters=5):
     t0 = time.perf_counter()
     batch.autotune()
     tune_s = time.perf_counter() - t0
+    sizes = [s[3] for s in specs]
     batch.iterate(betas)  # warm-up
-    ms = []
-    failed = {}
+    ms, rates = [], []
+    failed, failed_runs = {}, set()
     for _ in range(iters):
         st = batch.iterate(betas)
         ms.append(batch.last_ms())
-        for s, x in zip(specs, st):
+        # samples of the runs whose iteration succeeded (a run whose update buried
+        # every component stops, as the reference's update does, and its later
+        # iterations draw from a dead proposal: counted as failures, no samples)
+        rates.append(sum(n for n, x in zip(sizes, st) if x["status"] == 0) / (ms[-1] / 1e3))
+        for i, (s, x) in enumerate(zip(specs, st)):
             if x["status"] != 0:
                 key = f"{s[0]}:{x['status']}"
                 failed[key] = failed.get(key, 0) + 1
+                failed_runs.add(i)
     med = float(np.median(ms))
     cfg = batch.config()
     batch.free()
     del runs_b
     runs_s = make_runs(P.MIXED)
-    seq_s = _iterate_each(P, runs_s, betas, 2)
+    seq_s, seq_ok = _iterate_each(P, runs_s, betas, 2, sizes)
     for r in runs_s:
         r.free()
     runs_64 = make_runs(P.FP64)
-    fp64_s = _iterate_each(P, runs_64, betas, 1)
+    fp64_s, fp64_ok = _iterate_each(P, runs_64, betas, 1, sizes)
     for r in runs_64:
         r.free()
-    value = total / (med / 1e3)
+    value = float(np.median(rates))
     return {"workload": f"{R} runs, half SN (D~U{{6..20}}: 6 SN parameters + Gaussian nuisance in a flat box, "
                         f"start from the tempered Fisher matrix, dead components revived), half GMM "
                         f"(D~U{{2..20}}), K~U{{1..20}}, N~logU(1e3,1e5), beta from the log tempering schedule "
                         f"(t_min {TEMPER_TMIN}, {TEMPER_LEVELS} levels)",
             "samples_per_iter": total, "value": value, "unit": UNIT, "ms_per_iter": med,
-            "one_run_at_a_time_samples_per_s": total / seq_s, "speedup_vs_one_at_a_time": (seq_s * 1e3) / med,
-            "fp64_one_run_at_a_time_samples_per_s": total / fp64_s,
-            "speedup_mixed_vs_fp64": value / (total / fp64_s),
-            "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed,
-            "failed_note": "kind:status of run iterations that failed (-9005: every component dead)",
+            "one_run_at_a_time_samples_per_s": seq_ok / seq_s, "speedup_vs_one_at_a_time": (seq_s * 1e3) / med,
+            "fp64_one_run_at_a_time_samples_per_s": fp64_ok / fp64_s,
+            "speedup_mixed_vs_fp64": value / (fp64_ok / fp64_s),
+            "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed, "failed_runs": len(failed_runs),
+            "failed_note": "kind:status of timed run iterations that failed (-9005: the update buried every "
+                           "component; -9011: no sample with a weight, the later iterations of such a run); "
+                           "value counts the samples of the runs whose iteration succeeded",
             "timing": "CUDA events around each graph launch (library stream), median of iterations; the one-at-a-time "
                       "legs by host clock around a synchronised pass over all runs"}
 
@@ -633,6 +680,8 @@ def profile_case(args):
     P.load()
     if args.tensor_cores is not None:
         P.set_tensor_cores(args.tensor_cores)
+    if args.profile_case == "ragged":
+        return profile_ragged(P, W)
     N = args.nsamples
     box = None
     if args.profile_case == "mixture":
@@ -662,6 +711,38 @@ def profile_case(args):
     names = ["draw", "logq", "logpost", "weights", "em"]
     print(f"{args.profile_case} N={N}: ln Z = {st['ln_evidence']:.6f}; ms per iteration "
           + ", ".join(f"{k} {v / n:.4f}" for k, v in zip(names, ms)), flush=True)
+    return 0
+
+
+def profile_ragged(P, W, R=256):
+    """The batched workload's runs one at a time (mixed precision), every kernel
+    launched directly with per-stage CUDA events: the stage times summed over the
+    runs, by run kind, for one iteration after an untimed one."""
+    specs = ragged_specs(R)
+    cache = {}
+    names = ["draw", "logq", "logpost", "weights", "em"]
+    tot = {}
+    for s in specs:
+        pp, po, bx = build_spec(P, W, s, cache, beta0=s[5])
+        run = P.Run(pp, po, s[3], precision=P.MIXED, seed=s[4], box=bx)
+        if bx is not None:
+            run.set_dead_comp(P.DEAD_REVIVE, 0.1)
+        try:
+            run.iterate(s[5])
+            run.set_timing(True, stages=True)
+            run.iterate(s[5])
+            ms, n = run.stage_ms()
+        except P.PmcgError:
+            run.free()
+            continue
+        run.free()
+        t = tot.setdefault(s[0], [0.0] * 5 + [0])
+        for i in range(5):
+            t[i] += ms[i] / n
+        t[5] += s[3]
+    for kind, t in tot.items():
+        print(f"ragged {kind}: {t[5]} samples; ms summed over runs " +
+              ", ".join(f"{k} {v:.3f}" for k, v in zip(names, t[:5])), flush=True)
     return 0
 
 
@@ -814,6 +895,7 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
         "roofline": roof,
         "clocks": clocks,
     }
+    O = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
@@ -825,7 +907,7 @@ def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches,
     if not args.no_likelihoods:
         import torch
         l2 = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")
-        line["likelihoods"] = likelihood_bench(P, W, l2, torch.cuda.synchronize)
+        line["likelihoods"] = likelihood_bench(P, W, l2, torch.cuda.synchronize, O=O)
         del l2
     if not args.no_batch:
         line["batch"] = batch_bench(P, W)

@@ -1128,16 +1128,27 @@ __device__ __forceinline__ void body_em_factor(size_t N, const double *__restric
 // small-D tiles carry more rows); the list buffer holds a tile plus one pass
 // of listing (at most 256 entries).
 __host__ __device__ inline int em_tile_rows(int Dp) { return Dp <= 8 ? 4 * kTile32 : (Dp <= 16 ? 2 * kTile32 : kTile32); }
-__host__ __device__ inline int em_list_buf(int Dp) { return em_tile_rows(Dp) + 256; }
+__host__ __device__ inline int em_list_buf(int Dp) { return 2 * em_tile_rows(Dp) + 256; }
+// Row stride of the augmented whitened rows (Dp + 4 columns): a multiple of 4
+// floats (float4 rows) whose quotient by 4 is odd, so the 16-byte stores of 8
+// consecutive rows fall in 8 different 4-bank groups (conflict-free).
+__host__ __device__ inline int em_row_stride(int Dp) { return (((Dp + 4) / 4) & 1) ? Dp + 4 : Dp + 8; }
+// Row stride of the gathered sample rows (Dp columns), by the same rule.
+__host__ __device__ inline int em_x_stride(int Dp) { return ((Dp / 4) & 1) ? Dp : Dp + 4; }
 // A pair whose single-precision weight vt = exp(aw + lt) / itau underflows
 // (aw + lt below log FLT_MIN = -87.3) adds exactly nothing in FP32 and less
 // than 1e-38 relative in any precision: such pairs are skipped.
 constexpr float kEmLogMin = -87.0f;
 
+// Whitening schedule of one warp: a count, then up to 16 (slice, row block) tasks.
+constexpr int kEmSchedStride = 17;
+
 __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t *tile_bytes, size_t *red_bytes) {
   const int Dp = ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, G = threads / NB;
   const int T = em_tile_rows(Dp);
-  *tile_bytes = (size_t)(Dp * Dp + Dp + T * Da + T * (Dp + 1) + 3 * em_list_buf(Dp) + 40) * sizeof(float);
+  *tile_bytes = (size_t)(Dp * Dp + Dp + T * em_row_stride(Dp) + 2 * T * em_x_stride(Dp) + 3 * em_list_buf(Dp) + 40 +
+                         (threads / 32) * kEmSchedStride) *
+                sizeof(float);
   *red_bytes = (size_t)G * NB * 16 * sizeof(float2);
 }
 
@@ -1147,10 +1158,12 @@ __host__ __device__ inline void em32_layout(int D, int ldx, int threads, size_t 
 //
 // The chunk is scanned 256 samples at a time; the pairs whose weight does not
 // underflow (aw + lt > kEmLogMin) are compacted, in sample order (warp ballots
-// and a block prefix), into a staging list. Every full tile of 64 listed
-// samples is then gathered (x rows, stride ldx+1), whitened with L^-1 staged
-// transposed (float4 broadcasts; warps paired over i-blocks so their triangular
-// lengths balance), and accumulated: the augmented rows [a, 1, 1/tau, 0, 0]
+// and a block prefix), into a staging list. Every full tile of T listed
+// samples is then gathered (x rows in 16-byte copies, cp.async into one of two
+// buffers, the next tile's rows while this tile is processed), whitened with
+// L^-1 staged transposed (float4 broadcasts; the (slice, row block) tasks
+// spread over the warps longest first; rows stored as float4 at a stride that
+// keeps 8 consecutive rows in distinct banks), and accumulated: the augmented rows [a, 1, 1/tau, 0, 0]
 // with weight vt give in the lower triangle of sum vt a a^T: S2 (whitened), S1
 // (row Dp), St (Dp,Dp) and S0 (Dp+1,Dp). Each thread owns one 4x4 block for one
 // sample group; FP32 sums are flushed into float-float pairs every kFlushTiles tiles. The
@@ -1165,18 +1178,20 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   const int D = m.D, E = em_E(D);
   if (m.w[k] <= 0.0) return;
   const int Dp = m.ldx, Da = Dp + 4, nb = Da / 4, NB = nb * (nb + 1) / 2, nib = Dp / 4;
-  const int ldt = Dp + 1;
+  const int ldt = em_x_stride(Dp);
   const int G = blockDim.x / NB;
   float *sWT = reinterpret_cast<float *>(smem);   // [Dp][Dp]  (L^-1)^T
   float *sb = sWT + Dp * Dp;                      // [Dp]      L^-1 mu
   const int T = em_tile_rows(Dp), LB = em_list_buf(Dp);
   const int flush_tiles = kFlushTiles * kTile32 / T;  // the same rows per FP32 partial for every T
-  float *sa = sb + Dp;                            // [T][Da]
-  float *sx = sa + T * Da;                        // [T][ldt]
-  float *lvt = sx + T * ldt;                      // [LB] listed vt
+  const int lda = em_row_stride(Dp);
+  float *sa = sb + Dp;                            // [T][lda] augmented whitened rows
+  float *sx = sa + T * lda;                       // [2][T][ldt] gathered rows, two buffers
+  float *lvt = sx + 2 * T * ldt;                  // [LB] listed vt
   float *ltau = lvt + LB;                         // [LB] listed 1/tau
   int *lidx = reinterpret_cast<int *>(ltau + LB);  // [LB] listed sample offsets
   int *wcnt = lidx + LB;                          // [32] per-warp counts
+  int *sched = wcnt + 32;                         // [nwarp][kEmSchedStride] whitening tasks
   const size_t chunk = (N + S - 1) / S;
   const size_t n0 = (size_t)s * chunk, n1 = (n0 + chunk < N) ? n0 + chunk : N;
   const float nu = (float)m.df, rnd = 1.0f / ((float)m.df + (float)D);
@@ -1186,6 +1201,24 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
     sWT[j * Dp + i] = (i < D) ? m.W32[(size_t)k * D * Dp + (size_t)i * Dp + j] : 0.f;
   }
   for (int i = tid; i < Dp; i += blockDim.x) sb[i] = (i < D) ? m.b32[(size_t)k * D + i] : 0.f;
+  // The whitening tasks (32-row slice, 4-row block ib; cost ib + 1) of a tile,
+  // longest first, each to the least-loaded warp: every warp's share is within
+  // one task of the mean (which warp computes an output does not change it).
+  if (tid == 0) {
+    int *load = wcnt;   // free until the listing
+    for (int w = 0; w < nwarp; w++) { load[w] = 0; sched[w * kEmSchedStride] = 0; }
+    for (int ib = nib - 1; ib >= 0; ib--) {
+      for (int sl = 0; sl < T / 32; sl++) {
+        int best = 0;
+        for (int w = 1; w < nwarp; w++)
+          if (load[w] < load[best]) best = w;
+        int *sw = sched + best * kEmSchedStride;
+        if (sw[0] < kEmSchedStride - 1) sw[1 + sw[0]++] = (sl << 4) | ib;
+        load[best] += ib + 1;
+      }
+    }
+  }
+  __syncthreads();
   const int blk = tid % NB, grp = tid / NB;
   const bool active = grp < G;
   int bi = 0;
@@ -1199,44 +1232,59 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   for (int e = 0; e < 16; e++) { acc[e] = 0.f; chi[e] = 0.f; clo[e] = 0.f; }
   int tiles = 0;
 
-  // Accumulate listed entries [0, nt) (nt <= T).
-  auto process = [&](int nt) {
-    for (int r = tid; r < T; r += blockDim.x) {
-      float *row = sa + r * Da;
-      row[Dp] = 1.f;
-      row[Dp + 1] = (r < nt) ? ltau[r] : 1.f;
-      row[Dp + 2] = 0.f;
-      row[Dp + 3] = 0.f;
-    }
-    for (int e = tid; e < T * Dp; e += blockDim.x) {
-      const int r = e / Dp, i = e - r * Dp;
-      sx[r * ldt + i] = (r < nt) ? X[(n0 + (size_t)lidx[r]) * Dp + i] : 0.f;
-    }
-    __syncthreads();
-    for (int u = warp; u < (T / 32) * nib; u += nwarp) {
-      // 32-row slices; alternate slices run the row blocks in reverse order so
-      // consecutive warps pair a long triangle row with a short one
-      const int pair = u % nib, half = u / nib;
-      const int ib = (half & 1) == 0 ? pair : nib - 1 - pair;
-      const int r = half * 32 + lane;
-      float o0 = -sb[4 * ib], o1 = -sb[4 * ib + 1], o2 = -sb[4 * ib + 2], o3 = -sb[4 * ib + 3];
-      const float *xr = sx + r * ldt;
-      const int jmax = 4 * ib + 4;
-      for (int j = 0; j < jmax; j++) {
-        const float xv = xr[j];
-        const float4 w4 = *reinterpret_cast<const float4 *>(sWT + j * Dp + 4 * ib);
-        o0 = fmaf(w4.x, xv, o0); o1 = fmaf(w4.y, xv, o1); o2 = fmaf(w4.z, xv, o2); o3 = fmaf(w4.w, xv, o3);
+  // Gather the rows of listed entries [at, at + nt) (nt <= T) into dst, 16
+  // bytes per copy (cp.async, one commit group; rows past nt are zeroed).
+  const int cpr = Dp / 4;   // 16-byte chunks per row
+  auto gather = [&](int at, int nt, float *dst) {
+    for (int c = tid; c < T * cpr; c += blockDim.x) {
+      const int r = c / cpr, q = c - r * cpr;
+      float *d = dst + r * ldt + 4 * q;
+      if (r < nt) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(d)),
+                     "l"(X + (n0 + (size_t)lidx[at + r]) * Dp + 4 * q)
+                     : "memory");
+      } else {
+        *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      float *ar = sa + r * Da + 4 * ib;
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  // Accumulate listed entries [at, at + nt) (nt <= T) from their gathered rows
+  // src; `next`: a later gather is in flight (wait for all groups but that one).
+  auto process = [&](int at, int nt, const float *src, bool next) {
+    for (int r = tid; r < T; r += blockDim.x)
+      *reinterpret_cast<float4 *>(sa + r * lda + Dp) = make_float4(1.f, (r < nt) ? ltau[at + r] : 1.f, 0.f, 0.f);
+    if (next) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    const int ntask = sched[warp * kEmSchedStride];
+    for (int u = 0; u < ntask; u++) {
+      const int code = sched[warp * kEmSchedStride + 1 + u];
+      const int ib = code & 15;
+      const int r = (code >> 4) * 32 + lane;
+      float o0 = -sb[4 * ib], o1 = -sb[4 * ib + 1], o2 = -sb[4 * ib + 2], o3 = -sb[4 * ib + 3];
+      const float *xr = src + r * ldt;
+      const int jmax = 4 * ib + 4;
+      for (int j = 0; j < jmax; j += 4) {
+        const float4 x4 = *reinterpret_cast<const float4 *>(xr + j);
+        const float xs[4] = {x4.x, x4.y, x4.z, x4.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+          const float4 w4 = *reinterpret_cast<const float4 *>(sWT + (j + jj) * Dp + 4 * ib);
+          o0 = fmaf(w4.x, xs[jj], o0); o1 = fmaf(w4.y, xs[jj], o1);
+          o2 = fmaf(w4.z, xs[jj], o2); o3 = fmaf(w4.w, xs[jj], o3);
+        }
+      }
       const bool live = r < nt;
-      ar[0] = live ? o0 : 0.f; ar[1] = live ? o1 : 0.f; ar[2] = live ? o2 : 0.f; ar[3] = live ? o3 : 0.f;
+      *reinterpret_cast<float4 *>(sa + r * lda + 4 * ib) =
+          live ? make_float4(o0, o1, o2, o3) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
     if (active) {
       for (int q = grp; q < nt; q += G) {
-        const float w = lvt[q];
-        float4 ai = *reinterpret_cast<const float4 *>(sa + q * Da + 4 * bi);
-        const float4 aj = *reinterpret_cast<const float4 *>(sa + q * Da + 4 * bj);
+        const float w = lvt[at + q];
+        float4 ai = *reinterpret_cast<const float4 *>(sa + q * lda + 4 * bi);
+        const float4 aj = *reinterpret_cast<const float4 *>(sa + q * lda + 4 * bj);
         ai.x *= w; ai.y *= w; ai.z *= w; ai.w *= w;
         acc[0] = fmaf(ai.x, aj.x, acc[0]);   acc[1] = fmaf(ai.x, aj.y, acc[1]);
         acc[2] = fmaf(ai.x, aj.z, acc[2]);   acc[3] = fmaf(ai.x, aj.w, acc[3]);
@@ -1257,14 +1305,25 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
   };
 
   int fill = 0;  // listed entries (identical in every thread)
-  // Process full tiles and move the remainder (fill - T <= 256 entries) to the front.
+  int cur = 0;   // gather buffer of the next tile: sx + cur * T * ldt
+  // Process every full tile where it lies, the next tile's rows gathered while
+  // this one is processed, then move the remainder (fewer than T entries, so
+  // at most one per thread) to the front.
   auto drain = [&]() {
-    while (fill >= T) {
-      process(T);
-      const int rem = fill - T;
+    int at = 0;
+    if (fill >= T) gather(0, T, sx + cur * T * ldt);
+    while (fill - at >= T) {
+      const bool next = fill - at >= 2 * T;
+      if (next) gather(at + T, T, sx + (cur ^ 1) * T * ldt);
+      process(at, T, sx + cur * T * ldt, next);
+      at += T;
+      cur ^= 1;
+    }
+    if (at > 0) {
+      const int rem = fill - at;
       int ri = 0;
       float rv = 0.f, rt = 0.f;
-      if (tid < rem) { ri = lidx[T + tid]; rv = lvt[T + tid]; rt = ltau[T + tid]; }
+      if (tid < rem) { ri = lidx[at + tid]; rv = lvt[at + tid]; rt = ltau[at + tid]; }
       __syncthreads();
       if (tid < rem) { lidx[tid] = ri; lvt[tid] = rv; ltau[tid] = rt; }
       __syncthreads();
@@ -1299,19 +1358,27 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
         tot += cw;
       }
       const int pos = off + incl - c;   // position of this word's first entry in this pass
+      // the warp's entry range in this pass: [wlo, whi)
+      const int wlo = __shfl_sync(0xffffffffu, pos, 0), whi = __shfl_sync(0xffffffffu, pos + c, 31);
+      const unsigned ltmask = (1u << lane) - 1u;
       // emit in rounds that fit the list buffer, processing full tiles in
-      // between: a word's entries are listed by index alone, then the new
-      // entries' weights are read one entry per thread (a dense word would
-      // otherwise wait for its up to 32 entries' loads one after another)
+      // between. Each warp expands its own 32 words, one word per step and one
+      // bit per lane, so the entries of a word land in consecutive list slots
+      // (conflict-free) and a warp whose entries all lie outside the round
+      // skips it; then the new entries' weights are read one entry per thread.
       for (int done = 0; done < tot;) {
         const int take = min(LB - fill, tot - done);
-        uint32_t b = bits;
-        int p = pos;
-        while (b) {
-          const int j = __ffs(b) - 1;
-          b &= b - 1u;
-          if (p >= done && p < done + take) lidx[fill + p - done] = (int)(wi * 32 + j - n0);
-          p++;
+        if (whi > done && wlo < done + take) {
+          for (int j = 0; j < 32; j++) {
+            const uint32_t bj = __shfl_sync(0xffffffffu, bits, j);
+            const int pj = __shfl_sync(0xffffffffu, pos, j);
+            if (pj + __popc(bj) <= done || pj >= done + take) continue;   // warp-uniform
+            if ((bj >> lane) & 1u) {
+              const int p = pj + __popc(bj & ltmask);
+              if (p >= done && p < done + take)
+                lidx[fill + p - done] = (int)((wb + (size_t)(warp * 32 + j)) * 32 + lane - n0);
+            }
+          }
         }
         __syncthreads();
         for (int q = fill + tid; q < fill + take; q += blockDim.x) {
@@ -1319,7 +1386,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
           const float e = aw[n] + lt[(size_t)k * N + n];
           const float v = expf(e);
           const float it = (m.df > 0) ? (nu + Qv[(size_t)k * N + n]) * rnd : 1.f;
-          lvt[q] = v / it;
+          lvt[q] = (m.df > 0) ? v / it : v;
           ltau[q] = it;
         }
         fill += take;
@@ -1340,7 +1407,7 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
         act = true;
         const float v = expf(e);
         if (m.df > 0) it = (nu + Qv[(size_t)k * N + n]) * rnd;
-        vt = v / it;
+        vt = (m.df > 0) ? v / it : v;
       }
     }
     const unsigned bal = __ballot_sync(0xffffffffu, act);
@@ -1362,7 +1429,10 @@ __device__ __forceinline__ void body_em_stats_f32(const DevMixView &m, size_t N,
     __syncthreads();
     drain();
   }
-  if (fill > 0) process(fill);
+  if (fill > 0) {
+    gather(0, fill, sx + cur * T * ldt);
+    process(0, fill, sx + cur * T * ldt, false);
+  }
 #pragma unroll
   for (int e = 0; e < 16; e++) ff_add(chi[e], clo[e], acc[e], 0.f);
   __syncthreads();
