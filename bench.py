@@ -498,6 +498,10 @@ def batch_bench(P, W, R=256, iters=5):
                 failed_runs.add(i)
     med = float(np.median(ms))
     cfg = batch.config()
+    # one more iteration with its stages launched one by one (per-stage times)
+    batch.set_stage_timing(True)
+    batch.iterate(betas)
+    stage_ms = batch.stage_ms()
     batch.free()
     del runs_b
     runs_s = make_runs(P.MIXED)
@@ -518,6 +522,7 @@ def batch_bench(P, W, R=256, iters=5):
             "fp64_one_run_at_a_time_samples_per_s": fp64_ok / fp64_s,
             "speedup_mixed_vs_fp64": value / (fp64_ok / fp64_s),
             "config": cfg, "autotune_s": tune_s, "failed_run_iterations": failed, "failed_runs": len(failed_runs),
+            "stage_ms": stage_ms,
             "failed_note": "kind:status of timed run iterations that failed (-9005: the update buried every "
                            "component; -9011: no sample with a weight, the later iterations of such a run); "
                            "value counts the samples of the runs whose iteration succeeded",

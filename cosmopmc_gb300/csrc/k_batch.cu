@@ -11,9 +11,15 @@
 // single-run kernels execute, with the same tiling, so each run's results are
 // bit-identical alone and inside any batch.
 //
-// The launch, the upload of the per-iteration parameters (random-stream call,
-// beta) and the download of every run's statistics are captured once in a CUDA
-// graph. The samples per thread of the log-density stages and the resident
+// The SN likelihood is the one body that needs more resident warps than the
+// persistent kernel's two blocks per SM give: the SN runs' log-posterior items
+// run in a grouped kernel of their own (one warp per sample, standalone shape)
+// between the cooperative launch of the draw and log q stages and the one of
+// the remaining stages.
+//
+// The launches, the upload of the per-iteration parameters (random-stream
+// call, beta) and the download of every run's statistics are captured once in
+// a CUDA graph. The samples per thread of the log-density stages and the resident
 // blocks per SM are picked by an autotuner that times the non-mutating stages
 // (draw, log q, log posterior) and caches the choice per batch shape.
 #include <cooperative_groups.h>
@@ -197,6 +203,24 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const BatchDesc *__restri
   }
 }
 
+// The SN log-posterior of every SN run of the batch, one warp per sample, at
+// the standalone SN kernel's shape (128 threads, no register cap: many more
+// resident warps than the persistent kernel's two 256-thread blocks per SM,
+// which this latency-bound body needs). Launched between the cooperative
+// launch of the draw and log q stages and the one of the remaining stages;
+// the same body as the runs alone, so the same values.
+constexpr int kBSnThreads = 128;
+__global__ void __launch_bounds__(kBSnThreads) batch_sn_kernel(const BatchDesc *__restrict__ descs, int R,
+                                                               const uint32_t *__restrict__ pre) {
+  const uint32_t item = blockIdx.x;
+  if (item >= pre[R]) return;
+  const int r = find_run(pre, R, item);
+  const SnDev sn = descs[r].sn;   // by value, as the standalone kernel's parameter
+  const BatchDesc &d = descs[r];
+  const size_t n = (size_t)(item - pre[r]) * (kBSnThreads / 32) + (threadIdx.x >> 5);
+  body_sn<true>(sn, d.N, d.prop.D, nullptr, d.X32, d.prop.ldx, d.logpost, d.flg, n, 1, d.logpr);
+}
+
 // ------------------------------------------------------------------ host side
 static size_t items_of(int stg, const BatchDesc &d, int spt, int threads) {
   const size_t N = d.N;
@@ -206,7 +230,7 @@ static size_t items_of(int stg, const BatchDesc &d, int spt, int threads) {
     case kBLogq: return (N + (size_t)threads * spt - 1) / ((size_t)threads * spt);
     case kBLogpost:
       if (d.ptype == kPluginMix) return (N + (size_t)threads * spt - 1) / ((size_t)threads * spt);
-      if (d.ptype == kPluginSn) return (N + (threads / 32) - 1) / (threads / 32);
+      if (d.ptype == kPluginSn) return 0;   // batch_sn_kernel
       return (N + threads - 1) / threads;
     case kBPrior: return d.has_prior ? (N + threads - 1) / threads : 0;
     case kBWeights:
@@ -250,6 +274,8 @@ struct pmcg_batch {
   BatchDesc *d_desc = nullptr;
   BatchDyn *d_dyn = nullptr, *h_dyn = nullptr;
   uint32_t *d_starts = nullptr;
+  uint32_t *d_snpre = nullptr;   // prefix table of the SN kernel's items over the runs
+  uint32_t sn_items = 0;
   DevStats *d_stats = nullptr, *h_stats = nullptr;
   cudaStream_t s = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -258,6 +284,9 @@ struct pmcg_batch {
   cudaGraphExec_t gexec = nullptr;
   bool graph = false;
   float last_ms = 0.f;
+  bool stage_timing = false, staged_last = false;
+  cudaEvent_t sev[kBStages + 1] = {};
+  float stage_ms[kBStages] = {};
 };
 
 namespace pmcg {
@@ -286,8 +315,18 @@ static cudaError_t launch_batch(pmcg_batch *b, int first, int last) {
                             (const uint32_t *)b->d_starts, first, last, b->d_stats);
 }
 
-static cudaError_t launch_any(pmcg_batch *b, int first, int last) {
+static cudaError_t launch_coop(pmcg_batch *b, int first, int last) {
   return b->spt == 1 ? launch_batch<1>(b, first, last) : launch_batch<2>(b, first, last);
+}
+
+// Stages first..last; the log-posterior stage's SN items run in the SN kernel.
+static cudaError_t launch_any(pmcg_batch *b, int first, int last) {
+  if (b->sn_items == 0 || first > kBLogpost || last < kBLogpost) return launch_coop(b, first, last);
+  cudaError_t e = cudaSuccess;
+  if (first < kBLogpost && (e = launch_coop(b, first, kBLogpost - 1)) != cudaSuccess) return e;
+  batch_sn_kernel<<<b->sn_items, kBSnThreads, 0, b->s>>>(b->d_desc, b->R, b->d_snpre);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return launch_coop(b, kBLogpost, last);
 }
 
 // Prefix tables of all stages for the current samples-per-thread, and the grid.
@@ -308,6 +347,23 @@ static bool batch_configure(pmcg_batch *b, int spt, int bps, error **err) {
   }
   if (!BCK(cudaMemcpy(b->d_starts, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "starts"))
     return false;
+  {
+    std::vector<uint32_t> sp(b->R + 1);
+    uint64_t acc = 0;
+    for (int r = 0; r < b->R; r++) {
+      sp[r] = (uint32_t)acc;
+      const BatchDesc &d = b->hdesc[r];
+      if (d.ptype == kPluginSn) acc += (d.N + kBSnThreads / 32 - 1) / (kBSnThreads / 32);
+    }
+    if (acc > 0x7FFFFFF0ull) {
+      set_error(err, PMCG_EDIM, __LINE__, "batch too large: %llu SN work items", (unsigned long long)acc);
+      return false;
+    }
+    sp[b->R] = (uint32_t)acc;
+    b->sn_items = (uint32_t)acc;
+    if (!BCK(cudaMemcpy(b->d_snpre, sp.data(), sp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "SN items"))
+      return false;
+  }
   size_t smem = 0;
   for (const BatchDesc &d : b->hdesc) smem = std::max(smem, smem_of(d, b->threads));
   b->smem = smem;
@@ -408,6 +464,7 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
             BCK(cudaMalloc(&b->d_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
             BCK(cudaMallocHost(&b->h_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
             BCK(cudaMalloc(&b->d_starts, sizeof(uint32_t) * kBStages * (nruns + 1)), "prefix tables") &&
+            BCK(cudaMalloc(&b->d_snpre, sizeof(uint32_t) * (nruns + 1)), "prefix tables") &&
             BCK(cudaMalloc(&b->d_stats, sizeof(DevStats) * nruns), "stats") &&
             BCK(cudaMallocHost(&b->h_stats, sizeof(DevStats) * nruns), "stats") &&
             BCK(cudaMemcpy(b->d_desc, b->hdesc.data(), sizeof(BatchDesc) * nruns, cudaMemcpyHostToDevice),
@@ -447,7 +504,20 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
     b->h_dyn[r].pad = 0;
   }
   bool ok = BCK(cudaEventRecord(b->e0, b->s), "event");
-  if (ok && b->graph) {
+  b->staged_last = false;
+  if (ok && b->stage_timing) {
+    // the same stages, one launch each, events between them
+    for (int g = 0; ok && g <= kBStages; g++)
+      if (!b->sev[g]) ok = BCK(cudaEventCreate(&b->sev[g]), "event");
+    ok = ok && BCK(cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * b->R, cudaMemcpyHostToDevice, b->s),
+                   "parameters");
+    for (int g = 0; ok && g < kBStages; g++)
+      ok = BCK(cudaEventRecord(b->sev[g], b->s), "event") && BCK(launch_any(b, g, g), "batch stage");
+    ok = ok && BCK(cudaEventRecord(b->sev[kBStages], b->s), "event") &&
+         BCK(cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(DevStats) * b->R, cudaMemcpyDeviceToHost, b->s),
+             "stats");
+    b->staged_last = ok;
+  } else if (ok && b->graph) {
     ok = BCK(cudaGraphLaunch(b->gexec, b->s), "batch graph");
   } else if (ok) {
     ok = BCK(cudaMemcpyAsync(b->d_dyn, b->h_dyn, sizeof(BatchDyn) * b->R, cudaMemcpyHostToDevice, b->s),
@@ -458,6 +528,8 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
   ok = ok && BCK(cudaEventRecord(b->e1, b->s), "event") && BCK(cudaStreamSynchronize(b->s), "batch iteration");
   if (!ok) return;
   cudaEventElapsedTime(&b->last_ms, b->e0, b->e1);
+  if (b->staged_last)
+    for (int g = 0; g < kBStages; g++) cudaEventElapsedTime(&b->stage_ms[g], b->sev[g], b->sev[g + 1]);
   for (int r = 0; r < b->R; r++) {
     pmcg_run *run = b->runs[r];
     *run->w.hstats = b->h_stats[r];
@@ -527,6 +599,17 @@ extern "C" void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, 
 
 extern "C" double pmcg_batch_last_ms(const pmcg_batch *b) { return b->last_ms; }
 
+extern "C" void pmcg_batch_set_stage_timing(pmcg_batch *b, int on) {
+  if (b) b->stage_timing = on != 0;
+}
+
+extern "C" int pmcg_batch_stage_ms(const pmcg_batch *b, double *ms) {
+  static_assert(kBStages == PMCG_BATCH_STAGES, "stage count");
+  if (!b || !ms || !b->staged_last) return -1;
+  for (int g = 0; g < kBStages; g++) ms[g] = b->stage_ms[g];
+  return 0;
+}
+
 extern "C" void pmcg_batch_free(pmcg_batch **pb) {
   if (!pb || !*pb) return;
   pmcg_batch *b = *pb;
@@ -535,10 +618,13 @@ extern "C" void pmcg_batch_free(pmcg_batch **pb) {
   if (b->d_dyn) cudaFree(b->d_dyn);
   if (b->h_dyn) cudaFreeHost(b->h_dyn);
   if (b->d_starts) cudaFree(b->d_starts);
+  if (b->d_snpre) cudaFree(b->d_snpre);
   if (b->d_stats) cudaFree(b->d_stats);
   if (b->h_stats) cudaFreeHost(b->h_stats);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
+  for (cudaEvent_t e : b->sev)
+    if (e) cudaEventDestroy(e);
   if (b->s) cudaStreamDestroy(b->s);
   delete b;
   *pb = nullptr;

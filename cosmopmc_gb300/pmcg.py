@@ -220,6 +220,8 @@ SIGNATURES = [
     ("pmcg_batch_config", None, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)]),
     ("pmcg_batch_last_ms", C.c_double, [C.c_void_p]),
+    ("pmcg_batch_set_stage_timing", None, [C.c_void_p, C.c_int]),
+    ("pmcg_batch_stage_ms", C.c_int, [C.c_void_p, _dp]),
     ("pmcg_batch_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_server_create", C.c_void_p, [C.POINTER(ServerOpts), PErr]),
     ("pmcg_server_submit", C.c_int64, [C.c_void_p, C.POINTER(MixMvdensS), C.c_void_p, C.POINTER(ParaboxS),
@@ -705,6 +707,19 @@ class Batch:
 
     def last_ms(self):
         return load().pmcg_batch_last_ms(self.p)
+
+    BATCH_STAGES = ("draw", "logq", "logpost", "prior", "weight_tiles", "weight_merge", "em_factor", "em_stats",
+                    "em_finalise", "prep_comp", "renorm", "prep_consts")
+
+    def set_stage_timing(self, on):
+        load().pmcg_batch_set_stage_timing(self.p, 1 if on else 0)
+
+    def stage_ms(self):
+        """Per-stage ms of the last iteration (stage timing on), else None."""
+        ms = np.zeros(len(self.BATCH_STAGES))
+        if load().pmcg_batch_stage_ms(self.p, _dptr(ms)) != 0:
+            return None
+        return dict(zip(self.BATCH_STAGES, ms.tolist()))
 
     def free(self):
         if self.p:

@@ -576,6 +576,16 @@ void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *sta
 void pmcg_batch_autotune(pmcg_batch *b, error **err);
 void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, int *blocks_per_sm, int *grid, int *graph);
 double pmcg_batch_last_ms(const pmcg_batch *b);
+/* Stage timing (profiling): while on, each iteration launches its stages one
+ * by one (same stages, same results) with CUDA events between them;
+ * pmcg_batch_stage_ms fills ms[PMCG_BATCH_STAGES] with the last iteration's
+ * per-stage times (draw, log q, log posterior, subset prior, weight tiles,
+ * weight merge, EM weight factor, EM statistics, EM finalise, mixture
+ * preparation, renormalise, constants) and returns 0, or -1 when the last
+ * iteration was not timed by stage. */
+#define PMCG_BATCH_STAGES 12
+void pmcg_batch_set_stage_timing(pmcg_batch *b, int on);
+int pmcg_batch_stage_ms(const pmcg_batch *b, double *ms);
 void pmcg_batch_free(pmcg_batch **b);
 
 /* ------------------------------------------------------------------ *

@@ -115,3 +115,34 @@ def test_batch_autotune_keeps_results(pmcg):
     for it in range(2):
         assert a.iterate() == b.iterate()
     assert b.last_ms() > 0.0
+
+
+def test_batch_stage_timing_keeps_results(pmcg):
+    """The profiling mode launches the stages one by one: same statistics and
+    proposals as the single launch, and a per-stage time for every stage."""
+    P = pmcg
+    keep, runs_a, runs_b = [], [], []
+    for kind, D, K, N, seed in SPECS[:6]:
+        prop, post, box = make_run(P, kind, D, K, N, seed)
+        keep.append((prop, post, box))
+        runs_a.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+        runs_b.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+    a = P.Batch(runs_a)
+    b = P.Batch(runs_b)
+    assert b.stage_ms() is None
+    b.set_stage_timing(True)
+    for it in range(2):
+        assert a.iterate() == b.iterate(), it
+        sm = b.stage_ms()
+        assert sm is not None and set(sm) == set(P.Batch.BATCH_STAGES)
+        assert all(v >= 0.0 for v in sm.values()) and sum(sm.values()) <= b.last_ms() + 1e-3
+    for ra, rb in zip(runs_a, runs_b):
+        wa, ma, La = ra.proposal().arrays()
+        wb, mb, Lb = rb.proposal().arrays()
+        assert np.array_equal(wa, wb) and np.array_equal(ma, mb) and np.array_equal(La, Lb)
+    b.set_stage_timing(False)
+    a.iterate()
+    b.iterate()
+    assert b.stage_ms() is None
+    a.free()
+    b.free()
