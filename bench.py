@@ -842,8 +842,33 @@ def main():
     e2e = {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms_max, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h,
            "path": "simulate_mix_mvdens + generic_get_importance_weight + normalize + update_prop_rb + "
-                   "perplexity_and_ess + evidence, pinned pmc_simu host arrays"}
+                   "perplexity_and_ess + evidence, pinned pmc_simu host arrays",
+           "link": link_rates(N * D * 8)}
+    e2e["link"]["d2h_floor_ms"] = d2h / (e2e["link"]["d2h_gbs"] * 1e6)
     return finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches, stage_ms, nt, clocks, W)
+
+
+def link_rates(nbytes, reps=5):
+    """The host link on its own: one device -> pinned-host copy (and back) of the
+    FP64 sample's size, cudaMemcpyAsync through torch, CUDA events, best of reps."""
+    import torch
+    dev = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+    host = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"bytes": nbytes}
+    for tag, dst, src in (("d2h_gbs", host, dev), ("h2d_gbs", dev, host)):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[tag] = nbytes / (best * 1e6)
+    del dev, host
+    return out
 
 
 def finish(args, rank, world, value, step_ms_max, N, stats, fp64, e2e, launches, stage_ms, nt, clocks, W):

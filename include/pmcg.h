@@ -568,7 +568,12 @@ int pmcg_run_last_launches(const pmcg_run *r);
 typedef struct pmcg_batch pmcg_batch;
 pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err);
 /* betas [nruns] (NULL: all 1); stats [nruns] (NULL allowed). A run whose
- * iteration fails reports stats[r].status != 0 and keeps its proposal. */
+ * iteration fails reports stats[r].status != 0 without disturbing the others.
+ * A failure before the update (no sample in the box: PMCG_ENOWEIGHT) keeps the
+ * run's proposal; an update that buries every component (PMCG_ENEGWEIGHT, the
+ * reference's pmc_negWeight) leaves the buried proposal, as when the run is
+ * iterated alone: give the run a new proposal (pmcg_run_set_proposal) before
+ * iterating it again, or its later iterations report PMCG_ENOWEIGHT. */
 void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *stats, error **err);
 /* Time the non-mutating stages under each candidate (samples per thread of
  * the log-density stages, resident blocks per SM), keep the fastest and

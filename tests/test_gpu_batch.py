@@ -53,6 +53,8 @@ def make_run(P, kind, D, K, N, seed):
         post = P.Posterior(D, bmin, bmax).add_snia(wl["sn"])
         post.add_prior(np.zeros(nx), 0.0625 * np.eye(nx), indprior=np.r_[np.zeros(6, int), np.ones(nx, int)])
         return prop, post, P.Parabox(bmin, bmax)
+    if kind == "buried":  # 15 draws of one component: the update buries it (fewer than 20 draws)
+        return make_run(P, "mix", D, K, N, seed)
     if kind == "dead":  # every draw falls outside the box
         prop = P.MixMvdens.from_arrays([1.0], [[10.0, 10.0]], cov=[np.eye(2) * 0.01], df=-1).cholesky()
         target = P.MixMvdens.from_arrays([1.0], [[0.0, 0.0]], cov=[np.eye(2)], df=-1).cholesky()
@@ -62,7 +64,8 @@ def make_run(P, kind, D, K, N, seed):
 
 
 SPECS = [("mix", 2, 1, 1000, 1), ("mix", 5, 3, 3001, 2), ("mix", 13, 7, 20000, 3), ("mix", 20, 12, 9000, 5),
-         ("sn", 6, 5, 4000, 740), ("snprior", 9, 4, 3000, 741), ("tpl", 3, 4, 2500, 91), ("dead", 2, 1, 777, 9)]
+         ("sn", 6, 5, 4000, 740), ("snprior", 9, 4, 3000, 741), ("tpl", 3, 4, 2500, 91), ("buried", 2, 1, 15, 11),
+         ("dead", 2, 1, 777, 9)]
 
 
 def test_batch_is_bit_identical_to_runs_alone(pmcg):
@@ -76,12 +79,14 @@ def test_batch_is_bit_identical_to_runs_alone(pmcg):
     batch = P.Batch(batch_runs)
     cfg = batch.config()
     assert cfg["grid"] > 0
-    betas = [1.0, 0.5, 1.0, 0.8, 1.0, 0.7, 1.0, 1.0]
+    betas = [1.0, 0.5, 1.0, 0.8, 1.0, 0.7, 1.0, 1.0, 1.0]
     for it in range(3):
         bst = batch.iterate(betas)
         for r, (spec, run) in enumerate(zip(SPECS, alone_runs)):
             if spec[0] == "dead":
                 assert bst[r]["status"] == -9011
+            if spec[0] == "buried":  # PMCG_ENEGWEIGHT, then nothing left to draw from
+                assert bst[r]["status"] == (-9005 if it == 0 else -9011), (it, bst[r])
             if bst[r]["status"] != 0:  # the run alone fails with the same code
                 with pytest.raises(P.PmcgError) as ei:
                     run.iterate(betas[r])
@@ -93,6 +98,11 @@ def test_batch_is_bit_identical_to_runs_alone(pmcg):
             wb, mb, Lb = batch_runs[r].proposal().arrays()
             wa, ma, La = run.proposal().arrays()
             assert np.array_equal(wb, wa) and np.array_equal(mb, ma) and np.array_equal(Lb, La), (it, spec)
+        # the buried run: the same buried proposal in the batch and alone
+        rb = SPECS.index(next(sp for sp in SPECS if sp[0] == "buried"))
+        wb, mb, Lb = batch_runs[rb].proposal().arrays()
+        wa, ma, La = alone_runs[rb].proposal().arrays()
+        assert np.array_equal(wb, wa) and np.all(wb == 0.0) and np.array_equal(mb, ma), it
     # the failing run kept its proposal
     w, mu, L = batch_runs[-1].proposal().arrays()
     assert np.array_equal(mu, [[10.0, 10.0]])
