@@ -286,6 +286,26 @@ cudaError_t launch_fill_f64(double *p, size_t n, double v, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Samples with a non-zero flag (warp ballots, one integer atomic per warp: exact).
+__global__ void count_flags_kernel(size_t N, const short *__restrict__ flg, int *__restrict__ out) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  int c = 0;
+  for (size_t n0 = (size_t)blockIdx.x * blockDim.x; n0 < N; n0 += stride) {
+    const size_t n = n0 + threadIdx.x;
+    c += __popc(__ballot_sync(0xffffffffu, n < N && flg[n] != 0));
+  }
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+cudaError_t launch_count_flags(size_t N, const short *flg, int *out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int), s);
+  if (e != cudaSuccess || N == 0) return e;
+  size_t grid = (N + 255) / 256;
+  if (grid > 1024) grid = 1024;
+  count_flags_kernel<<<(unsigned)grid, 256, 0, s>>>(N, flg, out);
+  return cudaGetLastError();
+}
+
 // Draw counts per component from uploaded indices (integer atomics: exact).
 __global__ void counts_kernel(size_t N, int K, const int *__restrict__ idx, int *__restrict__ counts) {
   for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (size_t)gridDim.x * blockDim.x) {

@@ -188,13 +188,17 @@ static bool stage_weights(Work &w, double beta, bool with_logq, error **err, con
             "weight kernel");
 }
 
-static bool stage_em(Work &w, error **err) {
+// The EM update of mixture `mix` (read as the old proposal, written with the new
+// one) with the statistics `st` (read: the weight step's; written: the update's).
+static bool stage_em_into(Work &w, DevMix &mix, DevStats *st, error **err) {
   // statistics and the fused update; mixed: + the weight factor with the listing bits
   w.launches += w.prec ? 3 : 2;
-  return CK(launch_em(w.prec, w.prop, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
-                      w.empart, w.S, w.dstats, w.D, w.aw32, w.emmask, w.s),
+  return CK(launch_em(w.prec, mix, w.N, w.X64, w.X32, w.logw, w.logq, w.lt64, w.Q64, w.lt32, w.Q32, w.counts,
+                      w.empart, w.S, st, w.D, w.aw32, w.emmask, w.s),
             "EM kernels");
 }
+
+static bool stage_em(Work &w, error **err) { return stage_em_into(w, w.prop, w.dstats, err); }
 
 // Status of the statistics already copied to w.hstats.
 static bool check_stats(Work &w, error **err) {
@@ -1120,6 +1124,7 @@ struct SimMirror {
   cudaEvent_t ev[kDrawChunks] = {};      // range drawn and converted
   cudaEvent_t drawn = nullptr;           // the draw done and its flags saved (before the look-ahead)
   short *flg0 = nullptr;                 // the draw's flags, copied to the host behind X
+  int *dnok = nullptr, *hnok = nullptr;  // the draw's count of samples in the box (device, pinned host)
   bool x_valid = false;    // device X/flg/indices/counts match the host sample
   bool lt_valid = false;   // logq/lt/Q valid for (X, snapshot proposal)
   bool w_valid = false;    // logw and the device statistics valid
@@ -1131,6 +1136,22 @@ struct SimMirror {
   bool lp_valid = false;
   std::vector<double> snap_w, snap_mu, snap_L;
   double *mom = nullptr;   // scratch of the weighted moments (allocated on first use)
+  // Speculation (single precision, sample copied in ranges): after the
+  // look-ahead, while X still travels to the host, the weight step for the
+  // beta of the last two weight steps (when they agree), the normalisation and
+  // the EM update run ahead, the update into a second proposal (`spec_mix`, with
+  // its own statistics `spec_st`). The calls that follow use these results when
+  // their arguments match, else compute as usual; the same kernels on the same
+  // inputs, so the same values. spec: 0 none, 1 ready after the draw, 2 after
+  // a matching weight step, 3 after the normalisation; -1: started and not
+  // finished (the flags may have changed).
+  DevMix spec_mix;
+  DevStats *spec_st = nullptr;
+  short *flg1 = nullptr;   // the flags as the look-ahead left them (restored on a miss)
+  int spec = 0;
+  bool flg_dirty = false;  // the speculation changed w.flg; flg1 holds the flags before it
+  double spec_beta = 0.0;
+  double beta_last = NAN, beta_prev = NAN;
 };
 
 static void mirror_delete(SimMirror *m) {
@@ -1140,6 +1161,11 @@ static void mirror_delete(SimMirror *m) {
     if (e) cudaEventDestroy(e);
   if (m->drawn) cudaEventDestroy(m->drawn);
   if (m->flg0) cudaFree(m->flg0);
+  if (m->dnok) cudaFree(m->dnok);
+  if (m->hnok) cudaFreeHost(m->hnok);
+  if (m->flg1) cudaFree(m->flg1);
+  if (m->spec_st) cudaFree(m->spec_st);
+  devmix_free(m->spec_mix);
   if (m->cs) cudaStreamDestroy(m->cs);
   work_free(m->w);
   if (m->mom) cudaFree(m->mom);
@@ -1164,7 +1190,8 @@ static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error *
               CK(cudaStreamCreateWithFlags(&m->cs, cudaStreamNonBlocking), "copy stream");
     for (cudaEvent_t &e : m->ev) ok = ok && CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     ok = ok && CK(cudaEventCreateWithFlags(&m->drawn, cudaEventDisableTiming), "event") &&
-         CK(cudaMalloc(&m->flg0, sizeof(short) * psim->nsamples + 16), "flag copy");
+         CK(cudaMalloc(&m->flg0, sizeof(short) * psim->nsamples + 16), "flag copy") &&
+         CK(cudaMalloc(&m->dnok, sizeof(int)), "count") && CK(cudaMallocHost(&m->hnok, sizeof(int)), "count");
     if (!ok) {
       mirror_delete(m);
       m = nullptr;
@@ -1213,6 +1240,7 @@ static bool sync_proposal(SimMirror *m, const mix_mvdens *prop, error **err) {
   std::vector<double> w, mu, L;
   if (!flatten_mix(prop, w, mu, L, err)) return false;
   if (w == m->snap_w && mu == m->snap_mu && L == m->snap_L) return true;
+  m->spec = 0;
   if (!CK(devmix_upload(m->w.prop, w.data(), mu.data(), L.data(), m->w.s), "proposal upload")) return false;
   m->snap_w.swap(w);
   m->snap_mu.swap(mu);
@@ -1224,6 +1252,8 @@ static bool sync_proposal(SimMirror *m, const mix_mvdens *prop, error **err) {
 // Make the device sample match the host one (after a host-side rewrite).
 static bool sync_sample(SimMirror *m, const pmc_simu *psim, error **err) {
   if (m->x_valid) return true;
+  m->spec = 0;
+  m->flg_dirty = false;   // the host flags are uploaded below
   Work &w = m->w;
   bool ok = CK(cudaMemcpyAsync(w.X64, psim->X, 8 * w.N * w.D, cudaMemcpyHostToDevice, w.s), "X upload") &&
             CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload") &&
@@ -1239,8 +1269,12 @@ static bool sync_sample(SimMirror *m, const pmc_simu *psim, error **err) {
 }
 
 // Make the device log-weights and statistics match the host weights.
+static bool restore_flags(SimMirror *m, error **err);
+
 static bool sync_weights(SimMirror *m, const pmc_simu *psim, error **err) {
   if (m->w_valid) return true;
+  m->spec = 0;
+  if (!restore_flags(m, err)) return false;
   Work &w = m->w;
   m->lp_valid = false;  // w.logpost is overwritten below
   bool ok = CK(cudaMemcpyAsync(w.logpost, psim->weights, 8 * w.N, cudaMemcpyHostToDevice, w.s), "weights upload");
@@ -1262,8 +1296,47 @@ extern "C" int pmcg_set_tensor_cores(int on) {
 
 extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {
   SimMirror *m = find_mirror(psim);
-  if (m) m->x_valid = m->lt_valid = m->w_valid = m->lp_valid = false;
+  if (m) {
+    m->x_valid = m->lt_valid = m->w_valid = m->lp_valid = false;
+    m->spec = 0;
+  }
 }
+
+namespace pmcg {
+// The speculative weight step, normalisation and EM update (see SimMirror).
+static bool speculate(SimMirror *m, error **err) {
+  Work &w = m->w;
+  if (!m->spec_mix.arena &&
+      (!CK(devmix_alloc(m->spec_mix, w.K, w.D, w.df), "speculative proposal") ||
+       !CK(cudaMalloc(&m->spec_st, sizeof(DevStats)), "speculative statistics") ||
+       !CK(cudaMalloc(&m->flg1, sizeof(short) * w.N + 16), "flag copy"))) {
+    devmix_free(m->spec_mix);
+    return false;
+  }
+  if (!CK(cudaMemcpyAsync(m->flg1, w.flg, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags")) return false;
+  m->flg_dirty = true;  // the flags may change from here on: unless the results are used, they are restored
+  m->spec = -1;
+  m->spec_mix.cst = w.prop.cst;
+  if (!stage_weights(w, m->beta_last, true, err) ||
+      !CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise") ||
+      !CK(cudaMemcpyAsync(m->spec_st, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToDevice, w.s), "statistics") ||
+      !CK(cudaMemcpyAsync(m->spec_mix.arena, w.prop.arena, devmix_bytes(w.K, w.D), cudaMemcpyDeviceToDevice, w.s),
+          "proposal") ||
+      !stage_em_into(w, m->spec_mix, m->spec_st, err))
+    return false;
+  m->spec = 1;
+  m->spec_beta = m->beta_last;
+  return true;
+}
+
+// The flags as the look-ahead left them, when a speculation changed them and
+// its results are not used.
+static bool restore_flags(SimMirror *m, error **err) {
+  if (!m->flg_dirty) return true;
+  m->flg_dirty = false;
+  return CK(cudaMemcpyAsync(m->w.flg, m->flg1, 2 * m->w.N, cudaMemcpyDeviceToDevice, m->w.s), "flags");
+}
+}  // namespace pmcg
 
 extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, void *rng, parabox *pb,
                                       error **err) {
@@ -1310,26 +1383,29 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, void
   // samples by likelihood); indices and flags follow X on the copy stream, so
   // the look-ahead does not queue behind the host copies.
   ok = ok && CK(cudaMemcpyAsync(m->flg0, w.flg, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags") &&
+       CK(launch_count_flags(w.N, m->flg0, m->dnok, w.s), "count") &&
        CK(cudaEventRecord(m->drawn, w.s), "event") && CK(cudaStreamWaitEvent(m->cs, m->drawn, 0), "wait") &&
        CK(cudaMemcpyAsync(psim->indices, w.idx, 4 * w.N, cudaMemcpyDeviceToHost, m->cs), "indices") &&
-       CK(cudaMemcpyAsync(psim->flg, m->flg0, 2 * w.N, cudaMemcpyDeviceToHost, m->cs), "flg");
+       CK(cudaMemcpyAsync(psim->flg, m->flg0, 2 * w.N, cudaMemcpyDeviceToHost, m->cs), "flg") &&
+       CK(cudaMemcpyAsync(m->hnok, m->dnok, sizeof(int), cudaMemcpyDeviceToHost, m->cs), "count");
   // Look-ahead while X travels to the host: the weight step that follows a draw
   // needs log q under this proposal and, most often, the log-posterior of the
   // posterior it used last time; both are pure functions of X, queued after
   // the draw's flags are saved and not waited for here. The weight step keeps
   // what matches its arguments and recomputes the rest.
   bool lt = false, lp = false;
+  m->spec = 0;
   if (ok) {
     error *lerr = nullptr;
     lt = stage_logq(w, &lerr);
     if (lt && m->post && m->post->stamp == m->post_stamp) lp = stage_logpost(w, m->post, &lerr);
+    // the rest of the iteration, for the beta of the last two weight steps
+    if (lt && lp && C > 1 && m->beta_last == m->beta_prev && std::isfinite(m->beta_last)) speculate(m, &lerr);
     if (lerr) purgeError(&lerr);
   }
   const bool copied = CK(cudaStreamSynchronize(m->cs), "sample copy");  // even after a failure
   ok = ok && copied;
-  size_t nok = 0;
-  if (ok)
-    for (size_t n = 0; n < psim->nsamples; n++) nok += (psim->flg[n] != 0);
+  const size_t nok = ok ? (size_t)*m->hnok : 0;
   (*rcalls)++;
   if (!ok) {
     cudaStreamSynchronize(w.s);
@@ -1367,6 +1443,10 @@ extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim,
   if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err)) return 0;
   bool ok = m->lt_valid || stage_logq(w, err);
   const bool lp_hit = m->lp_valid && m->post == p && m->post_stamp == p->stamp;
+  const bool spec_hit = ok && lp_hit && m->spec == 1 && beta == m->spec_beta;
+  if (spec_hit) m->flg_dirty = false;   // the speculation's flags are this weight step's
+  else ok = ok && restore_flags(m, err);
+  m->spec = spec_hit ? 2 : 0;
   if (ok && !lp_hit) {
     // a look-ahead for another posterior flagged samples by its likelihood:
     // the draw's flags come back first
@@ -1374,7 +1454,9 @@ extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim,
     ok = ok && stage_logpost(w, p, err);
   }
   m->lp_valid = false;
-  ok = ok && stage_weights(w, beta, true, err);
+  m->beta_prev = m->beta_last;
+  m->beta_last = beta;
+  if (!spec_hit) ok = ok && stage_weights(w, beta, true, err);
   ok = ok && CK(cudaMemcpyAsync(psim->weights, w.logw, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
        CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg");
   if (!ok) return 0;
@@ -1395,10 +1477,14 @@ extern "C" double normalize_importance_weight(pmc_simu *psim, error **err) {
   if (!m) return 0.0;
   Work &w = m->w;
   if (!m->x_valid) {
+    m->spec = 0;
+    m->flg_dirty = false;
     if (!CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload")) return 0.0;
   }
   if (!sync_weights(m, psim, err)) return 0.0;
-  bool ok = CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise") &&
+  const bool spec_hit = m->spec == 2;  // normalised ahead from the same weights
+  m->spec = spec_hit ? 3 : 0;
+  bool ok = (spec_hit || CK(launch_normalise(w.N, w.logw, w.flg, w.dstats, w.wbar, w.s), "normalise")) &&
             CK(cudaMemcpyAsync(psim->weights, w.wbar, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "weights") &&
             CK(cudaStreamSynchronize(w.s), "normalise");
   if (!ok) return 0.0;
@@ -1424,6 +1510,8 @@ extern "C" void clip_weights(pmc_simu *psim, int nclipw, FILE *out, error **err)
   SimMirror *m = mirror_any(psim, err);
   if (!m) return;
   Work &w = m->w;
+  m->spec = 0;  // the weights change: an update made ahead no longer applies
+  if (!m->x_valid) m->flg_dirty = false;
   if (!m->x_valid && !CK(cudaMemcpyAsync(w.flg, psim->flg, 2 * w.N, cudaMemcpyHostToDevice, w.s), "flg upload"))
     return;
   if (!sync_weights(m, psim, err)) return;
@@ -1475,7 +1563,8 @@ extern "C" size_t importance_sample(pmc_simu *psim, const pmcg_posterior *post, 
   SimMirror *m = mirror_any(psim, err);
   if (!m) return 0;
   Work &w = m->w;
-  bool ok = sync_sample(m, psim, err) && stage_logpost(w, post, err) &&
+  m->spec = 0;
+  bool ok = sync_sample(m, psim, err) && restore_flags(m, err) && stage_logpost(w, post, err) &&
             CK(cudaMemcpyAsync(psim->weights, w.logpost, 8 * w.N, cudaMemcpyDeviceToHost, w.s), "log posterior") &&
             CK(cudaMemcpyAsync(psim->flg, w.flg, 2 * w.N, cudaMemcpyDeviceToHost, w.s), "flg") &&
             CK(cudaStreamSynchronize(w.s), "importance sample");
@@ -1622,9 +1711,21 @@ extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err
   if (!m) return;
   Work &w = m->w;
   if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err) || !sync_weights(m, psim, err)) return;
-  if (!m->lt_valid && !stage_logq(w, err)) return;
-  m->lt_valid = true;
-  if (!stage_em(w, err) || !fetch_stats(w, err)) return;
+  if (m->spec >= 2) {
+    // updated ahead from this sample, these weights and this proposal: the
+    // second proposal becomes the device proposal, with its statistics
+    m->spec = 0;
+    std::swap(w.prop, m->spec_mix);
+    if (!CK(cudaMemcpyAsync(w.dstats, m->spec_st, sizeof(DevStats), cudaMemcpyDeviceToDevice, w.s), "statistics"))
+      return;
+    m->lt_valid = true;
+    if (!fetch_stats(w, err)) return;
+  } else {
+    m->spec = 0;
+    if (!m->lt_valid && !stage_logq(w, err)) return;
+    m->lt_valid = true;
+    if (!stage_em(w, err) || !fetch_stats(w, err)) return;
+  }
   const int K = w.K, D = w.D;
   std::vector<double> wt(K), mu((size_t)K * D), L((size_t)K * D * D);
   bool ok = CK(cudaMemcpyAsync(wt.data(), w.prop.w, 8 * K, cudaMemcpyDeviceToHost, w.s), "proposal") &&

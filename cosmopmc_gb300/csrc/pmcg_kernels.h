@@ -228,6 +228,8 @@ cudaError_t launch_prior(int precision, const PriorDev &p, size_t N, int D, cons
 cudaError_t launch_fill_f64(double *p, size_t n, double v, cudaStream_t s);
 cudaError_t launch_x64_to_x32(size_t N, int D, int ldx, const double *X64, float *X32, cudaStream_t s);
 cudaError_t launch_counts(size_t N, int K, const int *idx, int *counts, cudaStream_t s);
+// *out = number of samples with flg != 0 (zeroes *out first).
+cudaError_t launch_count_flags(size_t N, const short *flg, int *out, cudaStream_t s);
 cudaError_t launch_log_weights(size_t N, double *w, const short *flg, cudaStream_t s);
 
 }  // namespace pmcg

@@ -240,8 +240,10 @@ double evidence(pmc_simu *psim, double *ln_evi, error **err);
 #define PMCG_TEMPERING_LOG    2
 double get_tempering_beta(int tempering, int iter, double t_min, int nmax, error **err);
 
-/* Tell the library that the caller rewrote psim->X on the host (the
- * device copy is re-uploaded before the next weight step). */
+/* Tell the library that the caller rewrote psim->X, flg or weights on the
+ * host: the device copy is re-uploaded before the next call, and whatever was
+ * evaluated ahead from it (log q, the log posterior, the weight step,
+ * normalisation and EM update of a repeated beta) is recomputed. */
 void pmcg_simu_host_modified(pmc_simu *psim);
 
 /* Importance sampling of an existing sample with another posterior

@@ -498,3 +498,54 @@ def test_tempered_weights(pmcg, oracle):
     X = r["X"]
     lw = 0.25 * (oracle.mix_logpdf(oracle_mix(oracle, target), X) - np.log(400.0)) - oracle.mix_logpdf(om, X)
     np.testing.assert_allclose(r["logw"], lw, rtol=1e-12, atol=1e-10)
+
+
+def test_dropin_speculation_equals_fresh_sequence(pmcg):
+    """Single precision, sample copied in ranges: after the draw the weight step
+    (for the beta of the last two weight steps), the normalisation and the EM
+    update run ahead while X travels to the host, and the calls that follow use
+    them when their arguments match. Every iteration of the pmclib sequence must
+    equal the same iteration on a fresh sample object (no history, nothing run
+    ahead) bit for bit: hits (repeated beta), beta misses, a posterior change and
+    a clip between the normalisation and the update."""
+    P = pmcg
+    wl = W.mixture_workload(D=8, K=4, Kt=2, nu=5, seed=17, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    target = make_mix(P, wt, mut, covt, -1)
+    post_a = P.Posterior(8).add_mix(target)
+    post_b = P.Posterior(8).add_mix(make_mix(P, wt[:1] / wt[0], mut[:1], covt[:1] * 2.0, -1))
+    P.set_dropin_precision(P.MIXED)
+    N = 40000   # eight draw ranges of at least 4096 samples
+    m = make_mix(P, w, mu, cov, df)
+    ps = P.PmcSimu(N, 8)
+    rng = P.Rng(23)
+    steps = [(1.0, post_a, 0), (1.0, post_a, 0), (1.0, post_a, 0), (1.0, post_a, 0), (0.5, post_a, 0),
+             (0.5, post_a, 0), (0.5, post_a, 0), (1.0, post_a, 0), (1.0, post_a, 0), (1.0, post_b, 0),
+             (1.0, post_b, 0), (1.0, post_b, 25), (1.0, post_b, 0)]
+    try:
+        for it, (beta, post, nclip) in enumerate(steps):
+            wa, mua, La = m.arrays()
+            mf = P.MixMvdens.from_arrays(wa, mua, L=La, df=m.df)
+            out = []
+            for mm, sim, r in ((m, ps, rng), (mf, P.PmcSimu(N, 8), P.Rng(23))):
+                r.p.contents.calls = it
+                P.simulate_mix_mvdens(sim, mm, r, None)
+                nok = P.importance_weights(sim, mm, post, beta)
+                lw = sim.weights.copy()
+                ls = P.normalize_importance_weight(sim)
+                if nclip:
+                    P.clip_weights(sim, nclip)
+                wb = sim.weights.copy()
+                P.update_prop_rb(mm, sim)
+                out.append((nok, lw, ls, wb, sim.flg.copy(), sim.X.copy(), P.perplexity_and_ess(sim),
+                            P.evidence(sim), mm.arrays()))
+            a, b = out
+            assert a[0] == b[0] and a[2] == b[2], it
+            for i in (1, 3, 4, 5):
+                np.testing.assert_array_equal(a[i], b[i], err_msg=f"iteration {it} field {i}")
+            assert a[6] == b[6] and a[7] == b[7], it
+            for x, y in zip(a[8], b[8]):
+                np.testing.assert_array_equal(x, y, err_msg=f"iteration {it} proposal")
+    finally:
+        P.set_dropin_precision(P.FP64)
