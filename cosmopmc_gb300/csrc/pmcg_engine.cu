@@ -1235,8 +1235,27 @@ void forget_posterior(const pmcg_posterior *p) {
     }
 }
 
+// The host proposal equals the mirror's snapshot (Cholesky-form components
+// compared in place, without flattening): bitwise on the means and the lower
+// triangles, by value on the weights.
+static bool same_as_snapshot(const SimMirror *m, const mix_mvdens *p) {
+  const int K = p->ncomp, D = p->ndim;
+  if ((int)m->snap_w.size() != K || m->snap_mu.size() != (size_t)K * D || m->snap_L.size() != (size_t)K * D * D)
+    return false;
+  for (int k = 0; k < K; k++) {
+    const mvdens *c = p->comp[k];
+    if (c->ndim != D || !c->chol || p->wght[k] != m->snap_w[k]) return false;
+    if (memcmp(c->mean, &m->snap_mu[(size_t)k * D], sizeof(double) * D) != 0) return false;
+    const double *Ls = &m->snap_L[(size_t)k * D * D];
+    for (int i = 0; i < D; i++)
+      if (memcmp(c->std + (size_t)i * D, Ls + (size_t)i * D, sizeof(double) * (i + 1)) != 0) return false;
+  }
+  return true;
+}
+
 // Upload the proposal when it differs from the mirror's snapshot.
 static bool sync_proposal(SimMirror *m, const mix_mvdens *prop, error **err) {
+  if (same_as_snapshot(m, prop)) return true;
   std::vector<double> w, mu, L;
   if (!flatten_mix(prop, w, mu, L, err)) return false;
   if (w == m->snap_w && mu == m->snap_mu && L == m->snap_L) return true;
@@ -1711,6 +1730,10 @@ extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err
   if (!m) return;
   Work &w = m->w;
   if (!sync_sample(m, psim, err) || !sync_proposal(m, proposal, err) || !sync_weights(m, psim, err)) return;
+  // From here the device proposal is the updated one; until it is copied back,
+  // the host proposal no longer matches the snapshot (a failed update leaves
+  // the host proposal as it was, which the next call then uploads).
+  m->snap_w.clear();
   if (m->spec >= 2) {
     // updated ahead from this sample, these weights and this proposal: the
     // second proposal becomes the device proposal, with its statistics
@@ -1745,8 +1768,12 @@ extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err
       c->det = 2.0 * ld;
     }
   }
-  // The device proposal now equals the host one.
-  flatten_mix(proposal, m->snap_w, m->snap_mu, m->snap_L, err);
+  // The device proposal now equals the host one: the downloaded arrays are the
+  // snapshot (the update writes zeros above the diagonal; a buried component
+  // keeps its parameters on the device and on the host).
+  m->snap_w.swap(wt);
+  m->snap_mu.swap(mu);
+  m->snap_L.swap(L);
   m->lt_valid = false;
 }
 
