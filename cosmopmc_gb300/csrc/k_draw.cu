@@ -13,9 +13,11 @@ __global__ void __launch_bounds__(128) draw_kernel(DevMixView m, size_t N, uint3
                                                    const double *__restrict__ pre_z,
                                                    const double *__restrict__ pre_chi2, double *__restrict__ X64,
                                                    float *__restrict__ X32, int *__restrict__ idx,
-                                                   short *__restrict__ flg, int *__restrict__ counts) {
+                                                   short *__restrict__ flg, int *__restrict__ counts,
+                                                   const uint32_t *__restrict__ callp) {
   extern __shared__ __align__(16) unsigned char s_raw[];
-  body_draw<MAXD, Real>(m, N, key0, key1, call, bmin, bmax, pre_u, pre_z, pre_chi2, X64, X32, idx, flg, counts,
+  const uint32_t c = callp ? *callp : call;
+  body_draw<MAXD, Real>(m, N, key0, key1, c, bmin, bmax, pre_u, pre_z, pre_chi2, X64, X32, idx, flg, counts,
                         (size_t)blockIdx.x * blockDim.x, s_raw);
 }
 
@@ -23,7 +25,7 @@ template <int MAXD, typename Real>
 static cudaError_t draw_dispatch(const DevMixView &m, size_t N, uint64_t seed, uint32_t call, const double *bmin,
                                  const double *bmax, const double *pre_u, const double *pre_z,
                                  const double *pre_chi2, double *X64, float *X32, int *idx, short *flg,
-                                 int *counts, cudaStream_t s) {
+                                 int *counts, cudaStream_t s, const uint32_t *callp) {
   const int bs = 128;
   const int ldo = (sizeof(Real) == 8) ? m.D : m.ldx;
   size_t smem = draw_smem<Real>(m.K, ldo, bs);
@@ -34,21 +36,21 @@ static cudaError_t draw_dispatch(const DevMixView &m, size_t N, uint64_t seed, u
     if (e != cudaSuccess) return e;
   }
   draw_kernel<MAXD, Real><<<grid, bs, smem, s>>>(m, N, (uint32_t)seed, (uint32_t)(seed >> 32), call, bmin, bmax,
-                                                 pre_u, pre_z, pre_chi2, X64, X32, idx, flg, counts);
+                                                 pre_u, pre_z, pre_chi2, X64, X32, idx, flg, counts, callp);
   return cudaGetLastError();
 }
 
 cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t seed, uint32_t call,
                         const double *bmin, const double *bmax, const double *pre_u, const double *pre_z,
                         const double *pre_chi2, double *X64, float *X32, int *idx, short *flg, int *counts,
-                        cudaStream_t s) {
+                        cudaStream_t s, const uint32_t *callp) {
   if (m.D < 1 || m.D > kMaxD || m.K < 1 || m.K > kMaxK) return cudaErrorInvalidValue;
 #define PMCG_DRAW(MD)                                                                                          \
   return precision == 0                                                                                        \
              ? draw_dispatch<MD, double>(m, N, seed, call, bmin, bmax, pre_u, pre_z, pre_chi2, X64, X32, idx,  \
-                                         flg, counts, s)                                                       \
+                                         flg, counts, s, callp)                                                \
              : draw_dispatch<MD, float>(m, N, seed, call, bmin, bmax, pre_u, pre_z, pre_chi2, X64, X32, idx,   \
-                                        flg, counts, s)
+                                        flg, counts, s, callp)
   if (m.D <= 8) { PMCG_DRAW(8); }
   if (m.D <= 16) { PMCG_DRAW(16); }
   if (m.D <= 32) { PMCG_DRAW(32); }

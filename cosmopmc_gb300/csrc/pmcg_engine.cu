@@ -108,10 +108,16 @@ static bool upload_box(Work &w, const double *bmin, const double *bmax, error **
          CK(cudaMemcpyAsync(w.bmax, bmax, sizeof(double) * w.D, cudaMemcpyHostToDevice, w.s), "box");
 }
 
+// Below this many samples the single-precision draw runs in one pass: the
+// component-ordered draw's two extra kernels (pick, bucket) only pay off when
+// there are enough samples per component to share a factor; the values are
+// the same either way.
+constexpr size_t kGroupedDrawMin = (size_t)1 << 15;
+
 static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **err,
                        const uint32_t *callp = nullptr) {
   if (!CK(cudaMemsetAsync(w.counts, 0, sizeof(int) * w.K, w.s), "counts")) return false;
-  if (w.prec == 1) {
+  if (w.prec == 1 && w.N >= kGroupedDrawMin) {
     w.launches += 3;
     return CK(launch_draw_grouped(w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
                                   w.X32, w.idx, w.flg, w.counts, w.perm, w.cursor, w.s, callp),
@@ -119,7 +125,7 @@ static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **
   }
   w.launches += 1;
   return CK(launch_draw(w.prec, w.prop.view(), w.N, seed, call, box ? w.bmin : nullptr, box ? w.bmax : nullptr,
-                        nullptr, nullptr, nullptr, w.X64, w.X32, w.idx, w.flg, w.counts, w.s),
+                        nullptr, nullptr, nullptr, w.X64, w.X32, w.idx, w.flg, w.counts, w.s, callp),
             "draw kernel");
 }
 

@@ -72,10 +72,11 @@ cudaError_t devmix_prepare(DevMix &m, cudaStream_t s);
 inline int round4(int d) { return (d + 3) & ~3; }
 
 // (a) draw. X64 [N x D] (FP64 path) or X32 [N x ldx] (mixed path). pre_* optional.
+// callp (optional): the call counter read from device memory instead of call.
 cudaError_t launch_draw(int precision, const DevMixView &m, size_t N, uint64_t seed, uint32_t call,
                         const double *bmin, const double *bmax, const double *pre_u, const double *pre_z,
                         const double *pre_chi2, double *X64, float *X32, int *idx, short *flg, int *counts,
-                        cudaStream_t s);
+                        cudaStream_t s, const uint32_t *callp = nullptr);
 
 // (a) single-precision draws in component order (three launches; counts must
 // start at zero). perm: N ints, cursor: 2K ints of scratch. Same values as
