@@ -221,6 +221,15 @@ __global__ void __launch_bounds__(kBSnThreads) batch_sn_kernel(const BatchDesc *
   body_sn<true>(sn, d.N, d.prop.D, nullptr, d.X32, d.prop.ldx, d.logpost, d.flg, n, 1, d.logpr);
 }
 
+// Every run's draw counts set to zero (one block per run): the batch's draws add
+// to them and its preparation stage zeroes them after each iteration.
+__global__ void batch_zero_counts_kernel(const BatchDesc *__restrict__ descs, int R) {
+  const int r = blockIdx.x;
+  if (r >= R) return;
+  const BatchDesc &d = descs[r];
+  for (int k = threadIdx.x; k < d.prop.K; k += blockDim.x) d.counts[k] = 0;
+}
+
 // ------------------------------------------------------------------ host side
 static size_t items_of(int stg, const BatchDesc &d, int spt, int threads) {
   const size_t N = d.N;
@@ -283,6 +292,8 @@ struct pmcg_batch {
   size_t smem = 0;
   cudaGraphExec_t gexec = nullptr;
   bool graph = false;
+  int cap = 0;              // runs the device and pinned arrays hold
+  int iters_bound = 0;      // iterations since the runs were bound (the graph is captured at the second)
   float last_ms = 0.f;
   bool stage_timing = false, staged_last = false;
   cudaEvent_t sev[kBStages + 1] = {};
@@ -409,26 +420,41 @@ static void capture_graph(pmcg_batch *b) {
 
 }  // namespace pmcg
 
-extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err) {
+namespace pmcg {
+static void free_arrays(pmcg_batch *b) {
+  if (b->d_desc) cudaFree(b->d_desc);
+  if (b->d_dyn) cudaFree(b->d_dyn);
+  if (b->h_dyn) cudaFreeHost(b->h_dyn);
+  if (b->d_starts) cudaFree(b->d_starts);
+  if (b->d_snpre) cudaFree(b->d_snpre);
+  if (b->d_stats) cudaFree(b->d_stats);
+  if (b->h_stats) cudaFreeHost(b->h_stats);
+  b->d_desc = nullptr; b->d_dyn = nullptr; b->h_dyn = nullptr; b->d_starts = nullptr; b->d_snpre = nullptr;
+  b->d_stats = nullptr; b->h_stats = nullptr;
+  b->cap = 0;
+}
+
+// Bind the runs: descriptors, capacity (kept across binds, grown when short),
+// the runs' streams drained, their draw counts zeroed, the tuned configuration
+// of this shape and the prefix tables. The graph is captured at the second
+// iteration after a bind, so a batch rebound every iteration does not pay for
+// captures it would use once.
+static bool batch_bind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **err) {
   if (nruns < 1 || !runs) {
-    set_error(err, PMCG_EARG, __LINE__, "pmcg_batch_create: no runs");
-    return nullptr;
+    set_error(err, PMCG_EARG, __LINE__, "batch: no runs");
+    return false;
   }
-  pmcg_batch *b = new pmcg_batch();
-  b->R = nruns;
-  b->runs.assign(runs, runs + nruns);
-  b->hdesc.resize(nruns);
+  std::vector<BatchDesc> hd(nruns);
   for (int r = 0; r < nruns; r++) {
     pmcg_run *run = runs[r];
     if (!run || run->w.prec != PMCG_MIXED || run->w.D > 32 || !run->post || run->post->plugins.size() != 1) {
       set_error(err, PMCG_EUNSUPPORTED, __LINE__,
                 "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood", r);
-      delete b;
-      return nullptr;
+      return false;
     }
     const Work &w = run->w;
     const Plugin &pl = run->post->plugins[0];
-    BatchDesc &d = b->hdesc[r];
+    BatchDesc &d = hd[r];
     memset(&d, 0, sizeof(d));
     d.prop = w.prop.view();
     d.ptype = pl.type;
@@ -455,27 +481,46 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
     d.logdetL = w.prop.logdetL; d.cw = w.prop.cw; d.lconst = w.prop.lconst;
     d.W32 = w.prop.W32; d.b32 = w.prop.b32; d.lconst32 = w.prop.lconst32; d.L32 = w.prop.L32; d.mu32 = w.prop.mu32;
   }
-  int dev = 0;
-  bool ok = BCK(cudaGetDevice(&dev), "device") &&
-            BCK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev), "SM count") &&
-            BCK(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking), "stream") &&
-            BCK(cudaEventCreate(&b->e0), "event") && BCK(cudaEventCreate(&b->e1), "event") &&
-            BCK(cudaMalloc(&b->d_desc, sizeof(BatchDesc) * nruns), "descriptors") &&
-            BCK(cudaMalloc(&b->d_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
-            BCK(cudaMallocHost(&b->h_dyn, sizeof(BatchDyn) * nruns), "parameters") &&
-            BCK(cudaMalloc(&b->d_starts, sizeof(uint32_t) * kBStages * (nruns + 1)), "prefix tables") &&
-            BCK(cudaMalloc(&b->d_snpre, sizeof(uint32_t) * (nruns + 1)), "prefix tables") &&
-            BCK(cudaMalloc(&b->d_stats, sizeof(DevStats) * nruns), "stats") &&
-            BCK(cudaMallocHost(&b->h_stats, sizeof(DevStats) * nruns), "stats") &&
-            BCK(cudaMemcpy(b->d_desc, b->hdesc.data(), sizeof(BatchDesc) * nruns, cudaMemcpyHostToDevice),
+  drop_graph(b);
+  if (nruns > b->cap) {
+    if (!BCK(cudaStreamSynchronize(b->s), "batch stream")) return false;
+    free_arrays(b);
+    const int cap = std::max(nruns, 16);
+    bool ok = BCK(cudaMalloc(&b->d_desc, sizeof(BatchDesc) * cap), "descriptors") &&
+              BCK(cudaMalloc(&b->d_dyn, sizeof(BatchDyn) * cap), "parameters") &&
+              BCK(cudaMallocHost(&b->h_dyn, sizeof(BatchDyn) * cap), "parameters") &&
+              BCK(cudaMalloc(&b->d_starts, sizeof(uint32_t) * kBStages * (cap + 1)), "prefix tables") &&
+              BCK(cudaMalloc(&b->d_snpre, sizeof(uint32_t) * (cap + 1)), "prefix tables") &&
+              BCK(cudaMalloc(&b->d_stats, sizeof(DevStats) * cap), "stats") &&
+              BCK(cudaMallocHost(&b->h_stats, sizeof(DevStats) * cap), "stats");
+    if (!ok) {
+      free_arrays(b);
+      return false;
+    }
+    b->cap = cap;
+  }
+  b->R = nruns;
+  b->runs.assign(runs, runs + nruns);
+  b->hdesc.swap(hd);
+  // the runs' own streams may still have work queued (proposal uploads): drain
+  // the busy ones (an idle stream answers the query at once)
+  for (int r = 0; r < nruns; r++) {
+    const cudaError_t q = cudaStreamQuery(runs[r]->w.s);
+    if (q == cudaErrorNotReady) {
+      if (!BCK(cudaStreamSynchronize(runs[r]->w.s), "run stream")) return false;
+    } else if (!BCK(q, "run stream")) {
+      return false;
+    }
+  }
+  bool ok = BCK(cudaMemcpyAsync(b->d_desc, b->hdesc.data(), sizeof(BatchDesc) * nruns, cudaMemcpyHostToDevice, b->s),
                 "descriptors");
   // The batch's draws add to the counts, which its preparation stage zeroes
   // after each iteration: start from zero (a fresh run's counts are
   // uninitialised; a run iterated alone holds that iteration's counts).
-  for (int r = 0; ok && r < nruns; r++)
-    ok = BCK(cudaMemsetAsync(runs[r]->w.counts, 0, sizeof(int) * runs[r]->w.K, runs[r]->w.s), "counts");
-  // the runs' own streams may still have work queued (proposal uploads)
-  for (int r = 0; ok && r < nruns; r++) ok = BCK(cudaStreamSynchronize(runs[r]->w.s), "run stream");
+  if (ok) {
+    batch_zero_counts_kernel<<<nruns, 128, 0, b->s>>>(b->d_desc, nruns);
+    ok = BCK(cudaGetLastError(), "counts") && BCK(cudaStreamSynchronize(b->s), "descriptors");
+  }
   // a tuned configuration for this shape, if any
   int spt = 2, bps = 1;
   {
@@ -489,12 +534,37 @@ extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error
     if (it != g_tune_cache.end()) { spt = it->second.first; bps = it->second.second; }
   }
   ok = ok && batch_configure(b, spt, bps, err);
+  b->iters_bound = 0;
+  return ok;
+}
+}  // namespace pmcg
+
+extern "C" pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err) {
+  if (nruns < 1 || !runs) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_batch_create: no runs");
+    return nullptr;
+  }
+  pmcg_batch *b = new pmcg_batch();
+  int dev = 0;
+  bool ok = BCK(cudaGetDevice(&dev), "device") &&
+            BCK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev), "SM count") &&
+            BCK(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking), "stream") &&
+            BCK(cudaEventCreate(&b->e0), "event") && BCK(cudaEventCreate(&b->e1), "event") &&
+            batch_bind(b, nruns, runs, err);
   if (!ok) {
     pmcg_batch_free(&b);
     return nullptr;
   }
-  capture_graph(b);
   return b;
+}
+
+extern "C" void pmcg_batch_rebind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **err) {
+  if (!b) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_batch_rebind: no batch");
+    return;
+  }
+  if (!BCK(cudaStreamSynchronize(b->s), "batch stream")) return;
+  batch_bind(b, nruns, runs, err);
 }
 
 extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *stats, error **err) {
@@ -503,6 +573,9 @@ extern "C" void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter
     b->h_dyn[r].call = b->runs[r]->calls;
     b->h_dyn[r].pad = 0;
   }
+  // the graph from the second iteration of a binding on (see batch_bind)
+  if (!b->graph && !b->stage_timing && b->iters_bound >= 1) capture_graph(b);
+  b->iters_bound++;
   bool ok = BCK(cudaEventRecord(b->e0, b->s), "event");
   b->staged_last = false;
   if (ok && b->stage_timing) {
@@ -614,13 +687,8 @@ extern "C" void pmcg_batch_free(pmcg_batch **pb) {
   if (!pb || !*pb) return;
   pmcg_batch *b = *pb;
   drop_graph(b);
-  if (b->d_desc) cudaFree(b->d_desc);
-  if (b->d_dyn) cudaFree(b->d_dyn);
-  if (b->h_dyn) cudaFreeHost(b->h_dyn);
-  if (b->d_starts) cudaFree(b->d_starts);
-  if (b->d_snpre) cudaFree(b->d_snpre);
-  if (b->d_stats) cudaFree(b->d_stats);
-  if (b->h_stats) cudaFreeHost(b->h_stats);
+  if (b->s) cudaStreamSynchronize(b->s);
+  free_arrays(b);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
   for (cudaEvent_t e : b->sev)

@@ -1331,11 +1331,17 @@ namespace pmcg {
 // The speculative weight step, normalisation and EM update (see SimMirror).
 static bool speculate(SimMirror *m, error **err) {
   Work &w = m->w;
-  if (!m->spec_mix.arena &&
-      (!CK(devmix_alloc(m->spec_mix, w.K, w.D, w.df), "speculative proposal") ||
-       !CK(cudaMalloc(&m->spec_st, sizeof(DevStats)), "speculative statistics") ||
-       !CK(cudaMalloc(&m->flg1, sizeof(short) * w.N + 16), "flag copy"))) {
+  // buffers on first use (each once; a failed allocation is retried next time)
+  if (!m->spec_mix.arena && !CK(devmix_alloc(m->spec_mix, w.K, w.D, w.df), "speculative proposal")) {
     devmix_free(m->spec_mix);
+    return false;
+  }
+  if (!m->spec_st && !CK(cudaMalloc(&m->spec_st, sizeof(DevStats)), "speculative statistics")) {
+    m->spec_st = nullptr;
+    return false;
+  }
+  if (!m->flg1 && !CK(cudaMalloc(&m->flg1, sizeof(short) * w.N + 16), "flag copy")) {
+    m->flg1 = nullptr;
     return false;
   }
   if (!CK(cudaMemcpyAsync(m->flg1, w.flg, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags")) return false;

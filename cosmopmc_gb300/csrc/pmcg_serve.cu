@@ -158,11 +158,16 @@ static void server_loop(pmcg_server *s) {
     if (s->active.empty()) continue;
     if ((int)s->active.size() > s->peak_jobs) s->peak_jobs = (int)s->active.size();
     if (s->dirty) {
-      if (s->batch) pmcg_batch_free(&s->batch);
+      // the resident set changed: bind it to the batch (its arrays are kept)
       std::vector<pmcg_run *> runs;
       for (Job *j : s->active) runs.push_back(j->run);
       error *e = nullptr;
-      s->batch = pmcg_batch_create((int)runs.size(), runs.data(), &e);
+      if (s->batch) {
+        pmcg_batch_rebind(s->batch, (int)runs.size(), runs.data(), &e);
+        if (isError(e)) pmcg_batch_free(&s->batch);
+      } else {
+        s->batch = pmcg_batch_create((int)runs.size(), runs.data(), &e);
+      }
       if (s->batch && s->opts.autotune) pmcg_batch_autotune(s->batch, &e);
       if (!s->batch) {
         int code = getErrorValue(e);

@@ -215,6 +215,7 @@ SIGNATURES = [
     ("pmcg_run_last_launches", C.c_int, [C.c_void_p]),
     ("pmcg_run_time_stage", C.c_double, [C.c_void_p, C.c_int, C.c_int, PErr]),
     ("pmcg_batch_create", C.c_void_p, [C.c_int, C.POINTER(C.c_void_p), PErr]),
+    ("pmcg_batch_rebind", None, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), PErr]),
     ("pmcg_batch_iterate", None, [C.c_void_p, _dp, C.POINTER(IterStats), PErr]),
     ("pmcg_batch_autotune", None, [C.c_void_p, PErr]),
     ("pmcg_batch_config", None, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -689,6 +690,13 @@ class Batch:
         self.runs = list(runs)
         arr = (C.c_void_p * len(self.runs))(*[r.p.value for r in self.runs])
         self.p = C.c_void_p(call("pmcg_batch_create", len(self.runs), arr))
+
+    def rebind(self, runs):
+        """Iterate another set of runs with this batch (pmcg_batch_rebind)."""
+        runs = list(runs)
+        arr = (C.c_void_p * len(runs))(*[r.p.value for r in runs])
+        call("pmcg_batch_rebind", self.p, len(runs), arr)
+        self.runs = runs
 
     def iterate(self, betas=None):
         R = len(self.runs)

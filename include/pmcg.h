@@ -569,6 +569,11 @@ int pmcg_run_last_launches(const pmcg_run *r);
  * runs; free it before them. */
 typedef struct pmcg_batch pmcg_batch;
 pmcg_batch *pmcg_batch_create(int nruns, pmcg_run *const *runs, error **err);
+/* Bind another set of runs to an existing batch (its device and pinned arrays
+ * are kept and grown when short; the CUDA graph is captured again at the second
+ * iteration of the new set). Cheaper than free + create when the set changes
+ * often (the serving loop). On failure the batch must be freed. */
+void pmcg_batch_rebind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **err);
 /* betas [nruns] (NULL: all 1); stats [nruns] (NULL allowed). A run whose
  * iteration fails reports stats[r].status != 0 without disturbing the others.
  * A failure before the update (no sample in the box: PMCG_ENOWEIGHT) keeps the

@@ -156,3 +156,33 @@ def test_batch_stage_timing_keeps_results(pmcg):
     assert b.stage_ms() is None
     a.free()
     b.free()
+
+
+def test_batch_rebind_equals_fresh_batches(pmcg):
+    """A batch rebound to another set of runs (some continuing, some new) gives
+    what fresh batches of the same runs give, bit for bit, over the rebinding
+    and the graph captured again after it."""
+    P = pmcg
+    specs = SPECS[:6]
+    keep, xs, ys = [], [], []
+    for kind, D, K, N, seed in specs:
+        prop, post, box = make_run(P, kind, D, K, N, seed)
+        keep.append((prop, post, box))
+        xs.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+        ys.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+    b = P.Batch(xs[:3])
+    f1 = P.Batch(ys[:3])
+    assert b.iterate() == f1.iterate()
+    b.rebind(xs[1:6])   # runs 1 and 2 continue, 3..5 join
+    f2 = P.Batch(ys[1:6])
+    for it in range(3):   # direct launch, then the graph captured and replayed
+        assert b.iterate() == f2.iterate(), it
+    for rx, ry in zip(xs[1:6], ys[1:6]):
+        wa, ma, La = rx.proposal().arrays()
+        wb, mb, Lb = ry.proposal().arrays()
+        assert np.array_equal(wa, wb) and np.array_equal(ma, mb) and np.array_equal(La, Lb)
+    b.rebind(xs[:1])    # fewer runs than before: the arrays are kept
+    f3 = P.Batch(ys[:1])
+    assert b.iterate() == f3.iterate()
+    for x in (b, f1, f2, f3):
+        x.free()
