@@ -852,43 +852,54 @@ static bool capture_run_graph(pmcg_run *r) {
   return true;
 }
 
-extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err) {
+namespace pmcg {
+// An iteration in two halves: the launch (a replayed graph is queued on the
+// run's stream without waiting; otherwise the stages run and their statistics
+// are fetched) and the completion (wait, check, timing, revival, statistics).
+static bool run_launch(pmcg_run *r, double beta, error **err) {
   Work &w = r->w;
   w.launches = 0;
-  bool ok = true;
   const bool stages = r->timing == 1;
   if (w.prec == PMCG_MIXED && !stages && !r->graph_off) {
     if (r->gexec && r->graph_tc != g_use_tensor_cores) drop_run_graph(r);
     if (!r->gexec && !capture_run_graph(r)) r->graph_off = true;
   }
+  r->pending_graph = false;
   if (r->gexec && !stages) {
     r->hpar->beta = beta;
     r->hpar->call = r->calls;
     if (r->timing) cudaEventRecord(r->ev[0], w.s);
-    ok = CK(cudaGraphLaunch(r->gexec, w.s), "iteration graph");
+    const bool ok = CK(cudaGraphLaunch(r->gexec, w.s), "iteration graph");
     if (r->timing) cudaEventRecord(r->ev[PMCG_NSTAGE], w.s);
-    ok = ok && CK(cudaStreamSynchronize(w.s), "iteration");
     w.launches = r->graph_launches;
     r->calls++;
     r->last_launches = w.launches;
-    if (!ok || !check_stats(w, err)) return;
-  } else {
-    auto mark = [&](int i) { if (r->timing) cudaEventRecord(r->ev[i], w.s); };
-    mark(0);
-    ok = stage_draw(w, r->box, r->seed, r->calls, err);
-    mark(1);
-    ok = ok && stage_logq(w, err);
-    mark(2);
-    ok = ok && stage_logpost(w, r->post, err);
-    mark(3);
-    ok = ok && stage_weights(w, beta, true, err);
-    mark(4);
-    ok = ok && stage_em(w, err);
-    mark(5);
-    r->calls++;
-    r->last_launches = w.launches;
-    if (!ok) return;
-    if (!fetch_stats(w, err)) return;
+    r->pending_graph = ok;
+    return ok;
+  }
+  auto mark = [&](int i) { if (r->timing) cudaEventRecord(r->ev[i], w.s); };
+  mark(0);
+  bool ok = stage_draw(w, r->box, r->seed, r->calls, err);
+  mark(1);
+  ok = ok && stage_logq(w, err);
+  mark(2);
+  ok = ok && stage_logpost(w, r->post, err);
+  mark(3);
+  ok = ok && stage_weights(w, beta, true, err);
+  mark(4);
+  ok = ok && stage_em(w, err);
+  mark(5);
+  r->calls++;
+  r->last_launches = w.launches;
+  return ok && fetch_stats(w, err);
+}
+
+static bool run_finish(pmcg_run *r, pmcg_iter_stats *stats, error **err) {
+  Work &w = r->w;
+  const bool stages = r->timing == 1;
+  if (r->pending_graph) {
+    r->pending_graph = false;
+    if (!CK(cudaStreamSynchronize(w.s), "iteration") || !check_stats(w, err)) return false;
   }
   if (r->timing) {
     float ms = 0.f;
@@ -903,7 +914,7 @@ extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stat
     }
     r->timed++;
   }
-  if (!run_revive_dead(r, err)) return;
+  if (!run_revive_dead(r, err)) return false;
   if (stats) {
     const DevStats &h = *w.hstats;
     stats->ln_evidence = h.ln_evidence;
@@ -915,6 +926,40 @@ extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stat
     stats->nok = (size_t)h.nok;
     stats->ndead = h.ndead;
   }
+  return true;
+}
+}  // namespace pmcg
+
+extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err) {
+  if (run_launch(r, beta, err)) run_finish(r, stats, err);
+}
+
+extern "C" void pmcg_run_iterate_async(pmcg_run *r, double beta, error **err) {
+  if (r->launched) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_iterate_async: the previous iteration was not waited for");
+    return;
+  }
+  r->launched = true;
+  r->launch_ok = run_launch(r, beta, &r->launch_err);
+  if (!r->launch_ok && !r->launch_err)
+    set_error(&r->launch_err, PMCG_ECUDA, __LINE__, "iteration launch failed");
+  (void)err;
+}
+
+extern "C" void pmcg_run_iterate_wait(pmcg_run *r, pmcg_iter_stats *stats, error **err) {
+  if (!r->launched) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_iterate_wait: no iteration was started");
+    return;
+  }
+  r->launched = false;
+  if (!r->launch_ok) {
+    r->pending_graph = false;
+    if (err && !*err) *err = r->launch_err;   // the launch's error chain, as a synchronous call gives it
+    else purgeError(&r->launch_err);
+    r->launch_err = nullptr;
+    return;
+  }
+  run_finish(r, stats, err);
 }
 
 extern "C" void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err) {
@@ -1053,6 +1098,8 @@ extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {
 
 extern "C" void pmcg_run_free(pmcg_run **r) {
   if (!r || !*r) return;
+  if ((*r)->w.s) cudaStreamSynchronize((*r)->w.s);   // an iteration may be in flight
+  purgeError(&(*r)->launch_err);
   drop_run_graph(*r);
   if ((*r)->dpar) cudaFree((*r)->dpar);
   if ((*r)->hpar) cudaFreeHost((*r)->hpar);

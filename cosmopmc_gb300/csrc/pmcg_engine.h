@@ -104,6 +104,11 @@ struct pmcg_run {
   cudaGraphExec_t gexec = nullptr;
   int graph_tc = -1, graph_launches = 0;
   bool graph_off = false;
+  // An iteration in flight: a graph launched and not yet waited for
+  // (pending_graph); pmcg_run_iterate_async's launch and its outcome.
+  bool pending_graph = false;
+  bool launched = false, launch_ok = false;
+  error *launch_err = nullptr;
   // Dead components (sdead_comp, exec/cosmo_pmc.c:239-284): buried (default) or
   // revived after each update; the box on the host for the revival's shifts.
   int dead_mode = PMCG_DEAD_BURY;

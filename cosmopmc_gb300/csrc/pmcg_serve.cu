@@ -4,9 +4,11 @@
 // tempering schedule, seed) from any thread; one server thread owns the GPU.
 // At every epoch boundary it admits queued jobs while free slots and the
 // device-memory budget allow (each job's footprint is the exact size of the
-// buffers its run allocates), rebuilds the batch over the resident jobs when
-// that set changed, and runs one iteration of every resident job in one
-// persistent launch (k_batch.cu). A job that arrives while others are on the
+// buffers its run allocates), binds the batch to the resident jobs when that
+// set changed, and runs one iteration of every resident job: the smaller jobs
+// in one persistent launch (k_batch.cu), jobs of at least alone_min_samples
+// samples with their own CUDA graphs on their own streams, concurrently. A job
+// that arrives while others are on the
 // GPU therefore joins the next epoch and overlaps with them. Each job's
 // arithmetic depends only on its own inputs, so its result is the same alone
 // and in any mix. Failed jobs (an iteration error) are retired with their
@@ -64,7 +66,7 @@ struct pmcg_server {
   std::map<int64_t, Job *> jobs;
   std::vector<Job *> active;
   pmcg_batch *batch = nullptr;
-  bool dirty = true, stop = false;
+  bool dirty = true, stop = false;   // dirty: a job was admitted or retired since the last binding
   int64_t next_id = 1;
   size_t bytes_in_use = 0, peak_bytes = 0;
   int peak_jobs = 0;
@@ -157,64 +159,84 @@ static void server_loop(pmcg_server *s) {
     }
     if (s->active.empty()) continue;
     if ((int)s->active.size() > s->peak_jobs) s->peak_jobs = (int)s->active.size();
+    // Jobs of at least alone_min_samples samples fill the GPU by themselves:
+    // they iterate on their own streams (their CUDA graphs, the tensor-core
+    // kernels) beside the batch of the smaller ones.
+    std::vector<Job *> small, large;
+    for (Job *j : s->active) (j->N >= s->opts.alone_min_samples ? large : small).push_back(j);
     if (s->dirty) {
-      // the resident set changed: bind it to the batch (its arrays are kept)
+      // a job came or went: bind the batched set to the batch (its arrays are
+      // kept). Run pointers are not compared: a new run may reuse a freed one's
+      // address.
       std::vector<pmcg_run *> runs;
-      for (Job *j : s->active) runs.push_back(j->run);
+      for (Job *j : small) runs.push_back(j->run);
       error *e = nullptr;
-      if (s->batch) {
+      if (runs.empty()) {
+        if (s->batch) pmcg_batch_free(&s->batch);
+      } else if (s->batch) {
         pmcg_batch_rebind(s->batch, (int)runs.size(), runs.data(), &e);
         if (isError(e)) pmcg_batch_free(&s->batch);
       } else {
         s->batch = pmcg_batch_create((int)runs.size(), runs.data(), &e);
       }
       if (s->batch && s->opts.autotune) pmcg_batch_autotune(s->batch, &e);
-      if (!s->batch) {
+      if (!runs.empty() && !s->batch) {
         int code = getErrorValue(e);
         purgeError(&e);
-        std::vector<Job *> act;
-        act.swap(s->active);
-        for (Job *j : act) retire(s, j, code ? code : PMCG_EUNSUPPORTED);
+        for (Job *j : small) retire(s, j, code ? code : PMCG_EUNSUPPORTED);
+        s->active.swap(large);
         continue;
       }
       purgeError(&e);
       s->dirty = false;
     }
-    const size_t R = s->active.size();
-    betas.resize(R);
-    st.assign(R, pmcg_iter_stats{});
-    for (size_t r = 0; r < R; r++) {
-      Job *j = s->active[r];
+    auto beta_of = [](Job *j) {
       error *e = nullptr;
-      betas[r] = get_tempering_beta(j->tempering, j->iter, j->tmin, j->niter, &e);
-      if (isError(e)) betas[r] = 1.0;
+      double bt = get_tempering_beta(j->tempering, j->iter, j->tmin, j->niter, &e);
+      if (isError(e)) bt = 1.0;
+      purgeError(&e);
+      return bt;
+    };
+    for (Job *j : large) {
+      error *e = nullptr;
+      pmcg_run_iterate_async(j->run, beta_of(j), &e);   // a launch error comes back from the wait
       purgeError(&e);
     }
-    error *e = nullptr;
-    pmcg_batch_iterate(s->batch, betas.data(), st.data(), &e);
-    if (isError(e)) {  // a launch failure: retire every resident job with the error
-      int code = getErrorValue(e);
+    const size_t R = small.size();
+    betas.resize(R);
+    st.assign(R, pmcg_iter_stats{});
+    for (size_t r = 0; r < R; r++) betas[r] = beta_of(small[r]);
+    int batch_code = 0;
+    if (R > 0) {
+      error *e = nullptr;
+      pmcg_batch_iterate(s->batch, betas.data(), st.data(), &e);
+      if (isError(e)) {  // a launch failure: retire every batched job with the error
+        batch_code = getErrorValue(e);
+        purgeError(&e);
+        pmcg_batch_free(&s->batch);
+        s->dirty = true;
+      }
+    }
+    std::vector<pmcg_iter_stats> lst(large.size());
+    std::vector<int> lcode(large.size(), 0);
+    for (size_t i = 0; i < large.size(); i++) {
+      error *e = nullptr;
+      pmcg_run_iterate_wait(large[i]->run, &lst[i], &e);
+      if (isError(e)) lcode[i] = getErrorValue(e);
       purgeError(&e);
-      pmcg_batch_free(&s->batch);
-      std::vector<Job *> act;
-      act.swap(s->active);
-      for (Job *j : act) retire(s, j, code);
-      continue;
     }
     s->epochs++;
     std::vector<Job *> keep;
-    for (size_t r = 0; r < R; r++) {
-      Job *j = s->active[r];
-      j->last = st[r];
+    auto settle = [&](Job *j, int code, const pmcg_iter_stats &js) {
+      j->last = js;
       j->iter++;
-      if (st[r].status != 0) retire(s, j, st[r].status);
+      if (code != 0) retire(s, j, code);
       else if (j->iter >= j->niter) retire(s, j, 0);
       else keep.push_back(j);
-    }
-    if (keep.size() != R) {
-      s->active.swap(keep);
-      s->dirty = true;
-    }
+    };
+    for (size_t r = 0; r < R; r++) settle(small[r], batch_code ? batch_code : st[r].status, st[r]);
+    for (size_t i = 0; i < large.size(); i++) settle(large[i], lcode[i], lst[i]);
+    s->active.swap(keep);
   }
   if (s->batch) pmcg_batch_free(&s->batch);
   for (Job *j : s->active)
@@ -236,6 +258,7 @@ extern "C" pmcg_server *pmcg_server_create(const pmcg_server_opts *opts, error *
   cudaGetDevice(&s->device);
   if (s->opts.max_jobs <= 0) s->opts.max_jobs = 512;
   if (!(s->opts.fshift > 0.0)) s->opts.fshift = 0.1;
+  if (s->opts.alone_min_samples == 0) s->opts.alone_min_samples = (size_t)1 << 16;
   if (s->opts.dead_comp != PMCG_DEAD_REVIVE) s->opts.dead_comp = PMCG_DEAD_BURY;
   if (s->opts.hbm_budget_bytes == 0) {
     size_t fr = 0, tot = 0;

@@ -98,7 +98,7 @@ class WeightStats(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_jobs", C.c_int), ("autotune", C.c_int),
-                ("dead_comp", C.c_int), ("fshift", C.c_double)]
+                ("dead_comp", C.c_int), ("fshift", C.c_double), ("alone_min_samples", C.c_size_t)]
 
 
 class JobResult(C.Structure):
@@ -204,6 +204,8 @@ SIGNATURES = [
     ("pmcg_run_create", C.c_void_p, [C.POINTER(MixMvdensS), C.c_void_p, C.POINTER(ParaboxS), C.c_size_t, C.c_int,
                                      C.c_uint64, PErr]),
     ("pmcg_run_iterate", None, [C.c_void_p, C.c_double, C.POINTER(IterStats), PErr]),
+    ("pmcg_run_iterate_async", None, [C.c_void_p, C.c_double, PErr]),
+    ("pmcg_run_iterate_wait", None, [C.c_void_p, C.POINTER(IterStats), PErr]),
     ("pmcg_run_get_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_run_get_sample", None, [C.c_void_p, C.POINTER(PmcSimuS), PErr]),
     ("pmcg_run_set_dead_comp", None, [C.c_void_p, C.c_int, C.c_double, PErr]),
@@ -630,6 +632,15 @@ class Run:
         call("pmcg_run_iterate", self.p, beta, C.byref(st))
         return st.as_dict()
 
+    def iterate_async(self, beta=1.0):
+        """Start an iteration (pmcg_run_iterate_async); finish it with iterate_wait."""
+        call("pmcg_run_iterate_async", self.p, beta)
+
+    def iterate_wait(self):
+        st = IterStats()
+        call("pmcg_run_iterate_wait", self.p, C.byref(st))
+        return st.as_dict()
+
     def proposal(self) -> MixMvdens:
         m = MixMvdens(self.K, self.D)
         call("pmcg_run_get_proposal", self.p, m.p)
@@ -744,8 +755,9 @@ class Batch:
 class Server:
     """Continuous-batching PMC server (pmcg_server_*)."""
 
-    def __init__(self, hbm_budget_bytes=0, max_jobs=0, autotune=False, dead_comp=DEAD_BURY, fshift=0.1):
-        o = ServerOpts(hbm_budget_bytes, max_jobs, 1 if autotune else 0, dead_comp, fshift)
+    def __init__(self, hbm_budget_bytes=0, max_jobs=0, autotune=False, dead_comp=DEAD_BURY, fshift=0.1,
+                 alone_min_samples=0):
+        o = ServerOpts(hbm_budget_bytes, max_jobs, 1 if autotune else 0, dead_comp, fshift, alone_min_samples)
         self.p = C.c_void_p(call("pmcg_server_create", C.byref(o)))
         self._keep = {}
 

@@ -516,6 +516,14 @@ pmcg_run *pmcg_run_create(const mix_mvdens *proposal, const pmcg_posterior *post
 /* One PMC iteration (draw, log q, log posterior, weights, evidence,
  * perplexity, EM update, dead-component burial). stats may be NULL. */
 void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err);
+/* The same iteration in two halves: _async queues it on the run's stream (a
+ * single-precision run replays its CUDA graph without waiting; otherwise the
+ * stages run to completion here) and _wait completes it (waits, checks,
+ * revives dead components in revive mode, fills stats; the launch's errors are
+ * reported here). Iterations of several runs started before any is waited for
+ * run concurrently on their streams. One iteration in flight per run. */
+void pmcg_run_iterate_async(pmcg_run *r, double beta, error **err);
+void pmcg_run_iterate_wait(pmcg_run *r, pmcg_iter_stats *stats, error **err);
 void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err);
 /* Replace the run's proposal (same ncomp/ndim/df), e.g. to restart or to
  * apply a host-side revive step between iterations. */
@@ -616,6 +624,9 @@ typedef struct {
   int autotune;             /* tune each new batch shape (cached per shape) */
   int dead_comp;            /* PMCG_DEAD_BURY (0) or PMCG_DEAD_REVIVE for every job with a prior box */
   double fshift;            /* revival shift (0: 0.1) */
+  size_t alone_min_samples; /* jobs of at least this many samples iterate with their own CUDA graph on
+                               their own stream (tensor-core kernels), beside the batch of the others
+                               (0: 2^16; SIZE_MAX: every job batched) */
 } pmcg_server_opts;
 typedef struct {
   int status;               /* 0 done, > 0 queued/running, < 0 PMCG_E* error */

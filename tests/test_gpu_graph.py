@@ -75,3 +75,31 @@ def test_graph_recaptured_when_tensor_cores_switch(pmcg):
         direct.free()
     finally:
         pmcg.set_tensor_cores(prev)
+
+
+def test_async_iterations_equal_synchronous(pmcg):
+    """pmcg_run_iterate_async / _wait: iterations of two runs started together and
+    waited for in turn equal the same runs iterated synchronously, in single
+    precision (a replayed graph in flight) and in FP64 (direct launches)."""
+    P = pmcg
+    wl = W.mixture_workload(D=8, K=4, Kt=2, nu=-1, seed=5, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+    post = P.Posterior(8).add_mix(target)
+    for prec in (P.MIXED, P.FP64):
+        a, b = (P.Run(prop, post, 30000, precision=prec, seed=s) for s in (1, 2))
+        a2, b2 = (P.Run(prop, post, 30000, precision=prec, seed=s) for s in (1, 2))
+        for it in range(3):
+            a.iterate_async(1.0)
+            b.iterate_async(0.5)
+            sa, sb = a.iterate_wait(), b.iterate_wait()
+            assert sa == a2.iterate(1.0) and sb == b2.iterate(0.5), (prec, it)
+        for x, y in ((a, a2), (b, b2)):
+            for u, v in zip(x.proposal().arrays(), y.proposal().arrays()):
+                assert np.array_equal(u, v)
+        with pytest.raises(P.PmcgError):
+            a.iterate_wait()            # nothing in flight
+        for r in (a, b, a2, b2):
+            r.free()

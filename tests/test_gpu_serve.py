@@ -95,3 +95,35 @@ def test_wait_is_bounded(pmcg):
         s.wait(jid, timeout=0.001)
     assert e.value.code == -9009
     s.free()  # stops after the current epoch
+
+
+def test_large_job_alone_beside_the_batch(pmcg):
+    """A job of at least alone_min_samples samples iterates with its own graph on
+    its own stream, beside the batch of the smaller jobs: its result is the same
+    as when served alone, and the small jobs' results are the same as when the
+    large job is batched with them (SIZE_MAX: every job batched)."""
+    P = pmcg
+    keep = []
+    big = ("mix", 10, 6, 70000, 321)
+    prop, post, box = _job(P, big, keep)
+    s1 = P.Server()
+    j = s1.submit(prop, post, big[3], 4, big[4], box=box)
+    alone, prop_alone = s1.wait(j, timeout=120, want_proposal=True)
+    s1.free()
+    assert alone["status"] == 0 and alone["iterations"] == 4
+    small = [_job(P, spec, keep) for spec in MIX[:4]]
+    res = {}
+    for name, opts in (("split", {}), ("batched", {"alone_min_samples": (1 << 64) - 1})):
+        s = P.Server(**opts)
+        ids = [s.submit(pp, po, spec[3], 3, spec[4], box=bx) for spec, (pp, po, bx) in zip(MIX[:4], small)]
+        jb = s.submit(prop, post, big[3], 4, big[4], box=box)
+        res[name] = ([s.wait(i, timeout=120) for i in ids], s.wait(jb, timeout=120, want_proposal=True))
+        s.free()
+    (small_split, (big_split, prop_split)) = res["split"]
+    (small_batched, _) = res["batched"]
+    for key in ("status", "iterations", "ln_evidence", "perplexity", "ess", "enc"):
+        assert big_split[key] == alone[key], (key, big_split[key], alone[key])
+        for a, b in zip(small_split, small_batched):
+            assert a[key] == b[key], (key, a, b)
+    for a, b in zip(prop_alone.arrays(), prop_split.arrays()):
+        assert np.array_equal(a, b)
