@@ -452,6 +452,10 @@ static bool batch_bind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **
                 "batch run %d: needs a mixed-precision run with D <= 32 and exactly one likelihood", r);
       return false;
     }
+    if (run->launched) {
+      set_error(err, PMCG_EARG, __LINE__, "batch run %d: an asynchronous iteration was not waited for", r);
+      return false;
+    }
     const Work &w = run->w;
     const Plugin &pl = run->post->plugins[0];
     BatchDesc &d = hd[r];

@@ -930,7 +930,16 @@ static bool run_finish(pmcg_run *r, pmcg_iter_stats *stats, error **err) {
 }
 }  // namespace pmcg
 
+// A run with an asynchronous iteration in flight accepts only pmcg_run_iterate_wait
+// (and pmcg_run_free, which waits for the stream).
+static bool run_in_flight(const pmcg_run *r, error **err, const char *fn) {
+  if (!r->launched) return false;
+  set_error(err, PMCG_EARG, __LINE__, "%s: an iteration started by pmcg_run_iterate_async was not waited for", fn);
+  return true;
+}
+
 extern "C" void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **err) {
+  if (run_in_flight(r, err, "pmcg_run_iterate")) return;
   if (run_launch(r, beta, err)) run_finish(r, stats, err);
 }
 
@@ -963,6 +972,7 @@ extern "C" void pmcg_run_iterate_wait(pmcg_run *r, pmcg_iter_stats *stats, error
 }
 
 extern "C" void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err) {
+  if (run_in_flight(r, err, "pmcg_run_get_proposal")) return;
   Work &w = r->w;
   if (out->ncomp != w.K || out->ndim != w.D) {
     set_error(err, PMCG_EDIM, __LINE__, "output proposal shape differs");
@@ -989,6 +999,7 @@ extern "C" void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err)
 }
 
 extern "C" void pmcg_run_set_proposal(pmcg_run *r, const mix_mvdens *proposal, error **err) {
+  if (run_in_flight(r, err, "pmcg_run_set_proposal")) return;
   Work &w = r->w;
   if (!proposal || proposal->ncomp != w.K || proposal->ndim != w.D || proposal->comp[0]->df != w.df) {
     set_error(err, PMCG_EDIM, __LINE__, "proposal shape differs from the run's");
@@ -1002,6 +1013,7 @@ extern "C" void pmcg_run_set_dead_comp(pmcg_run *r, int mode, double fshift, err
     set_error(err, PMCG_EARG, __LINE__, "pmcg_run_set_dead_comp: invalid mode %d or fshift %g", mode, fshift);
     return;
   }
+  if (run_in_flight(r, err, "pmcg_run_set_dead_comp")) return;
   if (mode == PMCG_DEAD_REVIVE && r->hmin.empty()) {
     set_error(err, PMCG_EARG, __LINE__, "reviving components needs the run's prior box");
     return;
@@ -1078,6 +1090,7 @@ bool run_revive_dead(pmcg_run *r, error **err) {
 }  // namespace pmcg
 
 extern "C" void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err) {
+  if (run_in_flight(r, err, "pmcg_run_get_sample")) return;
   Work &w = r->w;
   if (psim->ndim != w.D) { set_error(err, PMCG_EDIM, __LINE__, "sample dimension differs"); return; }
   pmc_simu_realloc(psim, w.N, err);
@@ -1131,6 +1144,7 @@ extern "C" int pmcg_run_iteration_ms(pmcg_run *r, double *ms) {
 }
 
 extern "C" double pmcg_run_time_stage(pmcg_run *r, int stage, int reps, error **err) {
+  if (run_in_flight(r, err, "pmcg_run_time_stage")) return -1.0;
   Work &w = r->w;
   if ((stage != 1 && stage != 2) || reps < 1 || r->calls == 0) {
     set_error(err, PMCG_EARG, __LINE__, "pmcg_run_time_stage: stage 1 or 2 of a run that has iterated, reps >= 1");

@@ -521,7 +521,9 @@ void pmcg_run_iterate(pmcg_run *r, double beta, pmcg_iter_stats *stats, error **
  * stages run to completion here) and _wait completes it (waits, checks,
  * revives dead components in revive mode, fills stats; the launch's errors are
  * reported here). Iterations of several runs started before any is waited for
- * run concurrently on their streams. One iteration in flight per run. */
+ * run concurrently on their streams. One iteration in flight per run: until
+ * its _wait, every other call on the run (and a batch holding it) returns
+ * PMCG_EARG; pmcg_run_free waits for the stream. */
 void pmcg_run_iterate_async(pmcg_run *r, double beta, error **err);
 void pmcg_run_iterate_wait(pmcg_run *r, pmcg_iter_stats *stats, error **err);
 void pmcg_run_get_proposal(pmcg_run *r, mix_mvdens *out, error **err);

@@ -101,5 +101,14 @@ def test_async_iterations_equal_synchronous(pmcg):
                 assert np.array_equal(u, v)
         with pytest.raises(P.PmcgError):
             a.iterate_wait()            # nothing in flight
+        a.iterate_async(1.0)
+        for call in (lambda: a.iterate(1.0), lambda: a.iterate_async(1.0), a.proposal):
+            with pytest.raises(P.PmcgError) as e:
+                call()                  # one iteration in flight: other calls are refused
+            assert e.value.code == -9008
+        a.iterate_wait()
+        a2.iterate(1.0)
+        for u, v in zip(a.proposal().arrays(), a2.proposal().arrays()):
+            assert np.array_equal(u, v)
         for r in (a, b, a2, b2):
             r.free()
