@@ -456,6 +456,7 @@ static bool batch_bind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **
       set_error(err, PMCG_EARG, __LINE__, "batch run %d: an asynchronous iteration was not waited for", r);
       return false;
     }
+    run->img_stale = true;                  // the batch's updates leave the operand image behind
     const Work &w = run->w;
     const Plugin &pl = run->post->plugins[0];
     BatchDesc &d = hd[r];

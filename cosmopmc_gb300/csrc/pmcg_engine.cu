@@ -859,6 +859,10 @@ namespace pmcg {
 static bool run_launch(pmcg_run *r, double beta, error **err) {
   Work &w = r->w;
   w.launches = 0;
+  if (r->img_stale) {
+    if (w.prop.bimg && !CK(launch_umma_bimage(w.prop.view(), w.prop.bimg, w.s), "operand image")) return false;
+    r->img_stale = false;
+  }
   const bool stages = r->timing == 1;
   if (w.prec == PMCG_MIXED && !stages && !r->graph_off) {
     if (r->gexec && r->graph_tc != g_use_tensor_cores) drop_run_graph(r);

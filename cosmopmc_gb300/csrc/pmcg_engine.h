@@ -108,6 +108,9 @@ struct pmcg_run {
   // (pending_graph); pmcg_run_iterate_async's launch and its outcome.
   bool pending_graph = false;
   bool launched = false, launch_ok = false;
+  // the proposal was updated by a batch, which keeps no tensor-core operand
+  // image: rebuilt before the run's next iteration alone
+  bool img_stale = false;
   error *launch_err = nullptr;
   // Dead components (sdead_comp, exec/cosmo_pmc.c:239-284): buried (default) or
   // revived after each update; the box on the host for the revival's shifts.

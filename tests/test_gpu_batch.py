@@ -186,3 +186,27 @@ def test_batch_rebind_equals_fresh_batches(pmcg):
     assert b.iterate() == f3.iterate()
     for x in (b, f1, f2, f3):
         x.free()
+
+
+def test_run_alone_after_a_batch_uses_the_updated_proposal(pmcg):
+    """A batch updates its runs' proposals without their tensor-core operand
+    image; a run iterated alone afterwards with the tensor cores rebuilds it:
+    its iteration equals that of a twin whose proposal was set again from the
+    host (which rebuilds everything from the FP64 proposal)."""
+    P = pmcg
+    kind, D, K, N, seed = SPECS[3]          # a 20-dimensional mixture
+    prop, post, box = make_run(P, kind, D, K, N, seed)
+    a, b = (P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box) for _ in range(2))
+    ba, bb = P.Batch([a]), P.Batch([b])
+    for _ in range(2):
+        assert ba.iterate() == bb.iterate()
+    ba.free()
+    bb.free()
+    b.set_proposal(b.proposal())
+    P.set_tensor_cores(True)
+    sa, sb = a.iterate(1.0), b.iterate(1.0)
+    assert sa == sb
+    for u, v in zip(a.proposal().arrays(), b.proposal().arrays()):
+        assert np.array_equal(u, v)
+    a.free()
+    b.free()
