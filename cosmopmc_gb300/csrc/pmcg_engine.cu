@@ -129,10 +129,13 @@ static bool stage_draw(Work &w, bool box, uint64_t seed, uint32_t call, error **
             "draw kernel");
 }
 
+// The handle's tensor-core setting, else the process default.
+static int tc_on(const Work &w) { return w.tc >= 0 ? w.tc : g_use_tensor_cores; }
+
 // Single-precision mixture log-density on the tensor cores (tcgen05) when the
 // switch is on and the mixture carries an operand image (D <= 32).
 static bool use_tensor_cores(const Work &w, const DevMix &m) {
-  return w.prec == 1 && g_use_tensor_cores && m.bimg != nullptr && m.D <= 32;
+  return w.prec == 1 && tc_on(w) && m.bimg != nullptr && m.D <= 32;
 }
 
 static bool stage_logq(Work &w, error **err) {
@@ -169,7 +172,7 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
       if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "SN kernel"))
         return false;
     } else if (pl.type == kPluginTpl) {
-      if (w.prec == 1 && g_use_tensor_cores && pl.tpl.uimg) {
+      if (w.prec == 1 && tc_on(w) && pl.tpl.uimg) {
         if (!CK(launch_tpl_umma(pl.tpl.uimg, pl.tpl.Dpar, w.N, w.X32, w.ldx, w.logpost, w.flg, &w.dstats->tc_err,
                                 w.s),
                 "tensor-core template kernel"))
@@ -847,7 +850,7 @@ static bool capture_run_graph(pmcg_run *r) {
     cudaGetLastError();  // the failed capture is not an error of the run
     return false;
   }
-  r->graph_tc = g_use_tensor_cores;
+  r->graph_tc = tc_on(w);
   r->graph_launches = w.launches;
   return true;
 }
@@ -865,7 +868,7 @@ static bool run_launch(pmcg_run *r, double beta, error **err) {
   }
   const bool stages = r->timing == 1;
   if (w.prec == PMCG_MIXED && !stages && !r->graph_off) {
-    if (r->gexec && r->graph_tc != g_use_tensor_cores) drop_run_graph(r);
+    if (r->gexec && r->graph_tc != tc_on(w)) drop_run_graph(r);
     if (!r->gexec && !capture_run_graph(r)) r->graph_off = true;
   }
   r->pending_graph = false;
@@ -1246,11 +1249,18 @@ static void mirror_delete(SimMirror *m) {
 
 static std::mutex g_mu;
 static std::unordered_map<const pmc_simu *, SimMirror *> g_sims;
+// Per-sample settings of the drop-in entry points (-1: the process default).
+struct SimSettings {
+  int prec = -1, tc = -1;
+};
+static std::unordered_map<const pmc_simu *, SimSettings> g_sim_set;
 
 static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error **err) {
   std::lock_guard<std::mutex> lk(g_mu);
   SimMirror *&m = g_sims[psim];
-  const int prec = g_dropin_precision;
+  const auto set = g_sim_set.find(psim);
+  const SimSettings ss = set == g_sim_set.end() ? SimSettings() : set->second;
+  const int prec = ss.prec >= 0 ? ss.prec : g_dropin_precision;
   if (m && (m->w.K != K || m->w.D != D || m->w.df != df || m->w.N != psim->nsamples || m->w.prec != prec)) {
     mirror_delete(m);
     m = nullptr;
@@ -1270,6 +1280,7 @@ static SimMirror *mirror_for(const pmc_simu *psim, int K, int D, int df, error *
       return nullptr;
     }
   }
+  m->w.tc = ss.tc;
   return m;
 }
 
@@ -1289,6 +1300,7 @@ static SimMirror *mirror_any(const pmc_simu *psim, error **err) {
 
 void forget_simu(const pmc_simu *p) {
   std::lock_guard<std::mutex> lk(g_mu);
+  g_sim_set.erase(p);
   auto it = g_sims.find(p);
   if (it == g_sims.end()) return;
   mirror_delete(it->second);
@@ -1382,6 +1394,39 @@ extern "C" int pmcg_set_tensor_cores(int on) {
   const int prev = g_use_tensor_cores;
   g_use_tensor_cores = on ? 1 : 0;
   return prev;
+}
+
+extern "C" int pmcg_run_set_tensor_cores(pmcg_run *r, int on, error **err) {
+  if (!r || on < -1 || on > 1) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_run_set_tensor_cores: on is 1, 0 or -1");
+    return -2;
+  }
+  if (run_in_flight(r, err, "pmcg_run_set_tensor_cores")) return -2;
+  const int prev = r->w.tc;
+  r->w.tc = on;
+  return prev;
+}
+
+extern "C" void pmcg_simu_set_precision(const pmc_simu *psim, int precision, error **err) {
+  if (!psim || (precision != -1 && precision != PMCG_FP64 && precision != PMCG_MIXED)) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_simu_set_precision: PMCG_FP64, PMCG_MIXED or -1");
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_sim_set[psim].prec = precision;   // a mirror of another precision is replaced at its next use
+}
+
+extern "C" void pmcg_simu_set_tensor_cores(const pmc_simu *psim, int on, error **err) {
+  if (!psim || on < -1 || on > 1) {
+    set_error(err, PMCG_EARG, __LINE__, "pmcg_simu_set_tensor_cores: on is 1, 0 or -1");
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_sim_set[psim].tc = on;
+  }
+  // whatever was evaluated ahead with the other kernel is evaluated again
+  pmcg_simu_host_modified(const_cast<pmc_simu *>(psim));
 }
 
 extern "C" void pmcg_simu_host_modified(pmc_simu *psim) {

@@ -37,6 +37,7 @@ struct Plugin {
 // Buffers and scratch for one sample of N points (one run or one drop-in mirror).
 struct Work {
   int K = 0, D = 0, df = -1, prec = 0, ldx = 0, S = 0;
+  int tc = -1;   // tensor cores for this handle: 1 on, 0 off, -1 the process default
   size_t N = 0;
   cudaStream_t s = nullptr;
   DevMix prop;

@@ -183,6 +183,8 @@ SIGNATURES = [
     ("evidence", C.c_double, [C.POINTER(PmcSimuS), _dp, PErr]),
     ("get_tempering_beta", C.c_double, [C.c_int, C.c_int, C.c_double, C.c_int, PErr]),
     ("pmcg_simu_host_modified", None, [C.POINTER(PmcSimuS)]),
+    ("pmcg_simu_set_precision", None, [C.POINTER(PmcSimuS), C.c_int, PErr]),
+    ("pmcg_simu_set_tensor_cores", None, [C.POINTER(PmcSimuS), C.c_int, PErr]),
     ("pmcg_set_dropin_precision", None, [C.c_int]),
     ("pmcg_set_tensor_cores", C.c_int, [C.c_int]),
     ("pmcg_posterior_alloc", C.c_void_p, [C.c_int, _dp, _dp, PErr]),
@@ -209,6 +211,7 @@ SIGNATURES = [
     ("pmcg_run_get_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_run_get_sample", None, [C.c_void_p, C.POINTER(PmcSimuS), PErr]),
     ("pmcg_run_set_dead_comp", None, [C.c_void_p, C.c_int, C.c_double, PErr]),
+    ("pmcg_run_set_tensor_cores", C.c_int, [C.c_void_p, C.c_int, PErr]),
     ("pmcg_run_set_proposal", None, [C.c_void_p, C.POINTER(MixMvdensS), PErr]),
     ("pmcg_run_free", None, [C.POINTER(C.c_void_p)]),
     ("pmcg_run_set_timing", None, [C.c_void_p, C.c_int]),
@@ -424,6 +427,16 @@ class PmcSimu:
 
     def host_modified(self):
         load().pmcg_simu_host_modified(self.p)
+
+    def set_precision(self, prec):
+        """Precision of the drop-in calls on this sample (FP64, MIXED, or -1:
+        the process default of set_dropin_precision)."""
+        call("pmcg_simu_set_precision", self.p, int(prec))
+
+    def set_tensor_cores(self, on):
+        """Tensor cores for the drop-in calls on this sample (True / False, or
+        None: the process default)."""
+        call("pmcg_simu_set_tensor_cores", self.p, -1 if on is None else (1 if on else 0))
 
     def write(self, path, par_names=None):
         """CosmoPMC sample file (out_pmc_simu_cosmo_pmc)."""
@@ -649,6 +662,12 @@ class Run:
     def set_dead_comp(self, mode, fshift=0.1):
         """DEAD_BURY (default) or DEAD_REVIVE (revive_comp, needs the run's box)."""
         call("pmcg_run_set_dead_comp", self.p, int(mode), float(fshift))
+
+    def set_tensor_cores(self, on):
+        """This run's tensor-core setting (True / False, or None: the process
+        default of set_tensor_cores); returns the previous one (None, 0 or 1)."""
+        prev = call("pmcg_run_set_tensor_cores", self.p, -1 if on is None else (1 if on else 0))
+        return None if prev < 0 else prev
 
     def set_proposal(self, m: MixMvdens):
         call("pmcg_run_set_proposal", self.p, m.p)

@@ -281,15 +281,25 @@ void pmcg_weighted_hist2d(pmc_simu *psim, int nbin, int p, int q, const double *
                           double *hist, error **err);
 
 /* Precision of the drop-in entry points above: PMCG_FP64 (default, the
- * plain FP64 path) or PMCG_MIXED. */
+ * plain FP64 path) or PMCG_MIXED. Process-wide default for every sample that
+ * has no setting of its own (pmcg_simu_set_precision). */
 void pmcg_set_dropin_precision(int precision);
+/* Per sample (the drop-in's handle, as the reference's pmc_simu is its
+ * iteration state): the precision of the drop-in calls on psim (PMCG_FP64,
+ * PMCG_MIXED, or -1 for the process default) and its tensor-core setting
+ * (1, 0, or -1 for the process default; changing it re-evaluates whatever was
+ * computed ahead). Kept until pmc_simu_free. Two samples in one process can
+ * run at different precisions. PMCG_EARG for other values. */
+void pmcg_simu_set_precision(const pmc_simu *psim, int precision, error **err);
+void pmcg_simu_set_tensor_cores(const pmc_simu *psim, int on, error **err);
 
 /* Single-precision (PMCG_MIXED) mixture log-densities with D <= 32 on the
  * tensor cores: tcgen05 TF32 products in three-term split form, TMEM
  * accumulators (1 = on, the default; 0 = the CUDA-core kernel). Batched runs
  * (pmcg_batch_*, the serving loop) always use the CUDA-core kernel, so a run
  * alone reproduces its batched results bit for bit with 0. Returns the
- * previous setting. No counterpart in the reference (a GPU execution choice). */
+ * previous setting. No counterpart in the reference (a GPU execution choice).
+ * Process-wide default for every run without a setting of its own. */
 int pmcg_set_tensor_cores(int on);
 
 /* ------------------------------------------------------------------ *
@@ -547,6 +557,11 @@ void pmcg_run_get_sample(pmcg_run *r, pmc_simu *psim, error **err);
 #define PMCG_DEAD_BURY   0
 #define PMCG_DEAD_REVIVE 1
 void pmcg_run_set_dead_comp(pmcg_run *r, int mode, double fshift, error **err);
+/* The run's tensor-core setting (1, 0, or -1: the process default of
+ * pmcg_set_tensor_cores); returns the previous one (-2 with PMCG_EARG for
+ * another value or while an asynchronous iteration is in flight). Two runs in
+ * one process can use different settings. */
+int pmcg_run_set_tensor_cores(pmcg_run *r, int on, error **err);
 void pmcg_run_free(pmcg_run **r);
 /* Timing with CUDA events on the run's stream. on = 1: per stage (draw,
  * logq, logpost, weights, em; every kernel launched directly), read with

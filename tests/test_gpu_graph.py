@@ -112,3 +112,39 @@ def test_async_iterations_equal_synchronous(pmcg):
             assert np.array_equal(u, v)
         for r in (a, b, a2, b2):
             r.free()
+
+
+def test_tensor_core_setting_per_run(pmcg):
+    """pmcg_run_set_tensor_cores: two runs in one process with different
+    settings; each equals a run that follows the process default set to its
+    own setting (and None returns a run to the default)."""
+    P = pmcg
+    wl = W.mixture_workload(D=16, K=8, Kt=3, nu=4, seed=8, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = P.MixMvdens.from_arrays(w, mu, cov=cov, df=df).cholesky()
+    target = P.MixMvdens.from_arrays(wt, mut, cov=covt, df=-1).cholesky()
+    post = P.Posterior(16).add_mix(target)
+    prev = P.set_tensor_cores(False)
+    try:
+        on, off = (P.Run(prop, post, 20000, precision=P.MIXED, seed=3) for _ in range(2))
+        assert on.set_tensor_cores(True) is None
+        off.set_tensor_cores(False)
+        P.set_tensor_cores(True)              # the default no longer decides for these two
+        s_on = [on.iterate(1.0) for _ in range(2)]
+        s_off = [off.iterate(1.0) for _ in range(2)]
+        ref = {}
+        for flag in (True, False):
+            P.set_tensor_cores(flag)
+            r = P.Run(prop, post, 20000, precision=P.MIXED, seed=3)
+            ref[flag] = ([r.iterate(1.0) for _ in range(2)], r.proposal().arrays())
+            r.free()
+        assert s_on == ref[True][0] and s_off == ref[False][0]
+        assert s_on != s_off                  # the two kernels round differently
+        for x, y in zip(on.proposal().arrays(), ref[True][1]):
+            assert np.array_equal(x, y)
+        assert off.set_tensor_cores(None) == 0
+        for r in (on, off):
+            r.free()
+    finally:
+        P.set_tensor_cores(prev)

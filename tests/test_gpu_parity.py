@@ -549,3 +549,45 @@ def test_dropin_speculation_equals_fresh_sequence(pmcg):
                 np.testing.assert_array_equal(x, y, err_msg=f"iteration {it} proposal")
     finally:
         P.set_dropin_precision(P.FP64)
+
+
+def test_dropin_precision_per_sample(pmcg):
+    """pmcg_simu_set_precision: with the process default single precision, a
+    sample set to FP64 gives what a sample under the FP64 default gives, bit
+    for bit, while another sample in the same process stays single precision."""
+    P = pmcg
+    wl = W.mixture_workload(D=6, K=3, Kt=2, nu=-1, seed=31, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    post = P.Posterior(6).add_mix(make_mix(P, wt, mut, covt, -1))
+    N = 5000
+
+    def one(sim, prec=None):
+        m = make_mix(P, w, mu, cov, df)
+        if prec is not None:
+            sim.set_precision(prec)
+        r = P.Rng(5)
+        P.simulate_mix_mvdens(sim, m, r, None)
+        P.importance_weights(sim, m, post, 1.0)
+        ls = P.normalize_importance_weight(sim)
+        P.update_prop_rb(m, sim)
+        return sim.X.copy(), sim.weights.copy(), ls, m.arrays()
+
+    try:
+        P.set_dropin_precision(P.FP64)
+        ref64 = one(P.PmcSimu(N, 6))
+        P.set_dropin_precision(P.MIXED)
+        ref32 = one(P.PmcSimu(N, 6))
+        a = one(P.PmcSimu(N, 6), P.FP64)
+        b = one(P.PmcSimu(N, 6))
+        for x, y in ((a, ref64), (b, ref32)):
+            np.testing.assert_array_equal(x[0], y[0])
+            np.testing.assert_array_equal(x[1], y[1])
+            assert x[2] == y[2]
+            for u, v in zip(x[3], y[3]):
+                np.testing.assert_array_equal(u, v)
+        assert not np.array_equal(a[1], b[1])
+        with pytest.raises(P.PmcgError):
+            P.PmcSimu(N, 6).set_precision(7)
+    finally:
+        P.set_dropin_precision(P.FP64)
