@@ -38,9 +38,9 @@ WORKLOAD = "mixture microbench: D=32, K=64 Student-t nu=3 (cond 1e6), 16-comp Ga
 
 # DRAM traffic of one launch of the tensor-core proposal log-density at the
 # mixture workload (N = 2^20): dram__bytes_read.sum + dram__bytes_write.sum of
-# one ncu capture at N = 262144 (34.20 + 75.77 MB), scaled by 4 (traffic grows
+# one ncu capture at N = 262144 (34.18 + 75.62 MB), scaled by 4 (traffic grows
 # with N).
-UMMA_TRAFFIC_BYTES = 4 * (34.20e6 + 75.77e6)
+UMMA_TRAFFIC_BYTES = 4 * (34.18e6 + 75.62e6)
 
 
 def parse():
