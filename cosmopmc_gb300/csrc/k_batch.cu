@@ -19,9 +19,10 @@
 //
 // The launches, the upload of the per-iteration parameters (random-stream
 // call, beta) and the download of every run's statistics are captured once in
-// a CUDA graph. The samples per thread of the log-density stages and the resident
-// blocks per SM are picked by an autotuner that times the non-mutating stages
-// (draw, log q, log posterior) and caches the choice per batch shape.
+// a CUDA graph. The grouped SN kernel's block size, the samples per thread of the
+// log-density stages and the resident blocks per SM are picked by an autotuner
+// that times the non-mutating stages (draw, log q, log posterior) and caches the
+// choice per batch shape.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -204,20 +205,21 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const BatchDesc *__restri
 }
 
 // The SN log-posterior of every SN run of the batch, one warp per sample, at
-// the standalone SN kernel's shape (128 threads, no register cap: many more
-// resident warps than the persistent kernel's two 256-thread blocks per SM,
-// which this latency-bound body needs). Launched between the cooperative
-// launch of the draw and log q stages and the one of the remaining stages;
-// the same body as the runs alone, so the same values.
-constexpr int kBSnThreads = 128;
-__global__ void __launch_bounds__(kBSnThreads) batch_sn_kernel(const BatchDesc *__restrict__ descs, int R,
-                                                               const uint32_t *__restrict__ pre) {
+// the standalone SN kernel's shape (no register cap: many more resident warps
+// than the persistent kernel's two 256-thread blocks per SM, which this
+// latency-bound body needs); THREADS (64, 128 or 256) is picked by the
+// autotuner. Launched between the cooperative launch of the draw and log q
+// stages and the one of the remaining stages; the same body as the runs
+// alone, so the same values whatever the block size.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) batch_sn_kernel(const BatchDesc *__restrict__ descs, int R,
+                                                           const uint32_t *__restrict__ pre) {
   const uint32_t item = blockIdx.x;
   if (item >= pre[R]) return;
   const int r = find_run(pre, R, item);
   const SnDev sn = descs[r].sn;   // by value, as the standalone kernel's parameter
   const BatchDesc &d = descs[r];
-  const size_t n = (size_t)(item - pre[r]) * (kBSnThreads / 32) + (threadIdx.x >> 5);
+  const size_t n = (size_t)(item - pre[r]) * (THREADS / 32) + (threadIdx.x >> 5);
   body_sn<true>(sn, d.N, d.prop.D, nullptr, d.X32, d.prop.ldx, d.logpost, d.flg, n, 1, d.logpr);
 }
 
@@ -270,7 +272,10 @@ struct TuneKey {
   bool operator<(const TuneKey &o) const { return shape < o.shape; }
 };
 static std::mutex g_tune_mu;
-static std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+struct TuneChoice {
+  int spt, bps, snt;   // samples per thread, blocks per SM, SN kernel threads per block
+};
+static std::map<TuneKey, TuneChoice> g_tune_cache;
 
 }  // namespace pmcg
 
@@ -289,6 +294,7 @@ struct pmcg_batch {
   cudaStream_t s = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int spt = 2, bps = 1, grid = 0, sms = 0, threads = 256;
+  int snt = 128;          // threads per block of the grouped SN kernel
   size_t smem = 0;
   cudaGraphExec_t gexec = nullptr;
   bool graph = false;
@@ -331,12 +337,19 @@ static cudaError_t launch_coop(pmcg_batch *b, int first, int last) {
 }
 
 // Stages first..last; the log-posterior stage's SN items run in the SN kernel.
+// The grouped SN kernel at the batch's block size.
+static cudaError_t launch_sn_group(pmcg_batch *b) {
+  if (b->snt == 64) batch_sn_kernel<64><<<b->sn_items, 64, 0, b->s>>>(b->d_desc, b->R, b->d_snpre);
+  else if (b->snt == 256) batch_sn_kernel<256><<<b->sn_items, 256, 0, b->s>>>(b->d_desc, b->R, b->d_snpre);
+  else batch_sn_kernel<128><<<b->sn_items, 128, 0, b->s>>>(b->d_desc, b->R, b->d_snpre);
+  return cudaGetLastError();
+}
+
 static cudaError_t launch_any(pmcg_batch *b, int first, int last) {
   if (b->sn_items == 0 || first > kBLogpost || last < kBLogpost) return launch_coop(b, first, last);
   cudaError_t e = cudaSuccess;
   if (first < kBLogpost && (e = launch_coop(b, first, kBLogpost - 1)) != cudaSuccess) return e;
-  batch_sn_kernel<<<b->sn_items, kBSnThreads, 0, b->s>>>(b->d_desc, b->R, b->d_snpre);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_sn_group(b)) != cudaSuccess) return e;
   return launch_coop(b, kBLogpost, last);
 }
 
@@ -364,7 +377,8 @@ static bool batch_configure(pmcg_batch *b, int spt, int bps, error **err) {
     for (int r = 0; r < b->R; r++) {
       sp[r] = (uint32_t)acc;
       const BatchDesc &d = b->hdesc[r];
-      if (d.ptype == kPluginSn) acc += (d.N + kBSnThreads / 32 - 1) / (kBSnThreads / 32);
+      const int wpb = b->snt / 32;    // samples (warps) per block
+      if (d.ptype == kPluginSn) acc += (d.N + wpb - 1) / wpb;
     }
     if (acc > 0x7FFFFFF0ull) {
       set_error(err, PMCG_EDIM, __LINE__, "batch too large: %llu SN work items", (unsigned long long)acc);
@@ -528,6 +542,7 @@ static bool batch_bind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **
   }
   // a tuned configuration for this shape, if any
   int spt = 2, bps = 1;
+  b->snt = 128;
   {
     TuneKey key;
     for (const BatchDesc &d : b->hdesc) {
@@ -536,7 +551,7 @@ static bool batch_bind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **
     }
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
-    if (it != g_tune_cache.end()) { spt = it->second.first; bps = it->second.second; }
+    if (it != g_tune_cache.end()) { spt = it->second.spt; bps = it->second.bps; b->snt = it->second.snt; }
   }
   ok = ok && batch_configure(b, spt, bps, err);
   b->iters_bound = 0;
@@ -634,6 +649,31 @@ extern "C" void pmcg_batch_autotune(pmcg_batch *b, error **err) {
   const int bpss[3] = {1, 2, 4};
   float best = 1e30f;
   int bspt = b->spt, bbps = b->bps;
+  // The grouped SN kernel's block size (its time does not depend on the other
+  // two knobs): timed alone, three times per candidate, the last two kept. It
+  // rewrites the SN runs' log-posteriors of the current sample (the same values).
+  if (b->sn_items > 0) {
+    const int snts[3] = {64, 128, 256};
+    float sbest = 1e30f;
+    int bsnt = b->snt;
+    for (int ti = 0; ti < 3; ti++) {
+      error *e = nullptr;
+      b->snt = snts[ti];
+      if (!batch_configure(b, b->spt, b->bps, &e)) { purgeError(&e); continue; }
+      float tmin = 1e30f;
+      for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(b->e0, b->s);
+        cudaError_t ce = launch_sn_group(b);
+        cudaEventRecord(b->e1, b->s);
+        if (ce != cudaSuccess || cudaStreamSynchronize(b->s) != cudaSuccess) { tmin = 1e30f; cudaGetLastError(); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->e0, b->e1);
+        if (rep > 0) tmin = std::min(tmin, ms);
+      }
+      if (tmin < sbest) { sbest = tmin; bsnt = snts[ti]; }
+    }
+    b->snt = bsnt;
+  }
   // Time draw..log posterior (they only overwrite the sample buffers, which
   // the next iteration redraws): twice per candidate, keep the faster.
   for (int si = 0; si < 2; si++) {
@@ -662,7 +702,7 @@ extern "C" void pmcg_batch_autotune(pmcg_batch *b, error **err) {
       key.shape.push_back((long long)d.N); key.shape.push_back(d.ptype);
     }
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = {b->spt, b->bps};
+    g_tune_cache[key] = {b->spt, b->bps, b->snt};
   }
   capture_graph(b);
 }
@@ -676,6 +716,8 @@ extern "C" void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, 
 }
 
 extern "C" double pmcg_batch_last_ms(const pmcg_batch *b) { return b->last_ms; }
+
+extern "C" int pmcg_batch_sn_block(const pmcg_batch *b) { return b ? b->snt : 0; }
 
 extern "C" void pmcg_batch_set_stage_timing(pmcg_batch *b, int on) {
   if (b) b->stage_timing = on != 0;

@@ -225,6 +225,7 @@ SIGNATURES = [
     ("pmcg_batch_autotune", None, [C.c_void_p, PErr]),
     ("pmcg_batch_config", None, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)]),
+    ("pmcg_batch_sn_block", C.c_int, [C.c_void_p]),
     ("pmcg_batch_last_ms", C.c_double, [C.c_void_p]),
     ("pmcg_batch_set_stage_timing", None, [C.c_void_p, C.c_int]),
     ("pmcg_batch_stage_ms", C.c_int, [C.c_void_p, _dp]),
@@ -741,7 +742,8 @@ class Batch:
     def config(self):
         v = [C.c_int() for _ in range(4)]
         load().pmcg_batch_config(self.p, *[C.byref(x) for x in v])
-        return dict(samples_per_thread=v[0].value, blocks_per_sm=v[1].value, grid=v[2].value, graph=v[3].value)
+        return dict(samples_per_thread=v[0].value, blocks_per_sm=v[1].value, grid=v[2].value, graph=v[3].value,
+                    sn_threads=load().pmcg_batch_sn_block(self.p))
 
     def last_ms(self):
         return load().pmcg_batch_last_ms(self.p)

@@ -607,11 +607,14 @@ void pmcg_batch_rebind(pmcg_batch *b, int nruns, pmcg_run *const *runs, error **
  * iterated alone: give the run a new proposal (pmcg_run_set_proposal) before
  * iterating it again, or its later iterations report PMCG_ENOWEIGHT. */
 void pmcg_batch_iterate(pmcg_batch *b, const double *betas, pmcg_iter_stats *stats, error **err);
-/* Time the non-mutating stages under each candidate (samples per thread of
- * the log-density stages, resident blocks per SM), keep the fastest and
- * cache it for batches of the same shape. */
+/* Time the non-mutating stages under each candidate (the grouped SN
+ * kernel's threads per block: 64, 128, 256; samples per thread of the
+ * log-density stages; resident blocks per SM), keep the fastest and cache it
+ * for batches of the same shape. Results do not depend on the choice. */
 void pmcg_batch_autotune(pmcg_batch *b, error **err);
 void pmcg_batch_config(const pmcg_batch *b, int *samples_per_thread, int *blocks_per_sm, int *grid, int *graph);
+/* Threads per block of the grouped SN kernel (the autotuner's third knob). */
+int pmcg_batch_sn_block(const pmcg_batch *b);
 double pmcg_batch_last_ms(const pmcg_batch *b);
 /* Stage timing (profiling): while on, each iteration launches its stages one
  * by one (same stages, same results) with CUDA events between them;
