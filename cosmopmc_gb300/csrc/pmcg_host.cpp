@@ -449,16 +449,17 @@ extern "C" void pmcg_out_pmc_simu_names(const char *name, const pmc_simu *psim, 
 // start with '#'). The weights come back normalised (isLog = 0) with logSum
 // and maxW of the file's unnormalised log-weights, every row counted (flg = 1)
 // and the component index restored from the second column. proposal, when
-// given, must match npar; clipping (nclipw > 0) is not provided.
+// given, must match npar. nclipw > 0: then clip_weights(psim, nclipw) (the
+// nclipw largest weights flagged out, the rest renormalised), as the resumed
+// run of exec/cosmo_pmc.c:416-417 asks with the run's nclipw.
 extern "C" pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, const mix_mvdens *proposal,
                                         int nclipw, error **err) {
   if (!f || npar < 1 || nsamples == 0) {
     set_error(err, PMCG_EARG, __LINE__, "pmc_simu_from_file: invalid arguments");
     return nullptr;
   }
-  if (nclipw > 0) {
-    set_error(err, PMCG_EUNSUPPORTED, __LINE__, "pmc_simu_from_file: weight clipping (nclipw = %d) is not provided",
-              nclipw);
+  if (nclipw < 0) {
+    set_error(err, PMCG_EARG, __LINE__, "pmc_simu_from_file: nclipw = %d", nclipw);
     return nullptr;
   }
   if (proposal && proposal->ndim != npar) {
@@ -511,6 +512,19 @@ extern "C" pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int 
   p->maxW = mx;
   p->nok = n;
   pmcg_simu_host_modified(p);
+  if (nclipw > 0) {
+    error *e = nullptr;
+    clip_weights(p, nclipw, nullptr, &e);
+    if (isError(e)) {
+      if (err && !*err) *err = e;
+      else purgeError(&e);
+      pmc_simu_free(&p);
+      return nullptr;
+    }
+    size_t nok = 0;
+    for (size_t i = 0; i < n; i++) nok += p->flg[i] != 0;
+    p->nok = nok;
+  }
   return p;
 }
 

@@ -447,13 +447,14 @@ class PmcSimu:
         call("pmcg_out_pmc_simu_names", str(path).encode(), self.p, names)
 
     @classmethod
-    def read(cls, path, nsamples, ndim, n_ded=0):
-        """pmc_simu_from_file: normalised weights (isLog = 0), logSum, indices."""
+    def read(cls, path, nsamples, ndim, n_ded=0, nclipw=0):
+        """pmc_simu_from_file: normalised weights (isLog = 0), logSum, indices;
+        nclipw > 0: the nclipw largest weights clipped (clip_weights)."""
         f = _libc().fopen(str(path).encode(), b"r")
         if not f:
             raise OSError(f"cannot open {path}")
         try:
-            p = call("pmc_simu_from_file", f, nsamples, ndim, n_ded, None, 0)
+            p = call("pmc_simu_from_file", f, nsamples, ndim, n_ded, None, int(nclipw))
         finally:
             _libc().fclose(f)
         obj = cls.__new__(cls)

@@ -129,7 +129,10 @@ typedef struct {
   int ndim;
   int n_ded;
   double *X;         /* [nsamples*ndim] row-major */
-  double *X_ded;     /* [nsamples*n_ded] (deduced parameters; not filled by the device path) */
+  double *X_ded;     /* [nsamples*n_ded] deduced parameters: left as they are by the device path,
+                        as the reference's retrieve_ded leaves them for the likelihoods that path
+                        evaluates (SNIa, Mvdens and MixMvdens register no deduced function:
+                        wrappers/src/sn.c:14, wrappers/src/param.c:1446-1447,1499-1500) */
   double *weights;   /* log-weights when isLog==1, normalised weights when isLog==0 */
   short *flg;        /* 1 = sample counts; 0 = outside the prior box or likelihood error */
   int *indices;      /* component each sample was drawn from */
@@ -161,7 +164,8 @@ void pmcg_out_pmc_simu_names(const char *name, const pmc_simu *psim, const char 
 /* Reads such a file (at most nsamples rows; exec/importance_sample.c:198,
  * exec/cosmo_pmc.c:416): weights normalised (isLog = 0, logSum, maxW of the
  * file's log-weights), flg = 1, indices from the second column. proposal
- * (optional) must match npar; nclipw > 0 is rejected (clipping not provided). */
+ * (optional) must match npar. nclipw > 0 then applies clip_weights(psim,
+ * nclipw) (below): the resumed run's clipping (exec/cosmo_pmc.c:416-417). */
 pmc_simu *pmc_simu_from_file(FILE *f, size_t nsamples, int npar, int n_ded, const mix_mvdens *proposal, int nclipw,
                              error **err);
 void pmc_simu_realloc(pmc_simu *psim, size_t nsamples, error **err);                /* cosmo_pmc.c:313 */

@@ -182,7 +182,7 @@ def test_sample_file_roundtrip(pmcg, tmp_path):
     libc.fclose.argtypes = [C.c_void_p]
     f = libc.fopen(str(path).encode(), b"r")
     with pytest.raises(pmcg.PmcgError):
-        pmcg.call("pmc_simu_from_file", f, 100, D, 0, None, 2)  # weight clipping is not provided
+        pmcg.call("pmc_simu_from_file", f, 100, D, 0, None, -1)  # nclipw < 0
     libc.fclose(f)
 
 

@@ -299,3 +299,27 @@ def test_clip_weights_matches_oracle(pmcg, oracle, normalised):
         wb /= wb.sum()
         np.testing.assert_allclose(ps.weights[keep], wb, rtol=1e-12)
         assert ps.s.logSum == pytest.approx(m + np.log(np.sum(np.exp(logw[keep] - m))), rel=1e-12)
+
+
+def test_sample_file_read_with_clipping(pmcg, tmp_path):
+    """pmc_simu_from_file with nclipw > 0 (the resumed run of
+    exec/cosmo_pmc.c:416-417): the sample read back equals the same file read
+    without clipping and then clipped with clip_weights."""
+    rng = np.random.default_rng(12)
+    N, D, k = 4000, 3, 7
+    ps = pmcg.PmcSimu(N, D)
+    ps.X[:] = rng.normal(size=(N, D))
+    logw = rng.normal(size=N) * 2
+    ps.weights[:] = np.exp(logw - logw.max()) / np.sum(np.exp(logw - logw.max()))
+    ps.flg[:] = 1
+    ps.indices[:] = rng.integers(0, 5, N)
+    ps.s.isLog = 0
+    ps.s.logSum = logw.max() + np.log(np.sum(np.exp(logw - logw.max())))
+    path = tmp_path / "pmcsim"
+    ps.write(path)
+    a = pmcg.PmcSimu.read(path, N, D, nclipw=k)
+    b = pmcg.PmcSimu.read(path, N, D)
+    pmcg.clip_weights(b, k)
+    np.testing.assert_array_equal(a.flg, b.flg)
+    np.testing.assert_array_equal(a.weights, b.weights)
+    assert a.s.logSum == b.s.logSum and a.s.nok == N - k
