@@ -31,8 +31,8 @@ static cudaError_t draw_dispatch(const DevMixView &m, size_t N, uint64_t seed, u
   size_t smem = draw_smem<Real>(m.K, ldo, bs);
   unsigned grid = (unsigned)((N + bs - 1) / bs);
   if (grid == 0) return cudaSuccess;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(draw_kernel<MAXD, Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    cudaError_t e = allow_dyn_smem(draw_kernel<MAXD, Real>, smem);
     if (e != cudaSuccess) return e;
   }
   draw_kernel<MAXD, Real><<<grid, bs, smem, s>>>(m, N, (uint32_t)seed, (uint32_t)(seed >> 32), call, bmin, bmax,

@@ -250,6 +250,7 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
   if (precision == 0) {
     if (E > 10 * 256) return cudaErrorInvalidValue;
     size_t smem = (size_t)(kTile64 * D + 2 * kTile64) * sizeof(double);
+    if ((e = allow_dyn_smem(em_stats_f64_kernel, smem)) != cudaSuccess) return e;
     em_stats_f64_kernel<<<dim3(S, m.K), 256, smem, s>>>(v, N, S, X64, logw, logq, lt64, Q64, st, partials);
   } else {
     const int Da = m.ldx + 4, nb = Da / 4, NB = nb * (nb + 1) / 2;
@@ -266,20 +267,16 @@ cudaError_t launch_em(int precision, DevMix &m, size_t N, const double *X64, con
     size_t tb, rb;
     em32_layout(D, m.ldx, 256, &tb, &rb);
     size_t smem = tb > rb ? tb : rb;
-    if (smem > 48 * 1024) {
-      e = cudaFuncSetAttribute(em_stats_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-    }
+    if ((e = allow_dyn_smem(em_stats_f32_kernel, smem)) != cudaSuccess) return e;
     em_stats_f32_kernel<<<dim3(m.K, S), 256, smem, s>>>(v, N, S, X32, aw32, lt32, Q32, partials, emmask);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int whitened = precision != 0;
   size_t usmem = finalize_smem(D, whitened);
   if (prepare_smem(D) > usmem) usmem = prepare_smem(D);
-  if (usmem > 48 * 1024) {
-    e = cudaFuncSetAttribute(em_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usmem);
-    if (e != cudaSuccess) return e;
-  }
+  // its static shared memory (the last block's weight and cumulative arrays)
+  // counts against the default 48 KB too
+  if ((e = allow_dyn_smem(em_update_kernel, usmem)) != cudaSuccess) return e;
   em_update_kernel<<<m.K, 256, usmem, s>>>(m, N, S, partials, counts, band_limit, whitened, st);
   return cudaGetLastError();
 }

@@ -60,17 +60,11 @@ cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X
   cudaError_t e;
   if (precision == 0) {
     size_t smem = tpl_smem<double>(t.P, 128);
-    if (smem > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(tpl_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
-      return e;
+    if ((e = allow_dyn_smem(tpl_kernel<double>, smem)) != cudaSuccess) return e;
     tpl_kernel<double><<<grid, 128, smem, s>>>(t, N, X64, X32, ldx, logpost, flg);
   } else {
     size_t smem = tpl_smem<float>(t.P, 128);
-    if (smem > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(tpl_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
-      return e;
+    if ((e = allow_dyn_smem(tpl_kernel<float>, smem)) != cudaSuccess) return e;
     tpl_kernel<float><<<grid, 128, smem, s>>>(t, N, X64, X32, ldx, logpost, flg);
   }
   return cudaGetLastError();

@@ -84,10 +84,7 @@ cudaError_t devmix_prepare(DevMix &m, cudaStream_t s) {
   DevMixView v = m.view();
   const size_t smem = prepare_smem(m.D);
   cudaError_t e;
-  if (smem > 48 * 1024 &&
-      (e = cudaFuncSetAttribute(mix_prepare_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-          cudaSuccess)
-    return e;
+  if ((e = allow_dyn_smem(mix_prepare_comp_kernel, smem)) != cudaSuccess) return e;
   mix_prepare_comp_kernel<<<m.K, 256, smem, s>>>(v, m.logdetL, m.Wt, m.b, m.W32, m.b32, m.L32, m.mu32);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -172,8 +169,7 @@ __global__ void __launch_bounds__(128) mixlogpdf_f32_kernel(DevMixView m, size_t
 
 template <typename KernelT>
 static cudaError_t set_smem(KernelT k, size_t smem) {
-  if (smem > 48 * 1024) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaSuccess;
+  return allow_dyn_smem(k, smem);
 }
 
 // Components staged per barrier for the FP32 log-pdf (about 40 KB of L^-1).

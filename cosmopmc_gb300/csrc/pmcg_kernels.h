@@ -5,6 +5,17 @@
 #include <stdint.h>
 #include "pmcg_common.cuh"
 
+// Allows `dyn` bytes of dynamic shared memory for kernel `fn` when the kernel's
+// static shared memory plus `dyn` exceeds the 48 KB a launch gets by default.
+template <typename KernelT>
+inline cudaError_t allow_dyn_smem(KernelT fn, size_t dyn) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, (const void *)fn);
+  if (e != cudaSuccess) return e;
+  if (dyn + fa.sharedSizeBytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
 namespace pmcg {
 
 constexpr int kMaxD = 64;    // largest parameter dimension

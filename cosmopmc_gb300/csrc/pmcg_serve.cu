@@ -7,7 +7,8 @@
 // buffers its run allocates), binds the batch to the resident jobs when that
 // set changed, and runs one iteration of every resident job: the smaller jobs
 // in one persistent launch (k_batch.cu), jobs of at least alone_min_samples
-// samples with their own CUDA graphs on their own streams, concurrently. A job
+// samples and jobs the batch does not take (D > 32, several likelihoods) with
+// their own CUDA graphs on their own streams, concurrently. A job
 // that arrives while others are on the
 // GPU therefore joins the next epoch and overlaps with them. Each job's
 // arithmetic depends only on its own inputs, so its result is the same alone
@@ -40,6 +41,7 @@ struct Job {
   double tmin = 0.0;
   uint64_t seed = 0;
   size_t bytes = 0;
+  bool alone = false;                  // iterates on its own stream, not in the batch
   // progress
   pmcg_run *run = nullptr;
   int iter = 0;
@@ -161,9 +163,10 @@ static void server_loop(pmcg_server *s) {
     if ((int)s->active.size() > s->peak_jobs) s->peak_jobs = (int)s->active.size();
     // Jobs of at least alone_min_samples samples fill the GPU by themselves:
     // they iterate on their own streams (their CUDA graphs, the tensor-core
-    // kernels) beside the batch of the smaller ones.
+    // kernels) beside the batch of the smaller ones; so do the jobs the batch
+    // does not take (D > 32, or not exactly one likelihood).
     std::vector<Job *> small, large;
-    for (Job *j : s->active) (j->N >= s->opts.alone_min_samples ? large : small).push_back(j);
+    for (Job *j : s->active) (j->alone ? large : small).push_back(j);
     if (s->dirty) {
       // a job came or went: bind the batched set to the batch (its arrays are
       // kept). Run pointers are not compared: a new run may reuse a freed one's
@@ -278,8 +281,8 @@ extern "C" int64_t pmcg_server_submit(pmcg_server *s, const mix_mvdens *proposal
     set_error(err, PMCG_EARG, __LINE__, "pmcg_server_submit: invalid job");
     return 0;
   }
-  if (proposal->ndim > 32 || post->plugins.size() != 1) {
-    set_error(err, PMCG_EUNSUPPORTED, __LINE__, "served jobs need D <= 32 and exactly one likelihood");
+  if (proposal->ndim > kMaxD || post->plugins.empty()) {
+    set_error(err, PMCG_EUNSUPPORTED, __LINE__, "served jobs need D <= %d and a likelihood", kMaxD);
     return 0;
   }
   Job *j = new Job();
@@ -297,6 +300,9 @@ extern "C" int64_t pmcg_server_submit(pmcg_server *s, const mix_mvdens *proposal
   j->tempering = tempering;
   j->tmin = t_min;
   j->seed = seed;
+  // the batch takes D <= 32 and one likelihood; larger jobs, and the others,
+  // iterate alone beside it
+  j->alone = nsamples >= s->opts.alone_min_samples || proposal->ndim > 32 || post->plugins.size() != 1;
   j->bytes = work_bytes(proposal->ncomp, proposal->ndim, proposal->comp[0]->df, PMCG_MIXED, nsamples);
   std::lock_guard<std::mutex> lk(s->mu);
   if (j->bytes > s->opts.hbm_budget_bytes) {

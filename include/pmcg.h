@@ -640,7 +640,8 @@ void pmcg_batch_free(pmcg_batch **b);
  * size of its run's buffers); every epoch runs one iteration of all resident
  * jobs in one batch launch, so jobs that arrive while others run join the next
  * epoch and overlap with them. A job's result depends only on its own inputs
- * (same alone and in any mix). Served jobs: D <= 32, one likelihood. */
+ * (same alone and in any mix). Served jobs: D <= 64; jobs with D > 32 or other
+ * than one likelihood iterate alone beside the batch, as the large ones. */
 typedef struct pmcg_server pmcg_server;
 typedef struct {
   size_t hbm_budget_bytes;  /* 0: 80% of the free device memory at creation */
@@ -650,7 +651,7 @@ typedef struct {
   double fshift;            /* revival shift (0: 0.1) */
   size_t alone_min_samples; /* jobs of at least this many samples iterate with their own CUDA graph on
                                their own stream (tensor-core kernels), beside the batch of the others
-                               (0: 2^16; SIZE_MAX: every job batched) */
+                               (0: 2^16; SIZE_MAX: every job the batch takes is batched) */
 } pmcg_server_opts;
 typedef struct {
   int status;               /* 0 done, > 0 queued/running, < 0 PMCG_E* error */

@@ -591,3 +591,29 @@ def test_dropin_precision_per_sample(pmcg):
             P.PmcSimu(N, 6).set_precision(7)
     finally:
         P.set_dropin_precision(P.FP64)
+
+
+@pytest.mark.parametrize("D", [40, 64])
+def test_run_mixed_beyond_the_tensor_cores(pmcg, D):
+    """Single precision for 32 < D <= 64 (CUDA-core log-density, the whitened EM
+    with its larger shared-memory layout): whole iterations against the FP64
+    path on the same draws, |dlogZ| <= 1e-3 and the updated means within
+    0.05 sigma."""
+    P = pmcg
+    wl = W.mixture_workload(D=D, K=4, Kt=2, nu=5, seed=D, prop_hi=2.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = make_mix(P, w, mu, cov, df)
+    post = P.Posterior(D).add_mix(make_mix(P, wt, mut, covt, -1))
+    r64 = P.Run(prop, post, 60000, precision=P.FP64, seed=9)
+    r32 = P.Run(prop, post, 60000, precision=P.MIXED, seed=9)
+    for it in range(3):
+        s64, s32 = r64.iterate(1.0), r32.iterate(1.0)
+        assert abs(s64["ln_evidence"] - s32["ln_evidence"]) <= 1e-3, (it, s64, s32)
+        w64, mu64, L64 = r64.proposal().arrays()
+        w32, mu32, L32 = r32.proposal().arrays()
+        live = (w64 > 0) & (w32 > 0)
+        sd = np.sqrt(np.diagonal(np.einsum("kij,klj->kil", L64, L64), axis1=1, axis2=2))
+        assert np.max(np.abs(mu64[live] - mu32[live]) / sd[live]) < 0.05, it
+    r64.free()
+    r32.free()

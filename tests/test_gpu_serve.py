@@ -127,3 +127,29 @@ def test_large_job_alone_beside_the_batch(pmcg):
             assert a[key] == b[key], (key, a, b)
     for a, b in zip(prop_alone.arrays(), prop_split.arrays()):
         assert np.array_equal(a, b)
+
+
+def test_job_the_batch_does_not_take_runs_alone(pmcg):
+    """A job with D > 32 (beyond the batch's limit) is served alone beside the
+    batch of the others: it completes with the result of the same run iterated
+    alone, and the batched jobs are unaffected."""
+    P = pmcg
+    keep = []
+    wide = ("mix", 40, 3, 6000, 77)          # D = 40: the batch takes D <= 32
+    prop, post, box = _job(P, wide, keep)
+    run = P.Run(prop, post, wide[3], precision=P.MIXED, seed=wide[4], box=box)
+    ref = [run.iterate(P.get_tempering_beta(P.TEMPERING_NONE, it, 1.0, 3)) for it in range(3)]
+    ref_prop = run.proposal().arrays()
+    run.free()
+    small = [_job(P, spec, keep) for spec in MIX[:3]]
+    s = P.Server()
+    ids = [s.submit(pp, po, spec[3], 3, spec[4], box=bx) for spec, (pp, po, bx) in zip(MIX[:3], small)]
+    jw = s.submit(prop, post, wide[3], 3, wide[4], box=box)
+    res = [s.wait(i, timeout=120) for i in ids]
+    rw, pw = s.wait(jw, timeout=120, want_proposal=True)
+    s.free()
+    assert all(r["status"] == 0 for r in res)
+    assert rw["status"] == 0 and rw["iterations"] == 3
+    assert rw["ln_evidence"] == ref[-1]["ln_evidence"] and rw["ess"] == ref[-1]["ess"]
+    for a, b in zip(pw.arrays(), ref_prop):
+        assert np.array_equal(a, b)
