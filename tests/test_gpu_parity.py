@@ -617,3 +617,24 @@ def test_run_mixed_beyond_the_tensor_cores(pmcg, D):
         assert np.max(np.abs(mu64[live] - mu32[live]) / sd[live]) < 0.05, it
     r64.free()
     r32.free()
+
+
+def test_run_mixed_at_the_largest_component_count(pmcg):
+    """K = 256 components (the largest supported; 32 tensor-core component
+    groups): whole iterations of the mixed path against the FP64 path on the
+    same draws, |dlogZ| <= 1e-3."""
+    P = pmcg
+    D, K = 8, 256
+    wl = W.mixture_workload(D=D, K=K, Kt=8, nu=4, seed=256, prop_hi=1.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = make_mix(P, w, mu, cov, df)
+    post = P.Posterior(D).add_mix(make_mix(P, wt, mut, covt, -1))
+    r64 = P.Run(prop, post, 200000, precision=P.FP64, seed=4)
+    r32 = P.Run(prop, post, 200000, precision=P.MIXED, seed=4)
+    for it in range(2):
+        s64, s32 = r64.iterate(1.0), r32.iterate(1.0)
+        assert abs(s64["ln_evidence"] - s32["ln_evidence"]) <= 1e-3, (it, s64, s32)
+        assert abs(s64["ess"] - s32["ess"]) <= 1e-3 * s64["ess"], (it, s64, s32)
+    r64.free()
+    r32.free()
