@@ -210,3 +210,27 @@ def test_run_alone_after_a_batch_uses_the_updated_proposal(pmcg):
         assert np.array_equal(u, v)
     a.free()
     b.free()
+
+
+def test_batch_at_its_largest_shapes(pmcg):
+    """Runs at the batch's limits (D = 32 with K = 64 Student-t components, and
+    K = 256 components) batched with a small run: bit-identical to the same runs
+    alone with the CUDA-core kernels."""
+    P = pmcg
+    specs = [("mix", 32, 64, 6000, 41), ("mix", 4, 256, 9000, 42), ("mix", 3, 2, 1500, 43)]
+    keep, xs, ys = [], [], []
+    for kind, D, K, N, seed in specs:
+        prop, post, box = make_run(P, kind, D, K, N, seed)
+        keep.append((prop, post, box))
+        xs.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+        ys.append(P.Run(prop, post, N, precision=P.MIXED, seed=seed, box=box))
+    b = P.Batch(xs)
+    for it in range(2):
+        bst = b.iterate()
+        for r, run in enumerate(ys):
+            ast = run.iterate(1.0)
+            ast["status"] = 0
+            assert bst[r] == ast, (it, specs[r], bst[r], ast)
+            for u, v in zip(xs[r].proposal().arrays(), run.proposal().arrays()):
+                assert np.array_equal(u, v), (it, specs[r])
+    b.free()
