@@ -638,3 +638,38 @@ def test_run_mixed_at_the_largest_component_count(pmcg):
         assert abs(s64["ess"] - s32["ess"]) <= 1e-3 * s64["ess"], (it, s64, s32)
     r64.free()
     r32.free()
+
+
+@pytest.mark.parametrize("N", [1, 33, 257])
+def test_run_tiny_and_ragged_sample_sizes(pmcg, N):
+    """N below and just above one tensor-core tile of 256 samples: the mixed path
+    (tensor cores on) and the FP64 path on the same draws either both fail with
+    the same code (too few samples: every component buried) or agree on ln Z to
+    1e-3 and on the draws' component indices."""
+    P = pmcg
+    wl = W.mixture_workload(D=12, K=4, Kt=2, nu=3, seed=N, prop_hi=1.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    prop = make_mix(P, w, mu, cov, df)
+    post = P.Posterior(12).add_mix(make_mix(P, wt, mut, covt, -1))
+    prev = P.set_tensor_cores(True)
+    try:
+        r64 = P.Run(prop, post, N, precision=P.FP64, seed=N)
+        r32 = P.Run(prop, post, N, precision=P.MIXED, seed=N)
+        out = []
+        for r in (r64, r32):
+            try:
+                out.append(("ok", r.iterate(1.0), r.sample().indices.copy()))
+            except P.PmcgError as e:
+                out.append(("err", e.code, None))
+        (k64, a64, i64), (k32, a32, i32) = out
+        assert k64 == k32, (N, out)
+        if k64 == "err":
+            assert a64 == a32
+        else:
+            assert abs(a64["ln_evidence"] - a32["ln_evidence"]) <= 1e-3, (N, a64, a32)
+            np.testing.assert_array_equal(i64, i32)
+        r64.free()
+        r32.free()
+    finally:
+        P.set_tensor_cores(prev)
