@@ -673,3 +673,48 @@ def test_run_tiny_and_ragged_sample_sizes(pmcg, N):
         r32.free()
     finally:
         P.set_tensor_cores(prev)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_dropin_final_iteration_with_a_larger_sample(pmcg, prec):
+    """The reference driver reallocates the sample for its last iteration
+    (nsamples x fsfinal, exec/cosmo_pmc.c:300-320): after iterations at N, the
+    iteration at 2N on the reallocated sample equals the same iteration on a
+    fresh sample of 2N from the same proposal and generator state."""
+    P = pmcg
+    wl = W.mixture_workload(D=6, K=3, Kt=2, nu=-1, seed=71, prop_hi=1.0)
+    w, mu, cov, df = wl["prop"]
+    wt, mut, covt, _ = wl["target"]
+    post = P.Posterior(6).add_mix(make_mix(P, wt, mut, covt, -1))
+    N = 30000
+    try:
+        P.set_dropin_precision(prec)
+        m = make_mix(P, w, mu, cov, df)
+        ps = P.PmcSimu(N, 6)
+        rng = P.Rng(19)
+        for it in range(3):
+            rng.p.contents.calls = it
+            P.simulate_mix_mvdens(ps, m, rng, None)
+            P.importance_weights(ps, m, post, 1.0)
+            P.normalize_importance_weight(ps)
+            P.update_prop_rb(m, ps)
+        wa, mua, La = m.arrays()
+        P.call("pmc_simu_realloc", ps.p, 2 * N)
+        fresh = P.PmcSimu(2 * N, 6)
+        out = []
+        for sim, mm in ((ps, m), (fresh, P.MixMvdens.from_arrays(wa, mua, L=La, df=m.df))):
+            r = P.Rng(19)
+            r.p.contents.calls = 3
+            P.simulate_mix_mvdens(sim, mm, r, None)
+            nok = P.importance_weights(sim, mm, post, 1.0)
+            ls = P.normalize_importance_weight(sim)
+            P.update_prop_rb(mm, sim)
+            out.append((nok, ls, sim.X.copy(), sim.weights.copy(), mm.arrays()))
+        a, b = out
+        assert a[0] == b[0] and a[1] == b[1]
+        np.testing.assert_array_equal(a[2], b[2])
+        np.testing.assert_array_equal(a[3], b[3])
+        for x, y in zip(a[4], b[4]):
+            np.testing.assert_array_equal(x, y)
+    finally:
+        P.set_dropin_precision(P.FP64)
