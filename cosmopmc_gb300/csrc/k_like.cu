@@ -22,9 +22,9 @@ namespace pmcg {
 template <bool F32, bool BATCH>
 __global__ void __launch_bounds__(128) sn_kernel(SnDev sn, size_t N, int D, const double *__restrict__ X64,
                                                  const float *__restrict__ X32, int ldx, double *__restrict__ logpost,
-                                                 short *__restrict__ flg) {
+                                                 short *__restrict__ flg, int assign, double add) {
   const size_t n = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  body_sn<F32, BATCH>(sn, N, D, X64, X32, ldx, logpost, flg, n, 0, 0.0);
+  body_sn<F32, BATCH>(sn, N, D, X64, X32, ldx, logpost, flg, n, assign, add);
 }
 
 // Single precision below 2^16 samples (a few waves of warps): loads batched
@@ -35,12 +35,14 @@ __global__ void __launch_bounds__(128) sn_kernel(SnDev sn, size_t N, int D, cons
 constexpr size_t kSnBatchBelow = (size_t)1 << 16;
 
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
-                      int ldx, double *logpost, short *flg, cudaStream_t s) {
+                      int ldx, double *logpost, short *flg, cudaStream_t s, int assign, double add) {
   if (N == 0) return cudaSuccess;
   unsigned grid = (unsigned)((N + 3) / 4);
-  if (precision == 0) sn_kernel<false, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
-  else if (N < kSnBatchBelow) sn_kernel<true, true><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
-  else sn_kernel<true, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg);
+  if (precision == 0)
+    sn_kernel<false, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg, assign, add);
+  else if (N < kSnBatchBelow)
+    sn_kernel<true, true><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg, assign, add);
+  else sn_kernel<true, false><<<grid, 128, 0, s>>>(sn, N, D, X64, X32, ldx, logpost, flg, assign, add);
   return cudaGetLastError();
 }
 

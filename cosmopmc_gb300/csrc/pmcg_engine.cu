@@ -149,14 +149,24 @@ static bool stage_logq(Work &w, error **err) {
             "mixture log-pdf kernel");
 }
 
-static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
+// all_values: every sample's log-posterior is wanted (the batched posterior
+// evaluation, importance_sample). Within an iteration the weight step reads it
+// only where flg = 1, so an SN Ia first likelihood writes logpr + log L itself
+// and the fill of logpr is left out (the same values where flg = 1).
+static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err, bool all_values = true) {
   if (p->npar != w.D) {
     set_error(err, PMCG_EDIM, __LINE__, "posterior has %d parameters, sample %d", p->npar, w.D);
     return false;
   }
-  w.launches += 1;
-  if (!CK(launch_fill_f64(w.logpost, w.N, p->logpr, w.s), "fill")) return false;
+  const bool sn_assigns = !all_values && !p->plugins.empty() && p->plugins[0].type == kPluginSn;
+  if (!sn_assigns) {
+    w.launches += 1;
+    if (!CK(launch_fill_f64(w.logpost, w.N, p->logpr, w.s), "fill")) return false;
+  }
+  bool first = true;
   for (const Plugin &pl : p->plugins) {
+    const bool assign = sn_assigns && first;
+    first = false;
     w.launches += 1;
     if (pl.type == kPluginMix) {
       if (use_tensor_cores(w, pl.mix)) {
@@ -169,7 +179,9 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err) {
                      "target mixture kernel"))
         return false;
     } else if (pl.type == kPluginSn) {
-      if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "SN kernel"))
+      if (!CK(launch_sn(w.prec, pl.sn, w.N, w.D, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s, assign ? 1 : 0,
+                        p->logpr),
+              "SN kernel"))
         return false;
     } else if (pl.type == kPluginTpl) {
       if (w.prec == 1 && tc_on(w) && pl.tpl.uimg) {
@@ -839,7 +851,8 @@ static bool capture_run_graph(pmcg_run *r) {
   w.launches = 0;
   bool ok = cudaMemcpyAsync(r->dpar, r->hpar, sizeof(pmcg_iter_params), cudaMemcpyHostToDevice, w.s) == cudaSuccess;
   ok = ok && stage_draw(w, r->box, r->seed, 0u, &cerr, &r->dpar->call) && stage_logq(w, &cerr) &&
-       stage_logpost(w, r->post, &cerr) && stage_weights(w, 1.0, true, &cerr, &r->dpar->beta) && stage_em(w, &cerr);
+       stage_logpost(w, r->post, &cerr, false) && stage_weights(w, 1.0, true, &cerr, &r->dpar->beta) &&
+       stage_em(w, &cerr);
   ok = ok && cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s) == cudaSuccess;
   const bool ended = cudaStreamEndCapture(w.s, &g) == cudaSuccess;
   ok = ok && ended && g && cudaGraphInstantiate(&r->gexec, g, 0) == cudaSuccess;
@@ -890,7 +903,7 @@ static bool run_launch(pmcg_run *r, double beta, error **err) {
   mark(1);
   ok = ok && stage_logq(w, err);
   mark(2);
-  ok = ok && stage_logpost(w, r->post, err);
+  ok = ok && stage_logpost(w, r->post, err, false);
   mark(3);
   ok = ok && stage_weights(w, beta, true, err);
   mark(4);
@@ -1159,7 +1172,7 @@ extern "C" double pmcg_run_time_stage(pmcg_run *r, int stage, int reps, error **
   }
   bool ok = true;
   if (!CK(cudaEventRecord(r->ev[0], w.s), "event")) return -1.0;
-  for (int i = 0; i < reps && ok; i++) ok = (stage == 1) ? stage_logq(w, err) : stage_logpost(w, r->post, err);
+  for (int i = 0; i < reps && ok; i++) ok = (stage == 1) ? stage_logq(w, err) : stage_logpost(w, r->post, err, false);
   if (!ok || !CK(cudaEventRecord(r->ev[1], w.s), "event") ||
       !CK(cudaMemcpyAsync(w.hstats, w.dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, w.s), "status") ||
       !CK(cudaStreamSynchronize(w.s), "stage timing"))
@@ -1539,7 +1552,7 @@ extern "C" size_t simulate_mix_mvdens(pmc_simu *psim, mix_mvdens *proposal, void
   if (ok) {
     error *lerr = nullptr;
     lt = stage_logq(w, &lerr);
-    if (lt && m->post && m->post->stamp == m->post_stamp) lp = stage_logpost(w, m->post, &lerr);
+    if (lt && m->post && m->post->stamp == m->post_stamp) lp = stage_logpost(w, m->post, &lerr, false);
     // the rest of the iteration, for the beta of the last two weight steps
     if (lt && lp && C > 1 && m->beta_last == m->beta_prev && std::isfinite(m->beta_last)) speculate(m, &lerr);
     if (lerr) purgeError(&lerr);
@@ -1592,7 +1605,7 @@ extern "C" size_t generic_get_importance_weight_and_deduced_verb(pmc_simu *psim,
     // a look-ahead for another posterior flagged samples by its likelihood:
     // the draw's flags come back first
     if (m->lp_valid) ok = CK(cudaMemcpyAsync(w.flg, m->flg0, 2 * w.N, cudaMemcpyDeviceToDevice, w.s), "flags");
-    ok = ok && stage_logpost(w, p, err);
+    ok = ok && stage_logpost(w, p, err, false);
   }
   m->lp_valid = false;
   m->beta_prev = m->beta_last;

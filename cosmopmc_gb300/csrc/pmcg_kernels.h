@@ -192,8 +192,10 @@ struct SnDev {
   float fdef_om = 0.3f, fdef_w0 = -1.0f, fdef_M = -19.3f, fdef_alpha = 0.0f, fdef_beta = 0.0f;
   void *arena = nullptr;
 };
+// assign != 0: logpost = add + logL for the samples it evaluates (the others
+// keep what logpost held); otherwise logpost += logL.
 cudaError_t launch_sn(int precision, const SnDev &sn, size_t N, int D, const double *X64, const float *X32,
-                      int ldx, double *logpost, short *flg, cudaStream_t s);
+                      int ldx, double *logpost, short *flg, cudaStream_t s, int assign = 0, double add = 0.0);
 
 // (c) dense template likelihood (whitened): logpost += -1/2 |dt - At phi(x)|^2.
 struct TplDev {
