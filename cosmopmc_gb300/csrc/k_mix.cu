@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(128) mixlogpdf_f64_kernel(DevMixView m, size_t
   if (act) {
     double r = mx + log(sm);
     if (accumulate) out[n] += r + add;
-    else out[n] = r;
+    else out[n] = r + add;
   }
 }
 

@@ -110,7 +110,7 @@ template <int D>
 __global__ void __launch_bounds__(kTuThreads, 1)
     tpl_umma_kernel(const unsigned char *__restrict__ uimg, size_t N, const float *__restrict__ X,
                     int ldx, double *__restrict__ logpost, const short *__restrict__ flg,
-                    int *__restrict__ errflag) {
+                    int *__restrict__ errflag, int assign, double add) {
   extern __shared__ __align__(1024) unsigned char tu_raw[];
   unsigned char *base = tu_raw + ((1024 - (smem_u32(tu_raw) & 1023)) & 1023);
   unsigned char *sAh = base, *sAl = base + kTuOpA;   // phi of the tile: hi, lo
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kTuThreads, 1)
         // in flight while the MMAs run
         n_prev = (blockIdx.x + (size_t)i * gridDim.x) * kTuTile + tid;
         f_prev = (n_prev < N) ? flg[n_prev] : (short)0;
-        lp_prev = (n_prev < N) ? logpost[n_prev] : 0.0;
+        lp_prev = (n_prev < N) ? (assign ? add : logpost[n_prev]) : 0.0;
         if (i + 1 < my_tiles) tu_fetch<D>(X, ldx, N, (blockIdx.x + (size_t)(i + 1) * gridDim.x) * kTuTile + tid, th);
       }
     }
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kTuThreads, 1)
 }
 
 cudaError_t launch_tpl_umma(const unsigned char *uimg, int Dp, size_t N, const float *X, int ldx, double *logpost,
-                            const short *flg, int *errflag, cudaStream_t s) {
+                            const short *flg, int *errflag, cudaStream_t s, int assign, double add) {
   if (N == 0) return cudaSuccess;
   if (!uimg || Dp < 1 || Dp > kTplUmmaMaxD) return cudaErrorInvalidValue;
   int dev = 0, sms = 0, maxsm = 0;
@@ -245,7 +245,8 @@ cudaError_t launch_tpl_umma(const unsigned char *uimg, int Dp, size_t N, const f
     if ((e = cudaFuncSetAttribute(tpl_umma_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
                                   kTuSmem)) != cudaSuccess)                                                   \
       return e;                                                                                               \
-    tpl_umma_kernel<DV><<<grid, kTuThreads, kTuSmem, s>>>(uimg, N, X, ldx, logpost, flg, errflag);           \
+    tpl_umma_kernel<DV><<<grid, kTuThreads, kTuSmem, s>>>(uimg, N, X, ldx, logpost, flg, errflag, assign,    \
+                                                          add);                                               \
     break;
   switch (Dp) {
     PMCG_TU(1) PMCG_TU(2) PMCG_TU(3) PMCG_TU(4) PMCG_TU(5) PMCG_TU(6)

@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kUmThreads, 1)
         if (mx[1] > -INFINITY) sum = fmaf(sm[1], ex2_approx((mx[1] - m) * kLog2e), sum);
         const double r = (double)m + (double)logf(sum);
         if (accumulate) out[n] += r + add;
-        else out[n] = r;
+        else out[n] = r + add;
       }
     }
     if (!ok) atomicExch(errflag, 1);

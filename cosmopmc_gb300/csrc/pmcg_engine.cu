@@ -151,31 +151,37 @@ static bool stage_logq(Work &w, error **err) {
 
 // all_values: every sample's log-posterior is wanted (the batched posterior
 // evaluation, importance_sample). Within an iteration the weight step reads it
-// only where flg = 1, so an SN Ia first likelihood writes logpr + log L itself
-// and the fill of logpr is left out (the same values where flg = 1).
+// only where flg = 1, so a first likelihood that can write logpr + log L
+// itself (SN Ia, a mixture, the tensor-core template) does, and the fill of
+// logpr is left out (the same values where flg = 1).
 static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err, bool all_values = true) {
   if (p->npar != w.D) {
     set_error(err, PMCG_EDIM, __LINE__, "posterior has %d parameters, sample %d", p->npar, w.D);
     return false;
   }
-  const bool sn_assigns = !all_values && !p->plugins.empty() && p->plugins[0].type == kPluginSn;
-  if (!sn_assigns) {
+  bool first_assigns = false;   // the first likelihood assigns
+  if (!all_values && !p->plugins.empty()) {
+    const Plugin &p0 = p->plugins[0];
+    first_assigns = p0.type == kPluginSn || p0.type == kPluginMix ||
+                 (p0.type == kPluginTpl && w.prec == 1 && tc_on(w) && p0.tpl.uimg);
+  }
+  if (!first_assigns) {
     w.launches += 1;
     if (!CK(launch_fill_f64(w.logpost, w.N, p->logpr, w.s), "fill")) return false;
   }
   bool first = true;
   for (const Plugin &pl : p->plugins) {
-    const bool assign = sn_assigns && first;
+    const bool assign = first_assigns && first;
     first = false;
     w.launches += 1;
     if (pl.type == kPluginMix) {
       if (use_tensor_cores(w, pl.mix)) {
-        if (!CK(launch_umma_logq(pl.mix.view(), pl.mix.bimg, w.N, w.X32, w.logpost, 1, 0.0, nullptr, nullptr,
-                                 &w.dstats->tc_err, w.s),
+        if (!CK(launch_umma_logq(pl.mix.view(), pl.mix.bimg, w.N, w.X32, w.logpost, assign ? 0 : 1,
+                                 assign ? p->logpr : 0.0, nullptr, nullptr, &w.dstats->tc_err, w.s),
                 "tensor-core target mixture kernel"))
           return false;
-      } else if (!CK(launch_mixlogpdf(w.prec, pl.mix.view(), w.N, w.X64, w.X32, w.logpost, 1, 0.0, nullptr,
-                                      nullptr, nullptr, nullptr, w.s),
+      } else if (!CK(launch_mixlogpdf(w.prec, pl.mix.view(), w.N, w.X64, w.X32, w.logpost, assign ? 0 : 1,
+                                      assign ? p->logpr : 0.0, nullptr, nullptr, nullptr, nullptr, w.s),
                      "target mixture kernel"))
         return false;
     } else if (pl.type == kPluginSn) {
@@ -186,7 +192,7 @@ static bool stage_logpost(Work &w, const pmcg_posterior *p, error **err, bool al
     } else if (pl.type == kPluginTpl) {
       if (w.prec == 1 && tc_on(w) && pl.tpl.uimg) {
         if (!CK(launch_tpl_umma(pl.tpl.uimg, pl.tpl.Dpar, w.N, w.X32, w.ldx, w.logpost, w.flg, &w.dstats->tc_err,
-                                w.s),
+                                w.s, assign ? 1 : 0, p->logpr),
                 "tensor-core template kernel"))
           return false;
       } else if (!CK(launch_tpl(w.prec, pl.tpl, w.N, w.X64, w.X32, w.ldx, w.logpost, w.flg, w.s), "template kernel")) {

@@ -218,8 +218,9 @@ constexpr int kGramMaxP = 96;
 constexpr int kTplUmmaMaxD = 12;
 size_t tpl_uimage_bytes();
 cudaError_t launch_tpl_uimage(const float *U32, unsigned char *img, cudaStream_t s);
+// assign != 0: logpost = add + log L where flg = 1; otherwise logpost += log L.
 cudaError_t launch_tpl_umma(const unsigned char *uimg, int Dp, size_t N, const float *X, int ldx, double *logpost,
-                            const short *flg, int *errflag, cudaStream_t s);
+                            const short *flg, int *errflag, cudaStream_t s, int assign = 0, double add = 0.0);
 cudaError_t launch_tpl(int precision, const TplDev &t, size_t N, const double *X64, const float *X32, int ldx,
                        double *logpost, const short *flg, cudaStream_t s);
 
