@@ -1228,6 +1228,9 @@ struct SimMirror {
   uint64_t post_stamp = 0;
   bool lp_valid = false;
   std::vector<double> snap_w, snap_mu, snap_L;
+  // the update's download buffers: swapped with the snapshot after each update,
+  // so they are allocated (and their pages touched) once, not every iteration
+  std::vector<double> upd_w, upd_mu, upd_L;
   double *mom = nullptr;   // scratch of the weighted moments (allocated on first use)
   // Speculation (single precision, sample copied in ranges): after the
   // look-ahead, while X still travels to the host, the weight step for the
@@ -1891,7 +1894,10 @@ extern "C" void update_prop_rb(mix_mvdens *proposal, pmc_simu *psim, error **err
     if (!stage_em(w, err) || !fetch_stats(w, err)) return;
   }
   const int K = w.K, D = w.D;
-  std::vector<double> wt(K), mu((size_t)K * D), L((size_t)K * D * D);
+  std::vector<double> &wt = m->upd_w, &mu = m->upd_mu, &L = m->upd_L;
+  wt.resize(K);
+  mu.resize((size_t)K * D);
+  L.resize((size_t)K * D * D);
   bool ok = CK(cudaMemcpyAsync(wt.data(), w.prop.w, 8 * K, cudaMemcpyDeviceToHost, w.s), "proposal") &&
             CK(cudaMemcpyAsync(mu.data(), w.prop.mu, 8 * mu.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
             CK(cudaMemcpyAsync(L.data(), w.prop.L, 8 * L.size(), cudaMemcpyDeviceToHost, w.s), "proposal") &&
