@@ -153,3 +153,33 @@ def test_job_the_batch_does_not_take_runs_alone(pmcg):
     assert rw["ln_evidence"] == ref[-1]["ln_evidence"] and rw["ess"] == ref[-1]["ess"]
     for a, b in zip(pw.arrays(), ref_prop):
         assert np.array_equal(a, b)
+
+
+def test_job_with_two_likelihoods_runs_alone(pmcg):
+    """A posterior with two likelihoods (two Gaussian-mixture targets; the batch
+    takes one) is served beside the batch and gives the run alone's result."""
+    P = pmcg
+    keep = []
+    spec = ("mix", 5, 3, 7000, 55)
+    prop, post1, box = _job(P, spec, keep)
+    from cosmopmc_gb300 import workloads as W
+    wl = W.mixture_workload(D=5, K=2, Kt=2, nu=-1, seed=56, prop_hi=1.0)
+    wt, mut, covt, _ = wl["target"]
+    post = P.Posterior(5)
+    for ww, mm, cc in ((wl["prop"][0], wl["prop"][1], wl["prop"][2]), (wt, mut, covt)):
+        post.add_mix(P.MixMvdens.from_arrays(ww, mm, cov=cc, df=-1).cholesky())
+    keep.append(post)
+    run = P.Run(prop, post, spec[3], precision=P.MIXED, seed=spec[4])
+    ref = [run.iterate(1.0) for _ in range(3)]
+    ref_prop = run.proposal().arrays()
+    run.free()
+    s = P.Server()
+    ids = [s.submit(pp, po, sp[3], 3, sp[4], box=bx) for sp, (pp, po, bx) in zip(MIX[:2], [_job(P, x, keep) for x in MIX[:2]])]
+    j = s.submit(prop, post, spec[3], 3, spec[4])
+    res = [s.wait(i, timeout=120) for i in ids]
+    rj, pj = s.wait(j, timeout=120, want_proposal=True)
+    s.free()
+    assert all(r["status"] == 0 for r in res)
+    assert rj["status"] == 0 and rj["ln_evidence"] == ref[-1]["ln_evidence"]
+    for a, b in zip(pj.arrays(), ref_prop):
+        assert np.array_equal(a, b)
